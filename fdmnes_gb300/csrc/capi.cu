@@ -1,0 +1,934 @@
+// capi.cu - the C-ABI of include/fdmgpu.h: handle, static upload, per-problem
+// planning of the band tiles, device pools and the launch sequences.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/fdmgpu.h"
+#include "fdm_internal.cuh"
+#include "fdm_kernels.h"
+
+using namespace fdm;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+fdmgpu_status fail(fdmgpu_status st, const std::string& msg) {
+  g_last_error = msg;
+  return st;
+}
+
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t _e = (call);                                                                       \
+    if (_e != cudaSuccess)                                                                         \
+      return fail(FDMGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e));            \
+  } while (0)
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t cap = 0;  // elements
+  cudaError_t reserve(size_t n) {
+    if (n <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t m = std::max<size_t>(n, 1);
+    cudaError_t e = cudaMalloc(&p, m * sizeof(T));
+    if (e == cudaSuccess) cap = m;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+template <typename T>
+cudaError_t upload(DevBuf<T>& b, const std::vector<T>& h, cudaStream_t s) {
+  cudaError_t e = b.reserve(h.size());
+  if (e != cudaSuccess) return e;
+  if (h.empty()) return cudaSuccess;
+  return cudaMemcpyAsync(b.p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+// One problem (one energy / spin block) of a batch, host side.
+struct HostProb {
+  Prob P;
+  std::vector<int> J0, J1, Imax, Imin;  // nt + 1
+  std::vector<int64_t> strip;           // nt + 1
+  int64_t ntiles = 0;
+  int64_t nnz_cap = 0;
+  int64_t nnz_profile = 0;
+  double flops_factor = 0, flops_solve = 0;
+  std::vector<int> in_i;
+  std::vector<double> in_d;
+  int nlmsa_max = 0;
+  uint64_t sig = 0;
+};
+
+struct Batch {
+  int precision = FDMGPU_PREC_FP64;
+  int max_energies = 0;
+  std::vector<HostProb> probs;
+  // results
+  std::vector<int> iters;
+  std::vector<double> resid;
+  std::vector<int> err;
+  bool ran = false;
+};
+
+}  // namespace
+
+struct fdmgpu_handle {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  // static structure
+  fdmgpu_grid g{};
+  StaticDev S{};
+  std::vector<int> inter_pt_h, nb_kind_h, nb_idx_h;
+  std::vector<double> nb_coef_h;
+  std::vector<int> n_inter_h, has_outer_h;       // per interstitial point
+  std::vector<std::vector<int>> nb_atoms_h;      // distinct atoms touched per interstitial point
+  std::vector<int> numia_h, isrt_h, ibord_h, nbordf_h;
+  std::vector<int> lato_h, mato_h;
+  DevBuf<int> d_inter_pt, d_nb_kind, d_nb_idx, d_numia, d_nbord, d_nbordf, d_ibord, d_isbord, d_isrt, d_lato, d_mato,
+      d_lso, d_mso;
+  DevBuf<double> d_nb_coef, d_rvol, d_clapl, d_poidsa, d_poidso, d_Kar, d_YsoT, d_Ylmato;
+  // batch pools
+  Batch batch;
+  DevBuf<Prob> d_probs;
+  DevBuf<int> d_J0, d_J1, d_Imax, d_Imin;
+  DevBuf<int64_t> d_strip;
+  DevBuf<int> d_ipool;
+  DevBuf<double> d_dpool;
+  DevBuf<double> d_env64, d_B64, d_X64, d_rs, d_cs, d_val, d_taull, d_tscratch, d_smr;
+  DevBuf<float> d_env32, d_Y32;
+  DevBuf<int> d_rowptr, d_col, d_err, d_active;
+  DevBuf<unsigned long long> d_red;  // dmax | xmax | amax
+  int* h_pinned_i = nullptr;
+  size_t h_pinned_i_cap = 0;
+  double* h_pinned_d = nullptr;
+  size_t h_pinned_d_cap = 0;
+  // graphs of the last plan
+  uint64_t plan_sig = 0;
+  uint64_t ptr_sig = 0;
+  int plan_prec = -1;
+  cudaGraphExec_t g_asm = nullptr, g_fac = nullptr, g_sol = nullptr, g_iter = nullptr;
+  StepPlan sp;
+  LaunchDims dims;
+  Tables tb{};
+  Pools pl{};
+  cudaEvent_t ev[6] = {};
+};
+
+namespace {
+
+inline int32_t F2(const int32_t* a, int64_t ld, int64_t i, int64_t j) { return a[(i - 1) + (j - 1) * ld]; }
+
+uint64_t mix(uint64_t h, uint64_t v) {
+  h ^= v + 0x9e3779b97f4a7c15ULL + (h << 6) + (h >> 2);
+  return h;
+}
+
+fdmgpu_status check_energy(const fdmgpu_handle* h, const fdmgpu_energy* e) {
+  if (!e) return fail(FDMGPU_ERR_ARG, "null energy arguments");
+  if (e->Cal_comp || e->E_comp || e->Spinorbite || e->Relativiste || e->Repres_comp || e->Ylm_comp || e->irregular ||
+      e->Base_hexa || e->n_RI != 1 || e->n_ato_RI != 1 || e->nphiato7 != 1 || h->g.nspino != 1 || !e->Basereel)
+    return fail(FDMGPU_ERR_UNSUPPORTED,
+                "this build provides the real-arithmetic regular solution (Cal_comp = E_comp = Spinorbite = "
+                "Relativiste = irregular = false, Basereel = true, nspino = 1)");
+  if (e->nligne <= 0 || e->nlmso <= 0 || e->nligneso != e->nligne - e->nlmso)
+    return fail(FDMGPU_ERR_ARG, "inconsistent nligne / nlmso / nligneso");
+  if (e->lmaxso < 0 || (e->lmaxso + 1) * (e->lmaxso + 1) < e->nlmso || e->nsort_r < h->g.nsort)
+    return fail(FDMGPU_ERR_ARG, "Bessel arrays too small for nlmso");
+  if (e->nlmso > h->g.nso1) return fail(FDMGPU_ERR_ARG, "nlmso exceeds the outer harmonic tables");
+  if (!e->new_ || !e->newinv || !e->lb1 || !e->lb2 || !e->ianew || !e->nlmsa || !e->Vr || !e->phiato ||
+      !e->Besselr || !e->Neumanr)
+    return fail(FDMGPU_ERR_ARG, "null array argument");
+  return FDMGPU_OK;
+}
+
+// Band tile plan of one problem from newind's lb1/lb2.
+fdmgpu_status plan_problem(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& hp) {
+  const int n = e->nligne;
+  const int nt = (n + TS - 1) / TS;
+  const int npad = nt * TS;
+  std::vector<int> fl(npad), lu(npad);
+  for (int p = 0; p < npad; ++p) {
+    if (p < n) {
+      const int ii = n - p;
+      const int l1 = e->lb1[ii - 1], l2 = e->lb2[ii - 1];
+      if (l1 < 1 || l2 > n || l1 > ii || l2 < ii) return fail(FDMGPU_ERR_ARG, "lb1/lb2 do not bracket the diagonal");
+      fl[p] = n - l2;
+      lu[p] = n - l1;
+    } else {
+      fl[p] = lu[p] = p;
+    }
+    if (p > 0 && lu[p] < lu[p - 1]) return fail(FDMGPU_ERR_ARG, "lb1 is not monotone");
+  }
+  hp.J0.assign(nt + 1, 0);
+  hp.J1.assign(nt + 1, 0);
+  hp.Imax.assign(nt + 1, 0);
+  hp.Imin.assign(nt + 1, 0);
+  hp.strip.assign(nt + 1, 0);
+  for (int I = 0; I < nt; ++I) {
+    int a = npad, b = 0;
+    for (int p = I * TS; p < (I + 1) * TS; ++p) {
+      a = std::min(a, fl[p]);
+      b = std::max(b, lu[p]);
+    }
+    hp.J0[I] = a / TS;
+    hp.J1[I] = b / TS;
+  }
+  for (int I = nt - 2; I >= 0; --I) hp.J0[I] = std::min(hp.J0[I], hp.J0[I + 1]);
+  for (int I = 1; I < nt; ++I) hp.J1[I] = std::max(hp.J1[I], hp.J1[I - 1]);
+  int64_t off = 0;
+  for (int I = 0; I < nt; ++I) {
+    hp.strip[I] = off;
+    off += hp.J1[I] - hp.J0[I] + 1;
+  }
+  hp.strip[nt] = off;
+  hp.ntiles = off;
+  for (int K = 0; K < nt; ++K) {
+    int im = K;
+    while (im + 1 < nt && hp.J0[im + 1] <= K) ++im;
+    hp.Imax[K] = im;
+    int mn = K;
+    while (mn - 1 >= 0 && hp.J1[mn - 1] >= K) --mn;
+    hp.Imin[K] = mn;
+  }
+  // algorithmic work of the profile: sum_k 2 l_k u_k and the two solves
+  std::vector<int64_t> cnt(npad + 1, 0);
+  for (int p = 0; p < n; ++p) cnt[fl[p]]++;
+  int64_t cum = 0, nnzL = 0, nnzU = 0;
+  double ff = 0;
+  for (int k = 0; k < n; ++k) {
+    cum += cnt[k];
+    const int64_t lk = cum - (k + 1);
+    const int64_t uk = lu[k] - k;
+    nnzL += lk;
+    nnzU += uk;
+    ff += 2.0 * (double)lk * (double)uk + (double)lk;
+  }
+  hp.flops_factor = ff;
+  hp.flops_solve = 2.0 * e->nlmso * (double)(nnzL + nnzU + n);
+  hp.nnz_profile = nnzL + nnzU + n;
+  // CSR capacity: structural nonzeros of calcMatRow
+  const fdmgpu_grid& g = h->g;
+  int64_t cap = (npad - n);
+  for (size_t k = 0; k < h->inter_pt_h.size(); ++k) {
+    cap += 1 + h->n_inter_h[k] + (h->has_outer_h[k] ? e->nlmso : 0);
+    for (int ia : h->nb_atoms_h[k]) cap += e->nlmsa[ia - 1];
+  }
+  cap += (int64_t)e->nlmso * (e->nlmso + g.nsortf);
+  for (int ia = 1; ia <= g.natome; ++ia) cap += (int64_t)e->nlmsa[ia - 1] * (h->nbordf_h[ia - 1] + e->nlmsa[ia - 1]);
+  hp.nnz_cap = cap;
+  // descriptor (offsets filled later)
+  Prob& P = hp.P;
+  memset(&P, 0, sizeof(P));
+  P.n = n;
+  P.nt = nt;
+  P.nlmso = e->nlmso;
+  P.nrt = (e->nlmso + TS - 1) / TS;
+  P.nligneso = e->nligneso;
+  P.lmaxso = e->lmaxso;
+  P.nlmagm = e->nlmagm;
+  P.ispin = e->ispin;
+  P.enervide = e->Enervide;
+  // signature of the plan
+  uint64_t s = mix(0, (uint64_t)n);
+  s = mix(s, (uint64_t)e->nlmso);
+  for (int i = 0; i < n; i += 7) s = mix(s, (uint64_t)e->lb1[i] * 131 + (uint64_t)e->lb2[i]);
+  for (int ia = 0; ia < g.natome; ++ia) s = mix(s, (uint64_t)e->nlmsa[ia] * 1000003u + (uint64_t)e->ianew[ia]);
+  hp.sig = s;
+  return FDMGPU_OK;
+}
+
+// Pack the per-energy inputs (selected spin) into flat host vectors.
+void pack_inputs(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& hp) {
+  const fdmgpu_grid& g = h->g;
+  hp.in_i.clear();
+  hp.in_d.clear();
+  // ints: new_(0:npoint), ianew, nlmsa
+  hp.in_i.insert(hp.in_i.end(), e->new_, e->new_ + g.npoint + 1);
+  hp.in_i.insert(hp.in_i.end(), e->ianew, e->ianew + g.natome);
+  hp.in_i.insert(hp.in_i.end(), e->nlmsa, e->nlmsa + g.natome);
+  hp.nlmsa_max = 0;
+  for (int ia = 0; ia < g.natome; ++ia) hp.nlmsa_max = std::max(hp.nlmsa_max, e->nlmsa[ia]);
+  // doubles: Vr(:, ispp)
+  const int ispp = std::min(e->ispin, g.nspin);
+  hp.in_d.insert(hp.in_d.end(), e->Vr + (int64_t)g.npoint * (ispp - 1), e->Vr + (int64_t)g.npoint * ispp);
+  // phiato(ib, Lm, isp, isol=1, iRI=1, ia, 1) -> (nbtm, nlmagm, natome)
+  const int isp = std::min(e->ispin, e->nspinp);
+  const int64_t d1 = e->nphiato1, d2 = e->nlmagm, d3 = e->nspinp, d4 = g.nspino, d5 = e->n_RI;
+  const size_t base = hp.in_d.size();
+  hp.in_d.resize(base + (size_t)g.nbtm * e->nlmagm * g.natome, 0.0);
+  const int nb = std::min<int>(e->nphiato1, g.nbtm);
+  for (int ia = 1; ia <= g.natome; ++ia)
+    for (int lm = 1; lm <= e->nlmagm; ++lm) {
+      const double* src = e->phiato + d1 * ((lm - 1) + d2 * ((isp - 1) + d3 * (0 + d4 * (0 + d5 * (int64_t)(ia - 1)))));
+      double* dst = hp.in_d.data() + base + (size_t)g.nbtm * ((lm - 1) + (size_t)e->nlmagm * (ia - 1));
+      memcpy(dst, src, sizeof(double) * nb);
+    }
+  // Bessel / Neumann (nsort_r, 0:lmaxso, ispq = 1) -> [ib][L]
+  const int nl = e->lmaxso + 1;
+  for (int which = 0; which < 2; ++which) {
+    const double* a = which == 0 ? e->Besselr : e->Neumanr;
+    const size_t b0 = hp.in_d.size();
+    hp.in_d.resize(b0 + (size_t)g.nsort * nl);
+    for (int ib = 0; ib < g.nsort; ++ib)
+      for (int L = 0; L < nl; ++L) hp.in_d[b0 + (size_t)ib * nl + L] = a[ib + (int64_t)e->nsort_r * L];
+  }
+}
+
+void build_step_plan(fdmgpu_handle* h) {
+  StepPlan& sp = h->sp;
+  auto& pr = h->batch.probs;
+  sp.ntmax = 0;
+  sp.nrtmax = 0;
+  for (auto& hp : pr) {
+    sp.ntmax = std::max(sp.ntmax, hp.P.nt);
+    sp.nrtmax = std::max(sp.nrtmax, hp.P.nrt);
+  }
+  const int N = sp.ntmax;
+  sp.panel.assign(N, 0);
+  sp.panel_rhs.assign(N, 0);
+  sp.trail.assign(N, 0);
+  sp.trail_rhs.assign(N, 0);
+  sp.fwd.assign(N, 0);
+  sp.bwd.assign(N, 0);
+  for (auto& hp : pr) {
+    for (int K = 0; K < hp.P.nt; ++K) {
+      const int nI = hp.Imax[K] - K, nJ = hp.J1[K] - K, nR = hp.P.nrt;
+      sp.panel[K] = std::max(sp.panel[K], nI + nJ);
+      sp.panel_rhs[K] = std::max(sp.panel_rhs[K], nI + nJ + nR);
+      sp.trail[K] = std::max(sp.trail[K], nI * nJ);
+      sp.trail_rhs[K] = std::max(sp.trail_rhs[K], nI * (nJ + nR));
+      sp.fwd[K] = std::max(sp.fwd[K], nI * nR);
+      sp.bwd[K] = std::max(sp.bwd[K], (K - hp.Imin[K]) * nR);
+    }
+  }
+}
+
+// Assign pool offsets, allocate device memory and upload plan tables.
+fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h) {
+  auto& pr = h->batch.probs;
+  const int np = (int)pr.size();
+  const bool mixed = h->batch.precision == FDMGPU_PREC_MIXED;
+  int64_t env = 0, rhs = 0, rowv = 0, csr = 0, taull = 0, scratch = 0;
+  int trow = 0;
+  LaunchDims& d = h->dims;
+  d = LaunchDims();
+  d.nprob = np;
+  d.npr = h->S.npr;
+  std::vector<int> J0, J1, Imax, Imin;
+  std::vector<int64_t> strip;
+  for (auto& hp : pr) {
+    Prob& P = hp.P;
+    P.trow = trow;
+    P.env = env * TS2;
+    P.rhs = rhs;
+    P.rowv = rowv;
+    P.csr = csr;
+    P.csr_cap = mixed ? hp.nnz_cap : 0;
+    P.taull = taull;
+    P.scratch = scratch;
+    trow += P.nt + 1;
+    env += hp.ntiles;
+    rhs += (int64_t)P.nt * P.nrt * TS2;
+    rowv += (int64_t)P.nt * TS + 1;
+    csr += mixed ? hp.nnz_cap : 0;
+    taull += (int64_t)P.nlm_abs * P.nlm_abs;
+    scratch += (int64_t)P.nlmso * (P.nlmso + P.nlm_abs);
+    J0.insert(J0.end(), hp.J0.begin(), hp.J0.end());
+    J1.insert(J1.end(), hp.J1.begin(), hp.J1.end());
+    Imax.insert(Imax.end(), hp.Imax.begin(), hp.Imax.end());
+    Imin.insert(Imin.end(), hp.Imin.begin(), hp.Imin.end());
+    strip.insert(strip.end(), hp.strip.begin(), hp.strip.end());
+    d.max_rows = std::max(d.max_rows, P.nt * TS);
+    d.max_tiles = std::max<int>(d.max_tiles, (int)hp.ntiles);
+    d.max_rhs_tiles = std::max(d.max_rhs_tiles, P.nt * P.nrt);
+    d.max_nlmso = std::max(d.max_nlmso, P.nlmso);
+    d.max_atom_rows = std::max(d.max_atom_rows, h->g.natome * hp.nlmsa_max);
+  }
+  cudaStream_t s = h->stream;
+  CK(upload(h->d_J0, J0, s));
+  CK(upload(h->d_J1, J1, s));
+  CK(upload(h->d_Imax, Imax, s));
+  CK(upload(h->d_Imin, Imin, s));
+  CK(upload(h->d_strip, strip, s));
+  if (h->d_env64.reserve((size_t)env * TS2) != cudaSuccess || h->d_B64.reserve(rhs) != cudaSuccess ||
+      h->d_X64.reserve(rhs) != cudaSuccess || h->d_err.reserve(np) != cudaSuccess ||
+      h->d_active.reserve(np) != cudaSuccess || h->d_red.reserve(3 * (size_t)np) != cudaSuccess ||
+      h->d_taull.reserve(2 * (size_t)std::max<int64_t>(taull, 1)) != cudaSuccess ||
+      h->d_tscratch.reserve(2 * (size_t)std::max<int64_t>(scratch, 1)) != cudaSuccess)
+    return fail(FDMGPU_ERR_NOMEM, "device allocation of the batch pools failed");
+  if (mixed) {
+    if (h->d_env32.reserve((size_t)env * TS2) != cudaSuccess || h->d_Y32.reserve(rhs) != cudaSuccess ||
+        h->d_rs.reserve(rowv) != cudaSuccess || h->d_cs.reserve(rowv) != cudaSuccess ||
+        h->d_rowptr.reserve(rowv) != cudaSuccess || h->d_col.reserve(csr) != cudaSuccess ||
+        h->d_val.reserve(csr) != cudaSuccess)
+      return fail(FDMGPU_ERR_NOMEM, "device allocation of the mixed precision pools failed");
+  }
+  h->tb.J0 = h->d_J0.p;
+  h->tb.J1 = h->d_J1.p;
+  h->tb.Imax = h->d_Imax.p;
+  h->tb.Imin = h->d_Imin.p;
+  h->tb.strip = h->d_strip.p;
+  Pools& pl = h->pl;
+  pl = Pools();
+  pl.env64 = h->d_env64.p;
+  pl.B64 = h->d_B64.p;
+  pl.X64 = h->d_X64.p;
+  pl.err = h->d_err.p;
+  pl.active = h->d_active.p;
+  pl.dmax = h->d_red.p;
+  pl.xmax = h->d_red.p + np;
+  pl.amax = h->d_red.p + 2 * np;
+  pl.taull = h->d_taull.p;
+  pl.tscratch = h->d_tscratch.p;
+  if (mixed) {
+    pl.env32 = h->d_env32.p;
+    pl.Y32 = h->d_Y32.p;
+    pl.rs = h->d_rs.p;
+    pl.cs = h->d_cs.p;
+    pl.rowptr = h->d_rowptr.p;
+    pl.col = h->d_col.p;
+    pl.val = h->d_val.p;
+  }
+  build_step_plan(h);
+  return FDMGPU_OK;
+}
+
+// Upload the per-problem inputs and descriptors (every run).
+fdmgpu_status upload_inputs(fdmgpu_handle* h) {
+  auto& pr = h->batch.probs;
+  size_t ni = 0, nd = 0;
+  for (auto& hp : pr) {
+    hp.P.in_new = ni;
+    hp.P.in_ianew = ni + h->g.npoint + 1;
+    hp.P.in_nlmsa = hp.P.in_ianew + h->g.natome;
+    ni += hp.in_i.size();
+    hp.P.in_vr = nd;
+    hp.P.in_phi = nd + h->g.npoint;
+    hp.P.in_bes = hp.P.in_phi + (int64_t)h->g.nbtm * hp.P.nlmagm * h->g.natome;
+    hp.P.in_neu = hp.P.in_bes + (int64_t)h->g.nsort * (hp.P.lmaxso + 1);
+    nd += hp.in_d.size();
+  }
+  if (ni > h->h_pinned_i_cap) {
+    if (h->h_pinned_i) cudaFreeHost(h->h_pinned_i);
+    CK(cudaMallocHost(&h->h_pinned_i, ni * sizeof(int)));
+    h->h_pinned_i_cap = ni;
+  }
+  if (nd > h->h_pinned_d_cap) {
+    if (h->h_pinned_d) cudaFreeHost(h->h_pinned_d);
+    CK(cudaMallocHost(&h->h_pinned_d, nd * sizeof(double)));
+    h->h_pinned_d_cap = nd;
+  }
+  CK(cudaStreamSynchronize(h->stream));  // the pinned buffers may still feed a previous copy
+  size_t oi = 0, od = 0;
+  std::vector<Prob> P;
+  for (auto& hp : pr) {
+    memcpy(h->h_pinned_i + oi, hp.in_i.data(), hp.in_i.size() * sizeof(int));
+    memcpy(h->h_pinned_d + od, hp.in_d.data(), hp.in_d.size() * sizeof(double));
+    oi += hp.in_i.size();
+    od += hp.in_d.size();
+    P.push_back(hp.P);
+  }
+  if (h->d_ipool.reserve(ni) != cudaSuccess || h->d_dpool.reserve(nd) != cudaSuccess)
+    return fail(FDMGPU_ERR_NOMEM, "device allocation of the input pools failed");
+  CK(cudaMemcpyAsync(h->d_ipool.p, h->h_pinned_i, ni * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->d_dpool.p, h->h_pinned_d, nd * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(upload(h->d_probs, P, h->stream));
+  h->pl.ipool = h->d_ipool.p;
+  h->pl.dpool = h->d_dpool.p;
+  return FDMGPU_OK;
+}
+
+// Main sequence in three captured parts, timed by events recorded between
+// the graph launches: (1) assemble (+ CSR copy and FP32 conversion when
+// mixed), (2) factor with the fused forward substitution, (3) backward
+// substitution (+ first update of x when mixed).
+void record_asm(fdmgpu_handle* h) {
+  cudaStream_t s = h->stream;
+  const Pools& pl = h->pl;
+  const Prob* probs = h->d_probs.p;
+  const int np = h->dims.nprob;
+  int64_t env = 0, rhs = 0;
+  for (auto& hp : h->batch.probs) {
+    env += hp.ntiles * TS2;
+    rhs += (int64_t)hp.P.nt * hp.P.nrt * TS2;
+  }
+  cudaMemsetAsync(pl.env64, 0, env * sizeof(double), s);
+  cudaMemsetAsync(pl.B64, 0, rhs * sizeof(double), s);
+  cudaMemsetAsync(pl.err, 0, np * sizeof(int), s);
+  launch_assemble(h->S, probs, pl, h->tb, h->dims, s);
+  if (h->batch.precision == FDMGPU_PREC_FP64) {
+    cudaMemcpyAsync(pl.X64, pl.B64, rhs * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  } else {
+    launch_csr(probs, pl, h->tb, h->dims, s);
+    launch_equilibrate_convert(probs, pl, h->tb, h->dims, s);
+  }
+}
+
+void record_factor(fdmgpu_handle* h) {
+  cudaStream_t s = h->stream;
+  const Pools& pl = h->pl;
+  const int np = h->dims.nprob;
+  if (h->batch.precision == FDMGPU_PREC_FP64)
+    launch_factor<double>(h->sp, pl.env64, pl.X64, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-10, s);
+  else
+    launch_factor<float>(h->sp, pl.env32, pl.Y32, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-30, s);
+}
+
+void record_solve(fdmgpu_handle* h) {
+  cudaStream_t s = h->stream;
+  const Pools& pl = h->pl;
+  const int np = h->dims.nprob;
+  if (h->batch.precision == FDMGPU_PREC_FP64) {
+    launch_backward<double>(h->sp, pl.env64, pl.X64, h->d_probs.p, h->tb, np, nullptr, s);
+  } else {
+    launch_backward<float>(h->sp, pl.env32, pl.Y32, h->d_probs.p, h->tb, np, nullptr, s);
+    cudaMemsetAsync(pl.dmax, 0, 3 * np * sizeof(unsigned long long), s);
+    launch_update_x(h->d_probs.p, pl, h->dims, 1, s);
+  }
+}
+
+void record_iter(fdmgpu_handle* h) {
+  cudaStream_t s = h->stream;
+  const Pools& pl = h->pl;
+  const Prob* probs = h->d_probs.p;
+  const int np = h->dims.nprob;
+  cudaMemsetAsync(pl.dmax, 0, 3 * np * sizeof(unsigned long long), s);
+  launch_residual(probs, pl, h->dims, s);
+  launch_forward<float>(h->sp, pl.env32, pl.Y32, probs, h->tb, np, pl.active, s);
+  launch_backward<float>(h->sp, pl.env32, pl.Y32, probs, h->tb, np, pl.active, s);
+  launch_update_x(probs, pl, h->dims, 0, s);
+}
+
+fdmgpu_status capture(fdmgpu_handle* h, void (*rec)(fdmgpu_handle*), cudaGraphExec_t* out) {
+  if (*out) {
+    cudaGraphExecDestroy(*out);
+    *out = nullptr;
+  }
+  cudaGraph_t graph;
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  rec(h);
+  CK(cudaStreamEndCapture(h->stream, &graph));
+  cudaError_t e = cudaGraphInstantiate(out, graph, 0);
+  cudaGraphDestroy(graph);
+  CK(e);
+  return FDMGPU_OK;
+}
+
+fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info) {
+  Batch& b = h->batch;
+  const int np = (int)b.probs.size();
+  if (np == 0) return fail(FDMGPU_ERR_ARG, "empty batch");
+  uint64_t sig = mix(0, (uint64_t)np);
+  for (auto& hp : b.probs) sig = mix(sig, hp.sig);
+  fdmgpu_status st;
+  cudaGetLastError();  // clear a stale error of an earlier call on this thread
+  const bool replan = sig != h->plan_sig || b.precision != h->plan_prec || !h->g_asm;
+  if (replan) {
+    st = allocate_and_upload_plan(h);
+    if (st) return st;
+  }
+  st = upload_inputs(h);
+  if (st) return st;
+  // the graphs hold device pointers: capture again whenever one moved
+  uint64_t ps = 0;
+  const void* ptrs[] = {h->d_probs.p, h->d_ipool.p, h->d_dpool.p, h->d_env64.p, h->d_env32.p, h->d_B64.p,
+                        h->d_X64.p,   h->d_Y32.p,   h->d_rs.p,    h->d_cs.p,    h->d_rowptr.p, h->d_col.p,
+                        h->d_val.p,   h->d_err.p,   h->d_active.p, h->d_red.p,  h->d_J0.p,   h->d_strip.p};
+  for (const void* q : ptrs) ps = mix(ps, (uint64_t)(uintptr_t)q);
+  if (replan || ps != h->ptr_sig) {
+    h->ptr_sig = ps;
+    st = capture(h, record_asm, &h->g_asm);
+    if (st) return st;
+    st = capture(h, record_factor, &h->g_fac);
+    if (st) return st;
+    st = capture(h, record_solve, &h->g_sol);
+    if (st) return st;
+    if (b.precision == FDMGPU_PREC_MIXED) {
+      st = capture(h, record_iter, &h->g_iter);
+      if (st) return st;
+    }
+    h->plan_sig = sig;
+    h->plan_prec = b.precision;
+  }
+  CK(cudaEventRecord(h->ev[0], h->stream));
+  CK(cudaGraphLaunch(h->g_asm, h->stream));
+  CK(cudaEventRecord(h->ev[1], h->stream));
+  CK(cudaGraphLaunch(h->g_fac, h->stream));
+  CK(cudaEventRecord(h->ev[2], h->stream));
+  CK(cudaGraphLaunch(h->g_sol, h->stream));
+  CK(cudaEventRecord(h->ev[3], h->stream));
+  b.iters.assign(np, 0);
+  b.resid.assign(np, 0.0);
+  b.err.assign(np, 0);
+  float ms_refine = 0;
+  if (b.precision == FDMGPU_PREC_MIXED) {
+    const int max_iter = 10;
+    const double tol = 1e-12;
+    std::vector<int> active(np, 1);
+    std::vector<unsigned long long> red(3 * np);
+    CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaEventRecord(h->ev[4], h->stream));
+    for (int it = 1; it <= max_iter; ++it) {
+      CK(cudaGraphLaunch(h->g_iter, h->stream));
+      CK(cudaMemcpyAsync(red.data(), h->d_red.p, 3 * np * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                         h->stream));
+      CK(cudaStreamSynchronize(h->stream));
+      int nact = 0;
+      for (int k = 0; k < np; ++k) {
+        if (!active[k]) continue;
+        double dm, xm, rm;
+        memcpy(&dm, &red[k], 8);
+        memcpy(&xm, &red[np + k], 8);
+        memcpy(&rm, &red[2 * np + k], 8);
+        b.iters[k] = it;
+        b.resid[k] = xm > 0 ? dm / xm : dm;
+        if (!(b.resid[k] <= tol)) {
+          if (!std::isfinite(b.resid[k])) active[k] = 0; else ++nact;
+        } else {
+          active[k] = 0;
+        }
+      }
+      if (nact == 0) break;
+      CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    }
+    CK(cudaEventRecord(h->ev[5], h->stream));
+    for (int k = 0; k < np; ++k)
+      if (!(b.resid[k] <= 1e-9)) b.err[k] = FDMGPU_ERR_NOT_CONVERGED;
+  }
+  if (b.probs[0].P.nlm_abs > 0) launch_taull(h->d_probs.p, h->pl, h->dims, h->pl.X64, h->stream);
+  std::vector<int> err(np);
+  CK(cudaMemcpyAsync(err.data(), h->d_err.p, np * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaGetLastError());
+  for (int k = 0; k < np; ++k)
+    if (err[k]) b.err[k] = err[k];
+  b.ran = true;
+  if (info) {
+    memset(info, 0, sizeof(*info));
+    for (auto& hp : b.probs) {
+      info->nnz_profile += hp.nnz_profile;
+      info->flops_factor += hp.flops_factor;
+      info->flops_solve += hp.flops_solve;
+    }
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, h->ev[0], h->ev[1]));
+    info->ms_assemble = t;
+    CK(cudaEventElapsedTime(&t, h->ev[1], h->ev[2]));
+    info->ms_factor = t;
+    CK(cudaEventElapsedTime(&t, h->ev[2], h->ev[3]));
+    info->ms_solve = t;
+    if (b.precision == FDMGPU_PREC_MIXED) {
+      CK(cudaEventElapsedTime(&ms_refine, h->ev[4], h->ev[5]));
+      info->ms_refine = ms_refine;
+      int mi = 0;
+      double mr = 0;
+      for (int k = 0; k < np; ++k) {
+        mi = std::max(mi, b.iters[k]);
+        mr = std::max(mr, b.resid[k]);
+      }
+      info->refine_iters = mi;
+      info->residual = mr;
+    }
+  }
+  for (int k = 0; k < np; ++k)
+    if (b.err[k]) {
+      char buf[160];
+      snprintf(buf, sizeof buf, "problem %d failed with status %d (zero pivot or no convergence)", k, b.err[k]);
+      g_last_error = buf;
+      return (fdmgpu_status)b.err[k];
+    }
+  return FDMGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fdmgpu_version(void) { return "fdmgpu 0.1 (sm_103a)"; }
+
+const char* fdmgpu_last_error(void) { return g_last_error.c_str(); }
+
+void fdmgpu_get_solver_params(int32_t* mpi_host_num_for_mumps, char solver[6]) {
+  if (mpi_host_num_for_mumps) *mpi_host_num_for_mumps = 1;
+  if (solver) memcpy(solver, "GPU  ", 6);
+}
+
+fdmgpu_status fdmgpu_create(const fdmgpu_grid* g, fdmgpu_handle** out) {
+  if (!g || !out) return fail(FDMGPU_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (g->nspino != 1 || g->ngrph < 1) return fail(FDMGPU_ERR_UNSUPPORTED, "nspino = 1 only in this build");
+  if (g->npoint <= 0 || g->npsom < g->npoint || g->nvois <= 0 || g->natome < 0)
+    return fail(FDMGPU_ERR_ARG, "inconsistent grid sizes");
+  fdmgpu_handle* h = new fdmgpu_handle();
+  h->g = *g;
+  CK(cudaGetDevice(&h->device));
+  CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  for (auto& e : h->ev) CK(cudaEventCreate(&e));
+  // derived neighbour descriptors of the interstitial points
+  const int nv = g->nvois;
+  std::vector<std::unordered_map<int, int>> atom_ib(g->natome + 1);
+  for (int ia = 1; ia <= g->natome; ++ia)
+    for (int ib = g->nbordf[ia - 1] + 1; ib <= g->nbord[ia - 1]; ++ib)
+      atom_ib[ia][F2(g->ibord, g->nbtm, ib, ia)] = ib;
+  std::unordered_map<int, int> outer_ib;
+  for (int ib = g->nsortf + 1; ib <= g->nsort; ++ib) outer_ib[g->isrt[ib - 1]] = ib;
+  for (int i = 1; i <= g->npoint; ++i) {
+    if (g->numia[i - 1] != 0) continue;
+    h->inter_pt_h.push_back(i);
+    int nint = 0, hout = 0;
+    std::vector<int> atoms;
+    for (int iv = 1; iv <= nv; ++iv) {
+      const int j = F2(g->ivois, g->npsom, i, iv);
+      if (j < 1 || j > g->npsom) {
+        fdmgpu_destroy(h);
+        return fail(FDMGPU_ERR_ARG, "neighbour table points outside the grid");
+      }
+      const int ia = g->numia[j - 1];
+      const double charac = g->Kar[std::abs(F2(g->isvois, g->npsom, i, iv)) - 1];
+      double cf = -g->clapl[iv];
+      cf = charac * cf;
+      cf = cf * g->rvol[i - 1];
+      int kind = 0, idx = j;
+      if (ia == 0) {
+        ++nint;
+      } else if (ia > 0) {
+        auto it = atom_ib[ia].find(j);
+        if (it == atom_ib[ia].end()) {
+          fdmgpu_destroy(h);
+          return fail(FDMGPU_ERR_ARG, "atom neighbour missing from the interior boundary list");
+        }
+        idx = it->second;
+        const int isym = std::abs(F2(g->isbord, g->nbtm, idx, ia));
+        if (isym != 1) cf = g->Kar[isym - 1] * cf;
+        kind = ia;
+        if (std::find(atoms.begin(), atoms.end(), ia) == atoms.end()) atoms.push_back(ia);
+      } else if (ia == -2) {
+        auto it = outer_ib.find(j);
+        if (it == outer_ib.end()) {
+          fdmgpu_destroy(h);
+          return fail(FDMGPU_ERR_ARG, "outer neighbour missing from isrt");
+        }
+        idx = it->second;
+        kind = -2;
+        hout = 1;
+      } else {
+        fdmgpu_destroy(h);
+        return fail(FDMGPU_ERR_ARG, "unexpected numia value");
+      }
+      h->nb_kind_h.push_back(kind);
+      h->nb_idx_h.push_back(idx);
+      h->nb_coef_h.push_back(cf);
+    }
+    h->n_inter_h.push_back(nint);
+    h->has_outer_h.push_back(hout);
+    h->nb_atoms_h.push_back(atoms);
+  }
+  h->nbordf_h.assign(g->nbordf, g->nbordf + g->natome);
+  cudaStream_t s = h->stream;
+  auto up_i = [&](DevBuf<int>& b, const int32_t* p, size_t n) {
+    return upload(b, std::vector<int>(p, p + n), s);
+  };
+  auto up_d = [&](DevBuf<double>& b, const double* p, size_t n) {
+    return upload(b, std::vector<double>(p, p + n), s);
+  };
+  cudaError_t e = cudaSuccess;
+  e = e ? e : upload(h->d_inter_pt, h->inter_pt_h, s);
+  e = e ? e : upload(h->d_nb_kind, h->nb_kind_h, s);
+  e = e ? e : upload(h->d_nb_idx, h->nb_idx_h, s);
+  e = e ? e : upload(h->d_nb_coef, h->nb_coef_h, s);
+  e = e ? e : up_i(h->d_numia, g->numia, g->npsom);
+  e = e ? e : up_i(h->d_nbord, g->nbord, g->natome);
+  e = e ? e : up_i(h->d_nbordf, g->nbordf, g->natome);
+  e = e ? e : up_i(h->d_ibord, g->ibord, (size_t)g->nbtm * g->natome);
+  e = e ? e : up_i(h->d_isbord, g->isbord, (size_t)g->nbtm * g->natome);
+  e = e ? e : up_i(h->d_isrt, g->isrt, g->nstm);
+  e = e ? e : up_i(h->d_lato, g->lato, (size_t)g->nlmsam * g->natome);
+  e = e ? e : up_i(h->d_mato, g->mato, (size_t)g->nlmsam * g->natome);
+  e = e ? e : up_i(h->d_lso, g->lso, g->nso1);
+  e = e ? e : up_i(h->d_mso, g->mso, g->nso1);
+  e = e ? e : up_d(h->d_rvol, g->rvol, g->nim);
+  e = e ? e : up_d(h->d_clapl, g->clapl, g->nvois + 1);
+  e = e ? e : up_d(h->d_poidsa, g->poidsa, (size_t)g->nbm * g->natome);
+  e = e ? e : up_d(h->d_poidso, g->poidso, g->nsm);
+  e = e ? e : up_d(h->d_Kar, g->Kar, 64);
+  e = e ? e : up_d(h->d_Ylmato, g->Ylmato, (size_t)g->nbtm * g->nlmmax * g->natome);
+  std::vector<double> ysot((size_t)g->nsort * g->nlmomax);
+  for (int ib = 0; ib < g->nsort; ++ib)
+    for (int lm = 0; lm < g->nlmomax; ++lm) ysot[(size_t)ib * g->nlmomax + lm] = g->Ylmso[ib + (int64_t)g->nsort * lm];
+  e = e ? e : upload(h->d_YsoT, ysot, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    fdmgpu_destroy(h);
+    return fail(FDMGPU_ERR_CUDA, std::string("static upload: ") + cudaGetErrorString(e));
+  }
+  StaticDev& S = h->S;
+  S.npoint = g->npoint;
+  S.npsom = g->npsom;
+  S.nvois = g->nvois;
+  S.natome = g->natome;
+  S.nbtm = g->nbtm;
+  S.nbm = g->nbm;
+  S.nsort = g->nsort;
+  S.nsortf = g->nsortf;
+  S.nlmmax = g->nlmmax;
+  S.nlmomax = g->nlmomax;
+  S.nlmsam = g->nlmsam;
+  S.nso1 = g->nso1;
+  S.npr = (int)h->inter_pt_h.size();
+  S.inter_pt = h->d_inter_pt.p;
+  S.nb_kind = h->d_nb_kind.p;
+  S.nb_idx = h->d_nb_idx.p;
+  S.nb_coef = h->d_nb_coef.p;
+  S.rvol = h->d_rvol.p;
+  S.clapl = h->d_clapl.p;
+  S.numia = h->d_numia.p;
+  S.nbord = h->d_nbord.p;
+  S.nbordf = h->d_nbordf.p;
+  S.ibord = h->d_ibord.p;
+  S.isrt = h->d_isrt.p;
+  S.poidsa = h->d_poidsa.p;
+  S.poidso = h->d_poidso.p;
+  S.Kar = h->d_Kar.p;
+  S.isbord = h->d_isbord.p;
+  S.YsoT = h->d_YsoT.p;
+  S.Ylmato = h->d_Ylmato.p;
+  S.lato = h->d_lato.p;
+  S.mato = h->d_mato.p;
+  S.lso = h->d_lso.p;
+  S.mso = h->d_mso.p;
+  setup_factor_kernels<float>();
+  setup_factor_kernels<double>();
+  *out = h;
+  return FDMGPU_OK;
+}
+
+void fdmgpu_destroy(fdmgpu_handle* h) {
+  if (!h) return;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->g_asm) cudaGraphExecDestroy(h->g_asm);
+  if (h->g_fac) cudaGraphExecDestroy(h->g_fac);
+  if (h->g_sol) cudaGraphExecDestroy(h->g_sol);
+  if (h->g_iter) cudaGraphExecDestroy(h->g_iter);
+  DevBuf<int>* ib[] = {&h->d_inter_pt, &h->d_nb_kind, &h->d_nb_idx, &h->d_numia, &h->d_nbord, &h->d_nbordf,
+                       &h->d_ibord,    &h->d_isbord,  &h->d_isrt,   &h->d_lato,  &h->d_mato,  &h->d_lso,
+                       &h->d_mso,      &h->d_J0,      &h->d_J1,     &h->d_Imax,  &h->d_Imin,  &h->d_ipool,
+                       &h->d_rowptr,   &h->d_col,     &h->d_err,    &h->d_active};
+  for (auto* b : ib) b->release();
+  DevBuf<double>* db[] = {&h->d_nb_coef, &h->d_rvol, &h->d_clapl, &h->d_poidsa, &h->d_poidso, &h->d_Kar,
+                          &h->d_YsoT,    &h->d_Ylmato, &h->d_dpool, &h->d_env64, &h->d_B64,  &h->d_X64,
+                          &h->d_rs,      &h->d_cs,   &h->d_val,   &h->d_taull,  &h->d_tscratch, &h->d_smr};
+  for (auto* b : db) b->release();
+  h->d_env32.release();
+  h->d_Y32.release();
+  h->d_strip.release();
+  h->d_probs.release();
+  h->d_red.release();
+  if (h->h_pinned_i) cudaFreeHost(h->h_pinned_i);
+  if (h->h_pinned_d) cudaFreeHost(h->h_pinned_d);
+  for (auto& e : h->ev)
+    if (e) cudaEventDestroy(e);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+}
+
+fdmgpu_status fdmgpu_batch_begin(fdmgpu_handle* h, int32_t precision, int32_t max_energies) {
+  if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
+  if (precision != FDMGPU_PREC_FP64 && precision != FDMGPU_PREC_MIXED)
+    return fail(FDMGPU_ERR_ARG, "unknown precision");
+  h->batch.probs.clear();
+  h->batch.precision = precision;
+  h->batch.max_energies = max_energies;
+  h->batch.ran = false;
+  h->batch.probs.reserve(std::max(0, (int)max_energies));
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_batch_add(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t iaabs) {
+  if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
+  fdmgpu_status st = check_energy(h, e);
+  if (st) return st;
+  if (h->batch.max_energies > 0 && (int)h->batch.probs.size() >= h->batch.max_energies)
+    return fail(FDMGPU_ERR_ARG, "batch is full");
+  HostProb hp;
+  st = plan_problem(h, e, hp);
+  if (st) return st;
+  if (iaabs >= 1 && iaabs <= h->g.natome) {
+    hp.P.iaabs = iaabs;
+    hp.P.nlm_abs = e->nlmsa[iaabs - 1];
+    hp.P.ianew_abs = e->ianew[iaabs - 1];
+    for (int lm = 1; lm <= hp.P.nlm_abs; ++lm) {
+      const int L = F2(h->g.lato, h->g.nlmsam, lm, iaabs), m = F2(h->g.mato, h->g.nlmsam, lm, iaabs);
+      if (L * L + L + 1 + m != lm) return fail(FDMGPU_ERR_UNSUPPORTED, "Taull needs the C1 harmonic order");
+    }
+  }
+  pack_inputs(h, e, hp);
+  h->batch.probs.push_back(std::move(hp));
+  h->batch.ran = false;
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_batch_run(fdmgpu_handle* h, fdmgpu_info* info) {
+  if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
+  return run_batch(h, info);
+}
+
+fdmgpu_status fdmgpu_batch_taull(fdmgpu_handle* h, int32_t k, double* taull, int32_t* nlm) {
+  if (!h || !h->batch.ran || k < 0 || k >= (int)h->batch.probs.size())
+    return fail(FDMGPU_ERR_ARG, "no such batch result");
+  const Prob& P = h->batch.probs[k].P;
+  if (nlm) *nlm = P.nlm_abs;
+  if (!taull) return FDMGPU_OK;
+  CK(cudaMemcpy(taull, h->d_taull.p + 2 * P.taull, sizeof(double) * 2 * P.nlm_abs * P.nlm_abs,
+                cudaMemcpyDeviceToHost));
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_batch_solution(fdmgpu_handle* h, int32_t k, double* smr) {
+  if (!h || !h->batch.ran || k < 0 || k >= (int)h->batch.probs.size())
+    return fail(FDMGPU_ERR_ARG, "no such batch result");
+  const Prob& P = h->batch.probs[k].P;
+  const size_t n = (size_t)P.n * P.nlmso;
+  if (h->d_smr.reserve(n) != cudaSuccess) return fail(FDMGPU_ERR_NOMEM, "solution buffer");
+  launch_solution_out(P, h->d_X64.p, h->d_smr.p, h->stream);
+  CK(cudaMemcpyAsync(smr, h->d_smr.p, n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_batch_stats(fdmgpu_handle* h, int32_t k, int32_t* iters, double* residual) {
+  if (!h || !h->batch.ran || k < 0 || k >= (int)h->batch.probs.size())
+    return fail(FDMGPU_ERR_ARG, "no such batch result");
+  if (iters) *iters = h->batch.iters[k];
+  if (residual) *residual = h->batch.resid[k];
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_mat_solve(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t precision, double* smr, double* smi,
+                               fdmgpu_info* info) {
+  (void)smi;
+  if (!h || !smr) return fail(FDMGPU_ERR_ARG, "null argument");
+  fdmgpu_status st = fdmgpu_batch_begin(h, precision, 1);
+  if (st) return st;
+  st = fdmgpu_batch_add(h, e, 0);
+  if (st) return st;
+  st = fdmgpu_batch_run(h, info);
+  if (st) return st;
+  return fdmgpu_batch_solution(h, 0, smr);
+}
+
+}  // extern "C"

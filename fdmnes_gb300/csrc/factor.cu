@@ -1,0 +1,246 @@
+// factor.cu - batched tile LU of the FDM band and the triangular solves.
+//
+// One launch handles one panel step K for every problem of a batch
+// (blockIdx.y = problem).  The elimination is the reference's no-pivot
+// Gaussian elimination (source/mat_solve_gaussian.f90:196-317) carried out in
+// reversed order as a right-looking LU on TS x TS tiles:
+//   k_panel     factor tile (K,K); L tiles (I,K) <- A(I,K) U(K,K)^-1;
+//               U tiles (K,J) and RHS tiles (K,R) <- L(K,K)^-1 A(K,.)
+//               (the RHS columns ride along, so the forward substitution of the
+//               reference's elimination loop, :231-262, is fused here);
+//   k_trailing  A(I,J) -= L(I,K) U(K,J) and Y(I,R) -= L(I,K) Y(K,R).
+// The backward substitution (the reference's resolution loop, :348-358) is
+// k_bwd_diag + k_bwd_update; k_fwd_* are used by the refinement solves.
+#include "fdm_internal.cuh"
+#include "fdm_kernels.h"
+
+namespace fdm {
+
+// Factor the diagonal tile (K,K) in place (one CTA per problem).
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_diag(T* env, const Prob* probs, Tables tb, int K, const int* active,
+                                                   int* err, double piv_thr) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (K >= P.nt || (active && !active[e])) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* D = reinterpret_cast<T*>(smem_raw);
+  __shared__ double mp;
+  T* dtile = tile_ptr(env, P, tb, K, K);
+  load_tile(D, dtile);
+  __syncthreads();
+  tile_lu(D, &mp);
+  __syncthreads();
+  store_tile(dtile, D);
+  // smallest |pivot| of the tile (padding rows carry 1); NaN also trips the test
+  if (threadIdx.x == 0 && !(mp >= piv_thr)) atomicExch(&err[e], (int)FDMGPU_ERR_ZERO_PIVOT);
+}
+
+// Panel of step K with the factored diagonal tile: L tiles (I,K), U tiles
+// (K,J) and, when fused, the RHS tiles (K,R).
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_panel(T* env, T* rhs, const Prob* probs, Tables tb, int K,
+                                                    int fuse_rhs, const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (K >= P.nt || (active && !active[e])) return;
+  const int nI = tb.Imax[P.trow + K] - K;
+  const int nJ = tb.J1[P.trow + K] - K;
+  const int nR = fuse_rhs ? P.nrt : 0;
+  const int w = blockIdx.x;
+  if (w >= nI + nJ + nR) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* D = reinterpret_cast<T*>(smem_raw);
+  T* W = D + TS * SP;
+  load_tile(D, tile_ptr(env, P, tb, K, K));
+  T* g;
+  if (w < nI) {
+    g = tile_ptr(env, P, tb, K + 1 + w, K);
+    load_tile(W, g);
+    __syncthreads();
+    tile_right_upper_solve(W, D);
+  } else if (w < nI + nJ) {
+    g = tile_ptr(env, P, tb, K, K + 1 + (w - nI));
+    load_tile(W, g);
+    __syncthreads();
+    tile_left_lower_unit_solve(W, D);
+  } else {
+    g = rhs_ptr(rhs, P, K, w - nI - nJ);
+    load_tile(W, g);
+    __syncthreads();
+    tile_left_lower_unit_solve(W, D);
+  }
+  __syncthreads();
+  store_tile(g, W);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_trailing(T* env, T* rhs, const Prob* probs, Tables tb, int K,
+                                                       int fuse_rhs, const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (K >= P.nt || (active && !active[e])) return;
+  const int nI = tb.Imax[P.trow + K] - K;
+  const int nJ = tb.J1[P.trow + K] - K;
+  const int nC = nJ + (fuse_rhs ? P.nrt : 0);
+  const int w = blockIdx.x;
+  if (w >= nI * nC) return;
+  const int I = K + 1 + w / nC;
+  const int c = w % nC;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* As = reinterpret_cast<T*>(smem_raw);
+  T* Bs = As + TS * SP;
+  const T* A = tile_ptr(env, P, tb, I, K);
+  const T* B;
+  T* C;
+  if (c < nJ) {
+    B = tile_ptr(env, P, tb, K, K + 1 + c);
+    C = tile_ptr(env, P, tb, I, K + 1 + c);
+  } else {
+    B = rhs_ptr(rhs, P, K, c - nJ);
+    C = rhs_ptr(rhs, P, I, c - nJ);
+  }
+  tile_gemm_sub(C, A, B, As, Bs);
+}
+
+// Forward substitution, unit lower L: Y(K,R) <- L(K,K)^-1 Y(K,R).
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_fwd_diag(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
+                                                       const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (K >= P.nt || (active && !active[e])) return;
+  const int R = blockIdx.x;
+  if (R >= P.nrt) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* D = reinterpret_cast<T*>(smem_raw);
+  T* W = D + TS * SP;
+  load_tile(D, tile_ptr(const_cast<T*>(env), P, tb, K, K));
+  T* g = rhs_ptr(rhs, P, K, R);
+  load_tile(W, g);
+  __syncthreads();
+  tile_left_lower_unit_solve(W, D);
+  __syncthreads();
+  store_tile(g, W);
+}
+
+// Y(I,R) -= L(I,K) Y(K,R) for I in (K, Imax(K)].
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_fwd_update(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
+                                                         const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (K >= P.nt || (active && !active[e])) return;
+  const int nI = tb.Imax[P.trow + K] - K;
+  const int w = blockIdx.x;
+  if (w >= nI * P.nrt) return;
+  const int I = K + 1 + w / P.nrt, R = w % P.nrt;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* As = reinterpret_cast<T*>(smem_raw);
+  T* Bs = As + TS * SP;
+  tile_gemm_sub(rhs_ptr(rhs, P, I, R), tile_ptr(const_cast<T*>(env), P, tb, I, K), rhs_ptr(rhs, P, K, R), As, Bs);
+}
+
+// Backward substitution, upper U: Y(K,R) <- U(K,K)^-1 Y(K,R).
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_bwd_diag(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
+                                                       const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (K >= P.nt || (active && !active[e])) return;
+  const int R = blockIdx.x;
+  if (R >= P.nrt) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* D = reinterpret_cast<T*>(smem_raw);
+  T* W = D + TS * SP;
+  load_tile(D, tile_ptr(const_cast<T*>(env), P, tb, K, K));
+  T* g = rhs_ptr(rhs, P, K, R);
+  load_tile(W, g);
+  __syncthreads();
+  tile_left_upper_solve(W, D);
+  __syncthreads();
+  store_tile(g, W);
+}
+
+// Y(I,R) -= U(I,K) Y(K,R) for I in [Imin(K), K).
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_bwd_update(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
+                                                         const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (K >= P.nt || (active && !active[e])) return;
+  const int i0 = tb.Imin[P.trow + K];
+  const int nI = K - i0;
+  const int w = blockIdx.x;
+  if (w >= nI * P.nrt) return;
+  const int I = i0 + w / P.nrt, R = w % P.nrt;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* As = reinterpret_cast<T*>(smem_raw);
+  T* Bs = As + TS * SP;
+  tile_gemm_sub(rhs_ptr(rhs, P, I, R), tile_ptr(const_cast<T*>(env), P, tb, I, K), rhs_ptr(rhs, P, K, R), As, Bs);
+}
+
+template <typename T>
+static size_t smem_bytes() { return 2 * TS * SP * sizeof(T); }
+
+template <typename T>
+void setup_factor_kernels() {
+  const int bytes = (int)smem_bytes<T>();
+  cudaFuncSetAttribute(k_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_trailing<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_fwd_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_fwd_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_bwd_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_bwd_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+template <typename T>
+void launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
+                   const int* active, int* err, double piv_thr, cudaStream_t s) {
+  const size_t sm = smem_bytes<T>();
+  for (int K = 0; K < sp.ntmax; ++K) {
+    k_diag<T><<<dim3(1, nprob), NTHREADS, sm, s>>>(env, probs, tb, K, active, err, piv_thr);
+    const int np = fuse_rhs ? sp.panel_rhs[K] : sp.panel[K];
+    if (np > 0) k_panel<T><<<dim3(np, nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
+    const int nt = fuse_rhs ? sp.trail_rhs[K] : sp.trail[K];
+    if (nt > 0) k_trailing<T><<<dim3(nt, nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
+  }
+}
+
+template <typename T>
+void launch_forward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
+                    const int* active, cudaStream_t s) {
+  const size_t sm = smem_bytes<T>();
+  for (int K = 0; K < sp.ntmax; ++K) {
+    k_fwd_diag<T><<<dim3(sp.nrtmax, nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+    if (sp.fwd[K] > 0) k_fwd_update<T><<<dim3(sp.fwd[K], nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+  }
+}
+
+template <typename T>
+void launch_backward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
+                     const int* active, cudaStream_t s) {
+  const size_t sm = smem_bytes<T>();
+  for (int K = sp.ntmax - 1; K >= 0; --K) {
+    k_bwd_diag<T><<<dim3(sp.nrtmax, nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+    if (sp.bwd[K] > 0) k_bwd_update<T><<<dim3(sp.bwd[K], nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+  }
+}
+
+template void setup_factor_kernels<float>();
+template void setup_factor_kernels<double>();
+template void launch_factor<float>(const StepPlan&, float*, float*, const Prob*, Tables, int, int, const int*, int*,
+                                   double, cudaStream_t);
+template void launch_factor<double>(const StepPlan&, double*, double*, const Prob*, Tables, int, int, const int*, int*,
+                                    double, cudaStream_t);
+template void launch_forward<float>(const StepPlan&, const float*, float*, const Prob*, Tables, int, const int*,
+                                    cudaStream_t);
+template void launch_forward<double>(const StepPlan&, const double*, double*, const Prob*, Tables, int, const int*,
+                                     cudaStream_t);
+template void launch_backward<float>(const StepPlan&, const float*, float*, const Prob*, Tables, int, const int*,
+                                     cudaStream_t);
+template void launch_backward<double>(const StepPlan&, const double*, double*, const Prob*, Tables, int, const int*,
+                                      cudaStream_t);
+
+}  // namespace fdm

@@ -1,0 +1,228 @@
+// fdm_internal.cuh - shared declarations of the GB300 FDM solver.
+//
+// Storage model.  One FDM system of order n (one energy, one spin block) is
+// held in REVERSED order: row p = n - ii and column q = n - jj, where ii/jj are
+// the reference's 1-based rows and columns.  The reference eliminates rows
+// bottom-up (UL, source/mat_solve_gaussian.f90:196-317); in reversed order the
+// same elimination is a top-down LU without pivoting, so the profile of the
+// reference (lb1 made monotone by newind, source/mat.f90:1874-1876) becomes a
+// variable band whose right edge lu(p) = n - lb1(ii) never decreases.
+//
+// The band is stored as dense TS x TS tiles (row-major inside a tile).  Row
+// block I keeps the contiguous run of tiles J0(I)..J1(I) that covers every
+// row's columns [n - lb2, n - lb1]; J0 is replaced by its suffix minimum so
+// that the rows touched by panel K form one range (K, Imax(K)].  Right-hand
+// sides are TS x TS tiles too: tile (I, R) holds rows I*TS.. and RHS columns
+// R*TS.. of one system.  Rows n..npad-1 are identity padding.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/fdmgpu.h"
+
+namespace fdm {
+
+constexpr int TS = 64;            // tile edge
+constexpr int TS2 = TS * TS;
+constexpr int NTHREADS = 256;     // threads of every tile kernel
+
+// Per-problem descriptor (device and host copy).
+struct Prob {
+  int n;          // order (nligne)
+  int nt;         // tiles per edge (ceil(n / TS))
+  int nlmso;      // right-hand sides
+  int nrt;        // RHS tiles (ceil(nlmso / TS))
+  int nligneso;   // rows before the outer-sphere rows
+  int lmaxso;
+  int nlmagm;
+  int ispin;      // 1-based spin block (selects the Vr column)
+  int iaabs;      // 1-based absorbing atom (Taull)
+  int nlm_abs;    // harmonics of the absorber
+  int ianew_abs;  // row offset of the absorber harmonics (1-based rows ianew+1..)
+  int trow;       // offset into J0 / J1 / strip arrays (per tile row)
+  double enervide;
+  int64_t env;    // element offset of the band tiles
+  int64_t rhs;    // element offset of the RHS tiles (nt * nrt * TS2)
+  int64_t rowv;   // offset into per-row vectors (npad entries): scales, csr row_ptr
+  int64_t csr;    // offset into CSR columns/values
+  int64_t csr_cap;    // CSR capacity of this problem (structural nonzeros of calcMatRow)
+  int64_t in_new;     // offset of new_(0:npoint) in the int pool
+  int64_t in_ianew;   // offset of ianew(natome)
+  int64_t in_nlmsa;   // offset of nlmsa(natome)
+  int64_t in_vr;      // offset of Vr(npoint) (the selected spin) in the double pool
+  int64_t in_phi;     // offset of phiato(nphiato1, nlmagm, natome) (spin-selected)
+  int64_t in_bes;     // offset of Bessel j(ib, L) in the double pool, [nsort][lmaxso+1]
+  int64_t in_neu;     // offset of Neumann n(ib, L), [nsort][lmaxso+1]
+  int64_t taull;      // offset of Taull (complex) for this problem
+  int64_t scratch;    // offset of the complex nlmso x (nlmso + nlm_abs) Taull scratch
+};
+
+// Per tile-row / tile-column tables of a problem, at Prob::trow.
+struct Tables {
+  const int* J0;      // first stored tile of row block I (suffix-min hull)
+  const int* J1;      // last stored tile of row block I
+  const int64_t* strip;  // tile offset of row block I's strip
+  const int* Imax;    // last row block with a stored tile in column K
+  const int* Imin;    // first row block whose strip reaches column K
+};
+
+template <typename T>
+__device__ __forceinline__ T* tile_ptr(T* env, const Prob& P, const Tables& tb, int I, int J) {
+  return env + P.env + (tb.strip[P.trow + I] + (J - tb.J0[P.trow + I])) * (int64_t)TS2;
+}
+template <typename T>
+__device__ __forceinline__ T* rhs_ptr(T* rhs, const Prob& P, int I, int R) {
+  return rhs + P.rhs + ((int64_t)I * P.nrt + R) * (int64_t)TS2;
+}
+
+// Static structure on the device (energy independent).
+struct StaticDev {
+  int npoint, npsom, nvois, natome, nbtm, nbm, nsort, nsortf, nlmmax, nlmomax, nlmsam, nso1;
+  int npr;                 // interstitial points
+  const int* inter_pt;     // (npr) interstitial point indices, 1-based
+  const int* nb_kind;      // (npr, nvois): 0 interstitial, ia>0 atom, -2 outer
+  const int* nb_idx;       // (npr, nvois): neighbour point j (1-based) or boundary index ib (1-based)
+  const double* nb_coef;   // (npr, nvois): (Kar * -clapl(iv)) * rvol(i) [* Kar(isbord)]
+  const double* rvol;      // (npoint)
+  const double* clapl;     // (0:nvois)
+  const int* numia;
+  const int* nbord;
+  const int* nbordf;
+  const int* ibord;        // (nbtm, natome)
+  const int* isrt;         // (nsort)
+  const double* poidsa;    // (nbm, natome)
+  const double* poidso;    // (nsortf)
+  const double* Kar;       // (64)
+  const int* isbord;       // (nbtm, natome)
+  const double* YsoT;      // (nsort, nlmomax) row-major: YsoT[ib * nlmomax + lm]
+  const double* Ylmato;    // (nbtm, nlmmax, natome) Fortran
+  const int* lato;         // (nlmsam, natome) for igrph = 1
+  const int* mato;
+  const int* lso;          // (nso1)
+  const int* mso;
+};
+
+// -------------------------------------------------------------------------
+// Tile routines (256 threads, TS = 64).  Shared tiles are row-major with a
+// padded stride.
+// -------------------------------------------------------------------------
+constexpr int SP = TS + 4;  // shared stride (keeps 16-byte alignment for float4/double2)
+
+template <typename T>
+__device__ __forceinline__ void load_tile(T* __restrict__ s, const T* __restrict__ g) {
+  for (int idx = threadIdx.x; idx < TS2; idx += NTHREADS) {
+    const int r = idx / TS, c = idx % TS;
+    s[r * SP + c] = g[idx];
+  }
+}
+template <typename T>
+__device__ __forceinline__ void store_tile(T* __restrict__ g, const T* __restrict__ s) {
+  for (int idx = threadIdx.x; idx < TS2; idx += NTHREADS) {
+    const int r = idx / TS, c = idx % TS;
+    g[idx] = s[r * SP + c];
+  }
+}
+
+// In-place LU without pivoting of the shared tile D (Doolittle: unit L below,
+// U on and above the diagonal).  Records the smallest |pivot| in *minpiv
+// (thread 0 only).
+template <typename T>
+__device__ void tile_lu(T* D, double* minpiv) {
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  double mp = 1e300;
+  for (int k = 0; k < TS; ++k) {
+    const T piv = D[k * SP + k];
+    if (threadIdx.x == 0) mp = fmin(mp, fabs((double)piv));
+    if (threadIdx.x > k && threadIdx.x < TS) D[threadIdx.x * SP + k] = D[threadIdx.x * SP + k] / piv;
+    __syncthreads();
+    for (int i = k + 1 + ty; i < TS; i += 16) {
+      const T l = D[i * SP + k];
+      for (int j = k + 1 + tx; j < TS; j += 16) D[i * SP + j] -= l * D[k * SP + j];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *minpiv = mp;
+}
+
+// W <- W * inv(U), U = upper triangle (with diagonal) of D.
+template <typename T>
+__device__ void tile_right_upper_solve(T* W, const T* D) {
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  for (int k = 0; k < TS; ++k) {
+    if (threadIdx.x < TS) W[threadIdx.x * SP + k] = W[threadIdx.x * SP + k] / D[k * SP + k];
+    __syncthreads();
+    for (int i = ty; i < TS; i += 16) {
+      const T x = W[i * SP + k];
+      for (int j = k + 1 + tx; j < TS; j += 16) W[i * SP + j] -= x * D[k * SP + j];
+    }
+    __syncthreads();
+  }
+}
+
+// W <- inv(L) * W, L = unit lower triangle of D.
+template <typename T>
+__device__ void tile_left_lower_unit_solve(T* W, const T* D) {
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  for (int k = 0; k < TS - 1; ++k) {
+    for (int i = k + 1 + ty; i < TS; i += 16) {
+      const T l = D[i * SP + k];
+      for (int j = tx; j < TS; j += 16) W[i * SP + j] -= l * W[k * SP + j];
+    }
+    __syncthreads();
+  }
+}
+
+// W <- inv(U) * W, U = upper triangle (with diagonal) of D.
+template <typename T>
+__device__ void tile_left_upper_solve(T* W, const T* D) {
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  for (int k = TS - 1; k >= 0; --k) {
+    if (threadIdx.x < TS) W[k * SP + threadIdx.x] = W[k * SP + threadIdx.x] / D[k * SP + k];
+    __syncthreads();
+    for (int i = ty; i < k; i += 16) {
+      const T u = D[i * SP + k];
+      for (int j = tx; j < TS; j += 16) W[i * SP + j] -= u * W[k * SP + j];
+    }
+    __syncthreads();
+  }
+}
+
+// C(global, row-major TS x TS) -= A(global) * B(global), all TS x TS tiles.
+// Shared use: As (TS x SP, A transposed) + Bs (TS x SP).
+template <typename T>
+__device__ void tile_gemm_sub(T* __restrict__ C, const T* __restrict__ A, const T* __restrict__ B, T* As, T* Bs) {
+  // stage A transposed: As[k * SP + r] = A[r * TS + k]
+  for (int idx = threadIdx.x; idx < TS2; idx += NTHREADS) {
+    const int r = idx / TS, k = idx % TS;
+    As[k * SP + r] = A[idx];
+    Bs[r * SP + k] = B[idx];
+  }
+  __syncthreads();
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+#pragma unroll 4
+  for (int k = 0; k < TS; ++k) {
+    T a[4], b[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = As[k * SP + ty * 4 + i];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) b[j] = Bs[k * SP + tx * 4 + j];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] += a[i] * b[j];
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    T* crow = C + (ty * 4 + i) * TS + tx * 4;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) crow[j] -= acc[i][j];
+  }
+}
+
+}  // namespace fdm

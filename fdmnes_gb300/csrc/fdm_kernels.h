@@ -1,0 +1,75 @@
+// fdm_kernels.h - host-side launch interface shared by the CUDA translation units.
+#pragma once
+
+#include <vector>
+#include <cuda_runtime.h>
+
+#include "fdm_internal.cuh"
+
+namespace fdm {
+
+// Largest number of work items per step over the problems of a batch.
+struct StepPlan {
+  int ntmax = 0;
+  int nrtmax = 0;
+  std::vector<int> panel, panel_rhs;   // L + U tiles (+ RHS tiles) of step K
+  std::vector<int> trail, trail_rhs;   // trailing tiles (+ RHS tiles) of step K
+  std::vector<int> fwd, bwd;           // forward / backward update tiles of step K
+};
+
+template <typename T> void setup_factor_kernels();
+template <typename T>
+void launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
+                   const int* active, int* err, double piv_thr, cudaStream_t s);
+template <typename T>
+void launch_forward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
+                    const int* active, cudaStream_t s);
+template <typename T>
+void launch_backward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
+                     const int* active, cudaStream_t s);
+
+// Device pools of one batch (pointers into device memory).
+struct Pools {
+  const int* ipool = nullptr;      // per-problem integer inputs
+  const double* dpool = nullptr;   // per-problem double inputs
+  double* env64 = nullptr;         // FP64 band tiles
+  float* env32 = nullptr;          // FP32 band tiles (mixed precision)
+  double* B64 = nullptr;           // FP64 right-hand sides (tiles)
+  double* X64 = nullptr;           // FP64 solution (tiles)
+  float* Y32 = nullptr;            // FP32 work right-hand sides (tiles)
+  double* rs = nullptr;            // row scales (per row, stride npad + 1)
+  double* cs = nullptr;            // column scales
+  int* rowptr = nullptr;           // CSR row pointers (stride npad + 1)
+  int* col = nullptr;              // CSR columns
+  double* val = nullptr;           // CSR values
+  double* taull = nullptr;         // complex Taull (interleaved)
+  double* tscratch = nullptr;      // complex Taull scratch
+  unsigned long long* dmax = nullptr;  // per problem max |correction| (double bits)
+  unsigned long long* xmax = nullptr;  // per problem max |x| (double bits)
+  unsigned long long* amax = nullptr;  // per problem scratch
+  int* err = nullptr;
+  int* active = nullptr;
+};
+
+struct LaunchDims {
+  int nprob = 0;
+  int max_rows = 0;        // max npad
+  int max_tiles = 0;       // max band tiles of one problem
+  int max_rhs_tiles = 0;   // max nt * nrt
+  int max_nlmso = 0;
+  int max_atom_rows = 0;   // natome * max nlmsa
+  int npr = 0;
+};
+
+void launch_assemble(const StaticDev& S, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
+                     cudaStream_t s);
+void launch_equilibrate_convert(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s);
+void launch_csr(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s);
+// X64 = cs * Y32 (first solve) or X64 += cs * Y32 (refinement), with max reductions.
+void launch_update_x(const Prob* probs, const Pools& pl, const LaunchDims& d, int first, cudaStream_t s);
+// Y32 = rs * (B64 - A X64) using the CSR copy of A.
+void launch_residual(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s);
+void launch_taull(const Prob* probs, const Pools& pl, const LaunchDims& d, const double* X, cudaStream_t s);
+void launch_solution_out(const Prob& P, const double* X, double* smr_dev, cudaStream_t s);
+
+}  // namespace fdm

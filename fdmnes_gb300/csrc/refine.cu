@@ -1,0 +1,288 @@
+// refine.cu - mixed precision support: equilibration, FP64 -> FP32 band
+// conversion, FP64 residual in CSR form and the refinement update.
+//
+// The FP32 factor is of the equilibrated matrix Dr A Dc, with Dr and Dc powers
+// of two (exact in FP64), so only the conversion to FP32 rounds.  The residual
+// b - A x is taken in FP64 from the assembled matrix (CSR copy of the nonzeros
+// of the FP64 band) and the correction is solved with the FP32 factors:
+//   x <- x + Dc * solve32(Dr * (b - A x)).
+#include <cfloat>
+#include "fdm_internal.cuh"
+#include "fdm_kernels.h"
+
+namespace fdm {
+
+__device__ __forceinline__ double pow2_inv_scale(double m) {
+  if (!(m > 0.0) || !isfinite(m)) return 1.0;
+  int ex;
+  frexp(m, &ex);           // m = f * 2^ex, f in [0.5, 1)
+  return ldexp(1.0, -ex);  // m * scale in [0.5, 1)
+}
+
+__device__ __forceinline__ void atomic_max_abs(unsigned long long* a, double v) {
+  atomicMax(a, (unsigned long long)__double_as_longlong(fabs(v)));
+}
+
+// Locate the row block of band tile w of a problem (strip has nt+1 entries).
+__device__ __forceinline__ int tile_row_of(const Tables& tb, const Prob& P, int64_t w) {
+  int lo = 0, hi = P.nt - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) / 2;
+    if (tb.strip[P.trow + mid] <= w) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Row scales: warp per row.
+__global__ void k_rowscale(const Prob* probs, const double* env, double* rs, Tables tb) {
+  const Prob P = probs[blockIdx.y];
+  const int p = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x % 32;
+  const int npad = P.nt * TS;
+  if (p >= npad) return;
+  const int I = p / TS;
+  const int j0 = tb.J0[P.trow + I], j1 = tb.J1[P.trow + I];
+  double m = 0.0;
+  for (int J = j0; J <= j1; ++J) {
+    const double* t = tile_ptr(const_cast<double*>(env), P, tb, I, J) + (p % TS) * TS;
+    m = fmax(m, fmax(fabs(t[lane]), fabs(t[lane + 32])));
+  }
+  for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) rs[P.rowv + p] = pow2_inv_scale(m);
+}
+
+// Column maxima of |rs(p) a(p,q)|: block per band tile, into colmax (double bits).
+__global__ void k_colmax(const Prob* probs, const double* env, const double* rs, unsigned long long* colmax,
+                         Tables tb) {
+  const Prob P = probs[blockIdx.y];
+  const int64_t w = blockIdx.x;
+  const int64_t ntiles = tb.strip[P.trow + P.nt];
+  if (w >= ntiles) return;
+  const int I = tile_row_of(tb, P, w);
+  const int J = tb.J0[P.trow + I] + (int)(w - tb.strip[P.trow + I]);
+  const double* t = env + P.env + w * TS2;
+  __shared__ double cm[4][TS];
+  const int c = threadIdx.x % TS, r0 = threadIdx.x / TS;
+  double m = 0.0;
+  for (int r = r0; r < TS; r += 4) m = fmax(m, fabs(rs[P.rowv + I * TS + r] * t[r * TS + c]));
+  cm[r0][c] = m;
+  __syncthreads();
+  if (threadIdx.x < TS) {
+    m = fmax(fmax(cm[0][c], cm[1][c]), fmax(cm[2][c], cm[3][c]));
+    atomic_max_abs(&colmax[P.rowv + J * TS + c], m);
+  }
+}
+
+__global__ void k_colscale_finish(const Prob* probs, double* cs) {
+  const Prob P = probs[blockIdx.y];
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= P.nt * TS) return;
+  unsigned long long* bits = reinterpret_cast<unsigned long long*>(cs);
+  const double m = __longlong_as_double((long long)bits[P.rowv + q]);
+  cs[P.rowv + q] = pow2_inv_scale(m);
+}
+
+// E32 = float(rs * cs * E64), tile by tile.
+__global__ void k_convert(const Prob* probs, const double* env64, float* env32, const double* rs, const double* cs,
+                          Tables tb) {
+  const Prob P = probs[blockIdx.y];
+  const int64_t w = blockIdx.x;
+  const int64_t ntiles = tb.strip[P.trow + P.nt];
+  if (w >= ntiles) return;
+  const int I = tile_row_of(tb, P, w);
+  const int J = tb.J0[P.trow + I] + (int)(w - tb.strip[P.trow + I]);
+  const double* t = env64 + P.env + w * TS2;
+  float* o = env32 + P.env + w * TS2;
+  for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) {
+    const int r = idx / TS, c = idx % TS;
+    o[idx] = (float)(rs[P.rowv + I * TS + r] * cs[P.rowv + J * TS + c] * t[idx]);
+  }
+}
+
+// Y32 = float(rs * B64) for every RHS tile.
+__global__ void k_rhs_scale(const Prob* probs, const double* B, float* Y, const double* rs) {
+  const Prob P = probs[blockIdx.y];
+  const int64_t w = blockIdx.x;
+  if (w >= (int64_t)P.nt * P.nrt) return;
+  const int I = (int)(w / P.nrt);
+  const double* b = B + P.rhs + w * TS2;
+  float* y = Y + P.rhs + w * TS2;
+  for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) y[idx] = (float)(rs[P.rowv + I * TS + idx / TS] * b[idx]);
+}
+
+// CSR of the nonzeros of the FP64 band: count per row (warp per row).
+__global__ void k_csr_count(const Prob* probs, const double* env, int* rowptr, Tables tb) {
+  const Prob P = probs[blockIdx.y];
+  const int p = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (p >= P.nt * TS) return;
+  const int I = p / TS;
+  int cnt = 0;
+  for (int J = tb.J0[P.trow + I]; J <= tb.J1[P.trow + I]; ++J) {
+    const double* t = tile_ptr(const_cast<double*>(env), P, tb, I, J) + (p % TS) * TS;
+    cnt += __popc(__ballot_sync(0xffffffffu, t[lane] != 0.0)) + __popc(__ballot_sync(0xffffffffu, t[lane + 32] != 0.0));
+  }
+  if (lane == 0) rowptr[P.rowv + p + 1] = cnt;
+}
+
+// Exclusive scan of the row counts of one problem (one block per problem).
+__global__ void k_csr_scan(const Prob* probs, int* rowptr) {
+  const Prob P = probs[blockIdx.y];
+  const int npad = P.nt * TS;
+  int* rp = rowptr + P.rowv;
+  __shared__ int part[1024];
+  const int per = (npad + blockDim.x - 1) / blockDim.x;
+  const int a = threadIdx.x * per, b = min(npad, a + per);
+  int s = 0;
+  for (int p = a; p < b; ++p) s += rp[p + 1];
+  part[threadIdx.x] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int acc = 0;
+    for (int k = 0; k < (int)blockDim.x; ++k) { const int v = part[k]; part[k] = acc; acc += v; }
+  }
+  __syncthreads();
+  int acc = part[threadIdx.x];
+  for (int p = a; p < b; ++p) { acc += rp[p + 1]; rp[p + 1] = acc; }
+  if (threadIdx.x == 0) rp[0] = 0;
+}
+
+__global__ void k_csr_fill(const Prob* probs, const double* env, const int* rowptr, int* col, double* val, Tables tb,
+                           int* err) {
+  const Prob P = probs[blockIdx.y];
+  const int p = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (p >= P.nt * TS) return;
+  const int I = p / TS;
+  int pos = rowptr[P.rowv + p];
+  const unsigned lower = (1u << lane) - 1u;
+  for (int J = tb.J0[P.trow + I]; J <= tb.J1[P.trow + I]; ++J) {
+    const double* t = tile_ptr(const_cast<double*>(env), P, tb, I, J) + (p % TS) * TS;
+    for (int h = 0; h < 2; ++h) {
+      const double v = t[lane + 32 * h];
+      const unsigned bal = __ballot_sync(0xffffffffu, v != 0.0);
+      if (v != 0.0) {
+        const int o = pos + __popc(bal & lower);
+        if (o < P.csr_cap) {
+          col[P.csr + o] = J * TS + lane + 32 * h;
+          val[P.csr + o] = v;
+        } else {
+          atomicExch(&err[blockIdx.y], (int)FDMGPU_ERR_ARG);
+        }
+      }
+      pos += __popc(bal);
+    }
+  }
+}
+
+// Y32 = float(rs * (B64 - A X64)), warp per row, lanes over RHS columns.
+__global__ void k_residual(const Prob* probs, const int* rowptr, const int* col, const double* val, const double* B,
+                           const double* X, float* Y, const double* rs, unsigned long long* rmax, const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (active && !active[e]) return;
+  const int p = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (p >= P.nt * TS) return;
+  const int k0 = rowptr[P.rowv + p], k1 = min(rowptr[P.rowv + p + 1], (int)P.csr_cap);
+  const int nrhs = P.nrt * TS;
+  const double sc = rs[P.rowv + p];
+  double rm = 0.0;
+  for (int r0 = 0; r0 < nrhs; r0 += 256) {
+    double acc[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int r = r0 + lane + 32 * t;
+      acc[t] = (r < nrhs) ? B[P.rhs + ((int64_t)(p / TS) * P.nrt + r / TS) * TS2 + (p % TS) * TS + (r % TS)] : 0.0;
+    }
+    for (int k = k0; k < k1; ++k) {
+      const int q = col[P.csr + k];
+      const double a = val[P.csr + k];
+      const double* xr = X + P.rhs + ((int64_t)(q / TS) * P.nrt) * TS2 + (q % TS) * TS;
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int r = r0 + lane + 32 * t;
+        if (r < nrhs) acc[t] -= a * xr[(int64_t)(r / TS) * TS2 + (r % TS)];
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int r = r0 + lane + 32 * t;
+      if (r < nrhs) {
+        rm = fmax(rm, fabs(acc[t]));
+        Y[P.rhs + ((int64_t)(p / TS) * P.nrt + r / TS) * TS2 + (p % TS) * TS + (r % TS)] = (float)(sc * acc[t]);
+      }
+    }
+  }
+  for (int o = 16; o; o >>= 1) rm = fmax(rm, __shfl_xor_sync(0xffffffffu, rm, o));
+  if (lane == 0) atomic_max_abs(&rmax[e], rm);
+}
+
+// X64 (+)= cs * Y32 over RHS tiles, with per-problem maxima of |d| and |x|.
+__global__ void k_update_x(const Prob* probs, const float* Y, double* X, const double* cs, int first,
+                           unsigned long long* dmax, unsigned long long* xmax, const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (active && !active[e]) return;
+  const int64_t w = blockIdx.x;
+  if (w >= (int64_t)P.nt * P.nrt) return;
+  const int I = (int)(w / P.nrt);
+  const float* y = Y + P.rhs + w * TS2;
+  double* x = X + P.rhs + w * TS2;
+  double dm = 0.0, xm = 0.0;
+  for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) {
+    const double d = cs[P.rowv + I * TS + idx / TS] * (double)y[idx];
+    const double xn = first ? d : x[idx] + d;
+    x[idx] = xn;
+    dm = fmax(dm, fabs(d));
+    xm = fmax(xm, fabs(xn));
+  }
+  for (int o = 16; o; o >>= 1) {
+    dm = fmax(dm, __shfl_xor_sync(0xffffffffu, dm, o));
+    xm = fmax(xm, __shfl_xor_sync(0xffffffffu, xm, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomic_max_abs(&dmax[e], dm);
+    atomic_max_abs(&xmax[e], xm);
+  }
+}
+
+// smr(Lm, ii) = X(n - ii, Lm) (Fortran layout, nlmso x nligne).
+__global__ void k_solution_out(Prob P, const double* X, double* smr) {
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)P.n * P.nlmso) return;
+  const int lm = (int)(t % P.nlmso);
+  const int ii = (int)(t / P.nlmso) + 1;
+  const int p = P.n - ii;
+  smr[t] = X[P.rhs + ((int64_t)(p / TS) * P.nrt + lm / TS) * TS2 + (p % TS) * TS + (lm % TS)];
+}
+
+void launch_equilibrate_convert(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s) {
+  const int np = d.nprob;
+  k_rowscale<<<dim3((d.max_rows + 7) / 8, np), 256, 0, s>>>(probs, pl.env64, pl.rs, tb);
+  k_colmax<<<dim3(d.max_tiles, np), 256, 0, s>>>(probs, pl.env64, pl.rs, reinterpret_cast<unsigned long long*>(pl.cs),
+                                                 tb);
+  k_colscale_finish<<<dim3((d.max_rows + 255) / 256, np), 256, 0, s>>>(probs, pl.cs);
+  k_convert<<<dim3(d.max_tiles, np), 256, 0, s>>>(probs, pl.env64, pl.env32, pl.rs, pl.cs, tb);
+  k_rhs_scale<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, pl.B64, pl.Y32, pl.rs);
+}
+
+void launch_csr(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s) {
+  const int np = d.nprob;
+  k_csr_count<<<dim3((d.max_rows + 7) / 8, np), 256, 0, s>>>(probs, pl.env64, pl.rowptr, tb);
+  k_csr_scan<<<dim3(1, np), 1024, 0, s>>>(probs, pl.rowptr);
+  k_csr_fill<<<dim3((d.max_rows + 7) / 8, np), 256, 0, s>>>(probs, pl.env64, pl.rowptr, pl.col, pl.val, tb, pl.err);
+}
+
+void launch_residual(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s) {
+  k_residual<<<dim3((d.max_rows + 7) / 8, d.nprob), 256, 0, s>>>(probs, pl.rowptr, pl.col, pl.val, pl.B64, pl.X64,
+                                                                 pl.Y32, pl.rs, pl.amax, pl.active);
+}
+
+void launch_update_x(const Prob* probs, const Pools& pl, const LaunchDims& d, int first, cudaStream_t s) {
+  k_update_x<<<dim3(d.max_rhs_tiles, d.nprob), 256, 0, s>>>(probs, pl.Y32, pl.X64, pl.cs, first, pl.dmax, pl.xmax,
+                                                            first ? nullptr : pl.active);
+}
+
+void launch_solution_out(const Prob& P, const double* X, double* smr_dev, cudaStream_t s) {
+  const int64_t n = (int64_t)P.n * P.nlmso;
+  k_solution_out<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, X, smr_dev);
+}
+
+}  // namespace fdm

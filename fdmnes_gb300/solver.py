@@ -1,0 +1,153 @@
+"""Host-side interface to libfdmgpu.so, mirroring the reference's mat_solve path.
+
+``FdmSolver(structure)`` uploads the energy-independent arguments once
+(``fdmgpu_create``).  ``mat_solve`` is the drop-in for the reference's
+``mat_solve`` (source/mat_solve_gaussian.f90:5): it returns ``smr`` with the
+reference's shape (nlmso, nligne), column-major.  ``spectrum`` is the batched
+path of ``mat`` (source/mat.f90:5-733): all energies in one launch sequence,
+returning the absorber's Taull per energy.
+
+There is no CPU fallback: if the CUDA library is missing or no GPU is visible
+the constructor raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import List, Sequence, Tuple
+
+import numpy as np
+
+from . import abi
+from . import cluster as CL
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libfdmgpu.so")
+
+PREC = {"fp64": 0, "mixed": 1}
+STATUS = {0: "OK", 1: "ERR_ARG", 2: "ERR_UNSUPPORTED", 3: "ERR_CUDA", 4: "ERR_ZERO_PIVOT",
+          5: "ERR_NOT_CONVERGED", 6: "ERR_NOMEM"}
+
+_lib = None
+
+
+class FdmError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def load_library(path: str = LIB_PATH):
+    """Load libfdmgpu.so and declare the C-ABI of include/fdmgpu.h."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"{path} is missing: build it with fdmnes_gb300.build.build()")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.fdmgpu_version.restype = C.c_char_p
+    L.fdmgpu_last_error.restype = C.c_char_p
+    L.fdmgpu_create.argtypes = [vp, C.POINTER(vp)]
+    L.fdmgpu_create.restype = C.c_int
+    L.fdmgpu_destroy.argtypes = [vp]
+    L.fdmgpu_destroy.restype = None
+    L.fdmgpu_mat_solve.argtypes = [vp, vp, C.c_int32, vp, vp, vp]
+    L.fdmgpu_mat_solve.restype = C.c_int
+    L.fdmgpu_get_solver_params.argtypes = [C.POINTER(C.c_int32), C.c_char_p]
+    L.fdmgpu_get_solver_params.restype = None
+    L.fdmgpu_batch_begin.argtypes = [vp, C.c_int32, C.c_int32]
+    L.fdmgpu_batch_add.argtypes = [vp, vp, C.c_int32]
+    L.fdmgpu_batch_run.argtypes = [vp, vp]
+    L.fdmgpu_batch_taull.argtypes = [vp, C.c_int32, vp, C.POINTER(C.c_int32)]
+    L.fdmgpu_batch_solution.argtypes = [vp, C.c_int32, vp]
+    L.fdmgpu_batch_stats.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
+    for f in ("fdmgpu_batch_begin", "fdmgpu_batch_add", "fdmgpu_batch_run", "fdmgpu_batch_taull",
+              "fdmgpu_batch_solution", "fdmgpu_batch_stats"):
+        getattr(L, f).restype = C.c_int
+    _lib = L
+    return L
+
+
+def _check(st: int):
+    if st != 0:
+        raise FdmError(st, load_library().fdmgpu_last_error().decode())
+
+
+def info_dict(info: abi.FdmInfo) -> dict:
+    return {k: getattr(info, k) for k, _ in abi.FdmInfo._fields_}
+
+
+class FdmSolver:
+    """One device handle holding the static structure of a cluster."""
+
+    def __init__(self, st: CL.Structure):
+        self.lib = load_library()
+        self.st = st
+        self.grid_args = abi.GridArgs(st)
+        h = C.c_void_p()
+        _check(self.lib.fdmgpu_create(C.addressof(self.grid_args.s), C.byref(h)))
+        self.h = h
+        self._batch_args: List[abi.EnergyArgs] = []
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fdmgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def mat_solve(self, ei: CL.EnergyInputs, ri: CL.RowIndex, precision: str = "fp64") -> Tuple[np.ndarray, dict]:
+        ea = abi.EnergyArgs(self.st, ei, ri)
+        smr = np.zeros((ei.nlmso, ri.nligne), order="F")
+        info = abi.FdmInfo()
+        _check(self.lib.fdmgpu_mat_solve(self.h, C.addressof(ea.s), PREC[precision], smr.ctypes.data, None,
+                                         C.addressof(info)))
+        return smr, info_dict(info)
+
+    def spectrum_begin(self, precision: str, n: int):
+        _check(self.lib.fdmgpu_batch_begin(self.h, PREC[precision], n))
+        self._batch_args = []
+
+    def spectrum_add(self, ei: CL.EnergyInputs, ri: CL.RowIndex, iaabs: int = 1):
+        ea = abi.EnergyArgs(self.st, ei, ri)
+        _check(self.lib.fdmgpu_batch_add(self.h, C.addressof(ea.s), iaabs))
+        self._batch_args.append(ea)
+
+    def spectrum_add_args(self, ea: abi.EnergyArgs, iaabs: int = 1):
+        _check(self.lib.fdmgpu_batch_add(self.h, C.addressof(ea.s), iaabs))
+
+    def spectrum_run(self) -> dict:
+        info = abi.FdmInfo()
+        _check(self.lib.fdmgpu_batch_run(self.h, C.addressof(info)))
+        return info_dict(info)
+
+    def taull(self, k: int) -> np.ndarray:
+        nl = C.c_int32(0)
+        _check(self.lib.fdmgpu_batch_taull(self.h, k, None, C.byref(nl)))
+        out = np.zeros(2 * nl.value * nl.value)
+        _check(self.lib.fdmgpu_batch_taull(self.h, k, out.ctypes.data, C.byref(nl)))
+        return out.view(np.complex128).reshape((nl.value, nl.value), order="F").copy()
+
+    def solution(self, k: int, nlmso: int, nligne: int) -> np.ndarray:
+        smr = np.zeros((nlmso, nligne), order="F")
+        _check(self.lib.fdmgpu_batch_solution(self.h, k, smr.ctypes.data))
+        return smr
+
+    def stats(self, k: int) -> Tuple[int, float]:
+        it = C.c_int32(0)
+        r = C.c_double(0)
+        _check(self.lib.fdmgpu_batch_stats(self.h, k, C.byref(it), C.byref(r)))
+        return it.value, r.value
+
+    def spectrum(self, items: Sequence[Tuple[CL.EnergyInputs, CL.RowIndex]], precision: str = "mixed",
+                 iaabs: int = 1):
+        self.spectrum_begin(precision, len(items))
+        for ei, ri in items:
+            self.spectrum_add(ei, ri, iaabs)
+        info = self.spectrum_run()
+        return [self.taull(k) for k in range(len(items))], info

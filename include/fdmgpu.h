@@ -1,0 +1,194 @@
+/*
+ * fdmgpu.h - C-ABI of the GB300 FDM assembly + solve (drop-in for FDMNES mat_solve).
+ *
+ * The reference solves, for one photon energy, the finite-difference system
+ * assembled row by row by calcMatRow (source/mat.f90:1034-1727) with either the
+ * Gaussian profile solver (source/mat_solve_gaussian.f90:5-372) or MUMPS
+ * (source/mat_solve_mumps.f90:5-261).  Both backends share the 86-argument
+ * Fortran interface `mat_solve` (source/mat_solve_gaussian.f90:5-12,
+ * source/mat_solve_mumps.f90:5-12) called from `mat` (source/mat.f90:186-194).
+ *
+ * This header restates that argument list as two plain structs:
+ *   fdmgpu_grid    - energy-independent arguments (grid, stencil, boundary
+ *                    tables, harmonics, representation tables); uploaded once
+ *                    per handle;
+ *   fdmgpu_energy  - arguments that change from one call to the next (row
+ *                    numbering from newind, potential, atomic boundary
+ *                    functions, outer Bessel/Neumann, energy, flags).
+ * Every array keeps the reference's Fortran layout: column-major, and index
+ * VALUES are 1-based exactly as the Fortran caller holds them.  No pointer is
+ * retained after a call returns.
+ *
+ * All entry points return an fdmgpu_status code; none of them aborts the
+ * process (the reference `stop`s on a zero pivot, source/mat_solve_gaussian.f90:265-302).
+ * Handles are not thread-safe: use one handle per host thread.
+ */
+#ifndef FDMGPU_H
+#define FDMGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+typedef enum {
+  FDMGPU_OK = 0,
+  FDMGPU_ERR_ARG = 1,          /* invalid argument / inconsistent sizes          */
+  FDMGPU_ERR_UNSUPPORTED = 2,  /* flag combination not provided by this build     */
+  FDMGPU_ERR_CUDA = 3,         /* CUDA runtime error (message via fdmgpu_last_error) */
+  FDMGPU_ERR_ZERO_PIVOT = 4,   /* |pivot| below threshold: the reference stops here */
+  FDMGPU_ERR_NOT_CONVERGED = 5,/* mixed precision refinement did not converge      */
+  FDMGPU_ERR_NOMEM = 6         /* device allocation failed                         */
+} fdmgpu_status;
+
+/* Arithmetic of the factorisation. */
+typedef enum {
+  FDMGPU_PREC_FP64 = 0,        /* plain FP64 profile LU: the correctness path          */
+  FDMGPU_PREC_MIXED = 1        /* FP32 profile LU + FP64 residual and refinement       */
+} fdmgpu_precision;
+
+/* Energy-independent arguments of mat_solve (source/mat_solve_gaussian.f90:17-67). */
+typedef struct fdmgpu_grid {
+  int32_t npoint;     /* grid points inside the FDM sphere                                   */
+  int32_t npsom;      /* grid points including the outer shell (leading dim of ivois/numia)  */
+  int32_t nvois;      /* neighbours per point (12 for iord = 4, cubic)                       */
+  int32_t natome;     /* atoms of the calculation cluster                                    */
+  int32_t nbm;        /* leading dim of poidsa                                               */
+  int32_t nbtm;       /* leading dim of ibord, isbord, Ylmato                                */
+  int32_t nim;        /* size of rvol                                                        */
+  int32_t nsm;        /* size of poidso                                                      */
+  int32_t nsort;      /* outer-boundary points (rows of Ylmso, Bessel)                       */
+  int32_t nsortf;     /* the first nsortf of them are inside the sphere                      */
+  int32_t nstm;       /* size of isrt                                                        */
+  int32_t nspin;      /* second dim of Vr                                                    */
+  int32_t nlmmax;     /* second dim of Ylmato                                                */
+  int32_t nlmomax;    /* second dim of Ylmso                                                 */
+  int32_t nlmsam;     /* leading dim of lato/mato/iato                                       */
+  int32_t nso1;       /* leading dim of lso/mso/iso                                          */
+  int32_t ngrph;      /* number of representations (1 for C1)                                */
+  int32_t nspino;     /* 1, or 2 with spin-orbit                                             */
+  const int32_t* ivois;   /* (npsom, nvois) neighbour point, 1-based                        */
+  const int32_t* isvois;  /* (npsom, nvois) symmetry operation of the neighbour             */
+  const int32_t* numia;   /* (npsom) 0 interstitial, ia>0 inside atom ia, -2 outside        */
+  const int32_t* nbord;   /* (natome) boundary points of each atom                          */
+  const int32_t* nbordf;  /* (natome) the first nbordf of them are outside the atom         */
+  const int32_t* ibord;   /* (nbtm, natome) boundary point, 1-based                         */
+  const int32_t* isbord;  /* (nbtm, natome) symmetry operation                              */
+  const int32_t* isrt;    /* (nstm) outer-boundary point, 1-based                           */
+  const int32_t* lato;    /* (nlmsam, natome, ngrph) L of atom harmonics                    */
+  const int32_t* mato;    /* (nlmsam, natome, ngrph) m                                      */
+  const int32_t* iato;    /* (nlmsam, natome, ngrph) spin of the solution                   */
+  const int32_t* lso;     /* (nso1, ngrph) L of outer harmonics                             */
+  const int32_t* mso;     /* (nso1, ngrph) m                                                */
+  const int32_t* iso;     /* (nso1, ngrph) spin                                             */
+  const double* clapl;    /* (0:nvois) Laplacian coefficients                               */
+  const double* cgrad;    /* (nvois) gradient coefficients                                  */
+  const double* rvol;     /* (nim) relative point volumes                                   */
+  const double* poidsa;   /* (nbm, natome) atom boundary weights                            */
+  const double* poidso;   /* (nsm) outer boundary weights                                   */
+  const double* Ylmato;   /* (nbtm, nlmmax, natome) real harmonics at atom boundary points  */
+  const double* Ylmso;    /* (nsort, nlmomax) real harmonics at outer boundary points       */
+  const double* Kar;      /* (64, nspino) characters, real part                             */
+  const double* Kari;     /* (64, nspino) characters, imaginary part                        */
+} fdmgpu_grid;
+
+/* Per-call arguments of mat_solve. */
+typedef struct fdmgpu_energy {
+  int32_t nligne;     /* matrix order                                                        */
+  int32_t nligneso;   /* rows before the outer-sphere rows (nligne - nlmso when regular)     */
+  int32_t nlmso;      /* outer harmonics = number of right-hand sides                        */
+  int32_t lmaxso;     /* outer l cut-off (Bessel second dim is 0:lmaxso)                     */
+  int32_t nlmagm;     /* second dim of phiato                                                */
+  int32_t nphiato1;   /* leading dim of phiato                                               */
+  int32_t nphiato7;   /* last dim of phiato (2 when phiato is complex)                       */
+  int32_t nspinp;     /* spin dim of phiato                                                  */
+  int32_t n_RI;       /* regular (1) or regular+irregular (2)                                */
+  int32_t n_ato_RI;   /* atomic solutions per harmonic                                       */
+  int32_t nspinr;     /* spin dim of the Bessel arrays                                       */
+  int32_t nsort_r;    /* leading dim of Besselr/Neumanr (nsort for real energies, else 0)    */
+  int32_t nsort_c;    /* leading dim of complex Bessel/Neuman                                */
+  int32_t igrph;      /* representation (1-based)                                            */
+  int32_t ispin;      /* spin block (1-based)                                                */
+  int32_t nicm;       /* leading dim of gradvr                                               */
+  /* flags (logical in the reference) */
+  int32_t Cal_comp, E_comp, Basereel, Base_hexa, irregular, Relativiste, Spinorbite,
+          Repres_comp, Ylm_comp, Test_reg;
+  double Enervide;    /* energy relative to vacuum (Ry)                                      */
+  double Eimag;       /* imaginary part of the energy (Ry)                                   */
+  const int32_t* new_;    /* (0:npoint) row of each point, 1-based, 0 for atom points       */
+  const int32_t* newinv;  /* (nligne) point of each row, 0 outer, -ia atom                  */
+  const int32_t* lb1;     /* (nligne) first column of each row                              */
+  const int32_t* lb2;     /* (nligne) last column of each row                               */
+  const int32_t* ianew;   /* (natome) row before the first harmonic row of each atom        */
+  const int32_t* nlmsa;   /* (natome) harmonics per atom                                    */
+  const double* Vr;       /* (npoint, nspin) potential at the grid points (Ry)              */
+  const double* gradvr;   /* (nicm, 3, nspin) potential gradient (relativistic / SO)        */
+  const double* phiato;   /* (nphiato1, nlmagm, nspinp, nspino, n_RI, natome, nphiato7)     */
+  const double* Besselr;  /* (nsort_r, 0:lmaxso, nspinr) real j_l * sqrt(k/pi)              */
+  const double* Neumanr;  /* (nsort_r, 0:lmaxso, nspinr) real n_l * sqrt(k/pi)              */
+  const double* Bessel;   /* (2, nsort_c, 0:lmaxso, nspinr) complex, interleaved re/im      */
+  const double* Neuman;   /* (2, nsort_c, 0:lmaxso, nspinr)                                 */
+} fdmgpu_energy;
+
+typedef struct fdmgpu_handle fdmgpu_handle;
+
+/* Per-call diagnostics. */
+typedef struct fdmgpu_info {
+  int64_t nnz_profile;      /* stored entries of the profile factor                          */
+  double flops_factor;      /* algorithmic flops of the factorisation (profile count)        */
+  double flops_solve;       /* algorithmic flops of one forward+backward solve               */
+  int32_t refine_iters;     /* refinement iterations used (mixed precision)                  */
+  double residual;          /* final max_k ||b_k - A x_k|| / ||b_k||                          */
+  double ms_assemble, ms_factor, ms_solve, ms_refine;   /* device time per phase             */
+} fdmgpu_info;
+
+/* Library version string. */
+const char* fdmgpu_version(void);
+
+/* Message of the last error on this thread. */
+const char* fdmgpu_last_error(void);
+
+/* Create a handle on the current CUDA device and upload the energy-independent
+ * arguments (the grid, stencil, boundary and harmonic tables that mat_solve
+ * receives on every call, source/mat_solve_gaussian.f90:30-67). */
+fdmgpu_status fdmgpu_create(const fdmgpu_grid* grid, fdmgpu_handle** out);
+
+/* Release every device resource held by the handle. */
+void fdmgpu_destroy(fdmgpu_handle* h);
+
+/* Drop-in for mat_solve (source/mat_solve_gaussian.f90:5-372 and
+ * source/mat_solve_mumps.f90:5-261): assemble the FDM matrix and the right-hand
+ * sides of one energy on the GPU, factorise, solve, and write the solution into
+ * smr (nlmso, nligne) column-major (and smi when Cal_comp).  Synchronous.
+ * smr/smi are host pointers.  info may be NULL. */
+fdmgpu_status fdmgpu_mat_solve(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t precision,
+                               double* smr, double* smi, fdmgpu_info* info);
+
+/* Counterpart of getSolverParams (source/mat_solve_gaussian.f90:376-389,
+ * source/mat_solve_mumps.f90:705-736): solver name "GPU" and group size 1. */
+void fdmgpu_get_solver_params(int32_t* mpi_host_num_for_mumps, char solver[6]);
+
+/*
+ * Batched spectrum: every energy of a spectrum (and every spin block) solved
+ * in one captured launch sequence, with the Taull contraction of `mat`
+ * (source/mat.f90:306-405) and its symmetrisation (source/mat.f90:598-644) on
+ * the device.  The caller adds the per-energy arguments, runs, then reads the
+ * absorber scattering amplitude Taull(nlm, nlm) (complex, interleaved re/im,
+ * column-major, nlm = nlmsa(iaabs)) of each energy.
+ */
+fdmgpu_status fdmgpu_batch_begin(fdmgpu_handle* h, int32_t precision, int32_t max_energies);
+fdmgpu_status fdmgpu_batch_add(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t iaabs);
+fdmgpu_status fdmgpu_batch_run(fdmgpu_handle* h, fdmgpu_info* info);
+/* Taull of energy k (0-based, in add order): writes nlm*nlm complex values. */
+fdmgpu_status fdmgpu_batch_taull(fdmgpu_handle* h, int32_t k, double* taull, int32_t* nlm);
+/* Solution of energy k (nlmso, nligne) column-major into smr (host). */
+fdmgpu_status fdmgpu_batch_solution(fdmgpu_handle* h, int32_t k, double* smr);
+/* Per-energy refinement diagnostics of the last run: iterations and residual. */
+fdmgpu_status fdmgpu_batch_stats(fdmgpu_handle* h, int32_t k, int32_t* iters, double* residual);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FDMGPU_H */

@@ -1,0 +1,109 @@
+"""CPU oracle of the FDM assembly + Gaussian solve (test infrastructure only).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use this
+package.  It loads oracle/_build/liboracle.so, built by ``make -C oracle``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+_lib = None
+
+
+def build() -> str:
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        L.oracle_mat_solve.argtypes = [vp, vp, vp, C.POINTER(C.c_int64), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double), C.POINTER(C.c_int32)]
+        L.oracle_assemble_dense.argtypes = [vp, vp, vp, vp]
+        L.oracle_newind.argtypes = [vp, vp, vp, vp, C.c_int, C.c_int32, vp, vp, vp, vp, vp]
+        L.oracle_cbessneur.argtypes = [C.c_double, C.c_double, C.c_int, vp, vp]
+        L.oracle_invcomp.argtypes = [C.c_int, vp]
+        L.oracle_taull.argtypes = [vp, vp, C.c_int, vp, vp, C.POINTER(C.c_int32)]
+        _lib = L
+    return _lib
+
+
+def mat_solve(grid_args, energy_args):
+    """Solution smr (nlmso, nligne) Fortran-ordered, plus timing and nnz."""
+    n, m = energy_args.nligne, energy_args.nlmso
+    smr = np.zeros((m, n), order="F")
+    nnz = C.c_int64(0)
+    tf, tt = C.c_double(0), C.c_double(0)
+    bad = C.c_int32(0)
+    st = lib().oracle_mat_solve(C.addressof(grid_args.s), C.addressof(energy_args.s), smr.ctypes.data,
+                                C.byref(nnz), C.byref(tf), C.byref(tt), C.byref(bad))
+    if st != 0:
+        raise RuntimeError(f"oracle_mat_solve failed with status {st} (row {bad.value})")
+    return smr, dict(nnz=nnz.value, time_fill=tf.value, time_tria=tt.value)
+
+
+def assemble_dense(grid_args, energy_args):
+    n, m = energy_args.nligne, energy_args.nlmso
+    A = np.zeros((n, n), order="F")
+    B = np.zeros((m, n), order="F")
+    st = lib().oracle_assemble_dense(C.addressof(grid_args.s), C.addressof(energy_args.s), A.ctypes.data,
+                                     B.ctypes.data)
+    if st != 0:
+        raise RuntimeError(f"oracle_assemble_dense failed with status {st}")
+    return A, B
+
+
+def taull(grid_args, energy_args, smr, iaabs=1):
+    nl = C.c_int32(0)
+    out = np.zeros(2 * 64 * 64)
+    smr = np.asfortranarray(smr)
+    st = lib().oracle_taull(C.addressof(grid_args.s), C.addressof(energy_args.s), iaabs, smr.ctypes.data,
+                            out.ctypes.data, C.byref(nl))
+    if st != 0:
+        raise RuntimeError(f"oracle_taull failed with status {st}")
+    k = nl.value
+    t = out[:2 * k * k].view(np.complex128).reshape((k, k), order="F")
+    return t.copy()
+
+
+def newind(grid_args, xyz4, distai, nlmsa, nlmso, nligne, npoint, natome):
+    new = np.zeros(npoint + 1, dtype=np.int32)
+    newinv = np.zeros(nligne, dtype=np.int32)
+    ianew = np.zeros(natome, dtype=np.int32)
+    lb1 = np.zeros(nligne, dtype=np.int32)
+    lb2 = np.zeros(nligne, dtype=np.int32)
+    xyz4 = np.ascontiguousarray(xyz4, dtype=np.float64)
+    distai = np.ascontiguousarray(distai, dtype=np.float64)
+    nlmsa = np.ascontiguousarray(nlmsa, dtype=np.int32)
+    st = lib().oracle_newind(C.addressof(grid_args.s), xyz4.ctypes.data, distai.ctypes.data, nlmsa.ctypes.data,
+                             nlmso, nligne, new.ctypes.data, newinv.ctypes.data, ianew.ctypes.data,
+                             lb1.ctypes.data, lb2.ctypes.data)
+    if st != 0:
+        raise RuntimeError("oracle_newind failed")
+    return new, newinv, ianew, lb1, lb2
+
+
+def cbessneur(fnorm, z, lmax):
+    b = np.zeros(lmax + 1)
+    nm = np.zeros(lmax + 1)
+    lib().oracle_cbessneur(float(fnorm), float(z), int(lmax), b.ctypes.data, nm.ctypes.data)
+    return b, nm
+
+
+def invcomp(a):
+    a = np.asfortranarray(a, dtype=np.complex128).copy(order="F")
+    st = lib().oracle_invcomp(a.shape[0], a.ctypes.data)
+    if st != 0:
+        raise RuntimeError("oracle_invcomp: singular")
+    return a
