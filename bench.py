@@ -1,0 +1,301 @@
+#!/usr/bin/env python3
+"""Benchmark: FDM energy points per second on one GB300.
+
+Workload (the batched Cu configuration): fcc Cu, 13-atom cluster, FDM sphere
+3.0 A, grid step 0.25 A, no symmetry reduction, 401 energies from -5 to 35 eV
+in steps of 0.1 eV, all solved in one batched launch sequence (assembly,
+FP32 profile LU with tile-local pivoting, refinement of the FP64 solution,
+Taull contraction).  One "step" is one full spectrum.
+
+* value  - energies / s with the per-energy inputs already in HBM
+           (fdmgpu_batch_rerun), CUDA events on the solver's stream;
+* e2e    - energies / s through the C-ABI from host buffers: per step the
+           inputs are packed and copied host -> device and every Taull is
+           copied back (fdmgpu_batch_begin/add/run/taull);
+* plain_fp64 - the same spectrum through the plain FP64 profile solve
+           (the correctness path) for the mixed-vs-FP64 comparison;
+* cpu_baseline - the CPU restatement of the reference's Gaussian solver
+           (oracle/) timed on the host cores on a sample of energies, one
+           energy per core as the reference's MPI energy loop does.
+
+``--impl reference`` times only that CPU restatement (the reference itself is
+Fortran and no Fortran compiler exists on either machine).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+E_MIN, E_MAX, E_STEP = -5.0, 35.0, 0.1
+METRIC = "FDM energy-points/sec on 1 GB300, mixed+batched vs plain FP64, at <=1e-6 rel error"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc = None
+        self.path = os.path.join(HERE, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                c = [x.strip() for x in line.split(",")]
+                if len(c) < 9:
+                    continue
+                try:
+                    sm.append(float(c[1]))
+                    smax.append(float(c[2]))
+                except ValueError:
+                    continue
+                for name, v in zip(names, c[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------- CPU baseline
+_W = {}
+
+
+def _oracle_init():
+    sys.path.insert(0, HERE)
+    from fdmnes_gb300 import abi, cluster as CL
+    st = CL.cu_structure()
+    _W["st"], _W["ga"] = st, abi.GridArgs(st)
+
+
+def _oracle_worker(args):
+    """One energy of the CPU restatement: the reference's per-rank work (mat_solve + Taull)."""
+    energy, = args
+    from fdmnes_gb300 import abi, cluster as CL
+    import oracle
+    st, ga = _W["st"], _W["ga"]
+    ei = CL.energy_inputs(st, energy)
+    ri = CL.newind(st, ei.nlmsa, ei.nlmso)
+    ea = abi.EnergyArgs(st, ei, ri)
+    t0 = time.perf_counter()
+    X, _ = oracle.mat_solve(ga, ea)
+    oracle.taull(ga, ea, X)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(n_energies: int):
+    """Oracle restatement on the host cores, one energy per process (spawned)."""
+    import oracle
+    oracle.build()
+    cores = min(os.cpu_count() or 1, n_energies)
+    energies = np.linspace(E_MIN, E_MAX, n_energies)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_oracle_init) as pool:
+        per = pool.map(_oracle_worker, [(float(e),) for e in energies], chunksize=1)
+    # the energies run concurrently, one per core, as the reference's MPI ranks do
+    # (source/fdm.f90:3484-3497): a spectrum of n energies takes the slowest rank's time
+    wall = max(per)
+    return {"value": n_energies / wall, "unit": "energies/s", "cores": cores, "kind": "port",
+            "sample": f"{n_energies} Cu energies {E_MIN}..{E_MAX} eV, one per process; "
+                      f"single-energy solve {min(per):.2f}-{max(per):.2f} s",
+            "wall_s": wall}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    n = max(1, min(os.cpu_count() or 1, 16))
+    cfg = {"workload": "Cu fcc 13 atoms, R=3.0 A, h=0.25 A, C1, real, energies -5..35 eV", "sample_energies": n}
+    times = []
+    for step in range(args.warmup + args.steps):
+        cb = cpu_baseline(n)
+        if step >= args.warmup:
+            times.append(cb)
+    v = statistics.median([c["value"] for c in times])
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "energies/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * n / v, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
+            "cpu_baseline": {"value": v, "unit": "energies/s", "cores": times[0]["cores"], "kind": "port",
+                             "sample": times[0]["sample"]},
+            "e2e": {"value": v, "unit": "energies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+    from fdmnes_gb300 import build as B, cluster as CL, xanes
+    from fdmnes_gb300.solver import FdmSolver
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    B.build()
+
+    energies = CL.energy_grid(E_MIN, E_MAX, E_STEP)
+    n_e = len(energies)
+    st = CL.cu_structure()
+    items = xanes.spectrum_inputs(st, energies)
+    sv = FdmSolver(st)
+
+    def barrier_sync():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # plain FP64 reference spectrum (correctness path), once
+    t0 = time.perf_counter()
+    T64, info64 = sv.spectrum(items, "fp64")
+    fp64_wall = time.perf_counter() - t0
+    info64 = sv.spectrum_rerun()  # device-resident timing of the FP64 path
+    fp64_ms = info64["ms_assemble"] + info64["ms_factor"] + info64["ms_solve"]
+
+    # mixed precision spectrum: warm-up (plans, graphs), then timed reruns
+    sv.spectrum_begin("mixed", n_e)
+    for ei, ri in items:
+        sv.spectrum_add(ei, ri)
+    info = sv.spectrum_run()
+    Tm = [sv.taull(k) for k in range(n_e)]
+    err_conv = xanes.convolved_relative_error(energies, Tm, T64)
+    err_taull = max(float(np.abs(a - b).max() / np.abs(b).max()) for a, b in zip(Tm, T64))
+    for _ in range(args.warmup):
+        sv.spectrum_rerun()
+
+    clk = ClockSampler()
+    clk.start()
+    barrier_sync()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    infos = []
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        infos.append(sv.spectrum_rerun())
+    barrier_sync()
+    wall = time.perf_counter() - t_wall
+    # device time of the spectrum: sum of the phases timed by CUDA events on the solver's stream
+    dev_ms = [i["ms_assemble"] + i["ms_factor"] + i["ms_solve"] + i["ms_refine"] for i in infos]
+    ms_step = max_over_ranks(statistics.mean(dev_ms))
+    value = world * n_e / (ms_step / 1000.0)
+
+    # end to end through the C-ABI from host buffers
+    h2d = d2h = 0
+    e2e_times = []
+    for s in range(args.steps):
+        barrier_sync()
+        t0 = time.perf_counter()
+        sv.spectrum_begin("mixed", n_e)
+        for ei, ri in items:
+            sv.spectrum_add(ei, ri)
+        sv.spectrum_run()
+        out = [sv.taull(k) for k in range(n_e)]
+        barrier_sync()
+        e2e_times.append(time.perf_counter() - t0)
+        if s == 0:
+            h2d = sum(ei.phiato.nbytes + ei.besselr.nbytes + ei.neumanr.nbytes + st.Vr[:, 0].nbytes +
+                      4 * (st.grid.npoint + 1 + 2 * st.natome) for ei, _ in items)
+            d2h = sum(t.nbytes for t in out)
+    clocks = clk.stop()
+    e2e_s = max_over_ranks(statistics.mean(e2e_times))
+
+    peaks, peak_kind = _peaks()
+    last = infos[-1]
+    achieved = last["flops_factor"] / (last["ms_factor"] / 1000.0) / 1e12
+    roof = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+            "frac": achieved / peaks["bf16_tflops"], "traffic": None,
+            "kernel": "FP32 profile LU phase (k_diag + k_panel + k_trailing<float>)",
+            "peak_note": f"bf16 dense tensor peak ({peak_kind}); the factor runs on the FP32 pipes "
+                         f"(73.1 TFLOP/s probed on this pool)", "frac_of_fp32_pipe": achieved / 73.1}
+    if rank != 0:
+        return
+    cb = cpu_baseline(min(os.cpu_count() or 1, 16)) if not args.no_cpu else None
+    line = {
+        "metric": METRIC, "value": value, "unit": "energies/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 factor + f64 refinement (df64 residual)", "data": "synthetic",
+        "config": {"workload": "Cu fcc a=3.61 A, 13-atom cluster, FDM radius 3.0 A, step 0.25 A, C1, "
+                               "401 energies -5..35 eV step 0.1 eV, batched mixed precision",
+                   "energies": n_e, "nligne": [min(r.nligne for _, r in items), max(r.nligne for _, r in items)],
+                   "nrhs": [min(e.nlmso for e, _ in items), max(e.nlmso for e, _ in items)],
+                   "l2": "working set ~100 GB per step, far above the 126 MB L2 (no flush needed)"},
+        "roofline": roof,
+        "cpu_baseline": cb and {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": world * n_e / e2e_s, "unit": "energies/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(last["n_kernels"]),
+        "clocks": clocks,
+        "plain_fp64": {"value": n_e / (fp64_ms / 1000.0), "unit": "energies/s", "ms_per_step": fp64_ms,
+                       "first_call_wall_s": fp64_wall},
+        "accuracy": {"convolved_rel_err_vs_fp64": err_conv, "taull_max_rel_err_vs_fp64": err_taull,
+                     "refine_iters_max": last["refine_iters"], "fp64_escalations": last["n_fallback"]},
+        "phases_ms": {k: last[k] for k in ("ms_assemble", "ms_factor", "ms_solve", "ms_refine")},
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -45,7 +45,7 @@ class FdmInfo(C.Structure):
     _fields_ = [("nnz_profile", C.c_int64), ("flops_factor", C.c_double), ("flops_solve", C.c_double),
                 ("refine_iters", C.c_int32), ("residual", C.c_double),
                 ("ms_assemble", C.c_double), ("ms_factor", C.c_double), ("ms_solve", C.c_double),
-                ("ms_refine", C.c_double)]
+                ("ms_refine", C.c_double), ("n_fallback", C.c_int32), ("n_kernels", C.c_int64)]
 
 
 def _pi(a: np.ndarray, keep: List):
@@ -60,31 +60,56 @@ def _pd(a: np.ndarray, keep: List):
     return a.ctypes.data_as(P_F64)
 
 
-class GridArgs:
-    """An FdmGrid struct built from a Structure (keeps its buffers alive)."""
+def grid_dict(st: CL.Structure) -> dict:
+    """The energy-independent mat_solve arguments of a Structure as plain arrays."""
+    g = st.grid
+    kar = np.zeros((64, 1), order="F")
+    kar[:, 0] = 1.0      # C1: identity character on every operation index used
+    return dict(
+        npoint=g.npoint, npsom=g.npso, nvois=g.nvois, natome=st.natome, nbm=g.nbm, nbtm=g.nbtm, nim=g.npoint,
+        nsm=max(g.nsortf, 1), nsort=g.nsort, nsortf=g.nsortf, nstm=g.nsort, nspin=st.nspin, nlmmax=st.nlmmax,
+        nlmomax=st.nlmomax, nlmsam=st.lato.shape[0], nso1=st.lso.shape[0], ngrph=1, nspino=1,
+        ivois=g.ivois, isvois=g.isvois, numia=g.numia, nbord=g.nbord, nbordf=g.nbordf, ibord=g.ibord,
+        isbord=g.isbord, isrt=g.isrt, lato=st.lato, mato=st.mato, iato=st.iato, lso=st.lso, mso=st.mso,
+        iso=st.iso, clapl=g.clapl, cgrad=g.cgrad, rvol=g.rvol, poidsa=g.poidsa, poidso=g.poidso,
+        Ylmato=st.Ylmato, Ylmso=st.Ylmso, Kar=kar, Kari=np.zeros((64, 1), order="F"))
 
-    def __init__(self, st: CL.Structure):
-        g = st.grid
+
+def energy_dict(st: CL.Structure, ei: CL.EnergyInputs, ri: CL.RowIndex) -> dict:
+    """The per-call mat_solve arguments of one energy (real path) as plain arrays."""
+    g = st.grid
+    return dict(
+        nligne=ri.nligne, nligneso=ri.nligneso, nlmso=ei.nlmso, lmaxso=ei.lmaxso, nlmagm=ei.nlmagm,
+        nphiato1=g.nbtm, nphiato7=1, nspinp=1, n_RI=1, n_ato_RI=1, nspinr=1, nsort_r=g.nsort, nsort_c=0,
+        igrph=1, ispin=ei.ispin, nicm=1, Cal_comp=0, E_comp=0, Basereel=1, Base_hexa=0, irregular=0,
+        Relativiste=0, Spinorbite=0, Repres_comp=0, Ylm_comp=0, Test_reg=0,
+        Enervide=ei.enervide, Eimag=ei.eimag, new_=ri.new, newinv=ri.newinv, lb1=ri.lb1, lb2=ri.lb2,
+        ianew=ri.ianew, nlmsa=ei.nlmsa, Vr=st.Vr, gradvr=np.zeros((1, 3, 1), order="F"), phiato=ei.phiato,
+        Besselr=ei.besselr, Neumanr=ei.neumanr)
+
+
+def _fill(struct_cls, d: dict, keep: List):
+    s = struct_cls()
+    for name, typ in struct_cls._fields_:
+        v = d.get(name)
+        if v is None:
+            continue
+        if typ is P_I32:
+            setattr(s, name, _pi(np.asarray(v), keep))
+        elif typ is P_F64:
+            setattr(s, name, _pd(np.asarray(v), keep))
+        else:
+            setattr(s, name, typ(v.item() if isinstance(v, np.ndarray) else v).value)
+    return s
+
+
+class GridArgs:
+    """An FdmGrid struct built from a Structure or from grid_dict() arrays."""
+
+    def __init__(self, src):
         self.keep: List = []
-        k = self.keep
-        s = FdmGrid()
-        s.npoint, s.npsom, s.nvois, s.natome = g.npoint, g.npso, g.nvois, st.natome
-        s.nbm, s.nbtm, s.nim, s.nsm = g.nbm, g.nbtm, g.npoint, max(g.nsortf, 1)
-        s.nsort, s.nsortf, s.nstm, s.nspin = g.nsort, g.nsortf, g.nsort, st.nspin
-        s.nlmmax, s.nlmomax = st.nlmmax, st.nlmomax
-        s.nlmsam, s.nso1, s.ngrph, s.nspino = st.lato.shape[0], st.lso.shape[0], 1, 1
-        s.ivois, s.isvois, s.numia = _pi(g.ivois, k), _pi(g.isvois, k), _pi(g.numia, k)
-        s.nbord, s.nbordf = _pi(g.nbord, k), _pi(g.nbordf, k)
-        s.ibord, s.isbord, s.isrt = _pi(g.ibord, k), _pi(g.isbord, k), _pi(g.isrt, k)
-        s.lato, s.mato, s.iato = _pi(st.lato, k), _pi(st.mato, k), _pi(st.iato, k)
-        s.lso, s.mso, s.iso = _pi(st.lso, k), _pi(st.mso, k), _pi(st.iso, k)
-        s.clapl, s.cgrad, s.rvol = _pd(g.clapl, k), _pd(g.cgrad, k), _pd(g.rvol, k)
-        s.poidsa, s.poidso = _pd(g.poidsa, k), _pd(g.poidso, k)
-        s.Ylmato, s.Ylmso = _pd(st.Ylmato, k), _pd(st.Ylmso, k)
-        kar = np.zeros((64, 1), order="F")
-        kar[:, 0] = 1.0      # C1: identity character on every operation index used
-        s.Kar, s.Kari = _pd(kar, k), _pd(np.zeros((64, 1), order="F"), k)
-        self.s = s
+        self.d = grid_dict(src) if isinstance(src, CL.Structure) else src
+        self.s = _fill(FdmGrid, self.d, self.keep)
 
     @property
     def ptr(self):
@@ -92,30 +117,14 @@ class GridArgs:
 
 
 class EnergyArgs:
-    """An FdmEnergy struct for one energy (real path, regular solution)."""
+    """An FdmEnergy struct for one energy, from (Structure, EnergyInputs, RowIndex)
+    or from energy_dict() arrays."""
 
-    def __init__(self, st: CL.Structure, ei: CL.EnergyInputs, ri: CL.RowIndex):
-        g = st.grid
+    def __init__(self, st, ei=None, ri=None):
         self.keep: List = []
-        k = self.keep
-        s = FdmEnergy()
-        s.nligne, s.nligneso, s.nlmso, s.lmaxso = ri.nligne, ri.nligneso, ei.nlmso, ei.lmaxso
-        s.nlmagm, s.nphiato1, s.nphiato7, s.nspinp = ei.nlmagm, g.nbtm, 1, 1
-        s.n_RI, s.n_ato_RI, s.nspinr = 1, 1, 1
-        s.nsort_r, s.nsort_c, s.igrph, s.ispin, s.nicm = g.nsort, 0, 1, ei.ispin, 1
-        s.Cal_comp = s.E_comp = s.Base_hexa = s.irregular = s.Relativiste = 0
-        s.Spinorbite = s.Repres_comp = s.Ylm_comp = s.Test_reg = 0
-        s.Basereel = 1
-        s.Enervide, s.Eimag = ei.enervide, ei.eimag
-        s.new_, s.newinv = _pi(ri.new, k), _pi(ri.newinv, k)
-        s.lb1, s.lb2, s.ianew, s.nlmsa = _pi(ri.lb1, k), _pi(ri.lb2, k), _pi(ri.ianew, k), _pi(ei.nlmsa, k)
-        s.Vr = _pd(st.Vr, k)
-        s.gradvr = _pd(np.zeros((1, 3, 1), order="F"), k)
-        s.phiato = _pd(ei.phiato, k)
-        s.Besselr, s.Neumanr = _pd(ei.besselr, k), _pd(ei.neumanr, k)
-        s.Bessel = s.Neuman = None
-        self.s = s
-        self.nligne, self.nlmso = ri.nligne, ei.nlmso
+        self.d = energy_dict(st, ei, ri) if ei is not None else st
+        self.s = _fill(FdmEnergy, self.d, self.keep)
+        self.nligne, self.nlmso = int(self.d["nligne"]), int(self.d["nlmso"])
 
     @property
     def ptr(self):

@@ -80,6 +80,7 @@ struct Batch {
   std::vector<HostProb> probs;
   // results
   std::vector<int> iters;
+  std::vector<int> fallback;   // solved again in FP64 after the mixed path missed its tolerance
   std::vector<double> resid;
   std::vector<int> err;
   bool ran = false;
@@ -111,7 +112,9 @@ struct fdmgpu_handle {
   DevBuf<double> d_dpool;
   DevBuf<double> d_env64, d_B64, d_X64, d_rs, d_cs, d_val, d_taull, d_tscratch, d_smr;
   DevBuf<float> d_env32, d_Y32;
-  DevBuf<int> d_rowptr, d_col, d_err, d_active;
+  DevBuf<float2> d_val2, d_Xs;
+  int residual_df64 = 1;
+  DevBuf<int> d_rowptr, d_col, d_err, d_active, d_piv;
   DevBuf<unsigned long long> d_red;  // dmax | xmax | amax
   int* h_pinned_i = nullptr;
   size_t h_pinned_i_cap = 0;
@@ -122,6 +125,7 @@ struct fdmgpu_handle {
   uint64_t ptr_sig = 0;
   int plan_prec = -1;
   cudaGraphExec_t g_asm = nullptr, g_fac = nullptr, g_sol = nullptr, g_iter = nullptr;
+  int64_t nk_asm = 0, nk_fac = 0, nk_sol = 0, nk_iter = 0;  // kernel nodes per graph
   StepPlan sp;
   LaunchDims dims;
   Tables tb{};
@@ -318,19 +322,29 @@ void build_step_plan(fdmgpu_handle* h) {
   }
 }
 
-// Assign pool offsets, allocate device memory and upload plan tables.
-fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h) {
+// Pool offsets of every problem and the launch dimensions of the batch.
+// Runs on every batch (the descriptors are rebuilt by fdmgpu_batch_add);
+// allocate_and_upload_plan() below runs only when the plan changes.
+struct Layout {
+  int64_t env = 0, rhs = 0, rowv = 0, csr = 0, taull = 0, scratch = 0;
+  std::vector<int> J0, J1, Imax, Imin;
+  std::vector<int64_t> strip;
+};
+
+void layout_batch(fdmgpu_handle* h, Layout& L) {
   auto& pr = h->batch.probs;
   const int np = (int)pr.size();
   const bool mixed = h->batch.precision == FDMGPU_PREC_MIXED;
-  int64_t env = 0, rhs = 0, rowv = 0, csr = 0, taull = 0, scratch = 0;
+  int64_t& env = L.env; int64_t& rhs = L.rhs; int64_t& rowv = L.rowv;
+  int64_t& csr = L.csr; int64_t& taull = L.taull; int64_t& scratch = L.scratch;
   int trow = 0;
   LaunchDims& d = h->dims;
   d = LaunchDims();
   d.nprob = np;
   d.npr = h->S.npr;
-  std::vector<int> J0, J1, Imax, Imin;
-  std::vector<int64_t> strip;
+  std::vector<int>& J0 = L.J0; std::vector<int>& J1 = L.J1;
+  std::vector<int>& Imax = L.Imax; std::vector<int>& Imin = L.Imin;
+  std::vector<int64_t>& strip = L.strip;
   for (auto& hp : pr) {
     Prob& P = hp.P;
     P.trow = trow;
@@ -359,6 +373,17 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h) {
     d.max_nlmso = std::max(d.max_nlmso, P.nlmso);
     d.max_atom_rows = std::max(d.max_atom_rows, h->g.natome * hp.nlmsa_max);
   }
+  d.rowv_total = rowv;
+}
+
+// Allocate the device pools of the batch and upload the plan tables.
+fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
+  const int np = (int)h->batch.probs.size();
+  const bool mixed = h->batch.precision == FDMGPU_PREC_MIXED;
+  const int64_t env = L.env, rhs = L.rhs, rowv = L.rowv, csr = L.csr, taull = L.taull, scratch = L.scratch;
+  const std::vector<int>& J0 = L.J0; const std::vector<int>& J1 = L.J1;
+  const std::vector<int>& Imax = L.Imax; const std::vector<int>& Imin = L.Imin;
+  const std::vector<int64_t>& strip = L.strip;
   cudaStream_t s = h->stream;
   CK(upload(h->d_J0, J0, s));
   CK(upload(h->d_J1, J1, s));
@@ -375,6 +400,8 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h) {
     if (h->d_env32.reserve((size_t)env * TS2) != cudaSuccess || h->d_Y32.reserve(rhs) != cudaSuccess ||
         h->d_rs.reserve(rowv) != cudaSuccess || h->d_cs.reserve(rowv) != cudaSuccess ||
         h->d_rowptr.reserve(rowv) != cudaSuccess || h->d_col.reserve(csr) != cudaSuccess ||
+        h->d_piv.reserve(rowv) != cudaSuccess || h->d_val2.reserve(csr) != cudaSuccess ||
+        h->d_Xs.reserve(rhs) != cudaSuccess ||
         h->d_val.reserve(csr) != cudaSuccess)
       return fail(FDMGPU_ERR_NOMEM, "device allocation of the mixed precision pools failed");
   }
@@ -401,6 +428,9 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h) {
     pl.rs = h->d_rs.p;
     pl.cs = h->d_cs.p;
     pl.rowptr = h->d_rowptr.p;
+    pl.piv = h->d_piv.p;
+    pl.val2 = h->d_val2.p;
+    pl.Xs = h->d_Xs.p;
     pl.col = h->d_col.p;
     pl.val = h->d_val.p;
   }
@@ -484,9 +514,9 @@ void record_factor(fdmgpu_handle* h) {
   const Pools& pl = h->pl;
   const int np = h->dims.nprob;
   if (h->batch.precision == FDMGPU_PREC_FP64)
-    launch_factor<double>(h->sp, pl.env64, pl.X64, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-10, s);
+    launch_factor<double>(h->sp, pl.env64, pl.X64, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-10, nullptr, s);
   else
-    launch_factor<float>(h->sp, pl.env32, pl.Y32, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-30, s);
+    launch_factor<float>(h->sp, pl.env32, pl.Y32, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-30, pl.piv, s);
 }
 
 void record_solve(fdmgpu_handle* h) {
@@ -508,13 +538,13 @@ void record_iter(fdmgpu_handle* h) {
   const Prob* probs = h->d_probs.p;
   const int np = h->dims.nprob;
   cudaMemsetAsync(pl.dmax, 0, 3 * np * sizeof(unsigned long long), s);
-  launch_residual(probs, pl, h->dims, s);
-  launch_forward<float>(h->sp, pl.env32, pl.Y32, probs, h->tb, np, pl.active, s);
+  launch_residual(probs, pl, h->dims, h->residual_df64, s);
+  launch_forward<float>(h->sp, pl.env32, pl.Y32, probs, h->tb, np, pl.active, pl.piv, s);
   launch_backward<float>(h->sp, pl.env32, pl.Y32, probs, h->tb, np, pl.active, s);
   launch_update_x(probs, pl, h->dims, 0, s);
 }
 
-fdmgpu_status capture(fdmgpu_handle* h, void (*rec)(fdmgpu_handle*), cudaGraphExec_t* out) {
+fdmgpu_status capture(fdmgpu_handle* h, void (*rec)(fdmgpu_handle*), cudaGraphExec_t* out, int64_t* nkernels) {
   if (*out) {
     cudaGraphExecDestroy(*out);
     *out = nullptr;
@@ -523,13 +553,23 @@ fdmgpu_status capture(fdmgpu_handle* h, void (*rec)(fdmgpu_handle*), cudaGraphEx
   CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
   rec(h);
   CK(cudaStreamEndCapture(h->stream, &graph));
+  size_t nn = 0;
+  CK(cudaGraphGetNodes(graph, nullptr, &nn));
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (nn) CK(cudaGraphGetNodes(graph, nodes.data(), &nn));
+  int64_t nk = 0;
+  for (auto nd : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++nk;
+  }
+  *nkernels = nk;
   cudaError_t e = cudaGraphInstantiate(out, graph, 0);
   cudaGraphDestroy(graph);
   CK(e);
   return FDMGPU_OK;
 }
 
-fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info) {
+fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   Batch& b = h->batch;
   const int np = (int)b.probs.size();
   if (np == 0) return fail(FDMGPU_ERR_ARG, "empty batch");
@@ -537,29 +577,37 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info) {
   for (auto& hp : b.probs) sig = mix(sig, hp.sig);
   fdmgpu_status st;
   cudaGetLastError();  // clear a stale error of an earlier call on this thread
+  sig = mix(sig, (uint64_t)h->residual_df64);
   const bool replan = sig != h->plan_sig || b.precision != h->plan_prec || !h->g_asm;
+  Layout lay;
+  layout_batch(h, lay);
   if (replan) {
-    st = allocate_and_upload_plan(h);
+    st = allocate_and_upload_plan(h, lay);
     if (st) return st;
   }
-  st = upload_inputs(h);
-  if (st) return st;
+  if (resident) {
+    if (replan || !b.ran) return fail(FDMGPU_ERR_ARG, "rerun needs an unchanged batch that has run once");
+  } else {
+    st = upload_inputs(h);
+    if (st) return st;
+  }
   // the graphs hold device pointers: capture again whenever one moved
   uint64_t ps = 0;
   const void* ptrs[] = {h->d_probs.p, h->d_ipool.p, h->d_dpool.p, h->d_env64.p, h->d_env32.p, h->d_B64.p,
                         h->d_X64.p,   h->d_Y32.p,   h->d_rs.p,    h->d_cs.p,    h->d_rowptr.p, h->d_col.p,
-                        h->d_val.p,   h->d_err.p,   h->d_active.p, h->d_red.p,  h->d_J0.p,   h->d_strip.p};
+                        h->d_val.p,   h->d_err.p,   h->d_active.p, h->d_red.p,  h->d_J0.p,   h->d_strip.p,
+                        h->d_piv.p,   h->d_val2.p,  h->d_Xs.p};
   for (const void* q : ptrs) ps = mix(ps, (uint64_t)(uintptr_t)q);
   if (replan || ps != h->ptr_sig) {
     h->ptr_sig = ps;
-    st = capture(h, record_asm, &h->g_asm);
+    st = capture(h, record_asm, &h->g_asm, &h->nk_asm);
     if (st) return st;
-    st = capture(h, record_factor, &h->g_fac);
+    st = capture(h, record_factor, &h->g_fac, &h->nk_fac);
     if (st) return st;
-    st = capture(h, record_solve, &h->g_sol);
+    st = capture(h, record_solve, &h->g_sol, &h->nk_sol);
     if (st) return st;
     if (b.precision == FDMGPU_PREC_MIXED) {
-      st = capture(h, record_iter, &h->g_iter);
+      st = capture(h, record_iter, &h->g_iter, &h->nk_iter);
       if (st) return st;
     }
     h->plan_sig = sig;
@@ -572,45 +620,74 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info) {
   CK(cudaEventRecord(h->ev[2], h->stream));
   CK(cudaGraphLaunch(h->g_sol, h->stream));
   CK(cudaEventRecord(h->ev[3], h->stream));
+  int64_t nkern = h->nk_asm + h->nk_fac + h->nk_sol;
   b.iters.assign(np, 0);
+  b.fallback.assign(np, 0);
   b.resid.assign(np, 0.0);
   b.err.assign(np, 0);
   float ms_refine = 0;
   if (b.precision == FDMGPU_PREC_MIXED) {
-    const int max_iter = 10;
-    const double tol = 1e-12;
-    std::vector<int> active(np, 1);
+    // Stop a problem when its relative correction max|dx|/max|x| is below tol,
+    // or when it stagnates (no halving for two steps: the residual arithmetic's
+    // floor); accept the result if the last correction is below tol_accept.
+    const int max_iter = 30;
+    const double tol = 1e-10;
+    const double tol_accept = h->residual_df64 ? 1e-7 : 1e-9;
+    std::vector<int> active(np, 1), slow(np, 0);
+    std::vector<double> prev(np, 1e300);
     std::vector<unsigned long long> red(3 * np);
     CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
     CK(cudaEventRecord(h->ev[4], h->stream));
     for (int it = 1; it <= max_iter; ++it) {
       CK(cudaGraphLaunch(h->g_iter, h->stream));
+      nkern += h->nk_iter;
       CK(cudaMemcpyAsync(red.data(), h->d_red.p, 3 * np * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                          h->stream));
       CK(cudaStreamSynchronize(h->stream));
       int nact = 0;
       for (int k = 0; k < np; ++k) {
         if (!active[k]) continue;
-        double dm, xm, rm;
+        double dm, xm;
         memcpy(&dm, &red[k], 8);
         memcpy(&xm, &red[np + k], 8);
-        memcpy(&rm, &red[2 * np + k], 8);
+        const double r = xm > 0 ? dm / xm : dm;
         b.iters[k] = it;
-        b.resid[k] = xm > 0 ? dm / xm : dm;
-        if (!(b.resid[k] <= tol)) {
-          if (!std::isfinite(b.resid[k])) active[k] = 0; else ++nact;
-        } else {
+        b.resid[k] = r;
+        if (!std::isfinite(r) || r <= tol) {
           active[k] = 0;
+        } else {
+          slow[k] = r > 0.5 * prev[k] ? slow[k] + 1 : 0;
+          if (slow[k] >= 2) active[k] = 0;
+          else ++nact;
         }
+        prev[k] = r;
       }
       if (nact == 0) break;
       CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
     }
+    // Precision escalation: problems whose refinement missed tol_accept are
+    // factorised again in FP64 (their FP64 band is still intact) and solved.
+    int nfail = 0;
+    for (int k = 0; k < np; ++k) {
+      active[k] = !(b.resid[k] <= tol_accept);
+      nfail += active[k];
+    }
+    if (nfail > 0) {
+      CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+      launch_copy_rhs(h->d_probs.p, h->pl, h->dims, h->stream);
+      nkern += 1 + 5 * (int64_t)h->sp.ntmax;
+      launch_factor<double>(h->sp, h->pl.env64, h->pl.X64, h->d_probs.p, h->tb, np, 1, h->d_active.p, h->pl.err,
+                            1e-10, nullptr, h->stream);
+      launch_backward<double>(h->sp, h->pl.env64, h->pl.X64, h->d_probs.p, h->tb, np, h->d_active.p, h->stream);
+      CK(cudaGetLastError());
+      for (int k = 0; k < np; ++k) b.fallback[k] = active[k];
+    }
     CK(cudaEventRecord(h->ev[5], h->stream));
-    for (int k = 0; k < np; ++k)
-      if (!(b.resid[k] <= 1e-9)) b.err[k] = FDMGPU_ERR_NOT_CONVERGED;
   }
-  if (b.probs[0].P.nlm_abs > 0) launch_taull(h->d_probs.p, h->pl, h->dims, h->pl.X64, h->stream);
+  if (b.probs[0].P.nlm_abs > 0) {
+    launch_taull(h->d_probs.p, h->pl, h->dims, h->pl.X64, h->stream);
+    nkern += 1;
+  }
   std::vector<int> err(np);
   CK(cudaMemcpyAsync(err.data(), h->d_err.p, np * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
   CK(cudaStreamSynchronize(h->stream));
@@ -620,6 +697,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info) {
   b.ran = true;
   if (info) {
     memset(info, 0, sizeof(*info));
+    info->n_kernels = nkern;
     for (auto& hp : b.probs) {
       info->nnz_profile += hp.nnz_profile;
       info->flops_factor += hp.flops_factor;
@@ -643,16 +721,21 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info) {
       }
       info->refine_iters = mi;
       info->residual = mr;
+      for (int k = 0; k < np; ++k) info->n_fallback += b.fallback[k];
     }
   }
+  // hard errors first; a refinement that did not reach its tolerance still
+  // leaves a usable solution and is reported per problem (fdmgpu_batch_stats)
+  fdmgpu_status worst = FDMGPU_OK;
   for (int k = 0; k < np; ++k)
-    if (b.err[k]) {
+    if (b.err[k] && (worst == FDMGPU_OK || worst == FDMGPU_ERR_NOT_CONVERGED)) {
       char buf[160];
-      snprintf(buf, sizeof buf, "problem %d failed with status %d (zero pivot or no convergence)", k, b.err[k]);
+      snprintf(buf, sizeof buf, "problem %d: status %d (%s)", k, b.err[k],
+               b.err[k] == FDMGPU_ERR_NOT_CONVERGED ? "refinement did not converge" : "zero pivot or bad input");
       g_last_error = buf;
-      return (fdmgpu_status)b.err[k];
+      worst = (fdmgpu_status)b.err[k];
     }
-  return FDMGPU_OK;
+  return worst;
 }
 
 }  // namespace
@@ -827,13 +910,15 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   DevBuf<int>* ib[] = {&h->d_inter_pt, &h->d_nb_kind, &h->d_nb_idx, &h->d_numia, &h->d_nbord, &h->d_nbordf,
                        &h->d_ibord,    &h->d_isbord,  &h->d_isrt,   &h->d_lato,  &h->d_mato,  &h->d_lso,
                        &h->d_mso,      &h->d_J0,      &h->d_J1,     &h->d_Imax,  &h->d_Imin,  &h->d_ipool,
-                       &h->d_rowptr,   &h->d_col,     &h->d_err,    &h->d_active};
+                       &h->d_rowptr,   &h->d_col,     &h->d_err,    &h->d_active, &h->d_piv};
   for (auto* b : ib) b->release();
   DevBuf<double>* db[] = {&h->d_nb_coef, &h->d_rvol, &h->d_clapl, &h->d_poidsa, &h->d_poidso, &h->d_Kar,
                           &h->d_YsoT,    &h->d_Ylmato, &h->d_dpool, &h->d_env64, &h->d_B64,  &h->d_X64,
                           &h->d_rs,      &h->d_cs,   &h->d_val,   &h->d_taull,  &h->d_tscratch, &h->d_smr};
   for (auto* b : db) b->release();
   h->d_env32.release();
+  h->d_val2.release();
+  h->d_Xs.release();
   h->d_Y32.release();
   h->d_strip.release();
   h->d_probs.release();
@@ -844,6 +929,13 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
     if (e) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
   delete h;
+}
+
+fdmgpu_status fdmgpu_set_residual_mode(fdmgpu_handle* h, int32_t mode) {
+  if (!h || (mode != FDMGPU_RESIDUAL_FP64 && mode != FDMGPU_RESIDUAL_DF64))
+    return fail(FDMGPU_ERR_ARG, "unknown residual mode");
+  h->residual_df64 = mode == FDMGPU_RESIDUAL_DF64;
+  return FDMGPU_OK;
 }
 
 fdmgpu_status fdmgpu_batch_begin(fdmgpu_handle* h, int32_t precision, int32_t max_energies) {
@@ -876,6 +968,7 @@ fdmgpu_status fdmgpu_batch_add(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t
       if (L * L + L + 1 + m != lm) return fail(FDMGPU_ERR_UNSUPPORTED, "Taull needs the C1 harmonic order");
     }
   }
+  hp.sig = mix(hp.sig, (uint64_t)hp.P.nlm_abs * 7919u + (uint64_t)hp.P.ianew_abs);
   pack_inputs(h, e, hp);
   h->batch.probs.push_back(std::move(hp));
   h->batch.ran = false;
@@ -884,7 +977,12 @@ fdmgpu_status fdmgpu_batch_add(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t
 
 fdmgpu_status fdmgpu_batch_run(fdmgpu_handle* h, fdmgpu_info* info) {
   if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
-  return run_batch(h, info);
+  return run_batch(h, info, false);
+}
+
+fdmgpu_status fdmgpu_batch_rerun(fdmgpu_handle* h, fdmgpu_info* info) {
+  if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
+  return run_batch(h, info, true);
 }
 
 fdmgpu_status fdmgpu_batch_taull(fdmgpu_handle* h, int32_t k, double* taull, int32_t* nlm) {
@@ -910,12 +1008,14 @@ fdmgpu_status fdmgpu_batch_solution(fdmgpu_handle* h, int32_t k, double* smr) {
   return FDMGPU_OK;
 }
 
-fdmgpu_status fdmgpu_batch_stats(fdmgpu_handle* h, int32_t k, int32_t* iters, double* residual) {
+fdmgpu_status fdmgpu_batch_stats(fdmgpu_handle* h, int32_t k, int32_t* iters, double* residual,
+                                 int32_t* fallback) {
   if (!h || !h->batch.ran || k < 0 || k >= (int)h->batch.probs.size())
     return fail(FDMGPU_ERR_ARG, "no such batch result");
   if (iters) *iters = h->batch.iters[k];
   if (residual) *residual = h->batch.resid[k];
-  return FDMGPU_OK;
+  if (fallback) *fallback = h->batch.fallback.empty() ? 0 : h->batch.fallback[k];
+  return (fdmgpu_status)h->batch.err[k];
 }
 
 fdmgpu_status fdmgpu_mat_solve(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t precision, double* smr, double* smi,
@@ -927,8 +1027,9 @@ fdmgpu_status fdmgpu_mat_solve(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t
   st = fdmgpu_batch_add(h, e, 0);
   if (st) return st;
   st = fdmgpu_batch_run(h, info);
-  if (st) return st;
-  return fdmgpu_batch_solution(h, 0, smr);
+  if (st && st != FDMGPU_ERR_NOT_CONVERGED) return st;
+  fdmgpu_status st2 = fdmgpu_batch_solution(h, 0, smr);
+  return st2 ? st2 : st;
 }
 
 }  // extern "C"

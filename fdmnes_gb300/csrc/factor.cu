@@ -16,22 +16,30 @@
 
 namespace fdm {
 
-// Factor the diagonal tile (K,K) in place (one CTA per problem).
+// Factor the diagonal tile (K,K) in place (one CTA per problem).  With piv,
+// partial pivoting among the tile's rows; the row order is stored in
+// piv[rowv + K*TS + r] and applied to the U and RHS tiles of block K when they
+// are loaded (the L tiles left of the diagonal keep the order in which the
+// earlier steps updated them, and the forward substitution permutes Y(K) at
+// step K, so P A = L U holds block by block).
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_diag(T* env, const Prob* probs, Tables tb, int K, const int* active,
-                                                   int* err, double piv_thr) {
+                                                   int* err, double piv_thr, int* piv) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
   if (K >= P.nt || (active && !active[e])) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* D = reinterpret_cast<T*>(smem_raw);
   __shared__ double mp;
+  __shared__ int perm[TS];
+  if (threadIdx.x < TS) perm[threadIdx.x] = threadIdx.x;
   T* dtile = tile_ptr(env, P, tb, K, K);
   load_tile(D, dtile);
   __syncthreads();
-  tile_lu(D, &mp);
+  tile_lu(D, &mp, piv ? perm : nullptr);
   __syncthreads();
   store_tile(dtile, D);
+  if (piv && threadIdx.x < TS) piv[P.rowv + (int64_t)K * TS + threadIdx.x] = perm[threadIdx.x];
   // smallest |pivot| of the tile (padding rows carry 1); NaN also trips the test
   if (threadIdx.x == 0 && !(mp >= piv_thr)) atomicExch(&err[e], (int)FDMGPU_ERR_ZERO_PIVOT);
 }
@@ -40,7 +48,7 @@ __global__ void __launch_bounds__(NTHREADS) k_diag(T* env, const Prob* probs, Ta
 // (K,J) and, when fused, the RHS tiles (K,R).
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_panel(T* env, T* rhs, const Prob* probs, Tables tb, int K,
-                                                    int fuse_rhs, const int* active) {
+                                                    int fuse_rhs, const int* active, const int* piv) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
   if (K >= P.nt || (active && !active[e])) return;
@@ -59,14 +67,10 @@ __global__ void __launch_bounds__(NTHREADS) k_panel(T* env, T* rhs, const Prob* 
     load_tile(W, g);
     __syncthreads();
     tile_right_upper_solve(W, D);
-  } else if (w < nI + nJ) {
-    g = tile_ptr(env, P, tb, K, K + 1 + (w - nI));
-    load_tile(W, g);
-    __syncthreads();
-    tile_left_lower_unit_solve(W, D);
   } else {
-    g = rhs_ptr(rhs, P, K, w - nI - nJ);
-    load_tile(W, g);
+    g = w < nI + nJ ? tile_ptr(env, P, tb, K, K + 1 + (w - nI)) : rhs_ptr(rhs, P, K, w - nI - nJ);
+    if (piv) load_tile_perm(W, g, piv + P.rowv + (int64_t)K * TS);
+    else load_tile(W, g);
     __syncthreads();
     tile_left_lower_unit_solve(W, D);
   }
@@ -106,7 +110,7 @@ __global__ void __launch_bounds__(NTHREADS) k_trailing(T* env, T* rhs, const Pro
 // Forward substitution, unit lower L: Y(K,R) <- L(K,K)^-1 Y(K,R).
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_fwd_diag(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
-                                                       const int* active) {
+                                                       const int* active, const int* piv) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
   if (K >= P.nt || (active && !active[e])) return;
@@ -117,7 +121,8 @@ __global__ void __launch_bounds__(NTHREADS) k_fwd_diag(const T* env, T* rhs, con
   T* W = D + TS * SP;
   load_tile(D, tile_ptr(const_cast<T*>(env), P, tb, K, K));
   T* g = rhs_ptr(rhs, P, K, R);
-  load_tile(W, g);
+  if (piv) load_tile_perm(W, g, piv + P.rowv + (int64_t)K * TS);
+  else load_tile(W, g);
   __syncthreads();
   tile_left_lower_unit_solve(W, D);
   __syncthreads();
@@ -197,12 +202,12 @@ void setup_factor_kernels() {
 
 template <typename T>
 void launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
-                   const int* active, int* err, double piv_thr, cudaStream_t s) {
+                   const int* active, int* err, double piv_thr, int* piv, cudaStream_t s) {
   const size_t sm = smem_bytes<T>();
   for (int K = 0; K < sp.ntmax; ++K) {
-    k_diag<T><<<dim3(1, nprob), NTHREADS, sm, s>>>(env, probs, tb, K, active, err, piv_thr);
+    k_diag<T><<<dim3(1, nprob), NTHREADS, sm, s>>>(env, probs, tb, K, active, err, piv_thr, piv);
     const int np = fuse_rhs ? sp.panel_rhs[K] : sp.panel[K];
-    if (np > 0) k_panel<T><<<dim3(np, nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
+    if (np > 0) k_panel<T><<<dim3(np, nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active, piv);
     const int nt = fuse_rhs ? sp.trail_rhs[K] : sp.trail[K];
     if (nt > 0) k_trailing<T><<<dim3(nt, nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
   }
@@ -210,10 +215,10 @@ void launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables
 
 template <typename T>
 void launch_forward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
-                    const int* active, cudaStream_t s) {
+                    const int* active, const int* piv, cudaStream_t s) {
   const size_t sm = smem_bytes<T>();
   for (int K = 0; K < sp.ntmax; ++K) {
-    k_fwd_diag<T><<<dim3(sp.nrtmax, nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+    k_fwd_diag<T><<<dim3(sp.nrtmax, nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, active, piv);
     if (sp.fwd[K] > 0) k_fwd_update<T><<<dim3(sp.fwd[K], nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, active);
   }
 }
@@ -231,13 +236,13 @@ void launch_backward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs
 template void setup_factor_kernels<float>();
 template void setup_factor_kernels<double>();
 template void launch_factor<float>(const StepPlan&, float*, float*, const Prob*, Tables, int, int, const int*, int*,
-                                   double, cudaStream_t);
+                                   double, int*, cudaStream_t);
 template void launch_factor<double>(const StepPlan&, double*, double*, const Prob*, Tables, int, int, const int*, int*,
-                                    double, cudaStream_t);
+                                    double, int*, cudaStream_t);
 template void launch_forward<float>(const StepPlan&, const float*, float*, const Prob*, Tables, int, const int*,
-                                    cudaStream_t);
+                                    const int*, cudaStream_t);
 template void launch_forward<double>(const StepPlan&, const double*, double*, const Prob*, Tables, int, const int*,
-                                     cudaStream_t);
+                                     const int*, cudaStream_t);
 template void launch_backward<float>(const StepPlan&, const float*, float*, const Prob*, Tables, int, const int*,
                                      cudaStream_t);
 template void launch_backward<double>(const StepPlan&, const double*, double*, const Prob*, Tables, int, const int*,

@@ -124,14 +124,48 @@ __device__ __forceinline__ void store_tile(T* __restrict__ g, const T* __restric
   }
 }
 
-// In-place LU without pivoting of the shared tile D (Doolittle: unit L below,
-// U on and above the diagonal).  Records the smallest |pivot| in *minpiv
-// (thread 0 only).
+// In-place LU of the shared tile D (Doolittle: unit L below, U on and above
+// the diagonal).  With perm != nullptr, partial pivoting among the rows of the
+// tile: perm[r] is the original tile row now at row r (perm must hold the
+// identity on entry).  Records the smallest |pivot| in *minpiv.
 template <typename T>
-__device__ void tile_lu(T* D, double* minpiv) {
+__device__ void tile_lu(T* D, double* minpiv, int* perm) {
   const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  __shared__ int prow;
   double mp = 1e300;
   for (int k = 0; k < TS; ++k) {
+    if (perm) {
+      if (threadIdx.x < 32) {
+        const int i1 = k + threadIdx.x, i2 = k + threadIdx.x + 32;
+        double v = i1 < TS ? fabs((double)D[i1 * SP + k]) : -1.0;
+        int bi = i1;
+        if (i2 < TS) {
+          const double v2 = fabs((double)D[i2 * SP + k]);
+          if (v2 > v) { v = v2; bi = i2; }
+        }
+        for (int o = 16; o; o >>= 1) {
+          const double ov = __shfl_xor_sync(0xffffffffu, v, o);
+          const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+          if (ov > v || (ov == v && oi < bi)) { v = ov; bi = oi; }
+        }
+        if (threadIdx.x == 0) prow = bi;
+      }
+      __syncthreads();
+      const int pr = prow;
+      if (pr != k) {
+        if (threadIdx.x < TS) {
+          const T t = D[k * SP + threadIdx.x];
+          D[k * SP + threadIdx.x] = D[pr * SP + threadIdx.x];
+          D[pr * SP + threadIdx.x] = t;
+        }
+        if (threadIdx.x == 0) {
+          const int t = perm[k];
+          perm[k] = perm[pr];
+          perm[pr] = t;
+        }
+      }
+      __syncthreads();
+    }
     const T piv = D[k * SP + k];
     if (threadIdx.x == 0) mp = fmin(mp, fabs((double)piv));
     if (threadIdx.x > k && threadIdx.x < TS) D[threadIdx.x * SP + k] = D[threadIdx.x * SP + k] / piv;
@@ -143,6 +177,15 @@ __device__ void tile_lu(T* D, double* minpiv) {
     __syncthreads();
   }
   if (threadIdx.x == 0) *minpiv = mp;
+}
+
+// Shared tile <- global tile with its rows permuted: s[r] = g[perm[r]].
+template <typename T>
+__device__ __forceinline__ void load_tile_perm(T* __restrict__ s, const T* __restrict__ g, const int* perm) {
+  for (int idx = threadIdx.x; idx < TS2; idx += NTHREADS) {
+    const int r = idx / TS, c = idx % TS;
+    s[r * SP + c] = g[perm[r] * TS + c];
+  }
 }
 
 // W <- W * inv(U), U = upper triangle (with diagonal) of D.

@@ -20,10 +20,10 @@ struct StepPlan {
 template <typename T> void setup_factor_kernels();
 template <typename T>
 void launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
-                   const int* active, int* err, double piv_thr, cudaStream_t s);
+                   const int* active, int* err, double piv_thr, int* piv, cudaStream_t s);
 template <typename T>
 void launch_forward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
-                    const int* active, cudaStream_t s);
+                    const int* active, const int* piv, cudaStream_t s);
 template <typename T>
 void launch_backward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
                      const int* active, cudaStream_t s);
@@ -40,8 +40,11 @@ struct Pools {
   double* rs = nullptr;            // row scales (per row, stride npad + 1)
   double* cs = nullptr;            // column scales
   int* rowptr = nullptr;           // CSR row pointers (stride npad + 1)
+  int* piv = nullptr;              // tile-local row order of the FP32 factor (stride npad + 1)
   int* col = nullptr;              // CSR columns
   double* val = nullptr;           // CSR values
+  float2* val2 = nullptr;          // CSR values as double-float (hi, lo)
+  float2* Xs = nullptr;            // solution as double-float (hi, lo), RHS tile layout
   double* taull = nullptr;         // complex Taull (interleaved)
   double* tscratch = nullptr;      // complex Taull scratch
   unsigned long long* dmax = nullptr;  // per problem max |correction| (double bits)
@@ -59,6 +62,7 @@ struct LaunchDims {
   int max_nlmso = 0;
   int max_atom_rows = 0;   // natome * max nlmsa
   int npr = 0;
+  int64_t rowv_total = 0;  // entries of the per-row vectors (sum of npad + 1)
 };
 
 void launch_assemble(const StaticDev& S, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
@@ -67,8 +71,9 @@ void launch_equilibrate_convert(const Prob* probs, const Pools& pl, Tables tb, c
 void launch_csr(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s);
 // X64 = cs * Y32 (first solve) or X64 += cs * Y32 (refinement), with max reductions.
 void launch_update_x(const Prob* probs, const Pools& pl, const LaunchDims& d, int first, cudaStream_t s);
-// Y32 = rs * (B64 - A X64) using the CSR copy of A.
-void launch_residual(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s);
+// Y32 = rs * (B64 - A X64) using the CSR copy of A, in FP64 or in double-float.
+void launch_residual(const Prob* probs, const Pools& pl, const LaunchDims& d, int df64, cudaStream_t s);
+void launch_copy_rhs(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s);
 void launch_taull(const Prob* probs, const Pools& pl, const LaunchDims& d, const double* X, cudaStream_t s);
 void launch_solution_out(const Prob& P, const double* X, double* smr_dev, cudaStream_t s);
 

@@ -145,8 +145,8 @@ __global__ void k_csr_scan(const Prob* probs, int* rowptr) {
   if (threadIdx.x == 0) rp[0] = 0;
 }
 
-__global__ void k_csr_fill(const Prob* probs, const double* env, const int* rowptr, int* col, double* val, Tables tb,
-                           int* err) {
+__global__ void k_csr_fill(const Prob* probs, const double* env, const int* rowptr, int* col, double* val, float2* val2,
+                           Tables tb, int* err) {
   const Prob P = probs[blockIdx.y];
   const int p = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x % 32;
   if (p >= P.nt * TS) return;
@@ -163,6 +163,8 @@ __global__ void k_csr_fill(const Prob* probs, const double* env, const int* rowp
         if (o < P.csr_cap) {
           col[P.csr + o] = J * TS + lane + 32 * h;
           val[P.csr + o] = v;
+          const float hi = (float)v;
+          val2[P.csr + o] = make_float2(hi, (float)(v - (double)hi));
         } else {
           atomicExch(&err[blockIdx.y], (int)FDMGPU_ERR_ARG);
         }
@@ -214,8 +216,81 @@ __global__ void k_residual(const Prob* probs, const int* rowptr, const int* col,
   if (lane == 0) atomic_max_abs(&rmax[e], rm);
 }
 
+// Double-float arithmetic (an FP64 stand-in on the FP32 pipes): a value is the
+// unevaluated sum hi + lo of two floats, about 48 significand bits.
+struct df {
+  float hi, lo;
+};
+// acc -= a * x with a = (ah, al), x = (xh, xl): the product ah*xh is split
+// exactly with an FMA, the cross terms are added at float precision, and the
+// high parts are summed with Knuth's two-sum.
+__device__ __forceinline__ void df_sub_prod(df& acc, float2 a, float2 x) {
+  const float p = a.x * x.x;
+  const float e = fmaf(a.x, x.x, -p);
+  const float t = fmaf(a.x, x.y, fmaf(a.y, x.x, e));
+  const float s = acc.hi - p;
+  const float bb = s - acc.hi;
+  const float err = (acc.hi - (s - bb)) + (-p - bb);
+  acc.hi = s;
+  acc.lo = acc.lo + (err - t);
+}
+__device__ __forceinline__ df df_norm(df a) {
+  const float s = a.hi + a.lo;
+  return df{s, a.lo - (s - a.hi)};
+}
+
+// Y32 = float(rs * (B - A X)) with A and X in double-float form.
+__global__ void k_residual_df(const Prob* probs, const int* rowptr, const int* col, const float2* val2, const double* B,
+                              const float2* Xs, float* Y, const double* rs, unsigned long long* rmax,
+                              const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (active && !active[e]) return;
+  const int p = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (p >= P.nt * TS) return;
+  const int k0 = rowptr[P.rowv + p], k1 = min(rowptr[P.rowv + p + 1], (int)P.csr_cap);
+  const int nrhs = P.nrt * TS;
+  const float sc = (float)rs[P.rowv + p];  // a power of two
+  double rm = 0.0;
+  for (int r0 = 0; r0 < nrhs; r0 += 256) {
+    df acc[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int r = r0 + lane + 32 * t;
+      const double b = (r < nrhs) ? B[P.rhs + ((int64_t)(p / TS) * P.nrt + r / TS) * TS2 + (p % TS) * TS + (r % TS)] : 0.0;
+      acc[t].hi = (float)b;
+      acc[t].lo = (float)(b - (double)acc[t].hi);
+    }
+    for (int k = k0; k < k1; ++k) {
+      const int q = col[P.csr + k];
+      const float2 a = val2[P.csr + k];
+      const float2* xr = Xs + P.rhs + ((int64_t)(q / TS) * P.nrt) * TS2 + (q % TS) * TS;
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int r = r0 + lane + 32 * t;
+        if (r < nrhs) df_sub_prod(acc[t], a, xr[(int64_t)(r / TS) * TS2 + (r % TS)]);
+      }
+      if (((k - k0) & 63) == 63) {
+#pragma unroll
+        for (int t = 0; t < 8; ++t) acc[t] = df_norm(acc[t]);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int r = r0 + lane + 32 * t;
+      if (r < nrhs) {
+        const float v = acc[t].hi + acc[t].lo;
+        rm = fmax(rm, fabs((double)v));
+        Y[P.rhs + ((int64_t)(p / TS) * P.nrt + r / TS) * TS2 + (p % TS) * TS + (r % TS)] = sc * v;
+      }
+    }
+  }
+  for (int o = 16; o; o >>= 1) rm = fmax(rm, __shfl_xor_sync(0xffffffffu, rm, o));
+  if (lane == 0) atomic_max_abs(&rmax[e], rm);
+}
+
 // X64 (+)= cs * Y32 over RHS tiles, with per-problem maxima of |d| and |x|.
-__global__ void k_update_x(const Prob* probs, const float* Y, double* X, const double* cs, int first,
+__global__ void k_update_x(const Prob* probs, const float* Y, double* X, float2* Xs, const double* cs, int first,
                            unsigned long long* dmax, unsigned long long* xmax, const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -225,11 +300,14 @@ __global__ void k_update_x(const Prob* probs, const float* Y, double* X, const d
   const int I = (int)(w / P.nrt);
   const float* y = Y + P.rhs + w * TS2;
   double* x = X + P.rhs + w * TS2;
+  float2* xs = Xs + P.rhs + w * TS2;
   double dm = 0.0, xm = 0.0;
   for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) {
     const double d = cs[P.rowv + I * TS + idx / TS] * (double)y[idx];
     const double xn = first ? d : x[idx] + d;
     x[idx] = xn;
+    const float hi = (float)xn;
+    xs[idx] = make_float2(hi, (float)(xn - (double)hi));
     dm = fmax(dm, fabs(d));
     xm = fmax(xm, fabs(xn));
   }
@@ -256,6 +334,8 @@ __global__ void k_solution_out(Prob P, const double* X, double* smr) {
 void launch_equilibrate_convert(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s) {
   const int np = d.nprob;
   k_rowscale<<<dim3((d.max_rows + 7) / 8, np), 256, 0, s>>>(probs, pl.env64, pl.rs, tb);
+  // cs first serves as the atomic column-max accumulator: it must start at 0
+  cudaMemsetAsync(pl.cs, 0, d.rowv_total * sizeof(double), s);
   k_colmax<<<dim3(d.max_tiles, np), 256, 0, s>>>(probs, pl.env64, pl.rs, reinterpret_cast<unsigned long long*>(pl.cs),
                                                  tb);
   k_colscale_finish<<<dim3((d.max_rows + 255) / 256, np), 256, 0, s>>>(probs, pl.cs);
@@ -267,17 +347,36 @@ void launch_csr(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims&
   const int np = d.nprob;
   k_csr_count<<<dim3((d.max_rows + 7) / 8, np), 256, 0, s>>>(probs, pl.env64, pl.rowptr, tb);
   k_csr_scan<<<dim3(1, np), 1024, 0, s>>>(probs, pl.rowptr);
-  k_csr_fill<<<dim3((d.max_rows + 7) / 8, np), 256, 0, s>>>(probs, pl.env64, pl.rowptr, pl.col, pl.val, tb, pl.err);
+  k_csr_fill<<<dim3((d.max_rows + 7) / 8, np), 256, 0, s>>>(probs, pl.env64, pl.rowptr, pl.col, pl.val, pl.val2, tb,
+                                                             pl.err);
 }
 
-void launch_residual(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s) {
-  k_residual<<<dim3((d.max_rows + 7) / 8, d.nprob), 256, 0, s>>>(probs, pl.rowptr, pl.col, pl.val, pl.B64, pl.X64,
-                                                                 pl.Y32, pl.rs, pl.amax, pl.active);
+void launch_residual(const Prob* probs, const Pools& pl, const LaunchDims& d, int df64, cudaStream_t s) {
+  if (df64)
+    k_residual_df<<<dim3((d.max_rows + 7) / 8, d.nprob), 256, 0, s>>>(probs, pl.rowptr, pl.col, pl.val2, pl.B64,
+                                                                      pl.Xs, pl.Y32, pl.rs, pl.amax, pl.active);
+  else
+    k_residual<<<dim3((d.max_rows + 7) / 8, d.nprob), 256, 0, s>>>(probs, pl.rowptr, pl.col, pl.val, pl.B64, pl.X64,
+                                                                   pl.Y32, pl.rs, pl.amax, pl.active);
 }
 
 void launch_update_x(const Prob* probs, const Pools& pl, const LaunchDims& d, int first, cudaStream_t s) {
-  k_update_x<<<dim3(d.max_rhs_tiles, d.nprob), 256, 0, s>>>(probs, pl.Y32, pl.X64, pl.cs, first, pl.dmax, pl.xmax,
-                                                            first ? nullptr : pl.active);
+  k_update_x<<<dim3(d.max_rhs_tiles, d.nprob), 256, 0, s>>>(probs, pl.Y32, pl.X64, pl.Xs, pl.cs, first, pl.dmax,
+                                                            pl.xmax, first ? nullptr : pl.active);
+}
+
+// X64 = B64 for the active problems (start of an FP64 re-solve).
+__global__ void k_copy_rhs(const Prob* probs, const double* B, double* X, const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (!active[e]) return;
+  const int64_t w = blockIdx.x;
+  if (w >= (int64_t)P.nt * P.nrt) return;
+  for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) X[P.rhs + w * TS2 + idx] = B[P.rhs + w * TS2 + idx];
+}
+
+void launch_copy_rhs(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s) {
+  k_copy_rhs<<<dim3(d.max_rhs_tiles, d.nprob), 256, 0, s>>>(probs, pl.B64, pl.X64, pl.active);
 }
 
 void launch_solution_out(const Prob& P, const double* X, double* smr_dev, cudaStream_t s) {

@@ -56,13 +56,17 @@ def load_library(path: str = LIB_PATH):
     L.fdmgpu_mat_solve.restype = C.c_int
     L.fdmgpu_get_solver_params.argtypes = [C.POINTER(C.c_int32), C.c_char_p]
     L.fdmgpu_get_solver_params.restype = None
+    L.fdmgpu_set_residual_mode.argtypes = [vp, C.c_int32]
+    L.fdmgpu_set_residual_mode.restype = C.c_int
     L.fdmgpu_batch_begin.argtypes = [vp, C.c_int32, C.c_int32]
     L.fdmgpu_batch_add.argtypes = [vp, vp, C.c_int32]
     L.fdmgpu_batch_run.argtypes = [vp, vp]
+    L.fdmgpu_batch_rerun.argtypes = [vp, vp]
     L.fdmgpu_batch_taull.argtypes = [vp, C.c_int32, vp, C.POINTER(C.c_int32)]
     L.fdmgpu_batch_solution.argtypes = [vp, C.c_int32, vp]
-    L.fdmgpu_batch_stats.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double)]
-    for f in ("fdmgpu_batch_begin", "fdmgpu_batch_add", "fdmgpu_batch_run", "fdmgpu_batch_taull",
+    L.fdmgpu_batch_stats.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double),
+                                     C.POINTER(C.c_int32)]
+    for f in ("fdmgpu_batch_begin", "fdmgpu_batch_add", "fdmgpu_batch_run", "fdmgpu_batch_rerun", "fdmgpu_batch_taull",
               "fdmgpu_batch_solution", "fdmgpu_batch_stats"):
         getattr(L, f).restype = C.c_int
     _lib = L
@@ -81,7 +85,8 @@ def info_dict(info: abi.FdmInfo) -> dict:
 class FdmSolver:
     """One device handle holding the static structure of a cluster."""
 
-    def __init__(self, st: CL.Structure):
+    def __init__(self, st):
+        """st: a cluster.Structure, or the grid_dict() arrays of one."""
         self.lib = load_library()
         self.st = st
         self.grid_args = abi.GridArgs(st)
@@ -89,6 +94,10 @@ class FdmSolver:
         _check(self.lib.fdmgpu_create(C.addressof(self.grid_args.s), C.byref(h)))
         self.h = h
         self._batch_args: List[abi.EnergyArgs] = []
+
+    def set_residual(self, mode: str):
+        """Residual arithmetic of the mixed path: 'df64' (default) or 'fp64'."""
+        _check(self.lib.fdmgpu_set_residual_mode(self.h, {"fp64": 0, "df64": 1}[mode]))
 
     def close(self):
         if getattr(self, "h", None):
@@ -102,28 +111,49 @@ class FdmSolver:
             pass
 
     def mat_solve(self, ei: CL.EnergyInputs, ri: CL.RowIndex, precision: str = "fp64") -> Tuple[np.ndarray, dict]:
-        ea = abi.EnergyArgs(self.st, ei, ri)
-        smr = np.zeros((ei.nlmso, ri.nligne), order="F")
+        return self.mat_solve_args(abi.EnergyArgs(self.st, ei, ri), precision)
+
+    def mat_solve_args(self, ea: abi.EnergyArgs, precision: str = "fp64") -> Tuple[np.ndarray, dict]:
+        """mat_solve on prepared arguments; returns smr (nlmso, nligne) and diagnostics."""
+        smr = np.zeros((ea.nlmso, ea.nligne), order="F")
         info = abi.FdmInfo()
-        _check(self.lib.fdmgpu_mat_solve(self.h, C.addressof(ea.s), PREC[precision], smr.ctypes.data, None,
-                                         C.addressof(info)))
-        return smr, info_dict(info)
+        st = self.lib.fdmgpu_mat_solve(self.h, C.addressof(ea.s), PREC[precision], smr.ctypes.data, None,
+                                       C.addressof(info))
+        if st not in (0, 5):
+            _check(st)
+        d = info_dict(info)
+        d["converged"] = st == 0
+        return smr, d
 
     def spectrum_begin(self, precision: str, n: int):
         _check(self.lib.fdmgpu_batch_begin(self.h, PREC[precision], n))
         self._batch_args = []
 
     def spectrum_add(self, ei: CL.EnergyInputs, ri: CL.RowIndex, iaabs: int = 1):
-        ea = abi.EnergyArgs(self.st, ei, ri)
-        _check(self.lib.fdmgpu_batch_add(self.h, C.addressof(ea.s), iaabs))
-        self._batch_args.append(ea)
+        self.spectrum_add_args(abi.EnergyArgs(self.st, ei, ri), iaabs)
 
     def spectrum_add_args(self, ea: abi.EnergyArgs, iaabs: int = 1):
         _check(self.lib.fdmgpu_batch_add(self.h, C.addressof(ea.s), iaabs))
+        self._batch_args.append(ea)
 
     def spectrum_run(self) -> dict:
+        """Run the batch.  Energies whose refinement missed its tolerance are
+        reported in ``info['not_converged']`` (their results stay readable)."""
         info = abi.FdmInfo()
-        _check(self.lib.fdmgpu_batch_run(self.h, C.addressof(info)))
+        st = self.lib.fdmgpu_batch_run(self.h, C.addressof(info))
+        if st not in (0, 5):
+            _check(st)
+        d = info_dict(info)
+        d["not_converged"] = [k for k in range(len(self._batch_args) or 0)
+                              if self.lib.fdmgpu_batch_stats(self.h, k, None, None, None) == 5]
+        return d
+
+    def spectrum_rerun(self) -> dict:
+        """Run the last batch again on the inputs already in device memory."""
+        info = abi.FdmInfo()
+        st = self.lib.fdmgpu_batch_rerun(self.h, C.addressof(info))
+        if st not in (0, 5):
+            _check(st)
         return info_dict(info)
 
     def taull(self, k: int) -> np.ndarray:
@@ -138,11 +168,16 @@ class FdmSolver:
         _check(self.lib.fdmgpu_batch_solution(self.h, k, smr.ctypes.data))
         return smr
 
-    def stats(self, k: int) -> Tuple[int, float]:
+    def stats(self, k: int) -> Tuple[int, float, bool]:
+        """Refinement iterations, final relative correction and whether energy k
+        was solved again in FP64 (precision escalation)."""
         it = C.c_int32(0)
         r = C.c_double(0)
-        _check(self.lib.fdmgpu_batch_stats(self.h, k, C.byref(it), C.byref(r)))
-        return it.value, r.value
+        fb = C.c_int32(0)
+        st = self.lib.fdmgpu_batch_stats(self.h, k, C.byref(it), C.byref(r), C.byref(fb))
+        if st not in (0, 5):
+            _check(st)
+        return it.value, r.value, bool(fb.value)
 
     def spectrum(self, items: Sequence[Tuple[CL.EnergyInputs, CL.RowIndex]], precision: str = "mixed",
                  iaabs: int = 1):

@@ -49,6 +49,13 @@ typedef enum {
   FDMGPU_PREC_MIXED = 1        /* FP32 profile LU + FP64 residual and refinement       */
 } fdmgpu_precision;
 
+/* Arithmetic of the refinement residual b - A x in the mixed precision path. */
+typedef enum {
+  FDMGPU_RESIDUAL_FP64 = 0,    /* native FP64                                          */
+  FDMGPU_RESIDUAL_DF64 = 1     /* double-float (hi + lo float pairs, ~48 bits) on the
+                                  FP32 pipes: the default, GB300 FP64 is ~60x slower    */
+} fdmgpu_residual_mode;
+
 /* Energy-independent arguments of mat_solve (source/mat_solve_gaussian.f90:17-67). */
 typedef struct fdmgpu_grid {
   int32_t npoint;     /* grid points inside the FDM sphere                                   */
@@ -142,6 +149,9 @@ typedef struct fdmgpu_info {
   int32_t refine_iters;     /* refinement iterations used (mixed precision)                  */
   double residual;          /* final max_k ||b_k - A x_k|| / ||b_k||                          */
   double ms_assemble, ms_factor, ms_solve, ms_refine;   /* device time per phase             */
+  int32_t n_fallback;       /* problems solved again in FP64 after the mixed path missed its
+                               tolerance (precision escalation)                               */
+  int64_t n_kernels;        /* kernels launched by the call (graph kernel nodes included)     */
 } fdmgpu_info;
 
 /* Library version string. */
@@ -166,6 +176,10 @@ void fdmgpu_destroy(fdmgpu_handle* h);
 fdmgpu_status fdmgpu_mat_solve(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t precision,
                                double* smr, double* smi, fdmgpu_info* info);
 
+/* Residual arithmetic of the mixed precision refinement (default DF64).
+ * No counterpart in the reference, which solves in FP64 only. */
+fdmgpu_status fdmgpu_set_residual_mode(fdmgpu_handle* h, int32_t mode);
+
 /* Counterpart of getSolverParams (source/mat_solve_gaussian.f90:376-389,
  * source/mat_solve_mumps.f90:705-736): solver name "GPU" and group size 1. */
 void fdmgpu_get_solver_params(int32_t* mpi_host_num_for_mumps, char solver[6]);
@@ -181,12 +195,19 @@ void fdmgpu_get_solver_params(int32_t* mpi_host_num_for_mumps, char solver[6]);
 fdmgpu_status fdmgpu_batch_begin(fdmgpu_handle* h, int32_t precision, int32_t max_energies);
 fdmgpu_status fdmgpu_batch_add(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t iaabs);
 fdmgpu_status fdmgpu_batch_run(fdmgpu_handle* h, fdmgpu_info* info);
+/* Run the last batch again on the inputs already in device memory (no host
+ * copies): the device-resident timing of a spectrum.  No counterpart in the
+ * reference. */
+fdmgpu_status fdmgpu_batch_rerun(fdmgpu_handle* h, fdmgpu_info* info);
 /* Taull of energy k (0-based, in add order): writes nlm*nlm complex values. */
 fdmgpu_status fdmgpu_batch_taull(fdmgpu_handle* h, int32_t k, double* taull, int32_t* nlm);
 /* Solution of energy k (nlmso, nligne) column-major into smr (host). */
 fdmgpu_status fdmgpu_batch_solution(fdmgpu_handle* h, int32_t k, double* smr);
-/* Per-energy refinement diagnostics of the last run: iterations and residual. */
-fdmgpu_status fdmgpu_batch_stats(fdmgpu_handle* h, int32_t k, int32_t* iters, double* residual);
+/* Per-energy diagnostics of the last run: refinement iterations, final
+ * relative correction max|dx|/max|x|, and whether the energy was solved again
+ * in FP64.  Returns the energy's status (FDMGPU_OK when it converged). */
+fdmgpu_status fdmgpu_batch_stats(fdmgpu_handle* h, int32_t k, int32_t* iters, double* residual,
+                                 int32_t* fallback);
 
 #ifdef __cplusplus
 }

@@ -1,0 +1,140 @@
+"""GPU parity of the CUDA path with the oracle, through the C-ABI.
+
+Tolerances:
+* golden / small problems (well conditioned): FP64 GPU vs oracle <= 1e-10
+  relative (max |diff| / max |ref|), the spec bar;
+* mixed precision vs oracle <= 1e-8 (double-float residual floor) and
+  <= 1e-10 with the FP64 residual;
+* the full 13-atom Cu matrix has condition number ~1e10 (measured), so two
+  FP64 eliminations of it differ by up to ~1e-8: there the size-independent
+  check is the normwise backward error of the GPU solution (<= 1e-14) and the
+  convolved cross-section of the mixed path vs FP64 (<= 1e-6).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def solver_mod():
+    from fdmnes_gb300 import build
+    build.build()
+    from fdmnes_gb300 import solver
+    return solver
+
+
+def test_golden_fp64_matches_oracle(solver_mod, golden):
+    from fdmnes_gb300 import abi
+    grid, energies = golden
+    sv = solver_mod.FdmSolver(grid)
+    for e in energies:
+        X, info = sv.mat_solve_args(abi.EnergyArgs(e), "fp64")
+        assert rel(X, e["smr"]) < 1e-10
+        assert info["n_kernels"] > 0
+    sv.spectrum_begin("fp64", len(energies))
+    for e in energies:
+        sv.spectrum_add_args(abi.EnergyArgs(e), 1)
+    sv.spectrum_run()
+    for k, e in enumerate(energies):
+        assert rel(sv.taull(k), e["taull"]) < 1e-10
+    sv.close()
+
+
+def test_golden_mixed_matches_oracle(solver_mod, golden):
+    from fdmnes_gb300 import abi
+    grid, energies = golden
+    sv = solver_mod.FdmSolver(grid)
+    for mode, tol in (("df64", 1e-8), ("fp64", 1e-10)):
+        sv.set_residual(mode)
+        for e in energies:
+            X, info = sv.mat_solve_args(abi.EnergyArgs(e), "mixed")
+            assert info["converged"]
+            assert rel(X, e["smr"]) < tol, (mode, rel(X, e["smr"]))
+    sv.close()
+
+
+def test_small_cluster_energies(solver_mod, oracle_lib):
+    from fdmnes_gb300 import abi, cluster as CL
+    st = CL.small_cu_structure()
+    ga = abi.GridArgs(st)
+    sv = solver_mod.FdmSolver(st)
+    for E in (-5.0, 3.0, 12.0, 27.0, 35.0):
+        ei = CL.energy_inputs(st, E)
+        ri = CL.newind(st, ei.nlmsa, ei.nlmso)
+        ea = abi.EnergyArgs(st, ei, ri)
+        Xo, _ = oracle_lib.mat_solve(ga, ea)
+        X, _ = sv.mat_solve(ei, ri, "fp64")
+        assert rel(X, Xo) < 1e-10, (E, rel(X, Xo))
+        To = oracle_lib.taull(ga, ea, Xo)
+        T, _ = sv.spectrum([(ei, ri)], "fp64")
+        assert rel(T[0], To) < 1e-10
+    sv.close()
+
+
+def test_full_cu_backward_error(solver_mod, oracle_lib):
+    """Normwise backward error ||B - A X|| / (||A|| ||X|| + ||B||) of the GPU
+    solution on the full 13-atom cluster, independent of its conditioning."""
+    from fdmnes_gb300 import abi, cluster as CL
+    st = CL.cu_structure()
+    ga = abi.GridArgs(st)
+    sv = solver_mod.FdmSolver(st)
+    ei = CL.energy_inputs(st, 10.0)
+    ri = CL.newind(st, ei.nlmsa, ei.nlmso)
+    ea = abi.EnergyArgs(st, ei, ri)
+    A, B = oracle_lib.assemble_dense(ga, ea)
+    nA = np.abs(A).sum(1).max()
+    for prec in ("fp64", "mixed"):
+        X, info = sv.mat_solve(ei, ri, prec)
+        R = B.T - A @ X.T
+        eta = np.abs(R).sum(0).max() / (nA * np.abs(X.T).sum(0).max() + np.abs(B.T).sum(0).max())
+        assert eta < 1e-14, (prec, eta)
+    sv.close()
+
+
+def test_spectrum_mixed_vs_fp64_cross_section(solver_mod):
+    from fdmnes_gb300 import cluster as CL, xanes
+    st = CL.cu_structure()
+    energies = np.linspace(-5.0, 35.0, 9)
+    items = xanes.spectrum_inputs(st, energies)
+    sv = solver_mod.FdmSolver(st)
+    T64, _ = sv.spectrum(items, "fp64")
+    Tm, info = sv.spectrum(items, "mixed")
+    assert xanes.convolved_relative_error(energies, Tm, T64) < 1e-6
+    # a replay of the same batch is bit-identical
+    info2 = sv.spectrum_rerun()
+    Tm2 = [sv.taull(k) for k in range(len(items))]
+    assert all(np.array_equal(a, b) for a, b in zip(Tm, Tm2))
+    assert info2["n_kernels"] == info["n_kernels"]
+    sv.close()
+
+
+def test_error_paths_keep_the_context_usable(solver_mod, golden):
+    """Failures are injected on the host (bad flags, bad profile, singular
+    input); the library returns a status and the next solve still works."""
+    from fdmnes_gb300 import abi
+    grid, energies = golden
+    sv = solver_mod.FdmSolver(grid)
+    e = dict(energies[0])
+    bad = dict(e, Spinorbite=1)
+    with pytest.raises(solver_mod.FdmError) as ex:
+        sv.mat_solve_args(abi.EnergyArgs(bad), "fp64")
+    assert ex.value.status == 2
+    lb1 = np.array(e["lb1"]).copy()
+    lb1[0] = 5  # row 1's profile no longer contains its diagonal
+    with pytest.raises(solver_mod.FdmError) as ex:
+        sv.mat_solve_args(abi.EnergyArgs(dict(e, lb1=lb1)), "fp64")
+    assert ex.value.status == 1
+    # singular matrix: all atomic boundary functions zero -> atom columns vanish
+    sing = dict(e, phiato=np.zeros_like(e["phiato"]))
+    with pytest.raises(solver_mod.FdmError) as ex:
+        sv.mat_solve_args(abi.EnergyArgs(sing), "fp64")
+    assert ex.value.status == 4
+    X, _ = sv.mat_solve_args(abi.EnergyArgs(e), "fp64")
+    assert rel(X, e["smr"]) < 1e-10
+    with pytest.raises(solver_mod.FdmError):
+        sv.spectrum_begin("fp64", 1)
+        sv.spectrum_rerun()
+    sv.close()

@@ -1,0 +1,149 @@
+"""CPU tests of the oracle restatement and of the input builders.
+
+The reference ships no tests or golden outputs and cannot be compiled here
+(Fortran), so the oracle is pinned by known-answer tests: exact stencil
+coefficients, closed-form/scipy special functions, a dense LU solve of the
+same assembled matrix, and committed golden outputs (tests/golden).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel
+from fdmnes_gb300 import abi, cluster as CL, xanes
+
+
+def test_stencil_coefficients_and_exactness():
+    st = CL.small_cu_structure()
+    g = st.grid
+    h = g.adimp
+    # source/general.f90:9758-9790: clapl = (4/3 h^2) {1, -1/16}, clapl(0) = -7.5/h^2
+    assert np.allclose(g.clapl[1:7], 4.0 / 3.0 / h ** 2, rtol=0, atol=1e-12)
+    assert np.allclose(g.clapl[7:13], -1.0 / 12.0 / h ** 2, rtol=0, atol=1e-12)
+    assert abs(g.clapl[0] + 7.5 / h ** 2) < 1e-12
+    # 4th-order Laplacian: exact on polynomials up to degree 5
+    offs = [(-1, 0, 0), (1, 0, 0), (0, -1, 0), (0, 1, 0), (0, 0, -1), (0, 0, 1),
+            (-2, 0, 0), (2, 0, 0), (0, -2, 0), (0, 2, 0), (0, 0, -2), (0, 0, 2)]
+    rng = np.random.default_rng(0)
+    x0 = rng.standard_normal(3)
+    for _ in range(5):
+        c = rng.standard_normal(6)
+        f = lambda p: c[0] * p[0] ** 5 + c[1] * p[1] ** 4 * p[0] + c[2] * p[2] ** 3 + c[3] * p[0] * p[1] * p[2] ** 2 \
+            + c[4] * p[1] ** 2 + c[5]
+        lap = (c[0] * 20 * x0[0] ** 3 + c[1] * 12 * x0[1] ** 2 * x0[0] + c[2] * 6 * x0[2]
+               + c[3] * 2 * x0[0] * x0[1] + c[4] * 2)
+        s = g.clapl[0] * f(x0) + sum(g.clapl[iv + 1] * f(x0 + h * np.array(o)) for iv, o in enumerate(offs))
+        assert abs(s - lap) < 1e-8 * max(1.0, abs(lap))
+
+
+def test_bessel_known_answers(oracle_lib):
+    d = np.load(CL.__file__.replace("fdmnes_gb300/cluster.py", "tests/golden/kat_special.npz"))
+    z, fnorm, jn, yn = d["z"], float(d["fnorm"]), d["jn"], d["yn"]
+    lmax = jn.shape[1] - 1
+    bs, nm = CL.cbessneur(fnorm, z, lmax)
+    for i, zz in enumerate(z):
+        lstable = int(max(1, zz))  # upward recursion of j_l is stable for l <~ z
+        assert np.allclose(bs[i, :lstable + 1], jn[i, :lstable + 1], rtol=1e-9, atol=0)
+        assert np.allclose(nm[i], yn[i], rtol=1e-10, atol=0)
+        b2, n2 = oracle_lib.cbessneur(fnorm, zz, lmax)
+        assert np.allclose(b2, bs[i], rtol=1e-13, atol=1e-300)
+        assert np.allclose(n2, nm[i], rtol=1e-13, atol=1e-300)
+    # closed forms of l = 0, 1
+    zz = 2.3
+    b, n = CL.cbessneur(1.0, np.array([zz]), 1)
+    assert abs(b[0, 0] - np.sin(zz) / zz) < 1e-15
+    assert abs(n[0, 1] - (-np.cos(zz) / zz ** 2 - np.sin(zz) / zz)) < 1e-15
+
+
+def test_real_harmonics_known_answers():
+    d = np.load(CL.__file__.replace("fdmnes_gb300/cluster.py", "tests/golden/kat_special.npz"))
+    y = CL.real_ylm(int(d["lmax_y"]), d["v"])
+    assert np.abs(y - d["ylm"]).max() < 1e-12
+
+
+def test_exchange_sort_matches_reference_rule():
+    rng = np.random.default_rng(3)
+    key = rng.integers(0, 6, size=60)
+    # brute-force restatement of source/general.f90:9529-9543 on integer keys
+    a = list(key)
+    idx = list(range(len(a)))
+    for i in range(len(a)):
+        for j in range(i + 1, len(a)):
+            if a[i] <= a[j]:
+                continue
+            a[i], a[j] = a[j], a[i]
+            idx[i], idx[j] = idx[j], idx[i]
+    assert list(CL._exchange_sort(key)) == idx
+
+
+def test_grid_sizes_of_cu_cluster():
+    st = CL.cu_structure()
+    g = st.grid
+    assert st.natome == 13
+    assert g.npoint == 7153 and g.npr == 4472
+    assert g.nbordf[0] > 0 and g.nsortf > 0
+
+
+def test_radial_solution_free_space():
+    # V = 0: the regular solution is proportional to r j_l(k r)
+    from scipy.special import spherical_jn
+    r = CL.radial_mesh(29, 4.0)
+    for L in range(4):
+        ec = 1.3
+        R = CL.sch_radial(r, np.zeros_like(r), ec, ec, L, 0.0)
+        sel = (r > 0.5) & (r < 2.0)
+        ratio = R[sel] / spherical_jn(L, np.sqrt(ec) * r[sel])
+        assert np.std(ratio) / abs(np.mean(ratio)) < 2e-3
+
+
+def test_newind_matches_oracle(oracle_lib):
+    st = CL.small_cu_structure()
+    ga = abi.GridArgs(st)
+    for E in (-5.0, 20.0):
+        ei = CL.energy_inputs(st, E)
+        ri = CL.newind(st, ei.nlmsa, ei.nlmso)
+        new, newinv, ianew, lb1, lb2 = oracle_lib.newind(ga, st.grid.xyz[3], st.distai, ei.nlmsa, ei.nlmso,
+                                                        ri.nligne, st.grid.npoint, st.natome)
+        assert (new == ri.new).all() and (newinv == ri.newinv).all() and (ianew == ri.ianew).all()
+        assert (lb1 == ri.lb1).all() and (lb2 == ri.lb2).all()
+
+
+def test_golden_oracle_reproduces(oracle_lib, golden):
+    grid, energies = golden
+    ga = abi.GridArgs(grid)
+    for e in energies:
+        ea = abi.EnergyArgs(e)
+        X, _ = oracle_lib.mat_solve(ga, ea)
+        assert np.array_equal(X, e["smr"])
+        T = oracle_lib.taull(ga, ea, X)
+        assert rel(T, e["taull"]) < 1e-13
+
+
+def test_gaussian_solver_against_dense_lu(oracle_lib, golden):
+    """Known-answer test: the restated no-pivot profile solver equals a dense
+    LAPACK solve of the same assembled matrix (tiny, well-conditioned case)."""
+    grid, energies = golden
+    for e in energies:
+        assert rel(e["smr"], e["dense_solution"]) < 1e-10
+    ga = abi.GridArgs(grid)
+    ea = abi.EnergyArgs(energies[0])
+    A, B = oracle_lib.assemble_dense(ga, ea)
+    X = np.linalg.solve(A, B.T).T
+    assert rel(X, energies[0]["smr"]) < 1e-10
+
+
+def test_invcomp_against_numpy(oracle_lib):
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal((40, 40)) + 1j * rng.standard_normal((40, 40))
+    assert rel(oracle_lib.invcomp(a), np.linalg.inv(a)) < 1e-11
+
+
+def test_lorentzian_convolution():
+    E = np.linspace(-5, 35, 401)
+    out = xanes.lorentzian_convolve(E, np.ones_like(E), 0.8)
+    mid = (E > 5) & (E < 25)
+    assert np.allclose(out[mid], 1.0, atol=0.05)
+    # a single bin is spread as the Lorentzian integral over that bin
+    x = np.zeros_like(E)
+    x[200] = 1.0
+    out = xanes.lorentzian_convolve(E, x, 0.8)
+    assert abs(out.sum() * 0.1 / 0.1 - 1.0) < 0.1 and np.argmax(out) == 200
