@@ -81,6 +81,7 @@ struct Batch {
   // results
   std::vector<int> iters;
   std::vector<int> fallback;   // solved again in FP64 after the mixed path missed its tolerance
+  std::vector<int> inner;      // GMRES steps summed over the refinement
   std::vector<double> resid;
   std::vector<int> err;
   bool ran = false;
@@ -111,9 +112,18 @@ struct fdmgpu_handle {
   DevBuf<int> d_ipool;
   DevBuf<double> d_dpool;
   DevBuf<double> d_env64, d_B64, d_X64, d_rs, d_cs, d_val, d_taull, d_tscratch, d_smr;
-  DevBuf<float> d_env32, d_Y32;
+  DevBuf<float> d_env32, d_Y32, d_dinv32;
+  DevBuf<double> d_dinv64;
   DevBuf<float2> d_val2, d_Xs;
+  DevBuf<float> d_valS, d_V, d_W;
+  DevBuf<unsigned char> d_gstate;
+  DevBuf<int> d_inner, d_jdone, d_notconv, d_active_gm;
   int residual_df64 = 1;
+  int refine_gmres = 0;   // GMRES-IR (1) or classical refinement (0)
+  int escalate_dfl = 1;   // escalation by a double-float (1) or an FP64 (0) factorisation
+  int gmres_m = 12;       // Krylov dimension of one GMRES cycle
+  int64_t ncols = 0;      // right-hand-side columns of the batch (sum of nrt * TS)
+  int64_t ncols_tmp = 0;
   DevBuf<int> d_rowptr, d_col, d_err, d_active, d_piv;
   DevBuf<unsigned long long> d_red;  // dmax | xmax | amax
   int* h_pinned_i = nullptr;
@@ -326,7 +336,7 @@ void build_step_plan(fdmgpu_handle* h) {
 // Runs on every batch (the descriptors are rebuilt by fdmgpu_batch_add);
 // allocate_and_upload_plan() below runs only when the plan changes.
 struct Layout {
-  int64_t env = 0, rhs = 0, rowv = 0, csr = 0, taull = 0, scratch = 0;
+  int64_t env = 0, rhs = 0, rowv = 0, csr = 0, taull = 0, scratch = 0, dinv = 0;
   std::vector<int> J0, J1, Imax, Imin;
   std::vector<int64_t> strip;
 };
@@ -336,11 +346,12 @@ void layout_batch(fdmgpu_handle* h, Layout& L) {
   const int np = (int)pr.size();
   const bool mixed = h->batch.precision == FDMGPU_PREC_MIXED;
   int64_t& env = L.env; int64_t& rhs = L.rhs; int64_t& rowv = L.rowv;
-  int64_t& csr = L.csr; int64_t& taull = L.taull; int64_t& scratch = L.scratch;
+  int64_t& csr = L.csr; int64_t& taull = L.taull; int64_t& scratch = L.scratch; int64_t& dinv = L.dinv;
   int trow = 0;
   LaunchDims& d = h->dims;
   d = LaunchDims();
   d.nprob = np;
+  h->ncols_tmp = 0;
   d.npr = h->S.npr;
   std::vector<int>& J0 = L.J0; std::vector<int>& J1 = L.J1;
   std::vector<int>& Imax = L.Imax; std::vector<int>& Imin = L.Imin;
@@ -353,8 +364,12 @@ void layout_batch(fdmgpu_handle* h, Layout& L) {
     P.rowv = rowv;
     P.csr = csr;
     P.csr_cap = mixed ? hp.nnz_cap : 0;
+    P.csr_col = h->ncols_tmp;
+    h->ncols_tmp += (int64_t)P.nrt * TS;
     P.taull = taull;
     P.scratch = scratch;
+    P.dinv = dinv;
+    dinv += (int64_t)2 * P.nt * TS2;
     trow += P.nt + 1;
     env += hp.ntiles;
     rhs += (int64_t)P.nt * P.nrt * TS2;
@@ -374,6 +389,7 @@ void layout_batch(fdmgpu_handle* h, Layout& L) {
     d.max_atom_rows = std::max(d.max_atom_rows, h->g.natome * hp.nlmsa_max);
   }
   d.rowv_total = rowv;
+  h->ncols = h->ncols_tmp;
 }
 
 // Allocate the device pools of the batch and upload the plan tables.
@@ -391,6 +407,7 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   CK(upload(h->d_Imin, Imin, s));
   CK(upload(h->d_strip, strip, s));
   if (h->d_env64.reserve((size_t)env * TS2) != cudaSuccess || h->d_B64.reserve(rhs) != cudaSuccess ||
+      h->d_dinv64.reserve(L.dinv) != cudaSuccess ||
       h->d_X64.reserve(rhs) != cudaSuccess || h->d_err.reserve(np) != cudaSuccess ||
       h->d_active.reserve(np) != cudaSuccess || h->d_red.reserve(3 * (size_t)np) != cudaSuccess ||
       h->d_taull.reserve(2 * (size_t)std::max<int64_t>(taull, 1)) != cudaSuccess ||
@@ -398,10 +415,15 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
     return fail(FDMGPU_ERR_NOMEM, "device allocation of the batch pools failed");
   if (mixed) {
     if (h->d_env32.reserve((size_t)env * TS2) != cudaSuccess || h->d_Y32.reserve(rhs) != cudaSuccess ||
+        h->d_dinv32.reserve(L.dinv) != cudaSuccess ||
         h->d_rs.reserve(rowv) != cudaSuccess || h->d_cs.reserve(rowv) != cudaSuccess ||
         h->d_rowptr.reserve(rowv) != cudaSuccess || h->d_col.reserve(csr) != cudaSuccess ||
         h->d_piv.reserve(rowv) != cudaSuccess || h->d_val2.reserve(csr) != cudaSuccess ||
-        h->d_Xs.reserve(rhs) != cudaSuccess ||
+        h->d_Xs.reserve(rhs) != cudaSuccess || h->d_valS.reserve(csr) != cudaSuccess ||
+        h->d_V.reserve((size_t)(h->gmres_m + 1) * rhs) != cudaSuccess || h->d_W.reserve(rhs) != cudaSuccess ||
+        h->d_gstate.reserve(gmres_state_bytes() * (size_t)std::max<int64_t>(h->ncols, 1)) != cudaSuccess ||
+        h->d_inner.reserve(np) != cudaSuccess || h->d_jdone.reserve(np) != cudaSuccess ||
+        h->d_notconv.reserve(np) != cudaSuccess || h->d_active_gm.reserve(np) != cudaSuccess ||
         h->d_val.reserve(csr) != cudaSuccess)
       return fail(FDMGPU_ERR_NOMEM, "device allocation of the mixed precision pools failed");
   }
@@ -413,6 +435,7 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   Pools& pl = h->pl;
   pl = Pools();
   pl.env64 = h->d_env64.p;
+  pl.dinv64 = h->d_dinv64.p;
   pl.B64 = h->d_B64.p;
   pl.X64 = h->d_X64.p;
   pl.err = h->d_err.p;
@@ -424,6 +447,7 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   pl.tscratch = h->d_tscratch.p;
   if (mixed) {
     pl.env32 = h->d_env32.p;
+    pl.dinv32 = h->d_dinv32.p;
     pl.Y32 = h->d_Y32.p;
     pl.rs = h->d_rs.p;
     pl.cs = h->d_cs.p;
@@ -431,6 +455,15 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
     pl.piv = h->d_piv.p;
     pl.val2 = h->d_val2.p;
     pl.Xs = h->d_Xs.p;
+    pl.valS = h->d_valS.p;
+    pl.V = h->d_V.p;
+    pl.vstride = rhs;
+    pl.W = h->d_W.p;
+    pl.gstate = h->d_gstate.p;
+    pl.inner_active = h->d_inner.p;
+    pl.active_gm = h->d_active_gm.p;
+    pl.jdone = h->d_jdone.p;
+    pl.notconv = h->d_notconv.p;
     pl.col = h->d_col.p;
     pl.val = h->d_val.p;
   }
@@ -506,6 +539,8 @@ void record_asm(fdmgpu_handle* h) {
   } else {
     launch_csr(probs, pl, h->tb, h->dims, s);
     launch_equilibrate_convert(probs, pl, h->tb, h->dims, s);
+    launch_csr_scale(probs, pl, h->dims, s);
+    cudaMemsetAsync(pl.notconv, 0, np * sizeof(int), s);
   }
 }
 
@@ -514,9 +549,9 @@ void record_factor(fdmgpu_handle* h) {
   const Pools& pl = h->pl;
   const int np = h->dims.nprob;
   if (h->batch.precision == FDMGPU_PREC_FP64)
-    launch_factor<double>(h->sp, pl.env64, pl.X64, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-10, nullptr, s);
+    launch_factor<double>(h->sp, pl.env64, pl.X64, pl.dinv64, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-10, nullptr, s);
   else
-    launch_factor<float>(h->sp, pl.env32, pl.Y32, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-30, pl.piv, s);
+    launch_factor<float>(h->sp, pl.env32, pl.Y32, pl.dinv32, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-30, pl.piv, s);
 }
 
 void record_solve(fdmgpu_handle* h) {
@@ -524,9 +559,9 @@ void record_solve(fdmgpu_handle* h) {
   const Pools& pl = h->pl;
   const int np = h->dims.nprob;
   if (h->batch.precision == FDMGPU_PREC_FP64) {
-    launch_backward<double>(h->sp, pl.env64, pl.X64, h->d_probs.p, h->tb, np, nullptr, s);
+    launch_backward<double>(h->sp, pl.env64, pl.X64, pl.dinv64, h->d_probs.p, h->tb, np, nullptr, s);
   } else {
-    launch_backward<float>(h->sp, pl.env32, pl.Y32, h->d_probs.p, h->tb, np, nullptr, s);
+    launch_backward<float>(h->sp, pl.env32, pl.Y32, pl.dinv32, h->d_probs.p, h->tb, np, nullptr, s);
     cudaMemsetAsync(pl.dmax, 0, 3 * np * sizeof(unsigned long long), s);
     launch_update_x(h->d_probs.p, pl, h->dims, 1, s);
   }
@@ -539,8 +574,12 @@ void record_iter(fdmgpu_handle* h) {
   const int np = h->dims.nprob;
   cudaMemsetAsync(pl.dmax, 0, 3 * np * sizeof(unsigned long long), s);
   launch_residual(probs, pl, h->dims, h->residual_df64, s);
-  launch_forward<float>(h->sp, pl.env32, pl.Y32, probs, h->tb, np, pl.active, pl.piv, s);
-  launch_backward<float>(h->sp, pl.env32, pl.Y32, probs, h->tb, np, pl.active, s);
+  if (h->refine_gmres) {
+    launch_gmres_cycle(h->sp, probs, pl, h->tb, h->dims, h->gmres_m, 1e-6f, s);
+  } else {
+    launch_forward<float>(h->sp, pl.env32, pl.Y32, pl.dinv32, probs, h->tb, np, pl.active, pl.piv, s);
+    launch_backward<float>(h->sp, pl.env32, pl.Y32, pl.dinv32, probs, h->tb, np, pl.active, s);
+  }
   launch_update_x(probs, pl, h->dims, 0, s);
 }
 
@@ -578,6 +617,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   fdmgpu_status st;
   cudaGetLastError();  // clear a stale error of an earlier call on this thread
   sig = mix(sig, (uint64_t)h->residual_df64);
+  sig = mix(sig, (uint64_t)(h->refine_gmres * 1000 + h->gmres_m));
   const bool replan = sig != h->plan_sig || b.precision != h->plan_prec || !h->g_asm;
   Layout lay;
   layout_batch(h, lay);
@@ -596,7 +636,9 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   const void* ptrs[] = {h->d_probs.p, h->d_ipool.p, h->d_dpool.p, h->d_env64.p, h->d_env32.p, h->d_B64.p,
                         h->d_X64.p,   h->d_Y32.p,   h->d_rs.p,    h->d_cs.p,    h->d_rowptr.p, h->d_col.p,
                         h->d_val.p,   h->d_err.p,   h->d_active.p, h->d_red.p,  h->d_J0.p,   h->d_strip.p,
-                        h->d_piv.p,   h->d_val2.p,  h->d_Xs.p};
+                        h->d_piv.p,   h->d_val2.p,  h->d_Xs.p,    h->d_valS.p,  h->d_V.p,    h->d_W.p,
+                        h->d_gstate.p, h->d_inner.p, h->d_jdone.p, h->d_notconv.p, h->d_dinv64.p,
+                        h->d_dinv32.p, h->d_active_gm.p};
   for (const void* q : ptrs) ps = mix(ps, (uint64_t)(uintptr_t)q);
   if (replan || ps != h->ptr_sig) {
     h->ptr_sig = ps;
@@ -623,30 +665,42 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   int64_t nkern = h->nk_asm + h->nk_fac + h->nk_sol;
   b.iters.assign(np, 0);
   b.fallback.assign(np, 0);
+  b.inner.assign(np, 0);
   b.resid.assign(np, 0.0);
   b.err.assign(np, 0);
   float ms_refine = 0;
   if (b.precision == FDMGPU_PREC_MIXED) {
-    // Stop a problem when its relative correction max|dx|/max|x| is below tol,
-    // or when it stagnates (no halving for two steps: the residual arithmetic's
-    // floor); accept the result if the last correction is below tol_accept.
-    const int max_iter = 30;
+    // Per problem: classical refinement x += LU^-1 r while it contracts (a step
+    // counts as slow when the correction does not halve); after two slow steps
+    // the problem switches to GMRES-IR cycles (when enabled); two slow GMRES
+    // cycles stop it.  A batched classical step costs about 1/300 of an FP64
+    // re-factorisation per problem, so slow convergence is preferred to
+    // escalation.  Stop at max|dx|/max|x| <= tol; results above tol_accept go
+    // to the FP64 escalation below.
+    const int max_iter = 40;
     const double tol = 1e-10;
     const double tol_accept = h->residual_df64 ? 1e-7 : 1e-9;
-    std::vector<int> active(np, 1), slow(np, 0);
+    std::vector<int> active(np, 1), slow(np, 0), gm(np, 0);
     std::vector<double> prev(np, 1e300);
     std::vector<unsigned long long> red(3 * np);
+    std::vector<int> jd(np, 0);
     CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    if (h->refine_gmres)
+      CK(cudaMemsetAsync(h->d_active_gm.p, 0, np * sizeof(int), h->stream));
     CK(cudaEventRecord(h->ev[4], h->stream));
     for (int it = 1; it <= max_iter; ++it) {
       CK(cudaGraphLaunch(h->g_iter, h->stream));
       nkern += h->nk_iter;
       CK(cudaMemcpyAsync(red.data(), h->d_red.p, 3 * np * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                          h->stream));
+      if (h->refine_gmres)
+        CK(cudaMemcpyAsync(jd.data(), h->d_jdone.p, np * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
       CK(cudaStreamSynchronize(h->stream));
       int nact = 0;
+      bool gm_changed = false;
       for (int k = 0; k < np; ++k) {
         if (!active[k]) continue;
+        if (gm[k]) b.inner[k] += jd[k];
         double dm, xm;
         memcpy(&dm, &red[k], 8);
         memcpy(&xm, &red[np + k], 8);
@@ -656,14 +710,30 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
         if (!std::isfinite(r) || r <= tol) {
           active[k] = 0;
         } else {
-          slow[k] = r > 0.5 * prev[k] ? slow[k] + 1 : 0;
-          if (slow[k] >= 2) active[k] = 0;
-          else ++nact;
+          slow[k] = (it > 1 && r > 0.5 * prev[k]) ? slow[k] + 1 : 0;
+          if (slow[k] >= 2) {
+            if (h->refine_gmres && !gm[k] && r > tol_accept * 1e-2) {
+              gm[k] = 1;
+              slow[k] = 0;
+              gm_changed = true;
+              ++nact;
+            } else {
+              active[k] = 0;
+            }
+          } else {
+            ++nact;
+          }
         }
         prev[k] = r;
       }
       if (nact == 0) break;
       CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+      if (gm_changed || h->refine_gmres) {
+        std::vector<int> agm(np);
+        for (int k = 0; k < np; ++k) agm[k] = active[k] && gm[k];
+        CK(cudaMemcpyAsync(h->d_active_gm.p, agm.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+      }
     }
     // Precision escalation: problems whose refinement missed tol_accept are
     // factorised again in FP64 (their FP64 band is still intact) and solved.
@@ -674,12 +744,34 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
     }
     if (nfail > 0) {
       CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
-      launch_copy_rhs(h->d_probs.p, h->pl, h->dims, h->stream);
-      nkern += 1 + 5 * (int64_t)h->sp.ntmax;
-      launch_factor<double>(h->sp, h->pl.env64, h->pl.X64, h->d_probs.p, h->tb, np, 1, h->d_active.p, h->pl.err,
-                            1e-10, nullptr, h->stream);
-      launch_backward<double>(h->sp, h->pl.env64, h->pl.X64, h->d_probs.p, h->tb, np, h->d_active.p, h->stream);
+      if (h->escalate_dfl) {
+        // double-float factorisation of the equilibrated matrix + 2 refinement steps
+        CK(cudaMemsetAsync(h->pl.dmax, 0, 3 * np * sizeof(unsigned long long), h->stream));
+        launch_dfl_escalation(h->sp, h->d_probs.p, h->pl, h->tb, h->dims, reinterpret_cast<dfl*>(h->pl.V), 2,
+                              h->stream);
+        nkern += 2 + 10 * (int64_t)h->sp.ntmax + 2 * (3 + 4 * (int64_t)h->sp.ntmax);
+      } else {
+        launch_copy_rhs(h->d_probs.p, h->pl, h->dims, h->stream);
+        nkern += 1 + 5 * (int64_t)h->sp.ntmax;
+        launch_factor<double>(h->sp, h->pl.env64, h->pl.X64, h->pl.dinv64, h->d_probs.p, h->tb, np, 1,
+                              h->d_active.p, h->pl.err, 1e-10, nullptr, h->stream);
+        launch_backward<double>(h->sp, h->pl.env64, h->pl.X64, h->pl.dinv64, h->d_probs.p, h->tb, np,
+                                h->d_active.p, h->stream);
+      }
       CK(cudaGetLastError());
+      if (h->escalate_dfl) {
+        std::vector<unsigned long long> red2(3 * np);
+        CK(cudaMemcpyAsync(red2.data(), h->d_red.p, 3 * np * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        for (int k = 0; k < np; ++k)
+          if (active[k]) {
+            double dm, xm;
+            memcpy(&dm, &red2[k], 8);
+            memcpy(&xm, &red2[np + k], 8);
+            b.resid[k] = xm > 0 ? dm / xm : dm;
+          }
+      }
       for (int k = 0; k < np; ++k) b.fallback[k] = active[k];
     }
     CK(cudaEventRecord(h->ev[5], h->stream));
@@ -896,6 +988,7 @@ fdmgpu_status fdmgpu_create(const fdmgpu_grid* g, fdmgpu_handle** out) {
   S.mso = h->d_mso.p;
   setup_factor_kernels<float>();
   setup_factor_kernels<double>();
+  setup_factor_kernels<dfl>();
   *out = h;
   return FDMGPU_OK;
 }
@@ -917,8 +1010,18 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
                           &h->d_rs,      &h->d_cs,   &h->d_val,   &h->d_taull,  &h->d_tscratch, &h->d_smr};
   for (auto* b : db) b->release();
   h->d_env32.release();
+  h->d_dinv32.release();
+  h->d_dinv64.release();
   h->d_val2.release();
   h->d_Xs.release();
+  h->d_valS.release();
+  h->d_V.release();
+  h->d_W.release();
+  h->d_gstate.release();
+  h->d_inner.release();
+  h->d_jdone.release();
+  h->d_notconv.release();
+  h->d_active_gm.release();
   h->d_Y32.release();
   h->d_strip.release();
   h->d_probs.release();
@@ -935,6 +1038,22 @@ fdmgpu_status fdmgpu_set_residual_mode(fdmgpu_handle* h, int32_t mode) {
   if (!h || (mode != FDMGPU_RESIDUAL_FP64 && mode != FDMGPU_RESIDUAL_DF64))
     return fail(FDMGPU_ERR_ARG, "unknown residual mode");
   h->residual_df64 = mode == FDMGPU_RESIDUAL_DF64;
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_set_refinement(fdmgpu_handle* h, int32_t mode, int32_t krylov_dim) {
+  if (!h || (mode != FDMGPU_REFINE_CLASSIC && mode != FDMGPU_REFINE_GMRES) || krylov_dim < 1 ||
+      krylov_dim > gmres_max_dim())
+    return fail(FDMGPU_ERR_ARG, "unknown refinement mode or Krylov dimension out of range");
+  h->refine_gmres = mode == FDMGPU_REFINE_GMRES;
+  h->gmres_m = krylov_dim;
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_set_escalation(fdmgpu_handle* h, int32_t mode) {
+  if (!h || (mode != FDMGPU_ESCALATE_FP64 && mode != FDMGPU_ESCALATE_DF64))
+    return fail(FDMGPU_ERR_ARG, "unknown escalation mode");
+  h->escalate_dfl = mode == FDMGPU_ESCALATE_DF64;
   return FDMGPU_OK;
 }
 
@@ -1009,10 +1128,11 @@ fdmgpu_status fdmgpu_batch_solution(fdmgpu_handle* h, int32_t k, double* smr) {
 }
 
 fdmgpu_status fdmgpu_batch_stats(fdmgpu_handle* h, int32_t k, int32_t* iters, double* residual,
-                                 int32_t* fallback) {
+                                 int32_t* fallback, int32_t* inner_iters) {
   if (!h || !h->batch.ran || k < 0 || k >= (int)h->batch.probs.size())
     return fail(FDMGPU_ERR_ARG, "no such batch result");
   if (iters) *iters = h->batch.iters[k];
+  if (inner_iters) *inner_iters = h->batch.inner.empty() ? 0 : h->batch.inner[k];
   if (residual) *residual = h->batch.resid[k];
   if (fallback) *fallback = h->batch.fallback.empty() ? 0 : h->batch.fallback[k];
   return (fdmgpu_status)h->batch.err[k];

@@ -23,8 +23,8 @@ namespace fdm {
 // earlier steps updated them, and the forward substitution permutes Y(K) at
 // step K, so P A = L U holds block by block).
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_diag(T* env, const Prob* probs, Tables tb, int K, const int* active,
-                                                   int* err, double piv_thr, int* piv) {
+__global__ void __launch_bounds__(NTHREADS) k_diag(T* env, T* dinv, const Prob* probs, Tables tb, int K,
+                                                   const int* active, int* err, double piv_thr, int* piv) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
   if (K >= P.nt || (active && !active[e])) return;
@@ -40,14 +40,21 @@ __global__ void __launch_bounds__(NTHREADS) k_diag(T* env, const Prob* probs, Ta
   __syncthreads();
   store_tile(dtile, D);
   if (piv && threadIdx.x < TS) piv[P.rowv + (int64_t)K * TS + threadIdx.x] = perm[threadIdx.x];
+  (void)dinv;
   // smallest |pivot| of the tile (padding rows carry 1); NaN also trips the test
   if (threadIdx.x == 0 && !(mp >= piv_thr)) atomicExch(&err[e], (int)FDMGPU_ERR_ZERO_PIVOT);
 }
 
 // Panel of step K with the factored diagonal tile: L tiles (I,K), U tiles
 // (K,J) and, when fused, the RHS tiles (K,R).
+// Separate register allocation for the two branches of the panel.
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_panel(T* env, T* rhs, const Prob* probs, Tables tb, int K,
+__device__ __noinline__ void panel_row_solve(T* g, const T* D, T* Ws) { row_solve_upper(g, D, Ws); }
+template <typename T>
+__device__ __noinline__ void panel_col_solve(T* g, const T* D, const int* perm) { col_solve_lower_unit(g, D, perm); }
+
+template <typename T>
+__global__ void __launch_bounds__(GEMM_THREADS) k_panel(T* env, T* rhs, const T* dinv, const Prob* probs, Tables tb, int K,
                                                     int fuse_rhs, const int* active, const int* piv) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -59,27 +66,21 @@ __global__ void __launch_bounds__(NTHREADS) k_panel(T* env, T* rhs, const Prob* 
   if (w >= nI + nJ + nR) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* D = reinterpret_cast<T*>(smem_raw);
-  T* W = D + TS * SP;
-  load_tile(D, tile_ptr(env, P, tb, K, K));
-  T* g;
-  if (w < nI) {
-    g = tile_ptr(env, P, tb, K + 1 + w, K);
-    load_tile(W, g);
-    __syncthreads();
-    tile_right_upper_solve(W, D);
-  } else {
-    g = w < nI + nJ ? tile_ptr(env, P, tb, K, K + 1 + (w - nI)) : rhs_ptr(rhs, P, K, w - nI - nJ);
-    if (piv) load_tile_perm(W, g, piv + P.rowv + (int64_t)K * TS);
-    else load_tile(W, g);
-    __syncthreads();
-    tile_left_lower_unit_solve(W, D);
-  }
+  T* Ws = D + TS * SP;
+  load_tile_n(D, tile_ptr(env, P, tb, K, K), GEMM_THREADS);
   __syncthreads();
-  store_tile(g, W);
+  if (w < nI) {
+    // L(I,K) = A(I,K) U_KK^-1
+    panel_row_solve(tile_ptr(env, P, tb, K + 1 + w, K), D, Ws);
+  } else {
+    // U(K,J) = L_KK^-1 P A(K,J) and Y(K,R) = L_KK^-1 P Y(K,R)
+    T* g = w < nI + nJ ? tile_ptr(env, P, tb, K, K + 1 + (w - nI)) : rhs_ptr(rhs, P, K, w - nI - nJ);
+    panel_col_solve(g, D, piv ? piv + P.rowv + (int64_t)K * TS : (const int*)nullptr);
+  }
 }
 
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_trailing(T* env, T* rhs, const Prob* probs, Tables tb, int K,
+__global__ void __launch_bounds__(GEMM_THREADS) k_trailing(T* env, T* rhs, const Prob* probs, Tables tb, int K,
                                                        int fuse_rhs, const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -104,13 +105,13 @@ __global__ void __launch_bounds__(NTHREADS) k_trailing(T* env, T* rhs, const Pro
     B = rhs_ptr(rhs, P, K, c - nJ);
     C = rhs_ptr(rhs, P, I, c - nJ);
   }
-  tile_gemm_sub(C, A, B, As, Bs);
+  tile_mm64<T, true>(C, A, B, (const int*)nullptr, As, Bs);
 }
 
-// Forward substitution, unit lower L: Y(K,R) <- L(K,K)^-1 Y(K,R).
+// Forward substitution, unit lower L: Y(K,R) <- L(K,K)^-1 P Y(K,R).
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_fwd_diag(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
-                                                       const int* active, const int* piv) {
+__global__ void __launch_bounds__(GEMM_THREADS) k_fwd_diag(const T* env, const T* dinv, T* rhs, const Prob* probs,
+                                                           Tables tb, int K, const int* active, const int* piv) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
   if (K >= P.nt || (active && !active[e])) return;
@@ -118,20 +119,15 @@ __global__ void __launch_bounds__(NTHREADS) k_fwd_diag(const T* env, T* rhs, con
   if (R >= P.nrt) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* D = reinterpret_cast<T*>(smem_raw);
-  T* W = D + TS * SP;
-  load_tile(D, tile_ptr(const_cast<T*>(env), P, tb, K, K));
-  T* g = rhs_ptr(rhs, P, K, R);
-  if (piv) load_tile_perm(W, g, piv + P.rowv + (int64_t)K * TS);
-  else load_tile(W, g);
+  load_tile_n(D, tile_ptr(const_cast<T*>(env), P, tb, K, K), GEMM_THREADS);
   __syncthreads();
-  tile_left_lower_unit_solve(W, D);
-  __syncthreads();
-  store_tile(g, W);
+  (void)dinv;
+  col_solve_lower_unit(rhs_ptr(rhs, P, K, R), D, piv ? piv + P.rowv + (int64_t)K * TS : (const int*)nullptr);
 }
 
 // Y(I,R) -= L(I,K) Y(K,R) for I in (K, Imax(K)].
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_fwd_update(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
+__global__ void __launch_bounds__(GEMM_THREADS) k_fwd_update(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
                                                          const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -143,13 +139,14 @@ __global__ void __launch_bounds__(NTHREADS) k_fwd_update(const T* env, T* rhs, c
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* As = reinterpret_cast<T*>(smem_raw);
   T* Bs = As + TS * SP;
-  tile_gemm_sub(rhs_ptr(rhs, P, I, R), tile_ptr(const_cast<T*>(env), P, tb, I, K), rhs_ptr(rhs, P, K, R), As, Bs);
+  tile_mm64<T, true>(rhs_ptr(rhs, P, I, R), tile_ptr(const_cast<T*>(env), P, tb, I, K), rhs_ptr(rhs, P, K, R),
+                     (const int*)nullptr, As, Bs);
 }
 
 // Backward substitution, upper U: Y(K,R) <- U(K,K)^-1 Y(K,R).
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_bwd_diag(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
-                                                       const int* active) {
+__global__ void __launch_bounds__(GEMM_THREADS) k_bwd_diag(const T* env, const T* dinv, T* rhs, const Prob* probs,
+                                                           Tables tb, int K, const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
   if (K >= P.nt || (active && !active[e])) return;
@@ -157,19 +154,15 @@ __global__ void __launch_bounds__(NTHREADS) k_bwd_diag(const T* env, T* rhs, con
   if (R >= P.nrt) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* D = reinterpret_cast<T*>(smem_raw);
-  T* W = D + TS * SP;
-  load_tile(D, tile_ptr(const_cast<T*>(env), P, tb, K, K));
-  T* g = rhs_ptr(rhs, P, K, R);
-  load_tile(W, g);
+  load_tile_n(D, tile_ptr(const_cast<T*>(env), P, tb, K, K), GEMM_THREADS);
   __syncthreads();
-  tile_left_upper_solve(W, D);
-  __syncthreads();
-  store_tile(g, W);
+  (void)dinv;
+  col_solve_upper(rhs_ptr(rhs, P, K, R), D);
 }
 
 // Y(I,R) -= U(I,K) Y(K,R) for I in [Imin(K), K).
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_bwd_update(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
+__global__ void __launch_bounds__(GEMM_THREADS) k_bwd_update(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
                                                          const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -182,17 +175,21 @@ __global__ void __launch_bounds__(NTHREADS) k_bwd_update(const T* env, T* rhs, c
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* As = reinterpret_cast<T*>(smem_raw);
   T* Bs = As + TS * SP;
-  tile_gemm_sub(rhs_ptr(rhs, P, I, R), tile_ptr(const_cast<T*>(env), P, tb, I, K), rhs_ptr(rhs, P, K, R), As, Bs);
+  tile_mm64<T, true>(rhs_ptr(rhs, P, I, R), tile_ptr(const_cast<T*>(env), P, tb, I, K), rhs_ptr(rhs, P, K, R),
+                     (const int*)nullptr, As, Bs);
 }
 
 template <typename T>
 static size_t smem_bytes() { return 2 * TS * SP * sizeof(T); }
+// the panel holds the diagonal tile plus two SPA-strided work tiles
+template <typename T>
+static size_t smem_bytes_panel() { return (TS * SP + 2 * TS * SPA) * sizeof(T); }
 
 template <typename T>
 void setup_factor_kernels() {
   const int bytes = (int)smem_bytes<T>();
   cudaFuncSetAttribute(k_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
-  cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes_panel<T>());
   cudaFuncSetAttribute(k_trailing<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_fwd_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_fwd_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -201,51 +198,60 @@ void setup_factor_kernels() {
 }
 
 template <typename T>
-void launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
+void launch_factor(const StepPlan& sp, T* env, T* rhs, T* dinv, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
                    const int* active, int* err, double piv_thr, int* piv, cudaStream_t s) {
   const size_t sm = smem_bytes<T>();
   for (int K = 0; K < sp.ntmax; ++K) {
-    k_diag<T><<<dim3(1, nprob), NTHREADS, sm, s>>>(env, probs, tb, K, active, err, piv_thr, piv);
+    k_diag<T><<<dim3(1, nprob), NTHREADS, sm, s>>>(env, dinv, probs, tb, K, active, err, piv_thr, piv);
     const int np = fuse_rhs ? sp.panel_rhs[K] : sp.panel[K];
-    if (np > 0) k_panel<T><<<dim3(np, nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active, piv);
+    if (np > 0)
+      k_panel<T><<<dim3(np, nprob), GEMM_THREADS, smem_bytes_panel<T>(), s>>>(env, rhs, dinv, probs, tb, K, fuse_rhs,
+                                                                             active, piv);
     const int nt = fuse_rhs ? sp.trail_rhs[K] : sp.trail[K];
-    if (nt > 0) k_trailing<T><<<dim3(nt, nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
+    if (nt > 0) k_trailing<T><<<dim3(nt, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
   }
 }
 
 template <typename T>
-void launch_forward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
+void launch_forward(const StepPlan& sp, const T* env, T* rhs, const T* dinv, const Prob* probs, Tables tb, int nprob,
                     const int* active, const int* piv, cudaStream_t s) {
   const size_t sm = smem_bytes<T>();
   for (int K = 0; K < sp.ntmax; ++K) {
-    k_fwd_diag<T><<<dim3(sp.nrtmax, nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, active, piv);
-    if (sp.fwd[K] > 0) k_fwd_update<T><<<dim3(sp.fwd[K], nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+    k_fwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, dinv, rhs, probs, tb, K, active, piv);
+    if (sp.fwd[K] > 0) k_fwd_update<T><<<dim3(sp.fwd[K], nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
   }
 }
 
 template <typename T>
-void launch_backward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
+void launch_backward(const StepPlan& sp, const T* env, T* rhs, const T* dinv, const Prob* probs, Tables tb, int nprob,
                      const int* active, cudaStream_t s) {
   const size_t sm = smem_bytes<T>();
   for (int K = sp.ntmax - 1; K >= 0; --K) {
-    k_bwd_diag<T><<<dim3(sp.nrtmax, nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, active);
-    if (sp.bwd[K] > 0) k_bwd_update<T><<<dim3(sp.bwd[K], nprob), NTHREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+    k_bwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, dinv, rhs, probs, tb, K, active);
+    if (sp.bwd[K] > 0) k_bwd_update<T><<<dim3(sp.bwd[K], nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
   }
 }
 
 template void setup_factor_kernels<float>();
+template void setup_factor_kernels<dfl>();
+template void launch_factor<dfl>(const StepPlan&, dfl*, dfl*, dfl*, const Prob*, Tables, int, int, const int*, int*,
+                                 double, int*, cudaStream_t);
+template void launch_forward<dfl>(const StepPlan&, const dfl*, dfl*, const dfl*, const Prob*, Tables, int, const int*,
+                                  const int*, cudaStream_t);
+template void launch_backward<dfl>(const StepPlan&, const dfl*, dfl*, const dfl*, const Prob*, Tables, int, const int*,
+                                   cudaStream_t);
 template void setup_factor_kernels<double>();
-template void launch_factor<float>(const StepPlan&, float*, float*, const Prob*, Tables, int, int, const int*, int*,
-                                   double, int*, cudaStream_t);
-template void launch_factor<double>(const StepPlan&, double*, double*, const Prob*, Tables, int, int, const int*, int*,
-                                    double, int*, cudaStream_t);
-template void launch_forward<float>(const StepPlan&, const float*, float*, const Prob*, Tables, int, const int*,
-                                    const int*, cudaStream_t);
-template void launch_forward<double>(const StepPlan&, const double*, double*, const Prob*, Tables, int, const int*,
+template void launch_factor<float>(const StepPlan&, float*, float*, float*, const Prob*, Tables, int, int, const int*,
+                                   int*, double, int*, cudaStream_t);
+template void launch_factor<double>(const StepPlan&, double*, double*, double*, const Prob*, Tables, int, int,
+                                    const int*, int*, double, int*, cudaStream_t);
+template void launch_forward<float>(const StepPlan&, const float*, float*, const float*, const Prob*, Tables, int,
+                                    const int*, const int*, cudaStream_t);
+template void launch_forward<double>(const StepPlan&, const double*, double*, const double*, const Prob*, Tables, int,
+                                     const int*, const int*, cudaStream_t);
+template void launch_backward<float>(const StepPlan&, const float*, float*, const float*, const Prob*, Tables, int,
                                      const int*, cudaStream_t);
-template void launch_backward<float>(const StepPlan&, const float*, float*, const Prob*, Tables, int, const int*,
-                                     cudaStream_t);
-template void launch_backward<double>(const StepPlan&, const double*, double*, const Prob*, Tables, int, const int*,
-                                      cudaStream_t);
+template void launch_backward<double>(const StepPlan&, const double*, double*, const double*, const Prob*, Tables, int,
+                                      const int*, cudaStream_t);
 
 }  // namespace fdm

@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include "../../include/fdmgpu.h"
+#include "dfloat.cuh"
 
 namespace fdm {
 
@@ -47,6 +48,7 @@ struct Prob {
   int64_t rowv;   // offset into per-row vectors (npad entries): scales, csr row_ptr
   int64_t csr;    // offset into CSR columns/values
   int64_t csr_cap;    // CSR capacity of this problem (structural nonzeros of calcMatRow)
+  int64_t csr_col;    // offset of this problem's per-column refinement state
   int64_t in_new;     // offset of new_(0:npoint) in the int pool
   int64_t in_ianew;   // offset of ianew(natome)
   int64_t in_nlmsa;   // offset of nlmsa(natome)
@@ -54,6 +56,7 @@ struct Prob {
   int64_t in_phi;     // offset of phiato(nphiato1, nlmagm, natome) (spin-selected)
   int64_t in_bes;     // offset of Bessel j(ib, L) in the double pool, [nsort][lmaxso+1]
   int64_t in_neu;     // offset of Neumann n(ib, L), [nsort][lmaxso+1]
+  int64_t dinv;       // element offset of the inverted diagonal tiles (L_KK^-1, U_KK^-1 per K)
   int64_t taull;      // offset of Taull (complex) for this problem
   int64_t scratch;    // offset of the complex nlmso x (nlmso + nlm_abs) Taull scratch
 };
@@ -115,6 +118,10 @@ __device__ __forceinline__ void load_tile(T* __restrict__ s, const T* __restrict
     const int r = idx / TS, c = idx % TS;
     s[r * SP + c] = g[idx];
   }
+}
+template <typename T>
+__device__ __forceinline__ void load_tile_n(T* __restrict__ s, const T* __restrict__ g, int nthreads) {
+  for (int idx = threadIdx.x; idx < TS2; idx += nthreads) s[(idx / TS) * SP + idx % TS] = g[idx];
 }
 template <typename T>
 __device__ __forceinline__ void store_tile(T* __restrict__ g, const T* __restrict__ s) {
@@ -266,6 +273,197 @@ __device__ void tile_gemm_sub(T* __restrict__ C, const T* __restrict__ A, const 
 #pragma unroll
     for (int j = 0; j < 4; ++j) crow[j] -= acc[i][j];
   }
+}
+
+// C = A * P B (C, A, B global TS x TS tiles; P the row order perm, nullable).
+// C may alias A or B: both are staged in shared memory first.
+template <typename T>
+__device__ void tile_gemm_assign(T* C, const T* A, const T* B, const int* perm, T* As, T* Bs) {
+  for (int idx = threadIdx.x; idx < TS2; idx += NTHREADS) {
+    const int r = idx / TS, k = idx % TS;
+    As[k * SP + r] = A[idx];
+    Bs[r * SP + k] = perm ? B[perm[r] * TS + k] : B[idx];
+  }
+  __syncthreads();
+  const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+#pragma unroll 4
+  for (int k = 0; k < TS; ++k) {
+    T a[4], b[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) a[i] = As[k * SP + ty * 4 + i];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) b[j] = Bs[k * SP + tx * 4 + j];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] += a[i] * b[j];
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    T* crow = C + (ty * 4 + i) * TS + tx * 4;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) crow[j] = acc[i][j];
+  }
+}
+
+// -------------------------------------------------------------------------
+// 64-thread tile product: C (-)= A * P B with every operand a TS x TS tile.
+// Thread (tx, ty) of the 8 x 8 thread grid owns rows {4ty + i, 32 + 4ty + i}
+// and columns {4tx + j, 32 + 4tx + j} (i, j < 4): an 8 x 8 register tile, fed
+// per k by eight scalar reads of A (row-major, odd stride: no bank conflicts)
+// and two 16-byte reads of B.  Shared use: As, Bs of TS x SP each.
+// -------------------------------------------------------------------------
+constexpr int GEMM_THREADS = 64;
+
+template <typename T> struct Vec4;
+template <> struct Vec4<float> { typedef float4 type; };
+
+template <typename T>
+__device__ __forceinline__ void ld4(const T* p, T* v) {
+  v[0] = p[0]; v[1] = p[1]; v[2] = p[2]; v[3] = p[3];
+}
+template <>
+__device__ __forceinline__ void ld4<float>(const float* p, float* v) {
+  const float4 q = *reinterpret_cast<const float4*>(p);
+  v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+}
+template <>
+__device__ __forceinline__ void ld4<double>(const double* p, double* v) {
+  const double2 a = *reinterpret_cast<const double2*>(p);
+  const double2 b = *reinterpret_cast<const double2*>(p + 2);
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+
+constexpr int SPA = TS + 1;  // odd stride of the A tile: conflict-free scalar column reads
+
+template <typename T, bool SUB>
+__device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const int* perm, T* As, T* Bs) {
+  const int t = threadIdx.x;
+  // stage: As[r][k] = A[r][k] (stride SPA), Bs[r][c] = B[perm ? perm[r] : r][c] (stride SP)
+  for (int idx = t; idx < TS2 / 4; idx += GEMM_THREADS) {
+    const int r = idx / (TS / 4), c4 = (idx % (TS / 4)) * 4;
+    T a[4], b[4];
+    ld4(A + r * TS + c4, a);
+    ld4(B + (perm ? perm[r] : r) * TS + c4, b);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      As[r * SPA + c4 + q] = a[q];
+      Bs[r * SP + c4 + q] = b[q];
+    }
+  }
+  __syncthreads();
+  const int tx = t % 8, ty = t / 8;
+  T acc[8][8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[i][j] = T(0);
+#pragma unroll 2
+  for (int k = 0; k < TS; ++k) {
+    T a[8], b[8];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      a[i] = As[(4 * ty + i) * SPA + k];
+      a[4 + i] = As[(32 + 4 * ty + i) * SPA + k];
+    }
+    ld4(Bs + k * SP + 4 * tx, b);
+    ld4(Bs + k * SP + 32 + 4 * tx, b + 4);
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] += a[i] * b[j];
+  }
+  __syncthreads();  // C may alias A or B, which are no longer read
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int row = (i < 4 ? 4 * ty + i : 32 + 4 * ty + (i - 4));
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      T* cp = C + row * TS + 32 * h + 4 * tx;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) cp[j] = SUB ? cp[j] - acc[i][4 * h + j] : acc[i][4 * h + j];
+    }
+  }
+}
+
+// -------------------------------------------------------------------------
+// Triangular substitution by 64 independent threads (no barriers inside).
+// The factored diagonal tile sits in shared memory with stride SP.
+// -------------------------------------------------------------------------
+
+// g <- L^-1 P g (L unit lower): thread c owns column c of the tile.
+template <typename T>
+__device__ __forceinline__ void col_solve_lower_unit(T* g, const T* Ls, const int* perm) {
+  const int c = threadIdx.x;
+  if (c >= TS) return;
+  T x[TS];
+#pragma unroll
+  for (int r = 0; r < TS; ++r) x[r] = g[(perm ? perm[r] : r) * TS + c];
+#pragma unroll
+  for (int k = 1; k < TS; ++k) {
+    T acc = x[k];
+#pragma unroll
+    for (int i = 0; i < k; ++i) acc -= Ls[k * SP + i] * x[i];
+    x[k] = acc;
+  }
+#pragma unroll
+  for (int r = 0; r < TS; ++r) g[r * TS + c] = x[r];
+}
+
+// g <- U^-1 g (U upper with diagonal): thread c owns column c.
+template <typename T>
+__device__ __forceinline__ void col_solve_upper(T* g, const T* Us) {
+  const int c = threadIdx.x;
+  if (c >= TS) return;
+  T x[TS];
+#pragma unroll
+  for (int r = 0; r < TS; ++r) x[r] = g[r * TS + c];
+#pragma unroll
+  for (int k = TS - 1; k >= 0; --k) {
+    T acc = x[k];
+#pragma unroll
+    for (int i = k + 1; i < TS; ++i) acc -= Us[k * SP + i] * x[i];
+    x[k] = acc / Us[k * SP + k];
+  }
+#pragma unroll
+  for (int r = 0; r < TS; ++r) g[r * TS + c] = x[r];
+}
+
+// g <- g U^-1 (U upper with diagonal): thread r owns row r, i.e. solves
+// U^T x = a by forward substitution.  The rows pass through shared memory Ws
+// (stride SPA) so that the global accesses stay coalesced and the row reads
+// conflict-free; U^T is staged into Ws's tail rows-first for contiguous reads.
+template <typename T>
+__device__ __forceinline__ void row_solve_upper(T* g, const T* Us, T* Ws) {
+  T* Ut = Ws + TS * SPA;  // Ut[k][i] = U[i][k], stride SPA
+  for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) {
+    const int a = idx / TS, b = idx % TS;
+    Ws[a * SPA + b] = g[idx];
+    Ut[b * SPA + a] = Us[a * SP + b];
+  }
+  __syncthreads();
+  const int r = threadIdx.x;
+  if (r < TS) {
+    T x[TS];
+#pragma unroll
+    for (int k = 0; k < TS; ++k) x[k] = Ws[r * SPA + k];
+#pragma unroll
+    for (int k = 0; k < TS; ++k) {
+      T acc = x[k];
+#pragma unroll
+      for (int i = 0; i < k; ++i) acc -= Ut[k * SPA + i] * x[i];
+      x[k] = acc / Ut[k * SPA + k];
+    }
+#pragma unroll
+    for (int k = 0; k < TS; ++k) Ws[r * SPA + k] = x[k];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) g[idx] = Ws[(idx / TS) * SPA + idx % TS];
 }
 
 }  // namespace fdm

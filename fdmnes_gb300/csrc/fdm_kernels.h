@@ -19,13 +19,13 @@ struct StepPlan {
 
 template <typename T> void setup_factor_kernels();
 template <typename T>
-void launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
+void launch_factor(const StepPlan& sp, T* env, T* rhs, T* dinv, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
                    const int* active, int* err, double piv_thr, int* piv, cudaStream_t s);
 template <typename T>
-void launch_forward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
+void launch_forward(const StepPlan& sp, const T* env, T* rhs, const T* dinv, const Prob* probs, Tables tb, int nprob,
                     const int* active, const int* piv, cudaStream_t s);
 template <typename T>
-void launch_backward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
+void launch_backward(const StepPlan& sp, const T* env, T* rhs, const T* dinv, const Prob* probs, Tables tb, int nprob,
                      const int* active, cudaStream_t s);
 
 // Device pools of one batch (pointers into device memory).
@@ -37,6 +37,8 @@ struct Pools {
   double* B64 = nullptr;           // FP64 right-hand sides (tiles)
   double* X64 = nullptr;           // FP64 solution (tiles)
   float* Y32 = nullptr;            // FP32 work right-hand sides (tiles)
+  double* dinv64 = nullptr;        // inverted diagonal tiles of the FP64 factor
+  float* dinv32 = nullptr;         // inverted diagonal tiles of the FP32 factor
   double* rs = nullptr;            // row scales (per row, stride npad + 1)
   double* cs = nullptr;            // column scales
   int* rowptr = nullptr;           // CSR row pointers (stride npad + 1)
@@ -52,6 +54,16 @@ struct Pools {
   unsigned long long* amax = nullptr;  // per problem scratch
   int* err = nullptr;
   int* active = nullptr;
+  // GMRES-IR
+  float* valS = nullptr;           // equilibrated FP32 CSR values
+  float* V = nullptr;              // Krylov basis, (m+1) vectors of vstride floats
+  int64_t vstride = 0;
+  float* W = nullptr;              // work vector
+  void* gstate = nullptr;          // per-column GMRES state
+  int* active_gm = nullptr;        // problems refined by GMRES cycles (subset of active)
+  int* inner_active = nullptr;
+  int* jdone = nullptr;
+  int* notconv = nullptr;
 };
 
 struct LaunchDims {
@@ -73,7 +85,14 @@ void launch_csr(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims&
 void launch_update_x(const Prob* probs, const Pools& pl, const LaunchDims& d, int first, cudaStream_t s);
 // Y32 = rs * (B64 - A X64) using the CSR copy of A, in FP64 or in double-float.
 void launch_residual(const Prob* probs, const Pools& pl, const LaunchDims& d, int df64, cudaStream_t s);
+void launch_csr_scale(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s);
+void launch_gmres_cycle(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, int m,
+                        float tol, cudaStream_t s);
+size_t gmres_state_bytes();
+int gmres_max_dim();
 void launch_copy_rhs(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s);
+void launch_dfl_escalation(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
+                           dfl* D, int iters, cudaStream_t s);
 void launch_taull(const Prob* probs, const Pools& pl, const LaunchDims& d, const double* X, cudaStream_t s);
 void launch_solution_out(const Prob& P, const double* X, double* smr_dev, cudaStream_t s);
 

@@ -375,6 +375,90 @@ __global__ void k_copy_rhs(const Prob* probs, const double* B, double* X, const 
   for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) X[P.rhs + w * TS2 + idx] = B[P.rhs + w * TS2 + idx];
 }
 
+// Escalation to a double-float factorisation of the equilibrated matrix:
+// envd = dfl(rs * cs * E64) in place over the FP64 band of the active problems.
+__global__ void k_env_to_dfl(const Prob* probs, double* env, const double* rs, const double* cs, Tables tb,
+                             const int* active) {
+  const Prob P = probs[blockIdx.y];
+  if (!active[blockIdx.y]) return;
+  const int64_t w = blockIdx.x;
+  if (w >= tb.strip[P.trow + P.nt]) return;
+  const int I = tile_row_of(tb, P, w);
+  const int J = tb.J0[P.trow + I] + (int)(w - tb.strip[P.trow + I]);
+  double* t = env + P.env + w * TS2;
+  dfl* o = reinterpret_cast<dfl*>(t);
+  for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) {
+    const double v = rs[P.rowv + I * TS + idx / TS] * cs[P.rowv + J * TS + idx % TS] * t[idx];
+    o[idx] = dfl(v);
+  }
+}
+
+// D = dfl(rs * B64) (from_b) or dfl(Y32) (already scaled) for the active problems.
+__global__ void k_rhs_to_dfl(const Prob* probs, const double* B, const float* Y, const double* rs, dfl* D, int from_b,
+                             const int* active) {
+  const Prob P = probs[blockIdx.y];
+  if (!active[blockIdx.y]) return;
+  const int64_t w = blockIdx.x;
+  if (w >= (int64_t)P.nt * P.nrt) return;
+  const int I = (int)(w / P.nrt);
+  for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) {
+    const int64_t o = P.rhs + w * TS2 + idx;
+    D[o] = from_b ? dfl(rs[P.rowv + I * TS + idx / TS] * B[o]) : dfl((double)Y[o]);
+  }
+}
+
+// X64 (+)= cs * D for the active problems, with the split copy and maxima.
+__global__ void k_dfl_to_x(const Prob* probs, const dfl* D, double* X, float2* Xs, const double* cs, int first,
+                           unsigned long long* dmax, unsigned long long* xmax, const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (!active[e]) return;
+  const int64_t w = blockIdx.x;
+  if (w >= (int64_t)P.nt * P.nrt) return;
+  const int I = (int)(w / P.nrt);
+  double dm = 0.0, xm = 0.0;
+  for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) {
+    const int64_t o = P.rhs + w * TS2 + idx;
+    const double d = cs[P.rowv + I * TS + idx / TS] * (double)D[o];
+    const double xn = first ? d : X[o] + d;
+    X[o] = xn;
+    const float hi = (float)xn;
+    Xs[o] = make_float2(hi, (float)(xn - (double)hi));
+    dm = fmax(dm, fabs(d));
+    xm = fmax(xm, fabs(xn));
+  }
+  for (int o = 16; o; o >>= 1) {
+    dm = fmax(dm, __shfl_xor_sync(0xffffffffu, dm, o));
+    xm = fmax(xm, __shfl_xor_sync(0xffffffffu, xm, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomic_max_abs(&dmax[e], dm);
+    atomic_max_abs(&xmax[e], xm);
+  }
+}
+
+// Double-float re-solve of the active problems: factorisation of Dr A Dc,
+// solve, then `iters` refinement steps with the double-float residual and the
+// double-float factors.  Scratch D (dfl, RHS layout) must hold rhs elements.
+void launch_dfl_escalation(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
+                           dfl* D, int iters, cudaStream_t s) {
+  const int np = d.nprob;
+  dfl* envd = reinterpret_cast<dfl*>(pl.env64);
+  k_env_to_dfl<<<dim3(d.max_tiles, np), 256, 0, s>>>(probs, pl.env64, pl.rs, pl.cs, tb, pl.active);
+  k_rhs_to_dfl<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, pl.B64, pl.Y32, pl.rs, D, 1, pl.active);
+  launch_factor<dfl>(sp, envd, D, nullptr, probs, tb, np, 1, pl.active, pl.err, 1e-30, pl.piv, s);
+  launch_backward<dfl>(sp, envd, D, nullptr, probs, tb, np, pl.active, s);
+  k_dfl_to_x<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, D, pl.X64, pl.Xs, pl.cs, 1, pl.dmax, pl.xmax, pl.active);
+  for (int it = 0; it < iters; ++it) {
+    launch_residual(probs, pl, d, 1, s);
+    k_rhs_to_dfl<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, pl.B64, pl.Y32, pl.rs, D, 0, pl.active);
+    launch_forward<dfl>(sp, envd, D, nullptr, probs, tb, np, pl.active, pl.piv, s);
+    launch_backward<dfl>(sp, envd, D, nullptr, probs, tb, np, pl.active, s);
+    k_dfl_to_x<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, D, pl.X64, pl.Xs, pl.cs, 0, pl.dmax, pl.xmax,
+                                                          pl.active);
+  }
+}
+
 void launch_copy_rhs(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s) {
   k_copy_rhs<<<dim3(d.max_rhs_tiles, d.nprob), 256, 0, s>>>(probs, pl.B64, pl.X64, pl.active);
 }

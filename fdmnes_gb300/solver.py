@@ -57,6 +57,10 @@ def load_library(path: str = LIB_PATH):
     L.fdmgpu_get_solver_params.argtypes = [C.POINTER(C.c_int32), C.c_char_p]
     L.fdmgpu_get_solver_params.restype = None
     L.fdmgpu_set_residual_mode.argtypes = [vp, C.c_int32]
+    L.fdmgpu_set_refinement.argtypes = [vp, C.c_int32, C.c_int32]
+    L.fdmgpu_set_refinement.restype = C.c_int
+    L.fdmgpu_set_escalation.argtypes = [vp, C.c_int32]
+    L.fdmgpu_set_escalation.restype = C.c_int
     L.fdmgpu_set_residual_mode.restype = C.c_int
     L.fdmgpu_batch_begin.argtypes = [vp, C.c_int32, C.c_int32]
     L.fdmgpu_batch_add.argtypes = [vp, vp, C.c_int32]
@@ -65,7 +69,7 @@ def load_library(path: str = LIB_PATH):
     L.fdmgpu_batch_taull.argtypes = [vp, C.c_int32, vp, C.POINTER(C.c_int32)]
     L.fdmgpu_batch_solution.argtypes = [vp, C.c_int32, vp]
     L.fdmgpu_batch_stats.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double),
-                                     C.POINTER(C.c_int32)]
+                                     C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     for f in ("fdmgpu_batch_begin", "fdmgpu_batch_add", "fdmgpu_batch_run", "fdmgpu_batch_rerun", "fdmgpu_batch_taull",
               "fdmgpu_batch_solution", "fdmgpu_batch_stats"):
         getattr(L, f).restype = C.c_int
@@ -98,6 +102,14 @@ class FdmSolver:
     def set_residual(self, mode: str):
         """Residual arithmetic of the mixed path: 'df64' (default) or 'fp64'."""
         _check(self.lib.fdmgpu_set_residual_mode(self.h, {"fp64": 0, "df64": 1}[mode]))
+
+    def set_refinement(self, mode: str = "gmres", krylov_dim: int = 12):
+        """Refinement of the mixed path: 'gmres' (GMRES-IR, default) or 'classic'."""
+        _check(self.lib.fdmgpu_set_refinement(self.h, {"classic": 0, "gmres": 1}[mode], krylov_dim))
+
+    def set_escalation(self, mode: str = "df64"):
+        """Re-solve arithmetic for energies the FP32 factors cannot refine: 'df64' or 'fp64'."""
+        _check(self.lib.fdmgpu_set_escalation(self.h, {"fp64": 0, "df64": 1}[mode]))
 
     def close(self):
         if getattr(self, "h", None):
@@ -145,7 +157,7 @@ class FdmSolver:
             _check(st)
         d = info_dict(info)
         d["not_converged"] = [k for k in range(len(self._batch_args) or 0)
-                              if self.lib.fdmgpu_batch_stats(self.h, k, None, None, None) == 5]
+                              if self.lib.fdmgpu_batch_stats(self.h, k, None, None, None, None) == 5]
         return d
 
     def spectrum_rerun(self) -> dict:
@@ -168,16 +180,17 @@ class FdmSolver:
         _check(self.lib.fdmgpu_batch_solution(self.h, k, smr.ctypes.data))
         return smr
 
-    def stats(self, k: int) -> Tuple[int, float, bool]:
-        """Refinement iterations, final relative correction and whether energy k
-        was solved again in FP64 (precision escalation)."""
+    def stats(self, k: int) -> Tuple[int, float, bool, int]:
+        """Refinement iterations, final relative correction, whether energy k was
+        solved again in FP64 (precision escalation) and its GMRES steps."""
         it = C.c_int32(0)
         r = C.c_double(0)
         fb = C.c_int32(0)
-        st = self.lib.fdmgpu_batch_stats(self.h, k, C.byref(it), C.byref(r), C.byref(fb))
+        inner = C.c_int32(0)
+        st = self.lib.fdmgpu_batch_stats(self.h, k, C.byref(it), C.byref(r), C.byref(fb), C.byref(inner))
         if st not in (0, 5):
             _check(st)
-        return it.value, r.value, bool(fb.value)
+        return it.value, r.value, bool(fb.value), inner.value
 
     def spectrum(self, items: Sequence[Tuple[CL.EnergyInputs, CL.RowIndex]], precision: str = "mixed",
                  iaabs: int = 1):

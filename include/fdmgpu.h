@@ -56,6 +56,19 @@ typedef enum {
                                   FP32 pipes: the default, GB300 FP64 is ~60x slower    */
 } fdmgpu_residual_mode;
 
+/* Refinement of the mixed precision path. */
+typedef enum {
+  FDMGPU_REFINE_CLASSIC = 0,   /* x += LU32^-1 r                                        */
+  FDMGPU_REFINE_GMRES = 1      /* GMRES-IR: GMRES(m) on LU32^-1 A per correction (default) */
+} fdmgpu_refinement;
+
+/* Re-solve of an energy whose mixed precision refinement missed its tolerance. */
+typedef enum {
+  FDMGPU_ESCALATE_FP64 = 0,    /* FP64 profile LU (no pivoting, as the reference)       */
+  FDMGPU_ESCALATE_DF64 = 1     /* double-float LU of the equilibrated matrix with
+                                  tile-local pivoting + 2 refinement steps (default)   */
+} fdmgpu_escalation;
+
 /* Energy-independent arguments of mat_solve (source/mat_solve_gaussian.f90:17-67). */
 typedef struct fdmgpu_grid {
   int32_t npoint;     /* grid points inside the FDM sphere                                   */
@@ -180,6 +193,14 @@ fdmgpu_status fdmgpu_mat_solve(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t
  * No counterpart in the reference, which solves in FP64 only. */
 fdmgpu_status fdmgpu_set_residual_mode(fdmgpu_handle* h, int32_t mode);
 
+/* Refinement scheme of the mixed precision path and the Krylov dimension of
+ * one GMRES cycle (1..16, default 12).  No counterpart in the reference. */
+fdmgpu_status fdmgpu_set_refinement(fdmgpu_handle* h, int32_t mode, int32_t krylov_dim);
+
+/* Escalation arithmetic for energies the FP32 factors cannot refine.  No
+ * counterpart in the reference. */
+fdmgpu_status fdmgpu_set_escalation(fdmgpu_handle* h, int32_t mode);
+
 /* Counterpart of getSolverParams (source/mat_solve_gaussian.f90:376-389,
  * source/mat_solve_mumps.f90:705-736): solver name "GPU" and group size 1. */
 void fdmgpu_get_solver_params(int32_t* mpi_host_num_for_mumps, char solver[6]);
@@ -203,11 +224,12 @@ fdmgpu_status fdmgpu_batch_rerun(fdmgpu_handle* h, fdmgpu_info* info);
 fdmgpu_status fdmgpu_batch_taull(fdmgpu_handle* h, int32_t k, double* taull, int32_t* nlm);
 /* Solution of energy k (nlmso, nligne) column-major into smr (host). */
 fdmgpu_status fdmgpu_batch_solution(fdmgpu_handle* h, int32_t k, double* smr);
-/* Per-energy diagnostics of the last run: refinement iterations, final
- * relative correction max|dx|/max|x|, and whether the energy was solved again
- * in FP64.  Returns the energy's status (FDMGPU_OK when it converged). */
+/* Per-energy diagnostics of the last run: refinement (outer) iterations,
+ * final relative correction max|dx|/max|x|, whether the energy was solved
+ * again in FP64, and the GMRES steps summed over the refinement.  Returns the
+ * energy's status (FDMGPU_OK when it converged).  Any pointer may be NULL. */
 fdmgpu_status fdmgpu_batch_stats(fdmgpu_handle* h, int32_t k, int32_t* iters, double* residual,
-                                 int32_t* fallback);
+                                 int32_t* fallback, int32_t* inner_iters);
 
 #ifdef __cplusplus
 }
