@@ -1152,4 +1152,26 @@ fdmgpu_status fdmgpu_mat_solve(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t
   return st2 ? st2 : st;
 }
 
+fdmgpu_status fdmgpu_taull_noalloc(const double* d_smr, int32_t nlmso, int32_t nligne, int32_t ianew_abs,
+                                   int32_t nlm_abs, double* d_taull, int32_t* d_status, void* stream) {
+  if (!d_smr || !d_taull) return fail(FDMGPU_ERR_ARG, "null device pointer");
+  if (nlmso < 1 || nlm_abs < 1 || nligne < nlmso || ianew_abs < 0 || (int64_t)ianew_abs + nlm_abs > nligne)
+    return fail(FDMGPU_ERR_ARG, "inconsistent nlmso / nligne / ianew_abs / nlm_abs");
+  if (nlmso > FDMGPU_TAULL_NOALLOC_MAX_NLMSO)
+    return fail(FDMGPU_ERR_ARG, "nlmso = " + std::to_string(nlmso) + " exceeds FDMGPU_TAULL_NOALLOC_MAX_NLMSO = " +
+                                    std::to_string(FDMGPU_TAULL_NOALLOC_MAX_NLMSO));
+  const int64_t need = (int64_t)nlmso * (nlmso + nlm_abs) * 16;
+  if (need > FDMGPU_TAULL_NOALLOC_SCRATCH_BYTES)
+    return fail(FDMGPU_ERR_ARG, "working matrix of " + std::to_string(need) + " bytes exceeds the " +
+                                    std::to_string(FDMGPU_TAULL_NOALLOC_SCRATCH_BYTES) + "-byte static scratch");
+  if (reinterpret_cast<uintptr_t>(d_taull) % 16 || reinterpret_cast<uintptr_t>(d_smr) % 8 ||
+      reinterpret_cast<uintptr_t>(d_status) % 4)
+    return fail(FDMGPU_ERR_ARG, "misaligned device pointer");
+  double2* scratch = nullptr;
+  CK(taull_noalloc_scratch(&scratch));
+  CK(launch_taull_noalloc(d_smr, nlmso, nligne, ianew_abs, nlm_abs, scratch, d_taull, d_status,
+                          static_cast<cudaStream_t>(stream)));
+  return FDMGPU_OK;
+}
+
 }  // extern "C"

@@ -93,6 +93,9 @@ int gmres_max_dim();
 void launch_copy_rhs(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s);
 void launch_dfl_escalation(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
                            dfl* D, int iters, cudaStream_t s);
+cudaError_t taull_noalloc_scratch(double2** out);
+cudaError_t launch_taull_noalloc(const double* smr, int nlmso, int nligne, int ianew_abs, int nlm_abs,
+                                 double2* scratch, double* taull, int* status, cudaStream_t s);
 void launch_taull(const Prob* probs, const Pools& pl, const LaunchDims& d, const double* X, cudaStream_t s);
 void launch_solution_out(const Prob& P, const double* X, double* smr_dev, cudaStream_t s);
 

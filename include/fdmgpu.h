@@ -231,6 +231,52 @@ fdmgpu_status fdmgpu_batch_solution(fdmgpu_handle* h, int32_t k, double* smr);
 fdmgpu_status fdmgpu_batch_stats(fdmgpu_handle* h, int32_t k, int32_t* iters, double* residual,
                                  int32_t* fallback, int32_t* inner_iters);
 
+/*
+ * Taull of one energy from a solution that is already in device memory,
+ * without allocating any device memory.  No counterpart in the reference,
+ * where mat forms Taull on the host right after mat_solve
+ * (source/mat.f90:306-405, symmetrised at :598-644).
+ *
+ * Who needs it: a caller that keeps smr on the GPU but may not allocate
+ * there.  Examples are a host code whose own memory pool already holds nearly
+ * all device memory, so a cudaMalloc here would fail, and a per-energy loop
+ * that shares the GPU with work on other streams, where cudaFree would stall
+ * all of it (cudaFree synchronises the whole device).  fdmgpu_batch_* allocate
+ * their pools on first use and are no use to such a caller.
+ *
+ * d_smr     device, (nlmso, nligne) column-major FP64: the layout
+ *           fdmgpu_mat_solve writes smr in.
+ * ianew_abs row offset of the absorber's rows, as ianew(iaabs) of mat_solve;
+ *           the absorber rows are ianew_abs + 1 .. ianew_abs + nlm_abs.
+ * d_taull   device, nlm_abs * nlm_abs complex values: interleaved re/im,
+ *           column-major, 16-byte aligned.  Same layout as
+ *           fdmgpu_batch_taull.
+ * d_status  device int32 or NULL.  The kernel sets it to FDMGPU_OK, or to
+ *           FDMGPU_ERR_ZERO_PIVOT when norm is singular.
+ * stream    a cudaStream_t, NULL for the default stream.  The call only
+ *           enqueues one kernel on it and returns.
+ *
+ * Limits: nlmso <= FDMGPU_TAULL_NOALLOC_MAX_NLMSO, and the working matrix,
+ * nlmso * (nlmso + nlm_abs) * 16 bytes, must fit in the fixed
+ * FDMGPU_TAULL_NOALLOC_SCRATCH_BYTES (2 MiB) array that the library's device
+ * image holds for it.  Larger sizes return FDMGPU_ERR_ARG and enqueue nothing.
+ * Nothing has to start at zero: the kernel writes every element of that array
+ * before reading it, and writes *d_status itself.
+ *
+ * Ordering: there is one such array per device, shared by all calls on that
+ * device.  Calls that can overlap on the GPU race on it: calls from several
+ * host threads, or on more than one stream.  The caller must order them, for
+ * example by issuing them all on one stream.
+ *
+ * The first call on each device looks up the array's address, with that
+ * device current.  That lookup can load the library's device code.  A caller
+ * that captures streams should make one call on each device before capture.
+ */
+#define FDMGPU_TAULL_NOALLOC_SCRATCH_BYTES (2 * 1024 * 1024)
+#define FDMGPU_TAULL_NOALLOC_MAX_NLMSO 512
+fdmgpu_status fdmgpu_taull_noalloc(const double* d_smr, int32_t nlmso, int32_t nligne, int32_t ianew_abs,
+                                   int32_t nlm_abs, double* d_taull, int32_t* d_status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
