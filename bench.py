@@ -175,11 +175,23 @@ def run_gpu(args):
     B.build()
 
     step = E_STEP if args.energies == 401 else (E_MAX - E_MIN) / max(args.energies - 1, 1)
-    energies = CL.energy_grid(E_MIN, E_MAX, step)
+    # N ranks: an N times finer spectrum, dealt round-robin over the ranks as the
+    # reference's MPI energy loop does (source/fdm.f90:3484-3497); every rank
+    # solves its own energies with no device collective (weak scaling)
+    from fdmnes_gb300 import shard
+    all_energies = CL.energy_grid(E_MIN, E_MAX, step / world)
+    mine = shard.energy_shard(len(all_energies), rank, world)
+    energies = all_energies[mine]
     n_e = len(energies)
+    n_all = len(all_energies)
     st = CL.cu_structure()
     items = xanes.spectrum_inputs(st, energies)
     sv = FdmSolver(st)
+    # operating point for the metric's <= 1e-6 cross-section bar: refinement
+    # stops at max|dx|/max|x| <= 1e-8 and accepts stalls up to 1e-6 (measured
+    # convolved error ~3e-9); the library default (1e-10) is kept for parity
+    TOL, TOL_ACCEPT = 1e-8, 1e-6
+    sv.set_tolerance(TOL, TOL_ACCEPT)
 
     def barrier_sync():
         torch.cuda.synchronize()
@@ -225,7 +237,7 @@ def run_gpu(args):
     # device time of the spectrum: sum of the phases timed by CUDA events on the solver's stream
     dev_ms = [i["ms_assemble"] + i["ms_factor"] + i["ms_solve"] + i["ms_refine"] for i in infos]
     ms_step = max_over_ranks(statistics.mean(dev_ms))
-    value = world * n_e / (ms_step / 1000.0)
+    value = n_all / (ms_step / 1000.0)
 
     # end to end through the C-ABI from host buffers
     h2d = d2h = 0
@@ -249,12 +261,26 @@ def run_gpu(args):
 
     peaks, peak_kind = _peaks()
     last = infos[-1]
-    achieved = last["flops_factor"] / (last["ms_factor"] / 1000.0) / 1e12
-    roof = {"bound": "tensor", "achieved": achieved, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
-            "frac": achieved / peaks["bf16_tflops"], "traffic": None,
-            "kernel": "FP32 profile LU phase (k_diag + k_panel + k_trailing<float>)",
-            "peak_note": f"bf16 dense tensor peak ({peak_kind}); the factor runs on the FP32 pipes "
-                         f"(73.1 TFLOP/s probed on this pool)", "frac_of_fp32_pipe": achieved / 73.1}
+    FP32_PIPE_TFLOPS = 73.1  # FP32 FMA rate probed on this GB300 pool (2 flops per FMA)
+
+    def roof(flops, ms, kernel, note):
+        ach = flops / (ms / 1000.0) / 1e12 if ms > 0 else 0.0
+        return {"bound": "tensor", "achieved": ach, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
+                "frac": ach / peaks["bf16_tflops"], "traffic": None, "kernel": kernel,
+                "peak_note": f"bf16 dense tensor peak ({peak_kind}); {note}",
+                "frac_of_fp32_pipe": ach / FP32_PIPE_TFLOPS}
+
+    # dominant phase of the step (launch list in profiles/): the double-float
+    # re-factorisation of the energies FP32 refinement cannot converge
+    roof_main = roof(last["flops_escalate_factor"], last["ms_escalate_factor"],
+                     "double-float escalation factor (k_diag/k_panel/k_trailing<dfl>), one launch sequence per step",
+                     "runs on the FP32 pipes, ~12 FP32 instructions per double-float multiply-add; flops counted "
+                     "as 2 per multiply-add of the profile")
+    roof_res = roof(last["flops_residual"], last["ms_residual_first"],
+                    "k_residual_df, first refinement step (all energies active)",
+                    "double-float residual on the FP32 pipes; 2 flops per CSR nonzero per right-hand side")
+    roof_fac = roof(last["flops_factor"], last["ms_factor"], "FP32 profile LU (k_diag + k_panel + k_trailing<float>)",
+                    "FP32 SIMT pipes")
     if rank != 0:
         return
     cb = cpu_baseline(min(os.cpu_count() or 1, 16)) if not args.no_cpu else None
@@ -263,18 +289,20 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 factor + f64 refinement (df64 residual)", "data": "synthetic",
         "config": {"workload": "Cu fcc a=3.61 A, 13-atom cluster, FDM radius 3.0 A, step 0.25 A, C1, "
-                               f"{n_e} energies -5..35 eV step {step:.2g} eV, batched mixed precision",
-                   "energies": n_e, "e_step_ev": step, "nligne": [min(r.nligne for _, r in items), max(r.nligne for _, r in items)],
+                               f"{n_all} energies -5..35 eV step {step / world:.2g} eV, batched mixed precision",
+                   "energies": n_all, "energies_per_gpu": n_e, "e_step_ev": step / world, "nligne": [min(r.nligne for _, r in items), max(r.nligne for _, r in items)],
                    "nrhs": [min(e.nlmso for e, _ in items), max(e.nlmso for e, _ in items)],
-                   "l2": "working set ~100 GB per step, far above the 126 MB L2 (no flush needed)"},
-        "roofline": roof,
+                   "l2": "working set ~100 GB per step, far above the 126 MB L2 (no flush needed)",
+                   "refine_tol": TOL, "refine_tol_accept": TOL_ACCEPT},
+        "roofline": roof_main,
+        "roofline_other": [roof_res, roof_fac],
         "cpu_baseline": cb and {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
-        "e2e": {"value": world * n_e / e2e_s, "unit": "energies/s", "h2d_bytes_per_step": int(h2d),
+        "e2e": {"value": n_all / e2e_s, "unit": "energies/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(last["n_kernels"]),
         "clocks": clocks,
         "plain_fp64": {"value": n_e / (fp64_ms / 1000.0), "unit": "energies/s", "ms_per_step": fp64_ms,
-                       "first_call_wall_s": fp64_wall},
+                       "first_call_wall_s": fp64_wall, "gpu_launches": int(info64["n_kernels"])},
         "accuracy": {"convolved_rel_err_vs_fp64": err_conv, "taull_max_rel_err_vs_fp64": err_taull,
                      "refine_iters_max": last["refine_iters"], "fp64_escalations": last["n_fallback"]},
         "phases_ms": {k: last[k] for k in ("ms_assemble", "ms_factor", "ms_solve", "ms_refine")},

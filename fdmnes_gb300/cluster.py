@@ -121,6 +121,58 @@ def fcc_cluster(name: str, a_ang: float, Z: int, r_cluster_ang: float,
                    pot_atoms=allp.T / BOHR, pot_Z=np.full(allp.shape[0], Z), pot_zeff=zeff)
 
 
+def rutile_cluster(r_cluster_ang: float, a_ang: float = 4.594, c_ang: float = 2.959, u: float = 0.305,
+                   r_pot_ang: float = 8.0) -> Cluster:
+    """Rutile TiO2 (P4_2/mnm) cluster centred on a Ti absorber.
+
+    Ti at (0,0,0) and (1/2,1/2,1/2); O at (u,u,0), (-u,-u,0), (1/2+u,1/2-u,1/2),
+    (1/2-u,1/2+u,1/2).  Prototypes: 0 = Ti absorber, 1 = Ti, 2 = O.
+    """
+    basis = [(22, (0.0, 0.0, 0.0)), (22, (0.5, 0.5, 0.5)),
+             (8, (u, u, 0.0)), (8, (-u, -u, 0.0)), (8, (0.5 + u, 0.5 - u, 0.5)), (8, (0.5 - u, 0.5 + u, 0.5))]
+    na = int(math.ceil(r_pot_ang / a_ang)) + 1
+    nc = int(math.ceil(r_pot_ang / c_ang)) + 1
+    pts, zs = [], []
+    for ix in range(-na, na + 1):
+        for iy in range(-na, na + 1):
+            for iz in range(-nc, nc + 1):
+                for Z, (bx, by, bz) in basis:
+                    pts.append(((ix + bx) * a_ang, (iy + by) * a_ang, (iz + bz) * c_ang))
+                    zs.append(Z)
+    pts = np.array(pts)
+    zs = np.array(zs)
+    d = np.sqrt((pts ** 2).sum(1))
+    order = np.lexsort((pts[:, 2], pts[:, 1], pts[:, 0], np.round(d, 6)))
+    pts, zs, d = pts[order], zs[order], d[order]
+    sel = d <= r_cluster_ang + 1e-6
+    allsel = d <= r_pot_ang + 1e-6
+    pos = pts[sel].T / BOHR
+    Zc = zs[sel]
+    itype = np.where(Zc == 22, 1, 2).astype(np.int32)
+    itype[0] = 0
+    zproto = np.array([22, 22, 8])
+    rmt = np.array([_fdm_rmt_angstrom(int(z)) for z in zproto]) / BOHR
+    rmtg = np.array([1.04, 1.04, 0.91]) / BOHR
+    allp, allz = pts[allsel], zs[allsel]
+    zeff = allz.astype(np.float64)
+    zeff[0] = allz[0] + 1.0  # Z+1 model of the core hole on the absorber
+    return Cluster(name="TiO2", pos=np.asfortranarray(pos), Z=Zc, itype=itype, rmt=rmt, rmtg=rmtg,
+                   zproto=zproto, pot_atoms=allp.T / BOHR, pot_Z=allz, pot_zeff=zeff)
+
+
+def move_shell(cl: Cluster, shell_radius_ang: float, delta_ang: float, tol_ang: float = 0.01) -> Cluster:
+    """The cluster with every atom at distance shell_radius_ang (+- tol) from the
+    absorber moved radially by delta_ang, in the cluster and in the atoms that
+    build the potential."""
+    def moved(pos):
+        out = np.array(pos, dtype=np.float64, copy=True)
+        d = np.sqrt((out ** 2).sum(0))
+        sel = np.abs(d * BOHR - shell_radius_ang) < tol_ang
+        out[:, sel] *= (d[sel] + delta_ang / BOHR) / d[sel]
+        return out
+    return dataclasses.replace(cl, pos=np.asfortranarray(moved(cl.pos)), pot_atoms=moved(cl.pot_atoms))
+
+
 def cu_cluster(r_cluster_ang: float = 2.6) -> Cluster:
     """fcc Cu, a = 3.61 A, absorber at the origin (13 atoms within 2.6 A)."""
     return fcc_cluster("Cu", 3.61, 29, r_cluster_ang, r_pot_ang=8.0, rmtg_ang=1.28)
@@ -595,10 +647,17 @@ class Structure:
     radial_r: List[np.ndarray]   # per prototype radial mesh
     radial_V: List[np.ndarray]   # per prototype radial potential
     nspin: int = 1
+    spin_split: float = 0.0    # Ry: spin block 1 is shifted by -split/2, block 2 by +split/2
 
     @property
     def natome(self):
         return self.cluster.natome
+
+    def spin_shift(self, ispin: int) -> float:
+        """Potential shift (Ry) of spin block ispin (1-based)."""
+        if self.nspin == 1:
+            return 0.0
+        return (-0.5 if ispin == 1 else 0.5) * self.spin_split
 
 
 def build_structure(cl: Cluster, adimp_ang: float, rsort_ang: float, e_max_ev: float,
@@ -685,7 +744,8 @@ def build_structure(cl: Cluster, adimp_ang: float, rsort_ang: float, e_max_ev: f
     return Structure(cluster=cl, grid=g, lmaxat_max=lmaxat_max, lmaxso_max=lmaxso_max,
                      nlmmax=nlmmax, nlmomax=nlmomax, Ylmato=Ylmato, Ylmso=Ylmso, rrel=rrel,
                      lato=lato, mato=mato, iato=iato, lso=lso, mso=mso, iso=iso, distai=distai,
-                     Vr=Vr, V0bd=v0, radial_r=radial_r, radial_V=radial_V, nspin=nspin)
+                     Vr=Vr, V0bd=v0, radial_r=radial_r, radial_V=radial_V, nspin=nspin,
+                     spin_split=spin_split_ev / RYDB)
 
 
 @dataclasses.dataclass
@@ -710,7 +770,8 @@ def energy_inputs(st: Structure, energy_ev: float, e_fermi_ev: float = -5.0, isp
     """Per-energy inputs: l cut-offs, atomic boundary functions, Bessel/Neumann."""
     cl, g = st.cluster, st.grid
     enervide = (energy_ev + e_fermi_ev) / RYDB
-    ecin = enervide - st.V0bd
+    dv = st.spin_shift(ispin)
+    ecin = enervide - (st.V0bd + dv)
     ecin_out = ecin
     if ecin_out < EPS10:
         raise ValueError("kinetic energy in the outer sphere must be positive for the real path")
@@ -732,7 +793,7 @@ def energy_inputs(st: Structure, energy_ev: float, e_fermi_ev: float = -5.0, isp
     for ia in range(natome):
         ipr = int(cl.itype[ia])
         r = st.radial_r[ipr]
-        Vrad = st.radial_V[ipr]
+        Vrad = st.radial_V[ipr] + dv
         nb = int(g.nbord[ia])
         rr = st.rrel[:nb, ia]
         idx = np.searchsorted(r, rr, side="right")   # first r(i) > rrel, 0-based

@@ -85,6 +85,7 @@ struct Batch {
   std::vector<double> resid;
   std::vector<int> err;
   bool ran = false;
+  bool lam_valid = false;  // the adjoint Lambda of the last vjp matches the batch's factors
 };
 
 }  // namespace
@@ -112,8 +113,8 @@ struct fdmgpu_handle {
   DevBuf<int> d_ipool;
   DevBuf<double> d_dpool;
   DevBuf<double> d_env64, d_B64, d_X64, d_rs, d_cs, d_val, d_taull, d_tscratch, d_smr;
-  DevBuf<float> d_env32, d_Y32, d_dinv32;
-  DevBuf<double> d_dinv64;
+  DevBuf<double> d_gT, d_lam, d_gpart, d_grad;  // adjoint
+  DevBuf<float> d_env32, d_Y32;
   DevBuf<float2> d_val2, d_Xs;
   DevBuf<float> d_valS, d_V, d_W;
   DevBuf<unsigned char> d_gstate;
@@ -122,6 +123,8 @@ struct fdmgpu_handle {
   int refine_gmres = 0;   // GMRES-IR (1) or classical refinement (0)
   int escalate_dfl = 1;   // escalation by a double-float (1) or an FP64 (0) factorisation
   int gmres_m = 12;       // Krylov dimension of one GMRES cycle
+  double tol = 0.0;         // refinement stop: max|dx|/max|x| (0: the default of the residual mode)
+  double tol_accept = 0.0;  // accepted without escalation when refinement stalls (0: default)
   int64_t ncols = 0;      // right-hand-side columns of the batch (sum of nrt * TS)
   int64_t ncols_tmp = 0;
   DevBuf<int> d_rowptr, d_col, d_err, d_active, d_piv;
@@ -134,13 +137,14 @@ struct fdmgpu_handle {
   uint64_t plan_sig = 0;
   uint64_t ptr_sig = 0;
   int plan_prec = -1;
-  cudaGraphExec_t g_asm = nullptr, g_fac = nullptr, g_sol = nullptr, g_iter = nullptr;
-  int64_t nk_asm = 0, nk_fac = 0, nk_sol = 0, nk_iter = 0;  // kernel nodes per graph
+  cudaGraphExec_t g_asm = nullptr, g_fac = nullptr, g_sol = nullptr, g_res = nullptr, g_iter = nullptr;
+  int64_t nk_asm = 0, nk_fac = 0, nk_sol = 0, nk_res = 0, nk_iter = 0;  // kernel nodes per graph
   StepPlan sp;
   LaunchDims dims;
   Tables tb{};
   Pools pl{};
-  cudaEvent_t ev[6] = {};
+  cudaEvent_t ev[10] = {};
+  DevBuf<int> d_nnz;  // CSR nonzeros per problem (algorithmic work of the residual)
 };
 
 namespace {
@@ -319,6 +323,8 @@ void build_step_plan(fdmgpu_handle* h) {
   sp.trail_rhs.assign(N, 0);
   sp.fwd.assign(N, 0);
   sp.bwd.assign(N, 0);
+  sp.tfwd.assign(N, 0);
+  sp.tbwd.assign(N, 0);
   for (auto& hp : pr) {
     for (int K = 0; K < hp.P.nt; ++K) {
       const int nI = hp.Imax[K] - K, nJ = hp.J1[K] - K, nR = hp.P.nrt;
@@ -328,6 +334,8 @@ void build_step_plan(fdmgpu_handle* h) {
       sp.trail_rhs[K] = std::max(sp.trail_rhs[K], nI * (nJ + nR));
       sp.fwd[K] = std::max(sp.fwd[K], nI * nR);
       sp.bwd[K] = std::max(sp.bwd[K], (K - hp.Imin[K]) * nR);
+      sp.tfwd[K] = std::max(sp.tfwd[K], nJ * nR);
+      sp.tbwd[K] = std::max(sp.tbwd[K], (K - hp.J0[K]) * nR);
     }
   }
 }
@@ -336,7 +344,7 @@ void build_step_plan(fdmgpu_handle* h) {
 // Runs on every batch (the descriptors are rebuilt by fdmgpu_batch_add);
 // allocate_and_upload_plan() below runs only when the plan changes.
 struct Layout {
-  int64_t env = 0, rhs = 0, rowv = 0, csr = 0, taull = 0, scratch = 0, dinv = 0;
+  int64_t env = 0, rhs = 0, rowv = 0, csr = 0, taull = 0, scratch = 0;
   std::vector<int> J0, J1, Imax, Imin;
   std::vector<int64_t> strip;
 };
@@ -346,7 +354,7 @@ void layout_batch(fdmgpu_handle* h, Layout& L) {
   const int np = (int)pr.size();
   const bool mixed = h->batch.precision == FDMGPU_PREC_MIXED;
   int64_t& env = L.env; int64_t& rhs = L.rhs; int64_t& rowv = L.rowv;
-  int64_t& csr = L.csr; int64_t& taull = L.taull; int64_t& scratch = L.scratch; int64_t& dinv = L.dinv;
+  int64_t& csr = L.csr; int64_t& taull = L.taull; int64_t& scratch = L.scratch;
   int trow = 0;
   LaunchDims& d = h->dims;
   d = LaunchDims();
@@ -368,15 +376,13 @@ void layout_batch(fdmgpu_handle* h, Layout& L) {
     h->ncols_tmp += (int64_t)P.nrt * TS;
     P.taull = taull;
     P.scratch = scratch;
-    P.dinv = dinv;
-    dinv += (int64_t)2 * P.nt * TS2;
     trow += P.nt + 1;
     env += hp.ntiles;
     rhs += (int64_t)P.nt * P.nrt * TS2;
     rowv += (int64_t)P.nt * TS + 1;
     csr += mixed ? hp.nnz_cap : 0;
     taull += (int64_t)P.nlm_abs * P.nlm_abs;
-    scratch += (int64_t)P.nlmso * (P.nlmso + P.nlm_abs);
+    scratch += (int64_t)P.nlmso * (P.nlmso + 2 * P.nlm_abs);  // N | Xa, then the adjoint's Q
     J0.insert(J0.end(), hp.J0.begin(), hp.J0.end());
     J1.insert(J1.end(), hp.J1.begin(), hp.J1.end());
     Imax.insert(Imax.end(), hp.Imax.begin(), hp.Imax.end());
@@ -407,7 +413,6 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   CK(upload(h->d_Imin, Imin, s));
   CK(upload(h->d_strip, strip, s));
   if (h->d_env64.reserve((size_t)env * TS2) != cudaSuccess || h->d_B64.reserve(rhs) != cudaSuccess ||
-      h->d_dinv64.reserve(L.dinv) != cudaSuccess ||
       h->d_X64.reserve(rhs) != cudaSuccess || h->d_err.reserve(np) != cudaSuccess ||
       h->d_active.reserve(np) != cudaSuccess || h->d_red.reserve(3 * (size_t)np) != cudaSuccess ||
       h->d_taull.reserve(2 * (size_t)std::max<int64_t>(taull, 1)) != cudaSuccess ||
@@ -415,7 +420,6 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
     return fail(FDMGPU_ERR_NOMEM, "device allocation of the batch pools failed");
   if (mixed) {
     if (h->d_env32.reserve((size_t)env * TS2) != cudaSuccess || h->d_Y32.reserve(rhs) != cudaSuccess ||
-        h->d_dinv32.reserve(L.dinv) != cudaSuccess ||
         h->d_rs.reserve(rowv) != cudaSuccess || h->d_cs.reserve(rowv) != cudaSuccess ||
         h->d_rowptr.reserve(rowv) != cudaSuccess || h->d_col.reserve(csr) != cudaSuccess ||
         h->d_piv.reserve(rowv) != cudaSuccess || h->d_val2.reserve(csr) != cudaSuccess ||
@@ -435,7 +439,6 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   Pools& pl = h->pl;
   pl = Pools();
   pl.env64 = h->d_env64.p;
-  pl.dinv64 = h->d_dinv64.p;
   pl.B64 = h->d_B64.p;
   pl.X64 = h->d_X64.p;
   pl.err = h->d_err.p;
@@ -447,7 +450,6 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   pl.tscratch = h->d_tscratch.p;
   if (mixed) {
     pl.env32 = h->d_env32.p;
-    pl.dinv32 = h->d_dinv32.p;
     pl.Y32 = h->d_Y32.p;
     pl.rs = h->d_rs.p;
     pl.cs = h->d_cs.p;
@@ -549,9 +551,9 @@ void record_factor(fdmgpu_handle* h) {
   const Pools& pl = h->pl;
   const int np = h->dims.nprob;
   if (h->batch.precision == FDMGPU_PREC_FP64)
-    launch_factor<double>(h->sp, pl.env64, pl.X64, pl.dinv64, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-10, nullptr, s);
+    launch_factor<double>(h->sp, pl.env64, pl.X64, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-10, nullptr, s);
   else
-    launch_factor<float>(h->sp, pl.env32, pl.Y32, pl.dinv32, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-30, pl.piv, s);
+    launch_factor<float>(h->sp, pl.env32, pl.Y32, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-30, pl.piv, s);
 }
 
 void record_solve(fdmgpu_handle* h) {
@@ -559,12 +561,21 @@ void record_solve(fdmgpu_handle* h) {
   const Pools& pl = h->pl;
   const int np = h->dims.nprob;
   if (h->batch.precision == FDMGPU_PREC_FP64) {
-    launch_backward<double>(h->sp, pl.env64, pl.X64, pl.dinv64, h->d_probs.p, h->tb, np, nullptr, s);
+    launch_backward<double>(h->sp, pl.env64, pl.X64, h->d_probs.p, h->tb, np, nullptr, s);
   } else {
-    launch_backward<float>(h->sp, pl.env32, pl.Y32, pl.dinv32, h->d_probs.p, h->tb, np, nullptr, s);
+    launch_backward<float>(h->sp, pl.env32, pl.Y32, h->d_probs.p, h->tb, np, nullptr, s);
     cudaMemsetAsync(pl.dmax, 0, 3 * np * sizeof(unsigned long long), s);
     launch_update_x(h->d_probs.p, pl, h->dims, 1, s);
   }
+}
+
+// One refinement step in two graphs: the residual, then the correction (so
+// that the first residual of a run can be timed on its own).
+void record_residual(fdmgpu_handle* h) {
+  cudaStream_t s = h->stream;
+  const Pools& pl = h->pl;
+  cudaMemsetAsync(pl.dmax, 0, 3 * h->dims.nprob * sizeof(unsigned long long), s);
+  launch_residual(h->d_probs.p, pl, h->dims, h->residual_df64, s);
 }
 
 void record_iter(fdmgpu_handle* h) {
@@ -572,13 +583,11 @@ void record_iter(fdmgpu_handle* h) {
   const Pools& pl = h->pl;
   const Prob* probs = h->d_probs.p;
   const int np = h->dims.nprob;
-  cudaMemsetAsync(pl.dmax, 0, 3 * np * sizeof(unsigned long long), s);
-  launch_residual(probs, pl, h->dims, h->residual_df64, s);
   if (h->refine_gmres) {
     launch_gmres_cycle(h->sp, probs, pl, h->tb, h->dims, h->gmres_m, 1e-6f, s);
   } else {
-    launch_forward<float>(h->sp, pl.env32, pl.Y32, pl.dinv32, probs, h->tb, np, pl.active, pl.piv, s);
-    launch_backward<float>(h->sp, pl.env32, pl.Y32, pl.dinv32, probs, h->tb, np, pl.active, s);
+    launch_forward<float>(h->sp, pl.env32, pl.Y32, probs, h->tb, np, pl.active, pl.piv, s);
+    launch_backward<float>(h->sp, pl.env32, pl.Y32, probs, h->tb, np, pl.active, s);
   }
   launch_update_x(probs, pl, h->dims, 0, s);
 }
@@ -637,8 +646,9 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
                         h->d_X64.p,   h->d_Y32.p,   h->d_rs.p,    h->d_cs.p,    h->d_rowptr.p, h->d_col.p,
                         h->d_val.p,   h->d_err.p,   h->d_active.p, h->d_red.p,  h->d_J0.p,   h->d_strip.p,
                         h->d_piv.p,   h->d_val2.p,  h->d_Xs.p,    h->d_valS.p,  h->d_V.p,    h->d_W.p,
-                        h->d_gstate.p, h->d_inner.p, h->d_jdone.p, h->d_notconv.p, h->d_dinv64.p,
-                        h->d_dinv32.p, h->d_active_gm.p};
+                        h->d_gstate.p, h->d_inner.p, h->d_jdone.p, h->d_notconv.p, h->d_active_gm.p,
+                        h->d_nb_coef.p, h->d_rvol.p, h->d_poidsa.p, h->d_poidso.p, h->d_Kar.p, h->d_YsoT.p,
+                        h->d_Ylmato.p};
   for (const void* q : ptrs) ps = mix(ps, (uint64_t)(uintptr_t)q);
   if (replan || ps != h->ptr_sig) {
     h->ptr_sig = ps;
@@ -649,6 +659,8 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
     st = capture(h, record_solve, &h->g_sol, &h->nk_sol);
     if (st) return st;
     if (b.precision == FDMGPU_PREC_MIXED) {
+      st = capture(h, record_residual, &h->g_res, &h->nk_res);
+      if (st) return st;
       st = capture(h, record_iter, &h->g_iter, &h->nk_iter);
       if (st) return st;
     }
@@ -669,6 +681,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   b.resid.assign(np, 0.0);
   b.err.assign(np, 0);
   float ms_refine = 0;
+  bool esc_timed = false;
   if (b.precision == FDMGPU_PREC_MIXED) {
     // Per problem: classical refinement x += LU^-1 r while it contracts (a step
     // counts as slow when the correction does not halve); after two slow steps
@@ -678,8 +691,8 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
     // escalation.  Stop at max|dx|/max|x| <= tol; results above tol_accept go
     // to the FP64 escalation below.
     const int max_iter = 40;
-    const double tol = 1e-10;
-    const double tol_accept = h->residual_df64 ? 1e-7 : 1e-9;
+    const double tol = h->tol > 0 ? h->tol : 1e-10;
+    const double tol_accept = h->tol_accept > 0 ? h->tol_accept : (h->residual_df64 ? 1e-7 : 1e-9);
     std::vector<int> active(np, 1), slow(np, 0), gm(np, 0);
     std::vector<double> prev(np, 1e300);
     std::vector<unsigned long long> red(3 * np);
@@ -689,8 +702,11 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
       CK(cudaMemsetAsync(h->d_active_gm.p, 0, np * sizeof(int), h->stream));
     CK(cudaEventRecord(h->ev[4], h->stream));
     for (int it = 1; it <= max_iter; ++it) {
+      if (it == 1) CK(cudaEventRecord(h->ev[6], h->stream));
+      CK(cudaGraphLaunch(h->g_res, h->stream));
+      if (it == 1) CK(cudaEventRecord(h->ev[7], h->stream));
       CK(cudaGraphLaunch(h->g_iter, h->stream));
-      nkern += h->nk_iter;
+      nkern += h->nk_res + h->nk_iter;
       CK(cudaMemcpyAsync(red.data(), h->d_red.p, 3 * np * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
                          h->stream));
       if (h->refine_gmres)
@@ -747,16 +763,16 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
       if (h->escalate_dfl) {
         // double-float factorisation of the equilibrated matrix + 2 refinement steps
         CK(cudaMemsetAsync(h->pl.dmax, 0, 3 * np * sizeof(unsigned long long), h->stream));
-        launch_dfl_escalation(h->sp, h->d_probs.p, h->pl, h->tb, h->dims, reinterpret_cast<dfl*>(h->pl.V), 2,
-                              h->stream);
-        nkern += 2 + 10 * (int64_t)h->sp.ntmax + 2 * (3 + 4 * (int64_t)h->sp.ntmax);
+        nkern += launch_dfl_escalation(h->sp, h->d_probs.p, h->pl, h->tb, h->dims, reinterpret_cast<dfl*>(h->pl.V),
+                                       2, h->stream, h->ev[8], h->ev[9]);
+        esc_timed = true;
       } else {
         launch_copy_rhs(h->d_probs.p, h->pl, h->dims, h->stream);
-        nkern += 1 + 5 * (int64_t)h->sp.ntmax;
-        launch_factor<double>(h->sp, h->pl.env64, h->pl.X64, h->pl.dinv64, h->d_probs.p, h->tb, np, 1,
-                              h->d_active.p, h->pl.err, 1e-10, nullptr, h->stream);
-        launch_backward<double>(h->sp, h->pl.env64, h->pl.X64, h->pl.dinv64, h->d_probs.p, h->tb, np,
-                                h->d_active.p, h->stream);
+        nkern += 1;
+        nkern += launch_factor<double>(h->sp, h->pl.env64, h->pl.X64, h->d_probs.p, h->tb, np, 1,
+                                       h->d_active.p, h->pl.err, 1e-10, nullptr, h->stream);
+        nkern += launch_backward<double>(h->sp, h->pl.env64, h->pl.X64, h->d_probs.p, h->tb, np,
+                                         h->d_active.p, h->stream);
       }
       CK(cudaGetLastError());
       if (h->escalate_dfl) {
@@ -787,6 +803,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   for (int k = 0; k < np; ++k)
     if (err[k]) b.err[k] = err[k];
   b.ran = true;
+  b.lam_valid = false;
   if (info) {
     memset(info, 0, sizeof(*info));
     info->n_kernels = nkern;
@@ -805,6 +822,21 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
     if (b.precision == FDMGPU_PREC_MIXED) {
       CK(cudaEventElapsedTime(&ms_refine, h->ev[4], h->ev[5]));
       info->ms_refine = ms_refine;
+      CK(cudaEventElapsedTime(&t, h->ev[6], h->ev[7]));
+      info->ms_residual_first = t;
+      // algorithmic work of that residual: 2 flops per nonzero per right-hand side
+      if (h->d_nnz.reserve(np) != cudaSuccess) return fail(FDMGPU_ERR_NOMEM, "nnz buffer");
+      launch_csr_nnz(h->d_probs.p, h->pl.rowptr, h->dims, h->d_nnz.p, h->stream);
+      std::vector<int> nnz(np);
+      CK(cudaMemcpyAsync(nnz.data(), h->d_nnz.p, np * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+      CK(cudaStreamSynchronize(h->stream));
+      for (int k = 0; k < np; ++k) info->flops_residual += 2.0 * nnz[k] * b.probs[k].P.nlmso;
+      if (esc_timed) {
+        CK(cudaEventElapsedTime(&t, h->ev[8], h->ev[9]));
+        info->ms_escalate_factor = t;
+        for (int k = 0; k < np; ++k)
+          if (b.fallback[k]) info->flops_escalate_factor += b.probs[k].flops_factor;
+      }
       int mi = 0;
       double mr = 0;
       for (int k = 0; k < np; ++k) {
@@ -1000,6 +1032,8 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   if (h->g_fac) cudaGraphExecDestroy(h->g_fac);
   if (h->g_sol) cudaGraphExecDestroy(h->g_sol);
   if (h->g_iter) cudaGraphExecDestroy(h->g_iter);
+  if (h->g_res) cudaGraphExecDestroy(h->g_res);
+  h->d_nnz.release();
   DevBuf<int>* ib[] = {&h->d_inter_pt, &h->d_nb_kind, &h->d_nb_idx, &h->d_numia, &h->d_nbord, &h->d_nbordf,
                        &h->d_ibord,    &h->d_isbord,  &h->d_isrt,   &h->d_lato,  &h->d_mato,  &h->d_lso,
                        &h->d_mso,      &h->d_J0,      &h->d_J1,     &h->d_Imax,  &h->d_Imin,  &h->d_ipool,
@@ -1007,11 +1041,10 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   for (auto* b : ib) b->release();
   DevBuf<double>* db[] = {&h->d_nb_coef, &h->d_rvol, &h->d_clapl, &h->d_poidsa, &h->d_poidso, &h->d_Kar,
                           &h->d_YsoT,    &h->d_Ylmato, &h->d_dpool, &h->d_env64, &h->d_B64,  &h->d_X64,
-                          &h->d_rs,      &h->d_cs,   &h->d_val,   &h->d_taull,  &h->d_tscratch, &h->d_smr};
+                          &h->d_rs,      &h->d_cs,   &h->d_val,   &h->d_taull,  &h->d_tscratch, &h->d_smr,
+                          &h->d_gT,      &h->d_lam,  &h->d_gpart, &h->d_grad};
   for (auto* b : db) b->release();
   h->d_env32.release();
-  h->d_dinv32.release();
-  h->d_dinv64.release();
   h->d_val2.release();
   h->d_Xs.release();
   h->d_valS.release();
@@ -1047,6 +1080,14 @@ fdmgpu_status fdmgpu_set_refinement(fdmgpu_handle* h, int32_t mode, int32_t kryl
     return fail(FDMGPU_ERR_ARG, "unknown refinement mode or Krylov dimension out of range");
   h->refine_gmres = mode == FDMGPU_REFINE_GMRES;
   h->gmres_m = krylov_dim;
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_set_tolerance(fdmgpu_handle* h, double tol, double tol_accept) {
+  if (!h || !(tol >= 0) || !(tol_accept >= 0) || tol >= 1 || tol_accept >= 1 || (tol > 0 && tol_accept > 0 && tol_accept < tol))
+    return fail(FDMGPU_ERR_ARG, "tolerances must satisfy 0 <= tol <= tol_accept < 1 (0 selects the default)");
+  h->tol = tol;
+  h->tol_accept = tol_accept;
   return FDMGPU_OK;
 }
 
@@ -1150,6 +1191,188 @@ fdmgpu_status fdmgpu_mat_solve(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t
   if (st && st != FDMGPU_ERR_NOT_CONVERGED) return st;
   fdmgpu_status st2 = fdmgpu_batch_solution(h, 0, smr);
   return st2 ? st2 : st;
+}
+
+fdmgpu_status fdmgpu_batch_vjp(fdmgpu_handle* h, const double* gtaull, double* grad_vr, double* ms) {
+  if (!h || !gtaull || !grad_vr) return fail(FDMGPU_ERR_ARG, "null argument");
+  Batch& b = h->batch;
+  if (!b.ran) return fail(FDMGPU_ERR_ARG, "vjp needs a batch that has run");
+  if (b.precision != FDMGPU_PREC_FP64)
+    return fail(FDMGPU_ERR_UNSUPPORTED, "vjp needs the factors of an FP64 batch");
+  const int np = h->dims.nprob;
+  for (int k = 0; k < np; ++k) {
+    if (b.probs[k].P.nlm_abs <= 0) return fail(FDMGPU_ERR_ARG, "vjp needs an absorber (iaabs > 0) in every energy");
+    if (b.err[k]) return fail((fdmgpu_status)b.err[k], "vjp of a batch with a failed energy");
+  }
+  cudaStream_t s = h->stream;
+  int64_t ntaull = 0, nrhs = 0;
+  for (auto& hp : b.probs) {
+    ntaull = std::max<int64_t>(ntaull, hp.P.taull + (int64_t)hp.P.nlm_abs * hp.P.nlm_abs);
+    nrhs = std::max<int64_t>(nrhs, hp.P.rhs + (int64_t)hp.P.nt * hp.P.nrt * TS2);
+  }
+  const int nspin = std::max(h->g.nspin, 1);
+  if (h->d_gT.reserve(ntaull) != cudaSuccess || h->d_lam.reserve(nrhs) != cudaSuccess ||
+      h->d_gpart.reserve((size_t)np * std::max(h->S.npr, 1)) != cudaSuccess ||
+      h->d_grad.reserve((size_t)h->g.npoint * nspin) != cudaSuccess)
+    return fail(FDMGPU_ERR_NOMEM, "device allocation of the adjoint pools failed");
+  // per-energy cotangents, concatenated in add order, placed at the Taull offsets
+  std::vector<double> gT(ntaull, 0.0);
+  int64_t off = 0;
+  for (auto& hp : b.probs) {
+    const int64_t mm = (int64_t)hp.P.nlm_abs * hp.P.nlm_abs;
+    std::copy(gtaull + off, gtaull + off + mm, gT.begin() + hp.P.taull);
+    off += mm;
+  }
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(h->ev[0], s));
+  CK(cudaMemcpyAsync(h->d_gT.p, gT.data(), ntaull * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(h->d_lam.p, 0, nrhs * sizeof(double), s));
+  CK(cudaMemsetAsync(h->d_grad.p, 0, (size_t)h->g.npoint * nspin * sizeof(double), s));
+  launch_taull_vjp(h->d_probs.p, h->dims, h->pl.X64, h->d_gT.p, h->pl.tscratch, h->d_lam.p, h->pl.err, s);
+  launch_forward_t<double>(h->sp, h->pl.env64, h->d_lam.p, h->d_probs.p, h->tb, np, nullptr, s);
+  launch_backward_t<double>(h->sp, h->pl.env64, h->d_lam.p, h->d_probs.p, h->tb, np, nullptr, nullptr, s);
+  launch_grad_vr(h->S, h->d_probs.p, h->pl.ipool, h->dims, nspin, h->pl.X64, h->d_lam.p, h->d_gpart.p,
+                 h->d_grad.p, s);
+  CK(cudaGetLastError());
+  CK(cudaEventRecord(h->ev[1], s));
+  CK(cudaMemcpyAsync(grad_vr, h->d_grad.p, (size_t)h->g.npoint * nspin * sizeof(double), cudaMemcpyDeviceToHost, s));
+  std::vector<int> err(np);
+  CK(cudaMemcpyAsync(err.data(), h->pl.err, np * sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  float t = 0;
+  CK(cudaEventElapsedTime(&t, h->ev[0], h->ev[1]));
+  if (ms) *ms = t;
+  for (int k = 0; k < np; ++k)
+    if (err[k]) return fail((fdmgpu_status)err[k], "singular normalisation matrix in the Taull adjoint");
+  b.lam_valid = true;
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_update_grid_values(fdmgpu_handle* h, const fdmgpu_grid* g) {
+  if (!h || !g) return fail(FDMGPU_ERR_ARG, "null argument");
+  const fdmgpu_grid& a = h->g;
+  if (g->npoint != a.npoint || g->npsom != a.npsom || g->nvois != a.nvois || g->natome != a.natome ||
+      g->nbm != a.nbm || g->nbtm != a.nbtm || g->nim != a.nim || g->nsm != a.nsm || g->nsort != a.nsort ||
+      g->nsortf != a.nsortf || g->nstm != a.nstm || g->nspin != a.nspin || g->nlmmax != a.nlmmax ||
+      g->nlmomax != a.nlmomax || g->nlmsam != a.nlmsam || g->nso1 != a.nso1 || g->ngrph != a.ngrph ||
+      g->nspino != a.nspino)
+    return fail(FDMGPU_ERR_ARG, "grid sizes differ from the handle's");
+  fdmgpu_handle* t = nullptr;
+  fdmgpu_status st = fdmgpu_create(g, &t);
+  if (st) return st;
+  // the integer structure must be the handle's: neighbour kinds and indices,
+  // boundary and outer-point tables
+  bool same = t->inter_pt_h == h->inter_pt_h && t->nb_kind_h == h->nb_kind_h && t->nb_idx_h == h->nb_idx_h &&
+              t->nbordf_h == h->nbordf_h;
+  auto same_dev = [&](const DevBuf<int>& x, const DevBuf<int>& y, size_t n) {
+    std::vector<int> u(n), v(n);
+    if (n == 0) return true;
+    if (cudaMemcpy(u.data(), x.p, n * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemcpy(v.data(), y.p, n * sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return false;
+    return u == v;
+  };
+  same = same && same_dev(t->d_numia, h->d_numia, a.npsom) && same_dev(t->d_nbord, h->d_nbord, a.natome) &&
+         same_dev(t->d_ibord, h->d_ibord, (size_t)a.nbtm * a.natome) && same_dev(t->d_isrt, h->d_isrt, a.nstm) &&
+         same_dev(t->d_lato, h->d_lato, (size_t)a.nlmsam * a.natome) &&
+         same_dev(t->d_mato, h->d_mato, (size_t)a.nlmsam * a.natome);
+  if (!same) {
+    fdmgpu_destroy(t);
+    return fail(FDMGPU_ERR_ARG, "the grid's integer structure (membership, boundary, neighbours) changed");
+  }
+  CK(cudaStreamSynchronize(h->stream));
+  std::swap(h->d_nb_coef, t->d_nb_coef);
+  std::swap(h->d_rvol, t->d_rvol);
+  std::swap(h->d_clapl, t->d_clapl);
+  std::swap(h->d_poidsa, t->d_poidsa);
+  std::swap(h->d_poidso, t->d_poidso);
+  std::swap(h->d_Kar, t->d_Kar);
+  std::swap(h->d_YsoT, t->d_YsoT);
+  std::swap(h->d_Ylmato, t->d_Ylmato);
+  h->S.nb_coef = t->S.nb_coef;
+  h->S.rvol = t->S.rvol;
+  h->S.clapl = t->S.clapl;
+  h->S.poidsa = t->S.poidsa;
+  h->S.poidso = t->S.poidso;
+  h->S.Kar = t->S.Kar;
+  h->S.YsoT = t->S.YsoT;
+  h->S.Ylmato = t->S.Ylmato;
+  h->nb_coef_h.swap(t->nb_coef_h);
+  fdmgpu_destroy(t);  // frees the previous value tables
+  h->batch.ran = false;  // the batch's factors belong to the previous values
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_batch_adjoint_dot(fdmgpu_handle* h, const fdmgpu_energy* const* e, int32_t n, double* out) {
+  if (!h || !e || !out) return fail(FDMGPU_ERR_ARG, "null argument");
+  Batch& b = h->batch;
+  const int np = (int)b.probs.size();
+  if (!b.lam_valid) return fail(FDMGPU_ERR_ARG, "adjoint_dot needs a vjp of the batch that has run");
+  if (n != np) return fail(FDMGPU_ERR_ARG, "one energy argument per batch energy is needed");
+  for (int k = 0; k < np; ++k) {
+    fdmgpu_status st = check_energy(h, e[k]);
+    if (st) return st;
+    HostProb hp;
+    st = plan_problem(h, e[k], hp);
+    if (st) return st;
+    const Prob& P0 = b.probs[k].P;
+    if (hp.P.n != P0.n || hp.P.nlmso != P0.nlmso || hp.ntiles != b.probs[k].ntiles ||
+        hp.J0 != b.probs[k].J0 || hp.J1 != b.probs[k].J1 ||
+        (P0.iaabs > 0 && e[k]->ianew[P0.iaabs - 1] != P0.ianew_abs))
+      return fail(FDMGPU_ERR_ARG, "energy " + std::to_string(k) + ": row structure differs from the batch's");
+  }
+  // the new inputs replace the batch's; the solutions X and Lambda stay
+  for (int k = 0; k < np; ++k) {
+    HostProb hp;
+    hp.P = b.probs[k].P;
+    pack_inputs(h, e[k], hp);
+    if (hp.in_i.size() != b.probs[k].in_i.size() || hp.in_d.size() != b.probs[k].in_d.size())
+      return fail(FDMGPU_ERR_ARG, "energy " + std::to_string(k) + ": input sizes differ from the batch's");
+    b.probs[k].in_i.swap(hp.in_i);
+    b.probs[k].in_d.swap(hp.in_d);
+  }
+  b.ran = false;  // the factors are overwritten below; X and Lambda stay valid
+  // CSR copy of the new matrices: an FP64 batch plans no CSR, so place it here
+  int64_t csr_off = 0;
+  for (auto& hp : b.probs) {
+    hp.P.csr = csr_off;
+    hp.P.csr_cap = hp.nnz_cap;
+    csr_off += hp.nnz_cap;
+  }
+  fdmgpu_status st = upload_inputs(h);
+  if (st) return st;
+  int64_t env = 0, rhs = 0, rowv = 0, csr = 0;
+  for (auto& hp : b.probs) {
+    env = std::max<int64_t>(env, (hp.P.env / TS2 + hp.ntiles) * TS2);
+    rhs = std::max<int64_t>(rhs, hp.P.rhs + (int64_t)hp.P.nt * hp.P.nrt * TS2);
+    rowv = std::max<int64_t>(rowv, hp.P.rowv + (int64_t)hp.P.nt * TS + 1);
+    csr = std::max<int64_t>(csr, hp.P.csr + hp.P.csr_cap);
+  }
+  if (h->d_rowptr.reserve(rowv) != cudaSuccess || h->d_col.reserve(csr) != cudaSuccess ||
+      h->d_val.reserve(csr) != cudaSuccess || h->d_val2.reserve(csr) != cudaSuccess ||
+      h->d_gpart.reserve((size_t)rowv + np) != cudaSuccess)
+    return fail(FDMGPU_ERR_NOMEM, "device allocation of the CSR pools failed");
+  Pools pl = h->pl;
+  pl.rowptr = h->d_rowptr.p;
+  pl.col = h->d_col.p;
+  pl.val = h->d_val.p;
+  pl.val2 = h->d_val2.p;
+  cudaStream_t s = h->stream;
+  CK(cudaGetLastError());
+  CK(cudaMemsetAsync(pl.env64, 0, env * sizeof(double), s));
+  CK(cudaMemsetAsync(pl.B64, 0, rhs * sizeof(double), s));
+  CK(cudaMemsetAsync(pl.err, 0, np * sizeof(int), s));
+  launch_assemble(h->S, h->d_probs.p, pl, h->tb, h->dims, s);
+  launch_csr(h->d_probs.p, pl, h->tb, h->dims, s);
+  launch_lambda_dot(h->d_probs.p, pl, h->dims, h->d_lam.p, h->d_gpart.p, h->d_gpart.p + rowv, s);
+  CK(cudaGetLastError());
+  std::vector<int> err(np);
+  CK(cudaMemcpyAsync(out, h->d_gpart.p + rowv, np * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(err.data(), pl.err, np * sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (int k = 0; k < np; ++k)
+    if (err[k]) return fail((fdmgpu_status)err[k], "assembly of energy " + std::to_string(k) + " failed");
+  return FDMGPU_OK;
 }
 
 fdmgpu_status fdmgpu_taull_noalloc(const double* d_smr, int32_t nlmso, int32_t nligne, int32_t ianew_abs,

@@ -23,7 +23,7 @@ namespace fdm {
 // earlier steps updated them, and the forward substitution permutes Y(K) at
 // step K, so P A = L U holds block by block).
 template <typename T>
-__global__ void __launch_bounds__(NTHREADS) k_diag(T* env, T* dinv, const Prob* probs, Tables tb, int K,
+__global__ void __launch_bounds__(NTHREADS) k_diag(T* env, const Prob* probs, Tables tb, int K,
                                                    const int* active, int* err, double piv_thr, int* piv) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -40,7 +40,6 @@ __global__ void __launch_bounds__(NTHREADS) k_diag(T* env, T* dinv, const Prob* 
   __syncthreads();
   store_tile(dtile, D);
   if (piv && threadIdx.x < TS) piv[P.rowv + (int64_t)K * TS + threadIdx.x] = perm[threadIdx.x];
-  (void)dinv;
   // smallest |pivot| of the tile (padding rows carry 1); NaN also trips the test
   if (threadIdx.x == 0 && !(mp >= piv_thr)) atomicExch(&err[e], (int)FDMGPU_ERR_ZERO_PIVOT);
 }
@@ -54,7 +53,7 @@ template <typename T>
 __device__ __noinline__ void panel_col_solve(T* g, const T* D, const int* perm) { col_solve_lower_unit(g, D, perm); }
 
 template <typename T>
-__global__ void __launch_bounds__(GEMM_THREADS) k_panel(T* env, T* rhs, const T* dinv, const Prob* probs, Tables tb, int K,
+__global__ void __launch_bounds__(GEMM_THREADS) k_panel(T* env, T* rhs, const Prob* probs, Tables tb, int K,
                                                     int fuse_rhs, const int* active, const int* piv) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -110,7 +109,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) k_trailing(T* env, T* rhs, const
 
 // Forward substitution, unit lower L: Y(K,R) <- L(K,K)^-1 P Y(K,R).
 template <typename T>
-__global__ void __launch_bounds__(GEMM_THREADS) k_fwd_diag(const T* env, const T* dinv, T* rhs, const Prob* probs,
+__global__ void __launch_bounds__(GEMM_THREADS) k_fwd_diag(const T* env, T* rhs, const Prob* probs,
                                                            Tables tb, int K, const int* active, const int* piv) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -121,7 +120,6 @@ __global__ void __launch_bounds__(GEMM_THREADS) k_fwd_diag(const T* env, const T
   T* D = reinterpret_cast<T*>(smem_raw);
   load_tile_n(D, tile_ptr(const_cast<T*>(env), P, tb, K, K), GEMM_THREADS);
   __syncthreads();
-  (void)dinv;
   col_solve_lower_unit(rhs_ptr(rhs, P, K, R), D, piv ? piv + P.rowv + (int64_t)K * TS : (const int*)nullptr);
 }
 
@@ -145,7 +143,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) k_fwd_update(const T* env, T* rh
 
 // Backward substitution, upper U: Y(K,R) <- U(K,K)^-1 Y(K,R).
 template <typename T>
-__global__ void __launch_bounds__(GEMM_THREADS) k_bwd_diag(const T* env, const T* dinv, T* rhs, const Prob* probs,
+__global__ void __launch_bounds__(GEMM_THREADS) k_bwd_diag(const T* env, T* rhs, const Prob* probs,
                                                            Tables tb, int K, const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -156,7 +154,6 @@ __global__ void __launch_bounds__(GEMM_THREADS) k_bwd_diag(const T* env, const T
   T* D = reinterpret_cast<T*>(smem_raw);
   load_tile_n(D, tile_ptr(const_cast<T*>(env), P, tb, K, K), GEMM_THREADS);
   __syncthreads();
-  (void)dinv;
   col_solve_upper(rhs_ptr(rhs, P, K, R), D);
 }
 
@@ -179,6 +176,75 @@ __global__ void __launch_bounds__(GEMM_THREADS) k_bwd_update(const T* env, T* rh
                      (const int*)nullptr, As, Bs);
 }
 
+// Transposed forward step K: W(K,R) <- U(K,K)^-T W(K,R).
+template <typename T>
+__global__ void __launch_bounds__(GEMM_THREADS) k_tfwd_diag(const T* env, T* rhs, const Prob* probs, Tables tb,
+                                                            int K, const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (K >= P.nt || (active && !active[e])) return;
+  const int R = blockIdx.x;
+  if (R >= P.nrt) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* D = reinterpret_cast<T*>(smem_raw);
+  load_tile_trans_n(D, tile_ptr(const_cast<T*>(env), P, tb, K, K), GEMM_THREADS);
+  __syncthreads();
+  col_solve_lower_trans(rhs_ptr(rhs, P, K, R), D);
+}
+
+// W(J,R) -= U(K,J)^T W(K,R) for J in (K, J1(K)].
+template <typename T>
+__global__ void __launch_bounds__(GEMM_THREADS) k_tfwd_update(const T* env, T* rhs, const Prob* probs, Tables tb,
+                                                              int K, const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (K >= P.nt || (active && !active[e])) return;
+  const int nJ = tb.J1[P.trow + K] - K;
+  const int w = blockIdx.x;
+  if (w >= nJ * P.nrt) return;
+  const int J = K + 1 + w / P.nrt, R = w % P.nrt;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* As = reinterpret_cast<T*>(smem_raw);
+  T* Bs = As + TS * SP;
+  tile_mm64<T, true, true>(rhs_ptr(rhs, P, J, R), tile_ptr(const_cast<T*>(env), P, tb, K, J), rhs_ptr(rhs, P, K, R),
+                           (const int*)nullptr, As, Bs);
+}
+
+// Transposed backward step K: W(K,R) <- P_K^T L(K,K)^-T W(K,R).
+template <typename T>
+__global__ void __launch_bounds__(GEMM_THREADS) k_tbwd_diag(const T* env, T* rhs, const Prob* probs, Tables tb,
+                                                            int K, const int* active, const int* piv) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (K >= P.nt || (active && !active[e])) return;
+  const int R = blockIdx.x;
+  if (R >= P.nrt) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* D = reinterpret_cast<T*>(smem_raw);
+  load_tile_trans_n(D, tile_ptr(const_cast<T*>(env), P, tb, K, K), GEMM_THREADS);
+  __syncthreads();
+  col_solve_upper_unit_trans(rhs_ptr(rhs, P, K, R), D, piv ? piv + P.rowv + (int64_t)K * TS : (const int*)nullptr);
+}
+
+// W(I,R) -= L(K,I)^T W(K,R) for I in [J0(K), K).
+template <typename T>
+__global__ void __launch_bounds__(GEMM_THREADS) k_tbwd_update(const T* env, T* rhs, const Prob* probs, Tables tb,
+                                                              int K, const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (K >= P.nt || (active && !active[e])) return;
+  const int i0 = tb.J0[P.trow + K];
+  const int nI = K - i0;
+  const int w = blockIdx.x;
+  if (w >= nI * P.nrt) return;
+  const int I = i0 + w / P.nrt, R = w % P.nrt;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* As = reinterpret_cast<T*>(smem_raw);
+  T* Bs = As + TS * SP;
+  tile_mm64<T, true, true>(rhs_ptr(rhs, P, I, R), tile_ptr(const_cast<T*>(env), P, tb, K, I), rhs_ptr(rhs, P, K, R),
+                           (const int*)nullptr, As, Bs);
+}
+
 template <typename T>
 static size_t smem_bytes() { return 2 * TS * SP * sizeof(T); }
 // the panel holds the diagonal tile plus two SPA-strided work tiles
@@ -195,63 +261,118 @@ void setup_factor_kernels() {
   cudaFuncSetAttribute(k_fwd_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_bwd_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_bwd_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_tfwd_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_tfwd_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_tbwd_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_tbwd_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 template <typename T>
-void launch_factor(const StepPlan& sp, T* env, T* rhs, T* dinv, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
-                   const int* active, int* err, double piv_thr, int* piv, cudaStream_t s) {
+int launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
+                  const int* active, int* err, double piv_thr, int* piv, cudaStream_t s) {
   const size_t sm = smem_bytes<T>();
+  int nk = 0;
   for (int K = 0; K < sp.ntmax; ++K) {
-    k_diag<T><<<dim3(1, nprob), NTHREADS, sm, s>>>(env, dinv, probs, tb, K, active, err, piv_thr, piv);
+    k_diag<T><<<dim3(1, nprob), NTHREADS, sm, s>>>(env, probs, tb, K, active, err, piv_thr, piv);
+    ++nk;
     const int np = fuse_rhs ? sp.panel_rhs[K] : sp.panel[K];
-    if (np > 0)
-      k_panel<T><<<dim3(np, nprob), GEMM_THREADS, smem_bytes_panel<T>(), s>>>(env, rhs, dinv, probs, tb, K, fuse_rhs,
+    if (np > 0) {
+      k_panel<T><<<dim3(np, nprob), GEMM_THREADS, smem_bytes_panel<T>(), s>>>(env, rhs, probs, tb, K, fuse_rhs,
                                                                              active, piv);
+      ++nk;
+    }
     const int nt = fuse_rhs ? sp.trail_rhs[K] : sp.trail[K];
-    if (nt > 0) k_trailing<T><<<dim3(nt, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
+    if (nt > 0) {
+      k_trailing<T><<<dim3(nt, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
+      ++nk;
+    }
   }
+  return nk;
 }
 
 template <typename T>
-void launch_forward(const StepPlan& sp, const T* env, T* rhs, const T* dinv, const Prob* probs, Tables tb, int nprob,
-                    const int* active, const int* piv, cudaStream_t s) {
+int launch_forward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
+                   const int* active, const int* piv, cudaStream_t s) {
+  const size_t sm = smem_bytes<T>();
+  int nk = 0;
+  for (int K = 0; K < sp.ntmax; ++K) {
+    k_fwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active, piv);
+    ++nk;
+    if (sp.fwd[K] > 0) {
+      k_fwd_update<T><<<dim3(sp.fwd[K], nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+      ++nk;
+    }
+  }
+  return nk;
+}
+
+template <typename T>
+int launch_backward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
+                    const int* active, cudaStream_t s) {
+  const size_t sm = smem_bytes<T>();
+  int nk = 0;
+  for (int K = sp.ntmax - 1; K >= 0; --K) {
+    k_bwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+    ++nk;
+    if (sp.bwd[K] > 0) {
+      k_bwd_update<T><<<dim3(sp.bwd[K], nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+      ++nk;
+    }
+  }
+  return nk;
+}
+
+template <typename T>
+void launch_forward_t(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
+                      const int* active, cudaStream_t s) {
   const size_t sm = smem_bytes<T>();
   for (int K = 0; K < sp.ntmax; ++K) {
-    k_fwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, dinv, rhs, probs, tb, K, active, piv);
-    if (sp.fwd[K] > 0) k_fwd_update<T><<<dim3(sp.fwd[K], nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+    k_tfwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+    if (sp.tfwd[K] > 0)
+      k_tfwd_update<T><<<dim3(sp.tfwd[K], nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
   }
 }
 
 template <typename T>
-void launch_backward(const StepPlan& sp, const T* env, T* rhs, const T* dinv, const Prob* probs, Tables tb, int nprob,
-                     const int* active, cudaStream_t s) {
+void launch_backward_t(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
+                       const int* active, const int* piv, cudaStream_t s) {
   const size_t sm = smem_bytes<T>();
   for (int K = sp.ntmax - 1; K >= 0; --K) {
-    k_bwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, dinv, rhs, probs, tb, K, active);
-    if (sp.bwd[K] > 0) k_bwd_update<T><<<dim3(sp.bwd[K], nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+    k_tbwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active, piv);
+    if (sp.tbwd[K] > 0)
+      k_tbwd_update<T><<<dim3(sp.tbwd[K], nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
   }
 }
+
+template void launch_forward_t<double>(const StepPlan&, const double*, double*, const Prob*, Tables, int, const int*,
+                                       cudaStream_t);
+template void launch_backward_t<double>(const StepPlan&, const double*, double*, const Prob*, Tables, int,
+                                        const int*, const int*, cudaStream_t);
+template void launch_forward_t<float>(const StepPlan&, const float*, float*, const Prob*, Tables, int, const int*,
+                                      cudaStream_t);
+template void launch_backward_t<float>(const StepPlan&, const float*, float*, const Prob*, Tables, int, const int*,
+                                       const int*, cudaStream_t);
 
 template void setup_factor_kernels<float>();
 template void setup_factor_kernels<dfl>();
-template void launch_factor<dfl>(const StepPlan&, dfl*, dfl*, dfl*, const Prob*, Tables, int, int, const int*, int*,
+template int launch_factor<dfl>(const StepPlan&, dfl*, dfl*, const Prob*, Tables, int, int, const int*, int*,
                                  double, int*, cudaStream_t);
-template void launch_forward<dfl>(const StepPlan&, const dfl*, dfl*, const dfl*, const Prob*, Tables, int, const int*,
+template int launch_forward<dfl>(const StepPlan&, const dfl*, dfl*, const Prob*, Tables, int, const int*,
                                   const int*, cudaStream_t);
-template void launch_backward<dfl>(const StepPlan&, const dfl*, dfl*, const dfl*, const Prob*, Tables, int, const int*,
+template int launch_backward<dfl>(const StepPlan&, const dfl*, dfl*, const Prob*, Tables, int, const int*,
                                    cudaStream_t);
 template void setup_factor_kernels<double>();
-template void launch_factor<float>(const StepPlan&, float*, float*, float*, const Prob*, Tables, int, int, const int*,
+template int launch_factor<float>(const StepPlan&, float*, float*, const Prob*, Tables, int, int, const int*,
                                    int*, double, int*, cudaStream_t);
-template void launch_factor<double>(const StepPlan&, double*, double*, double*, const Prob*, Tables, int, int,
+template int launch_factor<double>(const StepPlan&, double*, double*, const Prob*, Tables, int, int,
                                     const int*, int*, double, int*, cudaStream_t);
-template void launch_forward<float>(const StepPlan&, const float*, float*, const float*, const Prob*, Tables, int,
+template int launch_forward<float>(const StepPlan&, const float*, float*, const Prob*, Tables, int,
                                     const int*, const int*, cudaStream_t);
-template void launch_forward<double>(const StepPlan&, const double*, double*, const double*, const Prob*, Tables, int,
+template int launch_forward<double>(const StepPlan&, const double*, double*, const Prob*, Tables, int,
                                      const int*, const int*, cudaStream_t);
-template void launch_backward<float>(const StepPlan&, const float*, float*, const float*, const Prob*, Tables, int,
+template int launch_backward<float>(const StepPlan&, const float*, float*, const Prob*, Tables, int,
                                      const int*, cudaStream_t);
-template void launch_backward<double>(const StepPlan&, const double*, double*, const double*, const Prob*, Tables, int,
+template int launch_backward<double>(const StepPlan&, const double*, double*, const Prob*, Tables, int,
                                       const int*, cudaStream_t);
 
 }  // namespace fdm

@@ -56,7 +56,6 @@ struct Prob {
   int64_t in_phi;     // offset of phiato(nphiato1, nlmagm, natome) (spin-selected)
   int64_t in_bes;     // offset of Bessel j(ib, L) in the double pool, [nsort][lmaxso+1]
   int64_t in_neu;     // offset of Neumann n(ib, L), [nsort][lmaxso+1]
-  int64_t dinv;       // element offset of the inverted diagonal tiles (L_KK^-1, U_KK^-1 per K)
   int64_t taull;      // offset of Taull (complex) for this problem
   int64_t scratch;    // offset of the complex nlmso x (nlmso + nlm_abs) Taull scratch
 };
@@ -341,10 +340,34 @@ __device__ __forceinline__ void ld4<double>(const double* p, double* v) {
 
 constexpr int SPA = TS + 1;  // odd stride of the A tile: conflict-free scalar column reads
 
-template <typename T, bool SUB>
+// acc += a * b inside a dot product.  For double-float the accumulator is
+// kept unnormalised: the high parts are summed with Knuth's two-sum, the
+// rounding errors and the cross terms collect in lo, and mac_finish
+// renormalises once per dot product (about 12 FP32 operations per step
+// instead of 18 for a renormalised multiply and add).
+template <typename T>
+__device__ __forceinline__ void mac(T& acc, T a, T b) { acc += a * b; }
+template <>
+__device__ __forceinline__ void mac<dfl>(dfl& acc, dfl a, dfl b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  const float s = acc.hi + p;
+  const float bb = s - acc.hi;
+  const float err = (acc.hi - (s - bb)) + (p - bb);
+  acc.hi = s;
+  acc.lo += err + e;
+}
+template <typename T>
+__device__ __forceinline__ T mac_finish(T acc) { return acc; }
+template <>
+__device__ __forceinline__ dfl mac_finish<dfl>(dfl acc) { return df_fast_two_sum(acc.hi, acc.lo); }
+
+// TA: use the transpose of A (C (-)= A^T * P B).
+template <typename T, bool SUB, bool TA = false>
 __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const int* perm, T* As, T* Bs) {
   const int t = threadIdx.x;
-  // stage: As[r][k] = A[r][k] (stride SPA), Bs[r][c] = B[perm ? perm[r] : r][c] (stride SP)
+  // stage: As[r][k] = A[r][k] (A[k][r] when TA; stride SPA), Bs[r][c] = B[perm ? perm[r] : r][c] (stride SP)
   for (int idx = t; idx < TS2 / 4; idx += GEMM_THREADS) {
     const int r = idx / (TS / 4), c4 = (idx % (TS / 4)) * 4;
     T a[4], b[4];
@@ -352,7 +375,10 @@ __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const in
     ld4(B + (perm ? perm[r] : r) * TS + c4, b);
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      As[r * SPA + c4 + q] = a[q];
+      if (TA)
+        As[(c4 + q) * SPA + r] = a[q];
+      else
+        As[r * SPA + c4 + q] = a[q];
       Bs[r * SP + c4 + q] = b[q];
     }
   }
@@ -376,7 +402,7 @@ __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const in
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
-      for (int j = 0; j < 8; ++j) acc[i][j] += a[i] * b[j];
+      for (int j = 0; j < 8; ++j) mac(acc[i][j], a[i], b[j]);
   }
   __syncthreads();  // C may alias A or B, which are no longer read
 #pragma unroll
@@ -386,7 +412,10 @@ __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const in
     for (int h = 0; h < 2; ++h) {
       T* cp = C + row * TS + 32 * h + 4 * tx;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) cp[j] = SUB ? cp[j] - acc[i][4 * h + j] : acc[i][4 * h + j];
+      for (int j = 0; j < 4; ++j) {
+        const T v = mac_finish(acc[i][4 * h + j]);
+        cp[j] = SUB ? cp[j] - v : v;
+      }
     }
   }
 }
@@ -432,6 +461,62 @@ __device__ __forceinline__ void col_solve_upper(T* g, const T* Us) {
   }
 #pragma unroll
   for (int r = 0; r < TS; ++r) g[r * TS + c] = x[r];
+}
+
+// Transposed substitutions.  The caller stages the TRANSPOSE of the factored
+// diagonal tile (Dt[r][c] = D[c][r]) so that the inner loops read rows.
+
+// g <- U^-T g: with Ut = U^T (lower, diagonal of U), forward substitution.
+template <typename T>
+__device__ __forceinline__ void col_solve_lower_trans(T* g, const T* Ut) {
+  const int c = threadIdx.x;
+  if (c >= TS) return;
+  T x[TS];
+#pragma unroll
+  for (int r = 0; r < TS; ++r) x[r] = g[r * TS + c];
+#pragma unroll
+  for (int k = 0; k < TS; ++k) {
+    T acc = x[k];
+#pragma unroll
+    for (int i = 0; i < k; ++i) acc -= Ut[k * SP + i] * x[i];
+    x[k] = acc / Ut[k * SP + k];
+  }
+#pragma unroll
+  for (int r = 0; r < TS; ++r) g[r * TS + c] = x[r];
+}
+
+// g <- P^T L^-T g: with Lt = L^T (unit upper), backward substitution; perm[r]
+// is the original tile row at row r, so result row r goes to row perm[r].
+template <typename T>
+__device__ __forceinline__ void col_solve_upper_unit_trans(T* g, const T* Lt, const int* perm) {
+  const int c = threadIdx.x;
+  if (c >= TS) return;
+  T x[TS];
+#pragma unroll
+  for (int r = 0; r < TS; ++r) x[r] = g[r * TS + c];
+#pragma unroll
+  for (int k = TS - 2; k >= 0; --k) {
+    T acc = x[k];
+#pragma unroll
+    for (int i = k + 1; i < TS; ++i) acc -= Lt[k * SP + i] * x[i];
+    x[k] = acc;
+  }
+  if (perm) {
+    int pr[TS];
+#pragma unroll
+    for (int r = 0; r < TS; ++r) pr[r] = perm[r];
+#pragma unroll
+    for (int r = 0; r < TS; ++r) g[pr[r] * TS + c] = x[r];
+  } else {
+#pragma unroll
+    for (int r = 0; r < TS; ++r) g[r * TS + c] = x[r];
+  }
+}
+
+// Shared tile <- transpose of a global tile.
+template <typename T>
+__device__ __forceinline__ void load_tile_trans_n(T* __restrict__ s, const T* __restrict__ g, int nthreads) {
+  for (int idx = threadIdx.x; idx < TS2; idx += nthreads) s[(idx % TS) * SP + idx / TS] = g[idx];
 }
 
 // g <- g U^-1 (U upper with diagonal): thread r owns row r, i.e. solves

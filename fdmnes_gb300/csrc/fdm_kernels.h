@@ -15,18 +15,29 @@ struct StepPlan {
   std::vector<int> panel, panel_rhs;   // L + U tiles (+ RHS tiles) of step K
   std::vector<int> trail, trail_rhs;   // trailing tiles (+ RHS tiles) of step K
   std::vector<int> fwd, bwd;           // forward / backward update tiles of step K
+  std::vector<int> tfwd, tbwd;         // the same for the transposed solves (U^T, then L^T)
 };
 
 template <typename T> void setup_factor_kernels();
 template <typename T>
-void launch_factor(const StepPlan& sp, T* env, T* rhs, T* dinv, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
+int launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
                    const int* active, int* err, double piv_thr, int* piv, cudaStream_t s);
 template <typename T>
-void launch_forward(const StepPlan& sp, const T* env, T* rhs, const T* dinv, const Prob* probs, Tables tb, int nprob,
+int launch_forward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
                     const int* active, const int* piv, cudaStream_t s);
 template <typename T>
-void launch_backward(const StepPlan& sp, const T* env, T* rhs, const T* dinv, const Prob* probs, Tables tb, int nprob,
+int launch_backward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
                      const int* active, cudaStream_t s);
+
+// Transposed solves with the factors of launch_factor: U^T w = g (forward over
+// K), then the block-lower factor M of A = M U transposed (backward over K,
+// tile-local row orders undone).  Together they solve A^T x = g.
+template <typename T>
+void launch_forward_t(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
+                      const int* active, cudaStream_t s);
+template <typename T>
+void launch_backward_t(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
+                       const int* active, const int* piv, cudaStream_t s);
 
 // Device pools of one batch (pointers into device memory).
 struct Pools {
@@ -37,8 +48,6 @@ struct Pools {
   double* B64 = nullptr;           // FP64 right-hand sides (tiles)
   double* X64 = nullptr;           // FP64 solution (tiles)
   float* Y32 = nullptr;            // FP32 work right-hand sides (tiles)
-  double* dinv64 = nullptr;        // inverted diagonal tiles of the FP64 factor
-  float* dinv32 = nullptr;         // inverted diagonal tiles of the FP32 factor
   double* rs = nullptr;            // row scales (per row, stride npad + 1)
   double* cs = nullptr;            // column scales
   int* rowptr = nullptr;           // CSR row pointers (stride npad + 1)
@@ -91,11 +100,18 @@ void launch_gmres_cycle(const StepPlan& sp, const Prob* probs, const Pools& pl, 
 size_t gmres_state_bytes();
 int gmres_max_dim();
 void launch_copy_rhs(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s);
-void launch_dfl_escalation(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
-                           dfl* D, int iters, cudaStream_t s);
+int launch_dfl_escalation(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
+                           dfl* D, int iters, cudaStream_t s, cudaEvent_t ev_f0 = nullptr, cudaEvent_t ev_f1 = nullptr);
+void launch_csr_nnz(const Prob* probs, const int* rowptr, const LaunchDims& d, int* nnz, cudaStream_t s);
 cudaError_t taull_noalloc_scratch(double2** out);
 cudaError_t launch_taull_noalloc(const double* smr, int nlmso, int nligne, int ianew_abs, int nlm_abs,
                                  double2* scratch, double* taull, int* status, cudaStream_t s);
+void launch_taull_vjp(const Prob* probs, const LaunchDims& d, const double* X, const double* gT, double* scratch,
+                      double* G, int* err, cudaStream_t s);
+void launch_grad_vr(const StaticDev& S, const Prob* probs, const int* ipool, const LaunchDims& d, int nspin,
+                    const double* X, const double* Lam, double* part, double* grad, cudaStream_t s);
+void launch_lambda_dot(const Prob* probs, const Pools& pl, const LaunchDims& d, const double* Lam, double* rowpart,
+                       double* out, cudaStream_t s);
 void launch_taull(const Prob* probs, const Pools& pl, const LaunchDims& d, const double* X, cudaStream_t s);
 void launch_solution_out(const Prob& P, const double* X, double* smr_dev, cudaStream_t s);
 

@@ -245,8 +245,8 @@ void launch_csr_scale(const Prob* probs, const Pools& pl, const LaunchDims& d, c
 void launch_gmres_cycle(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, int m,
                         float tol, cudaStream_t s) {
   const int np = d.nprob;
-  launch_forward<float>(sp, pl.env32, pl.Y32, pl.dinv32, probs, tb, np, pl.active, pl.piv, s);
-  launch_backward<float>(sp, pl.env32, pl.Y32, pl.dinv32, probs, tb, np, pl.active, s);
+  launch_forward<float>(sp, pl.env32, pl.Y32, probs, tb, np, pl.active, pl.piv, s);
+  launch_backward<float>(sp, pl.env32, pl.Y32, probs, tb, np, pl.active, s);
   GmresState* st = reinterpret_cast<GmresState*>(pl.gstate);
   k_gmres_start<<<dim3(sp.nrtmax, np), 256, 0, s>>>(probs, pl.Y32, pl.V, st, pl.active_gm, pl.inner_active,
                                                     pl.jdone, pl.notconv);
@@ -254,8 +254,8 @@ void launch_gmres_cycle(const StepPlan& sp, const Prob* probs, const Pools& pl, 
     const float* Vj = pl.V + (int64_t)j * pl.vstride;
     k_spmv32<<<dim3((d.max_rows + 7) / 8, np), 256, 0, s>>>(probs, pl.rowptr, pl.col, pl.valS, Vj, pl.W,
                                                            pl.inner_active);
-    launch_forward<float>(sp, pl.env32, pl.W, pl.dinv32, probs, tb, np, pl.inner_active, pl.piv, s);
-    launch_backward<float>(sp, pl.env32, pl.W, pl.dinv32, probs, tb, np, pl.inner_active, s);
+    launch_forward<float>(sp, pl.env32, pl.W, probs, tb, np, pl.inner_active, pl.piv, s);
+    launch_backward<float>(sp, pl.env32, pl.W, probs, tb, np, pl.inner_active, s);
     k_gmres_arnoldi<<<dim3(sp.nrtmax, np), 256, 0, s>>>(probs, pl.V, pl.vstride, pl.W, st, pl.inner_active,
                                                         pl.notconv, j, tol);
     k_gmres_flags<<<(np + 127) / 128, 128, 0, s>>>(probs, np, pl.inner_active, pl.jdone, pl.notconv);

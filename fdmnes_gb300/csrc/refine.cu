@@ -440,23 +440,43 @@ __global__ void k_dfl_to_x(const Prob* probs, const dfl* D, double* X, float2* X
 // Double-float re-solve of the active problems: factorisation of Dr A Dc,
 // solve, then `iters` refinement steps with the double-float residual and the
 // double-float factors.  Scratch D (dfl, RHS layout) must hold rhs elements.
-void launch_dfl_escalation(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
-                           dfl* D, int iters, cudaStream_t s) {
+// Number of CSR nonzeros of every problem.
+__global__ void k_csr_nnz(const Prob* probs, int np, const int* rowptr, int* nnz) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= np) return;
+  const Prob P = probs[e];
+  nnz[e] = min(rowptr[P.rowv + P.nt * TS], (int)P.csr_cap);
+}
+
+void launch_csr_nnz(const Prob* probs, const int* rowptr, const LaunchDims& d, int* nnz, cudaStream_t s) {
+  k_csr_nnz<<<(d.nprob + 127) / 128, 128, 0, s>>>(probs, d.nprob, rowptr, nnz);
+}
+
+int launch_dfl_escalation(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
+                          dfl* D, int iters, cudaStream_t s, cudaEvent_t ev_f0, cudaEvent_t ev_f1) {
   const int np = d.nprob;
   dfl* envd = reinterpret_cast<dfl*>(pl.env64);
+  int nk = 0;
   k_env_to_dfl<<<dim3(d.max_tiles, np), 256, 0, s>>>(probs, pl.env64, pl.rs, pl.cs, tb, pl.active);
   k_rhs_to_dfl<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, pl.B64, pl.Y32, pl.rs, D, 1, pl.active);
-  launch_factor<dfl>(sp, envd, D, nullptr, probs, tb, np, 1, pl.active, pl.err, 1e-30, pl.piv, s);
-  launch_backward<dfl>(sp, envd, D, nullptr, probs, tb, np, pl.active, s);
+  nk += 2;
+  if (ev_f0) cudaEventRecord(ev_f0, s);
+  nk += launch_factor<dfl>(sp, envd, D, probs, tb, np, 1, pl.active, pl.err, 1e-30, pl.piv, s);
+  if (ev_f1) cudaEventRecord(ev_f1, s);
+  nk += launch_backward<dfl>(sp, envd, D, probs, tb, np, pl.active, s);
   k_dfl_to_x<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, D, pl.X64, pl.Xs, pl.cs, 1, pl.dmax, pl.xmax, pl.active);
+  ++nk;
   for (int it = 0; it < iters; ++it) {
     launch_residual(probs, pl, d, 1, s);
     k_rhs_to_dfl<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, pl.B64, pl.Y32, pl.rs, D, 0, pl.active);
-    launch_forward<dfl>(sp, envd, D, nullptr, probs, tb, np, pl.active, pl.piv, s);
-    launch_backward<dfl>(sp, envd, D, nullptr, probs, tb, np, pl.active, s);
+    nk += 2;
+    nk += launch_forward<dfl>(sp, envd, D, probs, tb, np, pl.active, pl.piv, s);
+    nk += launch_backward<dfl>(sp, envd, D, probs, tb, np, pl.active, s);
     k_dfl_to_x<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, D, pl.X64, pl.Xs, pl.cs, 0, pl.dmax, pl.xmax,
                                                           pl.active);
+    ++nk;
   }
+  return nk;
 }
 
 void launch_copy_rhs(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s) {

@@ -61,6 +61,8 @@ def load_library(path: str = LIB_PATH):
     L.fdmgpu_set_refinement.restype = C.c_int
     L.fdmgpu_set_escalation.argtypes = [vp, C.c_int32]
     L.fdmgpu_set_escalation.restype = C.c_int
+    L.fdmgpu_set_tolerance.argtypes = [vp, C.c_double, C.c_double]
+    L.fdmgpu_set_tolerance.restype = C.c_int
     L.fdmgpu_set_residual_mode.restype = C.c_int
     L.fdmgpu_batch_begin.argtypes = [vp, C.c_int32, C.c_int32]
     L.fdmgpu_batch_add.argtypes = [vp, vp, C.c_int32]
@@ -70,8 +72,13 @@ def load_library(path: str = LIB_PATH):
     L.fdmgpu_batch_solution.argtypes = [vp, C.c_int32, vp]
     L.fdmgpu_batch_stats.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double),
                                      C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
+    L.fdmgpu_batch_vjp.argtypes = [vp, vp, vp, C.POINTER(C.c_double)]
+    L.fdmgpu_update_grid_values.argtypes = [vp, vp]
+    L.fdmgpu_update_grid_values.restype = C.c_int
+    L.fdmgpu_batch_adjoint_dot.argtypes = [vp, vp, C.c_int32, vp]
+    L.fdmgpu_batch_adjoint_dot.restype = C.c_int
     for f in ("fdmgpu_batch_begin", "fdmgpu_batch_add", "fdmgpu_batch_run", "fdmgpu_batch_rerun", "fdmgpu_batch_taull",
-              "fdmgpu_batch_solution", "fdmgpu_batch_stats"):
+              "fdmgpu_batch_solution", "fdmgpu_batch_stats", "fdmgpu_batch_vjp"):
         getattr(L, f).restype = C.c_int
     _lib = L
     return L
@@ -110,6 +117,10 @@ class FdmSolver:
     def set_escalation(self, mode: str = "df64"):
         """Re-solve arithmetic for energies the FP32 factors cannot refine: 'df64' or 'fp64'."""
         _check(self.lib.fdmgpu_set_escalation(self.h, {"fp64": 0, "df64": 1}[mode]))
+
+    def set_tolerance(self, tol: float = 0.0, tol_accept: float = 0.0):
+        """Refinement stop (max|dx|/max|x|) and the stalled-but-accepted level; 0 = default."""
+        _check(self.lib.fdmgpu_set_tolerance(self.h, tol, tol_accept))
 
     def close(self):
         if getattr(self, "h", None):
@@ -191,6 +202,35 @@ class FdmSolver:
         if st not in (0, 5):
             _check(st)
         return it.value, r.value, bool(fb.value), inner.value
+
+    def vjp(self, g_taull: Sequence[np.ndarray]) -> Tuple[np.ndarray, float]:
+        """Gradient of L with respect to the grid potential Vr, given the
+        cotangents g_taull[k] = dL/d(Im Taull_k) (nlm x nlm real) of the energies
+        of the last FP64 batch.  Returns (dL/dVr of shape (npoint, nspin), device ms)."""
+        flat = np.concatenate([np.asarray(g, dtype=np.float64).ravel(order="F") for g in g_taull])
+        g = self.st.grid
+        grad = np.zeros((g.npoint, self.st.nspin), order="F")
+        ms = C.c_double(0)
+        _check(self.lib.fdmgpu_batch_vjp(self.h, flat.ctypes.data, grad.ctypes.data, C.byref(ms)))
+        return grad, ms.value
+
+    def update_grid_values(self, st) -> None:
+        """Switch the handle to the real-valued grid tables of st (same integer
+        structure).  The energy arguments built afterwards use st."""
+        ga = abi.GridArgs(st)
+        _check(self.lib.fdmgpu_update_grid_values(self.h, C.addressof(ga.s)))
+        self.st = st
+        self.grid_args = ga
+
+    def adjoint_dot(self, items: Sequence[Tuple[CL.EnergyInputs, CL.RowIndex]]) -> np.ndarray:
+        """Per energy, Lambda^T (B' - A' X) with A', B' assembled from items (one
+        per energy of the batch, same row structure) and the X, Lambda of the
+        last run + vjp."""
+        args = [abi.EnergyArgs(self.st, ei, ri) for ei, ri in items]
+        arr = (C.c_void_p * len(args))(*[C.addressof(a.s) for a in args])
+        out = np.zeros(len(args))
+        _check(self.lib.fdmgpu_batch_adjoint_dot(self.h, arr, len(args), out.ctypes.data))
+        return out
 
     def spectrum(self, items: Sequence[Tuple[CL.EnergyInputs, CL.RowIndex]], precision: str = "mixed",
                  iaabs: int = 1):

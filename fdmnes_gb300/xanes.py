@@ -38,6 +38,14 @@ def absorption(taull: np.ndarray) -> float:
     return float(-np.imag(np.trace(taull[1:4, 1:4])))
 
 
+def absorption_cotangent(taull: np.ndarray, g_sigma: float = 1.0) -> np.ndarray:
+    """dL/d(Im Taull) for L = g_sigma * absorption(taull): -g_sigma on the L = 1 diagonal."""
+    g = np.zeros(taull.shape, dtype=np.float64)
+    for a in (1, 2, 3):
+        g[a, a] = -g_sigma
+    return g
+
+
 def lorentzian_convolve(energies: np.ndarray, x: np.ndarray, half_width: float) -> np.ndarray:
     E = np.asarray(energies, dtype=np.float64)
     x = np.asarray(x, dtype=np.float64)

@@ -165,6 +165,10 @@ typedef struct fdmgpu_info {
   int32_t n_fallback;       /* problems solved again in FP64 after the mixed path missed its
                                tolerance (precision escalation)                               */
   int64_t n_kernels;        /* kernels launched by the call (graph kernel nodes included)     */
+  /* mixed precision only: the first refinement residual (all problems active)
+   * and the escalation's factorisation, each with its algorithmic flops       */
+  double ms_residual_first, flops_residual;
+  double ms_escalate_factor, flops_escalate_factor;
 } fdmgpu_info;
 
 /* Library version string. */
@@ -201,6 +205,13 @@ fdmgpu_status fdmgpu_set_refinement(fdmgpu_handle* h, int32_t mode, int32_t kryl
  * counterpart in the reference. */
 fdmgpu_status fdmgpu_set_escalation(fdmgpu_handle* h, int32_t mode);
 
+/* Stopping rule of the mixed precision refinement: an energy stops when the
+ * correction max|dx|/max|x| falls to tol (default 1e-10); when it stalls
+ * above tol it is accepted if at most tol_accept (default 1e-7 with the df64
+ * residual, 1e-9 with FP64), else solved again by escalation.  0 selects the
+ * default.  No counterpart in the reference. */
+fdmgpu_status fdmgpu_set_tolerance(fdmgpu_handle* h, double tol, double tol_accept);
+
 /* Counterpart of getSolverParams (source/mat_solve_gaussian.f90:376-389,
  * source/mat_solve_mumps.f90:705-736): solver name "GPU" and group size 1. */
 void fdmgpu_get_solver_params(int32_t* mpi_host_num_for_mumps, char solver[6]);
@@ -230,6 +241,38 @@ fdmgpu_status fdmgpu_batch_solution(fdmgpu_handle* h, int32_t k, double* smr);
  * energy's status (FDMGPU_OK when it converged).  Any pointer may be NULL. */
 fdmgpu_status fdmgpu_batch_stats(fdmgpu_handle* h, int32_t k, int32_t* iters, double* residual,
                                  int32_t* fallback, int32_t* inner_iters);
+
+/*
+ * Vector-Jacobian product of the last FP64 batch: given the cotangent
+ * gtaull = dL/d(Im Taull) of every energy (nlm*nlm reals per energy,
+ * column-major, concatenated in add order), writes dL/dVr into grad_vr
+ * (npoint, nspin), column-major like Vr.  It reuses the batch's factors
+ * (transposed solves A^T Lambda = dL/dX) and its solutions; Vr enters the FDM
+ * matrix on the diagonal of the grid rows (source/mat.f90:1151-1156).  Points
+ * inside atoms get 0.  ms (may be NULL) receives the device time.  No
+ * counterpart in the reference.
+ */
+fdmgpu_status fdmgpu_batch_vjp(fdmgpu_handle* h, const double* gtaull, double* grad_vr, double* ms);
+
+/*
+ * Parameter gradients through the adjoint.  For a parameter theta that moves
+ * matrix values but not the grid structure (a shell distance: atom positions,
+ * the potential and the atomic boundary functions change, grid membership and
+ * row numbering do not), dL/dtheta = Lambda^T (dB/dtheta - dA/dtheta X).
+ * fdmgpu_batch_adjoint_dot assembles A' and B' from the energy arguments e[k]
+ * (same row structure as the batch's energy k) and writes, per energy,
+ * out[k] = sum_c Lambda_c^T (B'_c - A' X_c) with the X and Lambda of the last
+ * fdmgpu_batch_run + fdmgpu_batch_vjp.  Central differences of out over
+ * theta +- h give dL/dtheta with O(h^2) error in the assembly only.  The
+ * batch's factors are overwritten: run the batch again before another vjp.
+ *
+ * fdmgpu_update_grid_values replaces the real-valued tables of the handle's
+ * grid (rvol, poidsa, poidso, Ylmato, Ylmso, Kar, clapl) by those of g, whose
+ * integer structure must equal the handle's (else FDMGPU_ERR_ARG).
+ * No counterparts in the reference.
+ */
+fdmgpu_status fdmgpu_update_grid_values(fdmgpu_handle* h, const fdmgpu_grid* g);
+fdmgpu_status fdmgpu_batch_adjoint_dot(fdmgpu_handle* h, const fdmgpu_energy* const* e, int32_t n, double* out);
 
 /*
  * Taull of one energy from a solution that is already in device memory,
