@@ -82,7 +82,7 @@ def energy_dict(st: CL.Structure, ei: CL.EnergyInputs, ri: CL.RowIndex) -> dict:
     g = st.grid
     return dict(
         nligne=ri.nligne, nligneso=ri.nligneso, nlmso=ei.nlmso, lmaxso=ei.lmaxso, nlmagm=ei.nlmagm,
-        nphiato1=g.nbtm, nphiato7=1, nspinp=1, n_RI=1, n_ato_RI=1, nspinr=1, nsort_r=g.nsort, nsort_c=0,
+        nphiato1=g.nbtm, nphiato7=1, nspinp=ei.phiato.shape[2], n_RI=1, n_ato_RI=1, nspinr=1, nsort_r=g.nsort, nsort_c=0,
         igrph=1, ispin=ei.ispin, nicm=1, Cal_comp=0, E_comp=0, Basereel=1, Base_hexa=0, irregular=0,
         Relativiste=0, Spinorbite=0, Repres_comp=0, Ylm_comp=0, Test_reg=0,
         Enervide=ei.enervide, Eimag=ei.eimag, new_=ri.new, newinv=ri.newinv, lb1=ri.lb1, lb2=ri.lb2,

@@ -760,7 +760,7 @@ class EnergyInputs:
     nlmsa: np.ndarray          # (natome,)
     nlmso: int
     nlmagm: int
-    phiato: np.ndarray         # (nbtm, nlmagm, nspinp=1, nspino=1, n_RI=1, natome, nphiato7=1) F
+    phiato: np.ndarray         # (nbtm, nlmagm, nspinp=nspin, nspino=1, n_RI=1, natome, nphiato7=1) F
     besselr: np.ndarray        # (nsort, 0:lmaxso, nspinr=1) F
     neumanr: np.ndarray
     ispin: int = 1
@@ -787,27 +787,33 @@ def energy_inputs(st: Structure, energy_ev: float, e_fermi_ev: float = -5.0, isp
     nlmso = (lmaxso + 1) ** 2
     lmax_g = int(lmaxat.max())
     nlmagm = (lmax_g + 1) ** 2
-    # radial solutions per prototype and L, then cal_phiato per atom
-    phiato = np.zeros((g.nbtm, nlmagm, 1, 1, 1, natome, 1), order="F")
+    # radial solutions per prototype, spin and L, then cal_phiato per atom.
+    # phiato holds every spin block (nspinp = nspin): the grid rows of
+    # calcMatRow read it at min(ispin, nspin) (source/mat.f90:1144,1296-1304).
+    nspinp = st.nspin
+    phiato = np.zeros((g.nbtm, nlmagm, nspinp, 1, 1, natome, 1), order="F")
     ur_cache: Dict[tuple, np.ndarray] = {}
-    for ia in range(natome):
-        ipr = int(cl.itype[ia])
-        r = st.radial_r[ipr]
-        Vrad = st.radial_V[ipr] + dv
-        nb = int(g.nbord[ia])
-        rr = st.rrel[:nb, ia]
-        idx = np.searchsorted(r, rr, side="right")   # first r(i) > rrel, 0-based
-        idx = np.clip(idx, 2, len(r) - 1)
-        for L in range(int(lmaxa[ia]) + 1):
-            key = (ipr, L)
-            if key not in ur_cache:
-                ur_cache[key] = sch_radial(r, Vrad, enervide, ecin, L, float(cl.zproto[ipr]) +
-                                           (1.0 if ipr == 0 else 0.0))
-            u = ur_cache[key]
-            phi = f_interp2(rr, r[idx - 2], r[idx - 1], r[idx], u[idx - 2], u[idx - 1], u[idx])
-            for m in range(-L, L + 1):
-                lm = L * L + L + m
-                phiato[:nb, lm, 0, 0, 0, ia, 0] = phi * st.Ylmato[:nb, lm, ia]
+    for isp in range(1, nspinp + 1):
+        dvs = st.spin_shift(isp)
+        ecs = enervide - (st.V0bd + dvs)
+        for ia in range(natome):
+            ipr = int(cl.itype[ia])
+            r = st.radial_r[ipr]
+            Vrad = st.radial_V[ipr] + dvs
+            nb = int(g.nbord[ia])
+            rr = st.rrel[:nb, ia]
+            idx = np.searchsorted(r, rr, side="right")   # first r(i) > rrel, 0-based
+            idx = np.clip(idx, 2, len(r) - 1)
+            for L in range(int(lmaxa[ia]) + 1):
+                key = (isp, ipr, L)
+                if key not in ur_cache:
+                    ur_cache[key] = sch_radial(r, Vrad, enervide, ecs, L, float(cl.zproto[ipr]) +
+                                               (1.0 if ipr == 0 else 0.0))
+                u = ur_cache[key]
+                phi = f_interp2(rr, r[idx - 2], r[idx - 1], r[idx], u[idx - 2], u[idx - 1], u[idx])
+                for m in range(-L, L + 1):
+                    lm = L * L + L + m
+                    phiato[:nb, lm, isp - 1, 0, 0, ia, 0] = phi * st.Ylmato[:nb, lm, ia]
     # phiso, non-Rydberg, real branch
     konder = math.sqrt(ecin_out)
     fnorm = math.sqrt(konder / math.pi)

@@ -168,6 +168,8 @@ fdmgpu_status check_energy(const fdmgpu_handle* h, const fdmgpu_energy* e) {
   if (e->lmaxso < 0 || (e->lmaxso + 1) * (e->lmaxso + 1) < e->nlmso || e->nsort_r < h->g.nsort)
     return fail(FDMGPU_ERR_ARG, "Bessel arrays too small for nlmso");
   if (e->nlmso > h->g.nso1) return fail(FDMGPU_ERR_ARG, "nlmso exceeds the outer harmonic tables");
+  if (e->ispin < 1 || e->nspinp < std::min(e->ispin, h->g.nspin))
+    return fail(FDMGPU_ERR_ARG, "phiato must hold spin block min(ispin, nspin) (nspinp too small)");
   if (!e->new_ || !e->newinv || !e->lb1 || !e->lb2 || !e->ianew || !e->nlmsa || !e->Vr || !e->phiato ||
       !e->Besselr || !e->Neumanr)
     return fail(FDMGPU_ERR_ARG, "null array argument");
@@ -285,7 +287,7 @@ void pack_inputs(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& hp) {
   const int ispp = std::min(e->ispin, g.nspin);
   hp.in_d.insert(hp.in_d.end(), e->Vr + (int64_t)g.npoint * (ispp - 1), e->Vr + (int64_t)g.npoint * ispp);
   // phiato(ib, Lm, isp, isol=1, iRI=1, ia, 1) -> (nbtm, nlmagm, natome)
-  const int isp = std::min(e->ispin, e->nspinp);
+  const int isp = std::min(e->ispin, g.nspin);  // calcMatRow reads phiato at min(ispin, nspin)
   const int64_t d1 = e->nphiato1, d2 = e->nlmagm, d3 = e->nspinp, d4 = g.nspino, d5 = e->n_RI;
   const size_t base = hp.in_d.size();
   hp.in_d.resize(base + (size_t)g.nbtm * e->nlmagm * g.natome, 0.0);

@@ -143,3 +143,31 @@ def test_error_paths_keep_the_context_usable(solver_mod, golden):
         sv.spectrum_rerun()
     sv.close()
 
+
+def test_rutile_spin_polarised_uneven_batch(solver_mod, oracle_lib):
+    """Rutile TiO2 (Ti absorber, 6 O neighbours, two atom types), two spin
+    blocks split by 1.5 eV, two energies: one batch of four problems of
+    different orders (1990 and 2122 rows) against the oracle.  These matrices
+    have condition numbers up to 2.3e8 (measured), so two FP64 eliminations
+    in different orders differ by ~1e-8 in smr; the Taull bar is 1e-8 for
+    FP64 and mixed alike.  phiato carries both spin blocks (nspinp = nspin),
+    as calcMatRow's grid rows read it at min(ispin, nspin)."""
+    from fdmnes_gb300 import abi, cluster as CL
+    st = CL.build_structure(CL.rutile_cluster(2.0), 0.3, 2.4, 30.0, nspin=2, spin_split_ev=1.5)
+    ga = abi.GridArgs(st)
+    items, refs = [], []
+    for E in (3.0, 25.0):
+        for isp in (1, 2):
+            ei = CL.energy_inputs(st, E, ispin=isp)
+            ri = CL.newind(st, ei.nlmsa, ei.nlmso)
+            ea = abi.EnergyArgs(st, ei, ri)
+            Xo, _ = oracle_lib.mat_solve(ga, ea)
+            items.append((ei, ri))
+            refs.append(oracle_lib.taull(ga, ea, Xo))
+    assert len({ri.nligne for _, ri in items}) > 1
+    sv = solver_mod.FdmSolver(st)
+    for prec, tol in (("fp64", 1e-8), ("mixed", 1e-8)):
+        T, _ = sv.spectrum(items, prec)
+        for k, (t, r) in enumerate(zip(T, refs)):
+            assert rel(t, r) < tol, (prec, k, rel(t, r))
+    sv.close()
