@@ -138,6 +138,42 @@ def cpu_baseline(n_energies: int):
             "wall_s": wall}
 
 
+def _superlu_worker(args):
+    """One energy through SciPy's SuperLU (splu, COLAMD ordering) on the same
+    assembled matrix: a labelled stand-in for the reference's MUMPS backend
+    (source/mat_solve_mumps.f90), which is not available here."""
+    energy, = args
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as sla
+    from fdmnes_gb300 import abi, cluster as CL
+    import oracle
+    st, ga = _W["st"], _W["ga"]
+    ei = CL.energy_inputs(st, energy)
+    ri = CL.newind(st, ei.nlmsa, ei.nlmso)
+    ea = abi.EnergyArgs(st, ei, ri)
+    A, B = oracle.assemble_dense(ga, ea)
+    As = sp.csc_matrix(A)
+    t0 = time.perf_counter()
+    lu = sla.splu(As)
+    lu.solve(np.ascontiguousarray(B.T))
+    return time.perf_counter() - t0
+
+
+def superlu_standin(n_energies: int):
+    import oracle
+    oracle.build()
+    cores = min(os.cpu_count() or 1, n_energies)
+    energies = np.linspace(E_MIN, E_MAX, n_energies)
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores, initializer=_oracle_init) as pool:
+        per = pool.map(_superlu_worker, [(float(e),) for e in energies], chunksize=1)
+    wall = max(per)
+    return {"value": n_energies / wall, "unit": "energies/s", "cores": cores,
+            "kind": "SciPy SuperLU stand-in for MUMPS (not the reference)",
+            "sample": f"{n_energies} Cu energies {E_MIN}..{E_MAX} eV, one per process, factor + solve only; "
+                      f"single-energy {min(per):.2f}-{max(per):.2f} s"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -284,6 +320,7 @@ def run_gpu(args):
     if rank != 0:
         return
     cb = cpu_baseline(min(os.cpu_count() or 1, 16)) if not args.no_cpu else None
+    slu = superlu_standin(min(os.cpu_count() or 1, 16)) if not args.no_cpu else None
     line = {
         "metric": METRIC, "value": value, "unit": "energies/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -297,6 +334,7 @@ def run_gpu(args):
         "roofline": roof_main,
         "roofline_other": [roof_res, roof_fac],
         "cpu_baseline": cb and {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "cpu_superlu_standin": slu,
         "e2e": {"value": n_all / e2e_s, "unit": "energies/s", "h2d_bytes_per_step": int(h2d),
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": int(last["n_kernels"]),

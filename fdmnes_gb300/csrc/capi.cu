@@ -114,13 +114,15 @@ struct fdmgpu_handle {
   DevBuf<double> d_dpool;
   DevBuf<double> d_env64, d_B64, d_X64, d_rs, d_cs, d_val, d_taull, d_tscratch, d_smr;
   DevBuf<double> d_gT, d_lam, d_gpart, d_grad;  // adjoint
-  DevBuf<float> d_env32, d_Y32;
+  DevBuf<float> d_env32, d_Y32, d_R32;
+  DevBuf<int> d_act_df, d_act_rec;
   DevBuf<float2> d_val2, d_Xs;
   DevBuf<float> d_valS, d_V, d_W;
   DevBuf<unsigned char> d_gstate;
   DevBuf<int> d_inner, d_jdone, d_notconv, d_active_gm;
   int residual_df64 = 1;
   int refine_gmres = 0;   // GMRES-IR (1) or classical refinement (0)
+  int refine_recur = 0;   // classical refinement with the residual updated by recurrence (1)
   int escalate_dfl = 1;   // escalation by a double-float (1) or an FP64 (0) factorisation
   int gmres_m = 12;       // Krylov dimension of one GMRES cycle
   double tol = 0.0;         // refinement stop: max|dx|/max|x| (0: the default of the residual mode)
@@ -426,7 +428,9 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
         h->d_rowptr.reserve(rowv) != cudaSuccess || h->d_col.reserve(csr) != cudaSuccess ||
         h->d_piv.reserve(rowv) != cudaSuccess || h->d_val2.reserve(csr) != cudaSuccess ||
         h->d_Xs.reserve(rhs) != cudaSuccess || h->d_valS.reserve(csr) != cudaSuccess ||
-        h->d_V.reserve((size_t)(h->gmres_m + 1) * rhs) != cudaSuccess || h->d_W.reserve(rhs) != cudaSuccess ||
+        h->d_V.reserve((size_t)(h->refine_gmres ? h->gmres_m + 1 : 2) * rhs) != cudaSuccess ||
+        h->d_W.reserve(rhs) != cudaSuccess || h->d_R32.reserve(rhs) != cudaSuccess ||
+        h->d_act_df.reserve(np) != cudaSuccess || h->d_act_rec.reserve(np) != cudaSuccess ||
         h->d_gstate.reserve(gmres_state_bytes() * (size_t)std::max<int64_t>(h->ncols, 1)) != cudaSuccess ||
         h->d_inner.reserve(np) != cudaSuccess || h->d_jdone.reserve(np) != cudaSuccess ||
         h->d_notconv.reserve(np) != cudaSuccess || h->d_active_gm.reserve(np) != cudaSuccess ||
@@ -453,6 +457,9 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   if (mixed) {
     pl.env32 = h->d_env32.p;
     pl.Y32 = h->d_Y32.p;
+    pl.R32 = h->d_R32.p;
+    pl.act_df = h->d_act_df.p;
+    pl.act_rec = h->d_act_rec.p;
     pl.rs = h->d_rs.p;
     pl.cs = h->d_cs.p;
     pl.rowptr = h->d_rowptr.p;
@@ -577,7 +584,17 @@ void record_residual(fdmgpu_handle* h) {
   cudaStream_t s = h->stream;
   const Pools& pl = h->pl;
   cudaMemsetAsync(pl.dmax, 0, 3 * h->dims.nprob * sizeof(unsigned long long), s);
-  launch_residual(h->d_probs.p, pl, h->dims, h->residual_df64, s);
+  if (h->refine_recur) {
+    // true residual where act_df is set (then restart the recurrence from it),
+    // the recurrence residual R32 elsewhere
+    Pools pd = pl;
+    pd.active = pl.act_df;
+    launch_residual(h->d_probs.p, pd, h->dims, h->residual_df64, s);
+    launch_copy_rhs32(h->d_probs.p, h->dims, pl.Y32, pl.R32, pl.act_df, s);
+    launch_copy_rhs32(h->d_probs.p, h->dims, pl.R32, pl.Y32, pl.act_rec, s);
+  } else {
+    launch_residual(h->d_probs.p, pl, h->dims, h->residual_df64, s);
+  }
 }
 
 void record_iter(fdmgpu_handle* h) {
@@ -592,6 +609,7 @@ void record_iter(fdmgpu_handle* h) {
     launch_backward<float>(h->sp, pl.env32, pl.Y32, probs, h->tb, np, pl.active, s);
   }
   launch_update_x(probs, pl, h->dims, 0, s);
+  if (h->refine_recur) launch_resid_update(probs, pl, h->dims, s);
 }
 
 fdmgpu_status capture(fdmgpu_handle* h, void (*rec)(fdmgpu_handle*), cudaGraphExec_t* out, int64_t* nkernels) {
@@ -650,7 +668,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
                         h->d_piv.p,   h->d_val2.p,  h->d_Xs.p,    h->d_valS.p,  h->d_V.p,    h->d_W.p,
                         h->d_gstate.p, h->d_inner.p, h->d_jdone.p, h->d_notconv.p, h->d_active_gm.p,
                         h->d_nb_coef.p, h->d_rvol.p, h->d_poidsa.p, h->d_poidso.p, h->d_Kar.p, h->d_YsoT.p,
-                        h->d_Ylmato.p};
+                        h->d_Ylmato.p, h->d_R32.p, h->d_act_df.p, h->d_act_rec.p};
   for (const void* q : ptrs) ps = mix(ps, (uint64_t)(uintptr_t)q);
   if (replan || ps != h->ptr_sig) {
     h->ptr_sig = ps;
@@ -697,6 +715,14 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
     const double tol_accept = h->tol_accept > 0 ? h->tol_accept : (h->residual_df64 ? 1e-7 : 1e-9);
     std::vector<int> active(np, 1), slow(np, 0), gm(np, 0);
     std::vector<double> prev(np, 1e300);
+    // recurrence mode: which problems take a true residual next, the last
+    // correction measured against a true residual
+    std::vector<int> use_df(np, 1), act_df(np, 1), act_rec(np, 0);
+    std::vector<double> prev_true(np, 1e300);
+    if (h->refine_recur) {
+      CK(cudaMemcpyAsync(h->d_act_df.p, act_df.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+      CK(cudaMemcpyAsync(h->d_act_rec.p, act_rec.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    }
     std::vector<unsigned long long> red(3 * np);
     std::vector<int> jd(np, 0);
     CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
@@ -724,6 +750,27 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
         memcpy(&xm, &red[np + k], 8);
         const double r = xm > 0 ? dm / xm : dm;
         b.iters[k] = it;
+        if (h->refine_recur) {
+          // Only a step that started from a true residual can accept or stop a
+          // problem; recurrence steps that look converged or stall call for one.
+          if (use_df[k]) {
+            b.resid[k] = r;
+            if (!std::isfinite(r) || r <= tol || (prev_true[k] < 1e299 && r > 0.5 * prev_true[k])) {
+              active[k] = 0;
+            } else {
+              prev_true[k] = r;
+              use_df[k] = 0;
+              slow[k] = 0;
+              ++nact;
+            }
+          } else {
+            slow[k] = (r > 0.5 * prev[k]) ? slow[k] + 1 : 0;
+            use_df[k] = (!std::isfinite(r) || r <= tol || slow[k] >= 2) ? 1 : 0;
+            ++nact;
+          }
+          prev[k] = r;
+          continue;
+        }
         b.resid[k] = r;
         if (!std::isfinite(r) || r <= tol) {
           active[k] = 0;
@@ -746,6 +793,15 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
       }
       if (nact == 0) break;
       CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+      if (h->refine_recur) {
+        for (int k = 0; k < np; ++k) {
+          act_df[k] = active[k] && use_df[k];
+          act_rec[k] = active[k] && !use_df[k];
+        }
+        CK(cudaMemcpyAsync(h->d_act_df.p, act_df.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->d_act_rec.p, act_rec.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaStreamSynchronize(h->stream));  // the host vectors are reused next step
+      }
       if (gm_changed || h->refine_gmres) {
         std::vector<int> agm(np);
         for (int k = 0; k < np; ++k) agm[k] = active[k] && gm[k];
@@ -1058,6 +1114,9 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   h->d_notconv.release();
   h->d_active_gm.release();
   h->d_Y32.release();
+  h->d_R32.release();
+  h->d_act_df.release();
+  h->d_act_rec.release();
   h->d_strip.release();
   h->d_probs.release();
   h->d_red.release();
@@ -1077,11 +1136,13 @@ fdmgpu_status fdmgpu_set_residual_mode(fdmgpu_handle* h, int32_t mode) {
 }
 
 fdmgpu_status fdmgpu_set_refinement(fdmgpu_handle* h, int32_t mode, int32_t krylov_dim) {
-  if (!h || (mode != FDMGPU_REFINE_CLASSIC && mode != FDMGPU_REFINE_GMRES) || krylov_dim < 1 ||
-      krylov_dim > gmres_max_dim())
+  if (!h || (mode != FDMGPU_REFINE_CLASSIC && mode != FDMGPU_REFINE_GMRES && mode != FDMGPU_REFINE_RECURRENCE) ||
+      krylov_dim < 1 || krylov_dim > gmres_max_dim())
     return fail(FDMGPU_ERR_ARG, "unknown refinement mode or Krylov dimension out of range");
   h->refine_gmres = mode == FDMGPU_REFINE_GMRES;
+  h->refine_recur = mode == FDMGPU_REFINE_RECURRENCE;
   h->gmres_m = krylov_dim;
+  h->plan_sig = 0;  // pool sizes and graphs depend on the mode: plan again
   return FDMGPU_OK;
 }
 

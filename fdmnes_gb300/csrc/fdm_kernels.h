@@ -63,6 +63,9 @@ struct Pools {
   unsigned long long* amax = nullptr;  // per problem scratch
   int* err = nullptr;
   int* active = nullptr;
+  float* R32 = nullptr;            // residual of the scaled system, updated by recurrence
+  int* act_df = nullptr;           // active problems that take a true (double-float) residual
+  int* act_rec = nullptr;          // active problems that take the recurrence residual
   // GMRES-IR
   float* valS = nullptr;           // equilibrated FP32 CSR values
   float* V = nullptr;              // Krylov basis, (m+1) vectors of vstride floats
@@ -102,6 +105,9 @@ int gmres_max_dim();
 void launch_copy_rhs(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s);
 int launch_dfl_escalation(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
                            dfl* D, int iters, cudaStream_t s, cudaEvent_t ev_f0 = nullptr, cudaEvent_t ev_f1 = nullptr);
+void launch_resid_update(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s);
+void launch_copy_rhs32(const Prob* probs, const LaunchDims& d, const float* src, float* dst, const int* mask,
+                       cudaStream_t s);
 void launch_csr_nnz(const Prob* probs, const int* rowptr, const LaunchDims& d, int* nnz, cudaStream_t s);
 cudaError_t taull_noalloc_scratch(double2** out);
 cudaError_t launch_taull_noalloc(const double* smr, int nlmso, int nligne, int ianew_abs, int nlm_abs,

@@ -261,19 +261,42 @@ __global__ void k_residual_df(const Prob* probs, const int* rowptr, const int* c
       acc[t].hi = (float)b;
       acc[t].lo = (float)(b - (double)acc[t].hi);
     }
-    for (int k = k0; k < k1; ++k) {
-      const int q = col[P.csr + k];
-      const float2 a = val2[P.csr + k];
-      const float2* xr = Xs + P.rhs + ((int64_t)(q / TS) * P.nrt) * TS2 + (q % TS) * TS;
-#pragma unroll
-      for (int t = 0; t < 8; ++t) {
-        const int r = r0 + lane + 32 * t;
-        if (r < nrhs) df_sub_prod(acc[t], a, xr[(int64_t)(r / TS) * TS2 + (r % TS)]);
+    // the row's nonzeros in chunks of 32: lane j fetches the column and value
+    // of nonzero j (one coalesced load each), broadcast by shuffles; two
+    // nonzeros per step keep 16 X loads in flight per lane
+    for (int kb = k0; kb < k1; kb += 32) {
+      const int nk = min(32, k1 - kb);
+      int qv = 0;
+      float2 av = make_float2(0.f, 0.f);
+      if (lane < nk) {
+        qv = col[P.csr + kb + lane];
+        av = val2[P.csr + kb + lane];
       }
-      if (((k - k0) & 63) == 63) {
+      for (int j = 0; j < nk; j += 2) {
+        const int q0 = __shfl_sync(0xffffffffu, qv, j);
+        const float2 a0 = make_float2(__shfl_sync(0xffffffffu, av.x, j), __shfl_sync(0xffffffffu, av.y, j));
+        const bool two = j + 1 < nk;
+        const int q1 = __shfl_sync(0xffffffffu, qv, two ? j + 1 : j);
+        const float2 a1 = two ? make_float2(__shfl_sync(0xffffffffu, av.x, j + 1), __shfl_sync(0xffffffffu, av.y, j + 1))
+                              : make_float2(0.f, 0.f);
+        const float2* xr0 = Xs + P.rhs + ((int64_t)(q0 / TS) * P.nrt) * TS2 + (q0 % TS) * TS;
+        const float2* xr1 = Xs + P.rhs + ((int64_t)(q1 / TS) * P.nrt) * TS2 + (q1 % TS) * TS;
+        float2 x0[8], x1[8];
 #pragma unroll
-        for (int t = 0; t < 8; ++t) acc[t] = df_norm(acc[t]);
+        for (int t = 0; t < 8; ++t) {
+          const int r = r0 + lane + 32 * t;
+          const int64_t o = (int64_t)(r / TS) * TS2 + (r % TS);
+          x0[t] = r < nrhs ? xr0[o] : make_float2(0.f, 0.f);
+          x1[t] = (r < nrhs && two) ? xr1[o] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          df_sub_prod(acc[t], a0, x0[t]);
+          df_sub_prod(acc[t], a1, x1[t]);
+        }
       }
+#pragma unroll
+      for (int t = 0; t < 8; ++t) acc[t] = df_norm(acc[t]);
     }
 #pragma unroll
     for (int t = 0; t < 8; ++t) {
@@ -287,6 +310,81 @@ __global__ void k_residual_df(const Prob* probs, const int* rowptr, const int* c
   }
   for (int o = 16; o; o >>= 1) rm = fmax(rm, __shfl_xor_sync(0xffffffffu, rm, o));
   if (lane == 0) atomic_max_abs(&rmax[e], rm);
+}
+
+// Residual by recurrence: R32 -= (Dr A Dc) Y32, the equilibrated FP32 matrix
+// times the correction just solved for, for the active problems.  Because the
+// corrections shrink geometrically, the FP32 rounding of this update is second
+// order in the FP32 unit roundoff relative to |A||x|; a true (double-float)
+// residual confirms convergence.  Warp per row, nonzeros in chunks of 32.
+__global__ void k_resid_update(const Prob* probs, const int* rowptr, const int* col, const float* valS, const float* Y,
+                               float* R, const int* active) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (!active[e]) return;
+  const int p = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (p >= P.nt * TS) return;
+  const int k0 = rowptr[P.rowv + p], k1 = min(rowptr[P.rowv + p + 1], (int)P.csr_cap);
+  const int nrhs = P.nrt * TS;
+  for (int r0 = 0; r0 < nrhs; r0 += 256) {
+    float acc[8];
+#pragma unroll
+    for (int t = 0; t < 8; ++t) acc[t] = 0.f;
+    for (int kb = k0; kb < k1; kb += 32) {
+      const int nk = min(32, k1 - kb);
+      int qv = 0;
+      float av = 0.f;
+      if (lane < nk) {
+        qv = col[P.csr + kb + lane];
+        av = valS[P.csr + kb + lane];
+      }
+      for (int j = 0; j < nk; j += 2) {
+        const bool two = j + 1 < nk;
+        const int q0 = __shfl_sync(0xffffffffu, qv, j), q1 = __shfl_sync(0xffffffffu, qv, two ? j + 1 : j);
+        const float a0 = __shfl_sync(0xffffffffu, av, j);
+        const float a1 = two ? __shfl_sync(0xffffffffu, av, j + 1) : 0.f;
+        const float* y0 = Y + P.rhs + ((int64_t)(q0 / TS) * P.nrt) * TS2 + (q0 % TS) * TS;
+        const float* y1 = Y + P.rhs + ((int64_t)(q1 / TS) * P.nrt) * TS2 + (q1 % TS) * TS;
+        float v0[8], v1[8];
+#pragma unroll
+        for (int t = 0; t < 8; ++t) {
+          const int r = r0 + lane + 32 * t;
+          const int64_t o = (int64_t)(r / TS) * TS2 + (r % TS);
+          v0[t] = r < nrhs ? y0[o] : 0.f;
+          v1[t] = (r < nrhs && two) ? y1[o] : 0.f;
+        }
+#pragma unroll
+        for (int t = 0; t < 8; ++t) acc[t] = fmaf(a1, v1[t], fmaf(a0, v0[t], acc[t]));
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 8; ++t) {
+      const int r = r0 + lane + 32 * t;
+      if (r < nrhs) R[P.rhs + ((int64_t)(p / TS) * P.nrt + r / TS) * TS2 + (p % TS) * TS + (r % TS)] -= acc[t];
+    }
+  }
+}
+
+// dst = src over the RHS tiles of the problems whose mask is set.
+__global__ void k_copy_rhs32(const Prob* probs, const float* src, float* dst, const int* mask) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (!mask[e]) return;
+  const int64_t w = blockIdx.x;
+  if (w >= (int64_t)P.nt * P.nrt) return;
+  const float4* a = reinterpret_cast<const float4*>(src + P.rhs + w * TS2);
+  float4* b = reinterpret_cast<float4*>(dst + P.rhs + w * TS2);
+  for (int idx = threadIdx.x; idx < TS2 / 4; idx += blockDim.x) b[idx] = a[idx];
+}
+
+void launch_resid_update(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s) {
+  k_resid_update<<<dim3((d.max_rows + 7) / 8, d.nprob), 256, 0, s>>>(probs, pl.rowptr, pl.col, pl.valS, pl.Y32, pl.R32,
+                                                                    pl.active);
+}
+
+void launch_copy_rhs32(const Prob* probs, const LaunchDims& d, const float* src, float* dst, const int* mask,
+                       cudaStream_t s) {
+  k_copy_rhs32<<<dim3(d.max_rhs_tiles, d.nprob), 256, 0, s>>>(probs, src, dst, mask);
 }
 
 // X64 (+)= cs * Y32 over RHS tiles, with per-problem maxima of |d| and |x|.

@@ -111,8 +111,8 @@ class FdmSolver:
         _check(self.lib.fdmgpu_set_residual_mode(self.h, {"fp64": 0, "df64": 1}[mode]))
 
     def set_refinement(self, mode: str = "gmres", krylov_dim: int = 12):
-        """Refinement of the mixed path: 'gmres' (GMRES-IR, default) or 'classic'."""
-        _check(self.lib.fdmgpu_set_refinement(self.h, {"classic": 0, "gmres": 1}[mode], krylov_dim))
+        """Refinement of the mixed path: 'classic' (default), 'recurrence' or 'gmres'."""
+        _check(self.lib.fdmgpu_set_refinement(self.h, {"classic": 0, "gmres": 1, "recurrence": 2}[mode], krylov_dim))
 
     def set_escalation(self, mode: str = "df64"):
         """Re-solve arithmetic for energies the FP32 factors cannot refine: 'df64' or 'fp64'."""

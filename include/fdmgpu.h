@@ -58,8 +58,10 @@ typedef enum {
 
 /* Refinement of the mixed precision path. */
 typedef enum {
-  FDMGPU_REFINE_CLASSIC = 0,   /* x += LU32^-1 r                                        */
-  FDMGPU_REFINE_GMRES = 1      /* GMRES-IR: GMRES(m) on LU32^-1 A per correction (default) */
+  FDMGPU_REFINE_CLASSIC = 0,   /* x += LU32^-1 r, r in double-float every step (default) */
+  FDMGPU_REFINE_GMRES = 1,     /* GMRES-IR: GMRES(m) on LU32^-1 A per correction        */
+  FDMGPU_REFINE_RECURRENCE = 2 /* classical, with r updated by r -= A dx in FP32 between
+                                  double-float residuals that start and confirm it      */
 } fdmgpu_refinement;
 
 /* Re-solve of an energy whose mixed precision refinement missed its tolerance. */
