@@ -40,10 +40,11 @@ __global__ void k_asm_pad(const Prob* probs, double* env, Tables tb, int* err) {
 }
 
 // Grid-point rows: one warp per interstitial point.
-__global__ void __launch_bounds__(256) k_asm_grid(StaticDev S, const Prob* probs, const int* ipool,
+__global__ void __launch_bounds__(256) k_asm_grid(const StaticDev* sites, const Prob* probs, const int* ipool,
                                                   const double* dpool, double* env, double* B, Tables tb, int* err) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
+  const StaticDev& S = sites[P.site];
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   const int k = blockIdx.x * 8 + warp;
   if (k >= S.npr) return;
@@ -101,10 +102,11 @@ __global__ void __launch_bounds__(256) k_asm_grid(StaticDev S, const Prob* probs
 
 // Outer-sphere rows: one thread per (row Lm, column Lmp) of the outer block and
 // of the right-hand side; then the boundary-point columns.
-__global__ void __launch_bounds__(256) k_asm_outer(StaticDev S, const Prob* probs, const double* dpool, double* env,
+__global__ void __launch_bounds__(256) k_asm_outer(const StaticDev* sites, const Prob* probs, const double* dpool, double* env,
                                                    double* B, Tables tb, int* err) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
+  const StaticDev& S = sites[P.site];
   const int nl = P.lmaxso + 1;
   const double* bes = dpool + P.in_bes;
   const double* neu = dpool + P.in_neu;
@@ -129,10 +131,11 @@ __global__ void __launch_bounds__(256) k_asm_outer(StaticDev S, const Prob* prob
   *rhs_at(B, P, p, Lmp - 1) = sm;
 }
 
-__global__ void __launch_bounds__(256) k_asm_outer_bnd(StaticDev S, const Prob* probs, const int* ipool, double* env,
+__global__ void __launch_bounds__(256) k_asm_outer_bnd(const StaticDev* sites, const Prob* probs, const int* ipool, double* env,
                                                        Tables tb, int* err) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
+  const StaticDev& S = sites[P.site];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= P.nlmso * S.nsortf) return;
   const int Lm = t / S.nsortf + 1, ib = t % S.nsortf + 1;
@@ -147,10 +150,11 @@ __global__ void __launch_bounds__(256) k_asm_outer_bnd(StaticDev S, const Prob* 
 
 // Atom rows: block per (atom, harmonic row); threads over the own-block
 // columns and then over the boundary points.
-__global__ void __launch_bounds__(128) k_asm_atom(StaticDev S, const Prob* probs, const int* ipool, const double* dpool,
+__global__ void __launch_bounds__(128) k_asm_atom(const StaticDev* sites, const Prob* probs, const int* ipool, const double* dpool,
                                                   double* env, Tables tb, int max_nlm, int* err) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
+  const StaticDev& S = sites[P.site];
   const int ia = blockIdx.x / max_nlm + 1;
   const int Lm = blockIdx.x % max_nlm + 1;
   const int* new_ = ipool + P.in_new;
@@ -185,19 +189,21 @@ __global__ void __launch_bounds__(128) k_asm_atom(StaticDev S, const Prob* probs
   }
 }
 
-void launch_assemble(const StaticDev& S, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
+void launch_assemble(const StaticDev* sites, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
                      cudaStream_t s) {
   const int np = d.nprob;
   k_asm_pad<<<dim3(1, np), TS, 0, s>>>(probs, pl.env64, tb, pl.err);
-  k_asm_grid<<<dim3((S.npr + 7) / 8, np), 256, 0, s>>>(S, probs, pl.ipool, pl.dpool, pl.env64, pl.B64, tb, pl.err);
+  if (d.npr > 0)
+    k_asm_grid<<<dim3((d.npr + 7) / 8, np), 256, 0, s>>>(sites, probs, pl.ipool, pl.dpool, pl.env64, pl.B64, tb,
+                                                         pl.err);
   const int nsq = d.max_nlmso * d.max_nlmso;
-  k_asm_outer<<<dim3((nsq + 255) / 256, np), 256, 0, s>>>(S, probs, pl.dpool, pl.env64, pl.B64, tb, pl.err);
-  const int nb = d.max_nlmso * S.nsortf;
-  if (nb > 0) k_asm_outer_bnd<<<dim3((nb + 255) / 256, np), 256, 0, s>>>(S, probs, pl.ipool, pl.env64, tb, pl.err);
-  const int max_nlm = d.max_atom_rows / (S.natome > 0 ? S.natome : 1);
-  if (d.max_atom_rows > 0)
-    k_asm_atom<<<dim3(S.natome * max_nlm, np), 128, 0, s>>>(S, probs, pl.ipool, pl.dpool, pl.env64, tb, max_nlm,
-                                                            pl.err);
+  k_asm_outer<<<dim3((nsq + 255) / 256, np), 256, 0, s>>>(sites, probs, pl.dpool, pl.env64, pl.B64, tb, pl.err);
+  const int nb = d.max_nlmso * d.max_nsortf;
+  if (nb > 0)
+    k_asm_outer_bnd<<<dim3((nb + 255) / 256, np), 256, 0, s>>>(sites, probs, pl.ipool, pl.env64, tb, pl.err);
+  if (d.max_natome > 0 && d.max_nlmsa > 0)
+    k_asm_atom<<<dim3(d.max_natome * d.max_nlmsa, np), 128, 0, s>>>(sites, probs, pl.ipool, pl.dpool, pl.env64, tb,
+                                                                    d.max_nlmsa, pl.err);
 }
 
 }  // namespace fdm

@@ -86,6 +86,7 @@ struct Batch {
   std::vector<int> err;
   bool ran = false;
   bool lam_valid = false;  // the adjoint Lambda of the last vjp matches the batch's factors
+  std::vector<fdmgpu_handle*> sites;  // grids of the batch's problems; sites[0] is the batch's own handle
 };
 
 }  // namespace
@@ -146,6 +147,7 @@ struct fdmgpu_handle {
   Tables tb{};
   Pools pl{};
   cudaEvent_t ev[10] = {};
+  DevBuf<StaticDev> d_sites;  // static tables of every site of the batch, indexed by Prob::site
   DevBuf<int> d_nnz;  // CSR nonzeros per problem (algorithmic work of the residual)
 };
 
@@ -364,7 +366,11 @@ void layout_batch(fdmgpu_handle* h, Layout& L) {
   d = LaunchDims();
   d.nprob = np;
   h->ncols_tmp = 0;
-  d.npr = h->S.npr;
+  for (auto* sh : h->batch.sites) {
+    d.npr = std::max(d.npr, sh->S.npr);
+    d.max_nsortf = std::max(d.max_nsortf, sh->S.nsortf);
+    d.max_natome = std::max(d.max_natome, sh->S.natome);
+  }
   std::vector<int>& J0 = L.J0; std::vector<int>& J1 = L.J1;
   std::vector<int>& Imax = L.Imax; std::vector<int>& Imin = L.Imin;
   std::vector<int64_t>& strip = L.strip;
@@ -396,7 +402,8 @@ void layout_batch(fdmgpu_handle* h, Layout& L) {
     d.max_tiles = std::max<int>(d.max_tiles, (int)hp.ntiles);
     d.max_rhs_tiles = std::max(d.max_rhs_tiles, P.nt * P.nrt);
     d.max_nlmso = std::max(d.max_nlmso, P.nlmso);
-    d.max_atom_rows = std::max(d.max_atom_rows, h->g.natome * hp.nlmsa_max);
+    d.max_atom_rows = std::max(d.max_atom_rows, h->batch.sites[P.site]->g.natome * hp.nlmsa_max);
+    d.max_nlmsa = std::max(d.max_nlmsa, hp.nlmsa_max);
   }
   d.rowv_total = rowv;
   h->ncols = h->ncols_tmp;
@@ -487,14 +494,15 @@ fdmgpu_status upload_inputs(fdmgpu_handle* h) {
   auto& pr = h->batch.probs;
   size_t ni = 0, nd = 0;
   for (auto& hp : pr) {
+    const fdmgpu_grid& g = h->batch.sites[hp.P.site]->g;
     hp.P.in_new = ni;
-    hp.P.in_ianew = ni + h->g.npoint + 1;
-    hp.P.in_nlmsa = hp.P.in_ianew + h->g.natome;
+    hp.P.in_ianew = ni + g.npoint + 1;
+    hp.P.in_nlmsa = hp.P.in_ianew + g.natome;
     ni += hp.in_i.size();
     hp.P.in_vr = nd;
-    hp.P.in_phi = nd + h->g.npoint;
-    hp.P.in_bes = hp.P.in_phi + (int64_t)h->g.nbtm * hp.P.nlmagm * h->g.natome;
-    hp.P.in_neu = hp.P.in_bes + (int64_t)h->g.nsort * (hp.P.lmaxso + 1);
+    hp.P.in_phi = nd + g.npoint;
+    hp.P.in_bes = hp.P.in_phi + (int64_t)g.nbtm * hp.P.nlmagm * g.natome;
+    hp.P.in_neu = hp.P.in_bes + (int64_t)g.nsort * (hp.P.lmaxso + 1);
     nd += hp.in_d.size();
   }
   if (ni > h->h_pinned_i_cap) {
@@ -522,6 +530,9 @@ fdmgpu_status upload_inputs(fdmgpu_handle* h) {
   CK(cudaMemcpyAsync(h->d_ipool.p, h->h_pinned_i, ni * sizeof(int), cudaMemcpyHostToDevice, h->stream));
   CK(cudaMemcpyAsync(h->d_dpool.p, h->h_pinned_d, nd * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   CK(upload(h->d_probs, P, h->stream));
+  std::vector<StaticDev> sites;
+  for (auto* sh : h->batch.sites) sites.push_back(sh->S);
+  CK(upload(h->d_sites, sites, h->stream));
   h->pl.ipool = h->d_ipool.p;
   h->pl.dpool = h->d_dpool.p;
   return FDMGPU_OK;
@@ -544,7 +555,7 @@ void record_asm(fdmgpu_handle* h) {
   cudaMemsetAsync(pl.env64, 0, env * sizeof(double), s);
   cudaMemsetAsync(pl.B64, 0, rhs * sizeof(double), s);
   cudaMemsetAsync(pl.err, 0, np * sizeof(int), s);
-  launch_assemble(h->S, probs, pl, h->tb, h->dims, s);
+  launch_assemble(h->d_sites.p, probs, pl, h->tb, h->dims, s);
   if (h->batch.precision == FDMGPU_PREC_FP64) {
     cudaMemcpyAsync(pl.X64, pl.B64, rhs * sizeof(double), cudaMemcpyDeviceToDevice, s);
   } else {
@@ -643,6 +654,11 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   if (np == 0) return fail(FDMGPU_ERR_ARG, "empty batch");
   uint64_t sig = mix(0, (uint64_t)np);
   for (auto& hp : b.probs) sig = mix(sig, hp.sig);
+  // the launch dimensions depend on the sites' grids
+  for (auto* sh : b.sites) {
+    sig = mix(sig, (uint64_t)(uintptr_t)sh);
+    sig = mix(sig, ((uint64_t)sh->S.npr << 32) ^ ((uint64_t)sh->S.nsortf << 16) ^ (uint64_t)sh->S.natome);
+  }
   fdmgpu_status st;
   cudaGetLastError();  // clear a stale error of an earlier call on this thread
   sig = mix(sig, (uint64_t)h->residual_df64);
@@ -668,7 +684,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
                         h->d_piv.p,   h->d_val2.p,  h->d_Xs.p,    h->d_valS.p,  h->d_V.p,    h->d_W.p,
                         h->d_gstate.p, h->d_inner.p, h->d_jdone.p, h->d_notconv.p, h->d_active_gm.p,
                         h->d_nb_coef.p, h->d_rvol.p, h->d_poidsa.p, h->d_poidso.p, h->d_Kar.p, h->d_YsoT.p,
-                        h->d_Ylmato.p, h->d_R32.p, h->d_act_df.p, h->d_act_rec.p};
+                        h->d_Ylmato.p, h->d_R32.p, h->d_act_df.p, h->d_act_rec.p, h->d_sites.p};
   for (const void* q : ptrs) ps = mix(ps, (uint64_t)(uintptr_t)q);
   if (replan || ps != h->ptr_sig) {
     h->ptr_sig = ps;
@@ -1114,6 +1130,7 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   h->d_notconv.release();
   h->d_active_gm.release();
   h->d_Y32.release();
+  h->d_sites.release();
   h->d_R32.release();
   h->d_act_df.release();
   h->d_act_rec.release();
@@ -1166,6 +1183,7 @@ fdmgpu_status fdmgpu_batch_begin(fdmgpu_handle* h, int32_t precision, int32_t ma
   if (precision != FDMGPU_PREC_FP64 && precision != FDMGPU_PREC_MIXED)
     return fail(FDMGPU_ERR_ARG, "unknown precision");
   h->batch.probs.clear();
+  h->batch.sites.assign(1, h);
   h->batch.precision = precision;
   h->batch.max_energies = max_energies;
   h->batch.ran = false;
@@ -1173,29 +1191,40 @@ fdmgpu_status fdmgpu_batch_begin(fdmgpu_handle* h, int32_t precision, int32_t ma
   return FDMGPU_OK;
 }
 
-fdmgpu_status fdmgpu_batch_add(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t iaabs) {
-  if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
-  fdmgpu_status st = check_energy(h, e);
+fdmgpu_status fdmgpu_batch_add_site(fdmgpu_handle* h, fdmgpu_handle* site, const fdmgpu_energy* e, int32_t iaabs) {
+  if (!h || !site) return fail(FDMGPU_ERR_ARG, "null handle");
+  if (site->device != h->device) return fail(FDMGPU_ERR_ARG, "the site handle lives on another device");
+  Batch& b = h->batch;
+  if (b.sites.empty()) b.sites.assign(1, h);
+  fdmgpu_status st = check_energy(site, e);
   if (st) return st;
-  if (h->batch.max_energies > 0 && (int)h->batch.probs.size() >= h->batch.max_energies)
-    return fail(FDMGPU_ERR_ARG, "batch is full");
+  if (b.max_energies > 0 && (int)b.probs.size() >= b.max_energies) return fail(FDMGPU_ERR_ARG, "batch is full");
+  int si = (int)(std::find(b.sites.begin(), b.sites.end(), site) - b.sites.begin());
+  if (si == (int)b.sites.size()) b.sites.push_back(site);
   HostProb hp;
-  st = plan_problem(h, e, hp);
+  st = plan_problem(site, e, hp);
   if (st) return st;
-  if (iaabs >= 1 && iaabs <= h->g.natome) {
+  hp.P.site = si;
+  const fdmgpu_grid& g = site->g;
+  if (iaabs >= 1 && iaabs <= g.natome) {
     hp.P.iaabs = iaabs;
     hp.P.nlm_abs = e->nlmsa[iaabs - 1];
     hp.P.ianew_abs = e->ianew[iaabs - 1];
     for (int lm = 1; lm <= hp.P.nlm_abs; ++lm) {
-      const int L = F2(h->g.lato, h->g.nlmsam, lm, iaabs), m = F2(h->g.mato, h->g.nlmsam, lm, iaabs);
+      const int L = F2(g.lato, g.nlmsam, lm, iaabs), m = F2(g.mato, g.nlmsam, lm, iaabs);
       if (L * L + L + 1 + m != lm) return fail(FDMGPU_ERR_UNSUPPORTED, "Taull needs the C1 harmonic order");
     }
   }
   hp.sig = mix(hp.sig, (uint64_t)hp.P.nlm_abs * 7919u + (uint64_t)hp.P.ianew_abs);
-  pack_inputs(h, e, hp);
-  h->batch.probs.push_back(std::move(hp));
-  h->batch.ran = false;
+  hp.sig = mix(hp.sig, (uint64_t)si * 104729u + 1u);
+  pack_inputs(site, e, hp);
+  b.probs.push_back(std::move(hp));
+  b.ran = false;
   return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_batch_add(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t iaabs) {
+  return fdmgpu_batch_add_site(h, h, e, iaabs);
 }
 
 fdmgpu_status fdmgpu_batch_run(fdmgpu_handle* h, fdmgpu_info* info) {
@@ -1262,6 +1291,7 @@ fdmgpu_status fdmgpu_batch_vjp(fdmgpu_handle* h, const double* gtaull, double* g
   if (!b.ran) return fail(FDMGPU_ERR_ARG, "vjp needs a batch that has run");
   if (b.precision != FDMGPU_PREC_FP64)
     return fail(FDMGPU_ERR_UNSUPPORTED, "vjp needs the factors of an FP64 batch");
+  if (b.sites.size() > 1) return fail(FDMGPU_ERR_UNSUPPORTED, "vjp of a batch over several sites");
   const int np = h->dims.nprob;
   for (int k = 0; k < np; ++k) {
     if (b.probs[k].P.nlm_abs <= 0) return fail(FDMGPU_ERR_ARG, "vjp needs an absorber (iaabs > 0) in every energy");
@@ -1371,6 +1401,7 @@ fdmgpu_status fdmgpu_batch_adjoint_dot(fdmgpu_handle* h, const fdmgpu_energy* co
   Batch& b = h->batch;
   const int np = (int)b.probs.size();
   if (!b.lam_valid) return fail(FDMGPU_ERR_ARG, "adjoint_dot needs a vjp of the batch that has run");
+  if (b.sites.size() > 1) return fail(FDMGPU_ERR_UNSUPPORTED, "adjoint_dot of a batch over several sites");
   if (n != np) return fail(FDMGPU_ERR_ARG, "one energy argument per batch energy is needed");
   for (int k = 0; k < np; ++k) {
     fdmgpu_status st = check_energy(h, e[k]);
@@ -1425,7 +1456,7 @@ fdmgpu_status fdmgpu_batch_adjoint_dot(fdmgpu_handle* h, const fdmgpu_energy* co
   CK(cudaMemsetAsync(pl.env64, 0, env * sizeof(double), s));
   CK(cudaMemsetAsync(pl.B64, 0, rhs * sizeof(double), s));
   CK(cudaMemsetAsync(pl.err, 0, np * sizeof(int), s));
-  launch_assemble(h->S, h->d_probs.p, pl, h->tb, h->dims, s);
+  launch_assemble(h->d_sites.p, h->d_probs.p, pl, h->tb, h->dims, s);
   launch_csr(h->d_probs.p, pl, h->tb, h->dims, s);
   launch_lambda_dot(h->d_probs.p, pl, h->dims, h->d_lam.p, h->d_gpart.p, h->d_gpart.p + rowv, s);
   CK(cudaGetLastError());

@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) k_panel(T* env, T* rhs, const Pr
 }
 
 template <typename T>
-__global__ void __launch_bounds__(GEMM_THREADS) k_trailing(T* env, T* rhs, const Prob* probs, Tables tb, int K,
+__global__ void __launch_bounds__(MMThreads<T>::value) k_trailing(T* env, T* rhs, const Prob* probs, Tables tb, int K,
                                                        int fuse_rhs, const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) k_fwd_diag(const T* env, T* rhs,
 
 // Y(I,R) -= L(I,K) Y(K,R) for I in (K, Imax(K)].
 template <typename T>
-__global__ void __launch_bounds__(GEMM_THREADS) k_fwd_update(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
+__global__ void __launch_bounds__(MMThreads<T>::value) k_fwd_update(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
                                                          const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -159,7 +159,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) k_bwd_diag(const T* env, T* rhs,
 
 // Y(I,R) -= U(I,K) Y(K,R) for I in [Imin(K), K).
 template <typename T>
-__global__ void __launch_bounds__(GEMM_THREADS) k_bwd_update(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
+__global__ void __launch_bounds__(MMThreads<T>::value) k_bwd_update(const T* env, T* rhs, const Prob* probs, Tables tb, int K,
                                                          const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -194,7 +194,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) k_tfwd_diag(const T* env, T* rhs
 
 // W(J,R) -= U(K,J)^T W(K,R) for J in (K, J1(K)].
 template <typename T>
-__global__ void __launch_bounds__(GEMM_THREADS) k_tfwd_update(const T* env, T* rhs, const Prob* probs, Tables tb,
+__global__ void __launch_bounds__(MMThreads<T>::value) k_tfwd_update(const T* env, T* rhs, const Prob* probs, Tables tb,
                                                               int K, const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -228,7 +228,7 @@ __global__ void __launch_bounds__(GEMM_THREADS) k_tbwd_diag(const T* env, T* rhs
 
 // W(I,R) -= L(K,I)^T W(K,R) for I in [J0(K), K).
 template <typename T>
-__global__ void __launch_bounds__(GEMM_THREADS) k_tbwd_update(const T* env, T* rhs, const Prob* probs, Tables tb,
+__global__ void __launch_bounds__(MMThreads<T>::value) k_tbwd_update(const T* env, T* rhs, const Prob* probs, Tables tb,
                                                               int K, const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -283,7 +283,7 @@ int launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables 
     }
     const int nt = fuse_rhs ? sp.trail_rhs[K] : sp.trail[K];
     if (nt > 0) {
-      k_trailing<T><<<dim3(nt, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
+      k_trailing<T><<<dim3(nt, nprob), MMThreads<T>::value, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
       ++nk;
     }
   }
@@ -299,7 +299,7 @@ int launch_forward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, 
     k_fwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active, piv);
     ++nk;
     if (sp.fwd[K] > 0) {
-      k_fwd_update<T><<<dim3(sp.fwd[K], nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+      k_fwd_update<T><<<dim3(sp.fwd[K], nprob), MMThreads<T>::value, sm, s>>>(env, rhs, probs, tb, K, active);
       ++nk;
     }
   }
@@ -315,7 +315,7 @@ int launch_backward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs,
     k_bwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
     ++nk;
     if (sp.bwd[K] > 0) {
-      k_bwd_update<T><<<dim3(sp.bwd[K], nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+      k_bwd_update<T><<<dim3(sp.bwd[K], nprob), MMThreads<T>::value, sm, s>>>(env, rhs, probs, tb, K, active);
       ++nk;
     }
   }
@@ -329,7 +329,7 @@ void launch_forward_t(const StepPlan& sp, const T* env, T* rhs, const Prob* prob
   for (int K = 0; K < sp.ntmax; ++K) {
     k_tfwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
     if (sp.tfwd[K] > 0)
-      k_tfwd_update<T><<<dim3(sp.tfwd[K], nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+      k_tfwd_update<T><<<dim3(sp.tfwd[K], nprob), MMThreads<T>::value, sm, s>>>(env, rhs, probs, tb, K, active);
   }
 }
 
@@ -340,7 +340,7 @@ void launch_backward_t(const StepPlan& sp, const T* env, T* rhs, const Prob* pro
   for (int K = sp.ntmax - 1; K >= 0; --K) {
     k_tbwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active, piv);
     if (sp.tbwd[K] > 0)
-      k_tbwd_update<T><<<dim3(sp.tbwd[K], nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
+      k_tbwd_update<T><<<dim3(sp.tbwd[K], nprob), MMThreads<T>::value, sm, s>>>(env, rhs, probs, tb, K, active);
   }
 }
 

@@ -42,6 +42,7 @@ struct Prob {
   int nlm_abs;    // harmonics of the absorber
   int ianew_abs;  // row offset of the absorber harmonics (1-based rows ianew+1..)
   int trow;       // offset into J0 / J1 / strip arrays (per tile row)
+  int site;       // index of the problem's grid (absorbing site) in the batch's site table
   double enervide;
   int64_t env;    // element offset of the band tiles
   int64_t rhs;    // element offset of the RHS tiles (nt * nrt * TS2)
@@ -363,12 +364,22 @@ __device__ __forceinline__ T mac_finish(T acc) { return acc; }
 template <>
 __device__ __forceinline__ dfl mac_finish<dfl>(dfl acc) { return df_fast_two_sum(acc.hi, acc.lo); }
 
-// TA: use the transpose of A (C (-)= A^T * P B).
+// Threads of the tile-product kernels.  Double-float accumulators take two
+// registers each, so that type uses 128 threads with 8 x 4 accumulators per
+// thread (half the registers, twice the warps) instead of 64 threads with 8 x 8.
+template <typename T> struct MMThreads { static constexpr int value = GEMM_THREADS; };
+template <> struct MMThreads<dfl> { static constexpr int value = 128; };
+
+// TA: use the transpose of A (C (-)= A^T * P B).  Thread (tx, ty) owns rows
+// {4ty + i, 32 + 4ty + i} (i < 4) and columns {4tx + j, 32 + 4tx + j} (64
+// threads) or {4tx + j} (128 threads), j < 4.
 template <typename T, bool SUB, bool TA = false>
 __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const int* perm, T* As, T* Bs) {
+  constexpr int NT = MMThreads<T>::value;
+  constexpr int CW = NT == 128 ? 4 : 8;  // columns per thread
   const int t = threadIdx.x;
   // stage: As[r][k] = A[r][k] (A[k][r] when TA; stride SPA), Bs[r][c] = B[perm ? perm[r] : r][c] (stride SP)
-  for (int idx = t; idx < TS2 / 4; idx += GEMM_THREADS) {
+  for (int idx = t; idx < TS2 / 4; idx += NT) {
     const int r = idx / (TS / 4), c4 = (idx % (TS / 4)) * 4;
     T a[4], b[4];
     ld4(A + r * TS + c4, a);
@@ -383,33 +394,33 @@ __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const in
     }
   }
   __syncthreads();
-  const int tx = t % 8, ty = t / 8;
-  T acc[8][8];
+  const int tx = t % (NT / 8), ty = t / (NT / 8);
+  T acc[8][CW];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < 8; ++j) acc[i][j] = T(0);
+    for (int j = 0; j < CW; ++j) acc[i][j] = T(0);
 #pragma unroll 2
   for (int k = 0; k < TS; ++k) {
-    T a[8], b[8];
+    T a[8], b[CW];
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
       a[i] = As[(4 * ty + i) * SPA + k];
       a[4 + i] = As[(32 + 4 * ty + i) * SPA + k];
     }
     ld4(Bs + k * SP + 4 * tx, b);
-    ld4(Bs + k * SP + 32 + 4 * tx, b + 4);
+    if (CW == 8) ld4(Bs + k * SP + 32 + 4 * tx, b + 4);
 #pragma unroll
     for (int i = 0; i < 8; ++i)
 #pragma unroll
-      for (int j = 0; j < 8; ++j) mac(acc[i][j], a[i], b[j]);
+      for (int j = 0; j < CW; ++j) mac(acc[i][j], a[i], b[j]);
   }
   __syncthreads();  // C may alias A or B, which are no longer read
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     const int row = (i < 4 ? 4 * ty + i : 32 + 4 * ty + (i - 4));
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
+    for (int h = 0; h < CW / 4; ++h) {
       T* cp = C + row * TS + 32 * h + 4 * tx;
 #pragma unroll
       for (int j = 0; j < 4; ++j) {

@@ -85,11 +85,14 @@ struct LaunchDims {
   int max_rhs_tiles = 0;   // max nt * nrt
   int max_nlmso = 0;
   int max_atom_rows = 0;   // natome * max nlmsa
-  int npr = 0;
+  int npr = 0;             // max interstitial points over the batch's sites
+  int max_nsortf = 0;      // max outer-boundary points inside the sphere over the sites
+  int max_natome = 0;      // max atoms over the sites
+  int max_nlmsa = 0;       // max harmonics of one atom over the batch
   int64_t rowv_total = 0;  // entries of the per-row vectors (sum of npad + 1)
 };
 
-void launch_assemble(const StaticDev& S, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
+void launch_assemble(const StaticDev* sites, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
                      cudaStream_t s);
 void launch_equilibrate_convert(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s);
 void launch_csr(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s);

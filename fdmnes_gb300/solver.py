@@ -73,6 +73,8 @@ def load_library(path: str = LIB_PATH):
     L.fdmgpu_batch_stats.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double),
                                      C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.fdmgpu_batch_vjp.argtypes = [vp, vp, vp, C.POINTER(C.c_double)]
+    L.fdmgpu_batch_add_site.argtypes = [vp, vp, vp, C.c_int32]
+    L.fdmgpu_batch_add_site.restype = C.c_int
     L.fdmgpu_update_grid_values.argtypes = [vp, vp]
     L.fdmgpu_update_grid_values.restype = C.c_int
     L.fdmgpu_batch_adjoint_dot.argtypes = [vp, vp, C.c_int32, vp]
@@ -155,9 +157,18 @@ class FdmSolver:
     def spectrum_add(self, ei: CL.EnergyInputs, ri: CL.RowIndex, iaabs: int = 1):
         self.spectrum_add_args(abi.EnergyArgs(self.st, ei, ri), iaabs)
 
-    def spectrum_add_args(self, ea: abi.EnergyArgs, iaabs: int = 1):
-        _check(self.lib.fdmgpu_batch_add(self.h, C.addressof(ea.s), iaabs))
+    def spectrum_add_args(self, ea: abi.EnergyArgs, iaabs: int = 1, site: "FdmSolver" = None):
+        """Add one energy; with site, an energy of another absorbing site (its own
+        FdmSolver and grid) joins this batch."""
+        if site is None or site is self:
+            _check(self.lib.fdmgpu_batch_add(self.h, C.addressof(ea.s), iaabs))
+        else:
+            _check(self.lib.fdmgpu_batch_add_site(self.h, site.h, C.addressof(ea.s), iaabs))
+            self._sites = getattr(self, "_sites", []) + [site]
         self._batch_args.append(ea)
+
+    def spectrum_add_site(self, site: "FdmSolver", ei: CL.EnergyInputs, ri: CL.RowIndex, iaabs: int = 1):
+        self.spectrum_add_args(abi.EnergyArgs(site.st, ei, ri), iaabs, site)
 
     def spectrum_run(self) -> dict:
         """Run the batch.  Energies whose refinement missed its tolerance are

@@ -228,6 +228,13 @@ void fdmgpu_get_solver_params(int32_t* mpi_host_num_for_mumps, char solver[6]);
  */
 fdmgpu_status fdmgpu_batch_begin(fdmgpu_handle* h, int32_t precision, int32_t max_energies);
 fdmgpu_status fdmgpu_batch_add(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t iaabs);
+/* Add an energy of another absorbing site: e refers to the grid of the handle
+ * `site` (its own fdmgpu_create), and the problem joins h's batch, so the
+ * energies of several sites with different grids and orders run in one
+ * launch sequence.  fdmgpu_batch_add(h, e, iaabs) is the case site = h.  The
+ * site handle must outlive the batch's runs.  vjp and adjoint_dot need a
+ * single-site batch. */
+fdmgpu_status fdmgpu_batch_add_site(fdmgpu_handle* h, fdmgpu_handle* site, const fdmgpu_energy* e, int32_t iaabs);
 fdmgpu_status fdmgpu_batch_run(fdmgpu_handle* h, fdmgpu_info* info);
 /* Run the last batch again on the inputs already in device memory (no host
  * copies): the device-resident timing of a spectrum.  No counterpart in the

@@ -171,3 +171,38 @@ def test_rutile_spin_polarised_uneven_batch(solver_mod, oracle_lib):
         for k, (t, r) in enumerate(zip(T, refs)):
             assert rel(t, r) < tol, (prec, k, rel(t, r))
     sv.close()
+
+
+def test_two_sites_in_one_batch(solver_mod, oracle_lib):
+    """Energies of two absorbing sites with different grids (the small Cu
+    cluster and the spin-polarised rutile cluster) in one batch, FP64 and
+    mixed: each energy's Taull equals that of its own single-site batch
+    (same kernels, same arithmetic: 1e-13) and the oracle's (1e-8, the
+    rutile conditioning)."""
+    from fdmnes_gb300 import abi, cluster as CL
+    st_a = CL.small_cu_structure()
+    st_b = CL.build_structure(CL.rutile_cluster(2.0), 0.3, 2.4, 30.0, nspin=2, spin_split_ev=1.5)
+    sa, sb = solver_mod.FdmSolver(st_a), solver_mod.FdmSolver(st_b)
+    items = []  # (site, ei, ri)
+    for E in (3.0, 20.0):
+        ei = CL.energy_inputs(st_a, E)
+        items.append((sa, ei, CL.newind(st_a, ei.nlmsa, ei.nlmso)))
+        for isp in (1, 2):
+            ei = CL.energy_inputs(st_b, E, ispin=isp)
+            items.append((sb, ei, CL.newind(st_b, ei.nlmsa, ei.nlmso)))
+    for prec in ("fp64", "mixed"):
+        sa.spectrum_begin(prec, len(items))
+        for site, ei, ri in items:
+            sa.spectrum_add_site(site, ei, ri)
+        sa.spectrum_run()
+        mixed_T = [sa.taull(k) for k in range(len(items))]
+        for k, (site, ei, ri) in enumerate(items):
+            T1, _ = site.spectrum([(ei, ri)], prec)
+            assert rel(mixed_T[k], T1[0]) < 1e-13, (prec, k, rel(mixed_T[k], T1[0]))
+            if prec == "fp64" and k < 3:
+                ga = abi.GridArgs(site.st)
+                ea = abi.EnergyArgs(site.st, ei, ri)
+                Xo, _ = oracle_lib.mat_solve(ga, ea)
+                assert rel(mixed_T[k], oracle_lib.taull(ga, ea, Xo)) < 1e-8
+    sa.close()
+    sb.close()
