@@ -835,11 +835,35 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
     if (nfail > 0) {
       CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
       if (h->escalate_dfl) {
-        // double-float factorisation of the equilibrated matrix + 2 refinement steps
-        CK(cudaMemsetAsync(h->pl.dmax, 0, 3 * np * sizeof(unsigned long long), h->stream));
-        nkern += launch_dfl_escalation(h->sp, h->d_probs.p, h->pl, h->tb, h->dims, reinterpret_cast<dfl*>(h->pl.V),
-                                       2, h->stream, h->ev[8], h->ev[9]);
+        // double-float factorisation of the equilibrated matrix, then
+        // double-float refinement steps.  The double-float factors contract
+        // the error by orders of magnitude per step, so the solution after a
+        // step whose correction is within tol_accept is far more accurate than
+        // that correction: stop there (one step is the rule, three at most).
+        dfl* D = reinterpret_cast<dfl*>(h->pl.V);
+        nkern += launch_dfl_escalation(h->sp, h->d_probs.p, h->pl, h->tb, h->dims, D, h->stream, h->ev[8], h->ev[9]);
         esc_timed = true;
+        std::vector<int> act2 = active;
+        std::vector<unsigned long long> red2(3 * np);
+        for (int step = 0; step < 3; ++step) {
+          CK(cudaMemsetAsync(h->pl.dmax, 0, 3 * np * sizeof(unsigned long long), h->stream));
+          nkern += launch_dfl_refine_step(h->sp, h->d_probs.p, h->pl, h->tb, h->dims, D, h->stream);
+          CK(cudaMemcpyAsync(red2.data(), h->d_red.p, 3 * np * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                             h->stream));
+          CK(cudaStreamSynchronize(h->stream));
+          int more = 0;
+          for (int k = 0; k < np; ++k)
+            if (act2[k]) {
+              double dm, xm;
+              memcpy(&dm, &red2[k], 8);
+              memcpy(&xm, &red2[np + k], 8);
+              b.resid[k] = xm > 0 ? dm / xm : dm;
+              act2[k] = !(b.resid[k] <= tol_accept);
+              more += act2[k];
+            }
+          if (!more) break;
+          CK(cudaMemcpyAsync(h->d_active.p, act2.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+        }
       } else {
         launch_copy_rhs(h->d_probs.p, h->pl, h->dims, h->stream);
         nkern += 1;
@@ -849,22 +873,14 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
                                          h->d_active.p, h->stream);
       }
       CK(cudaGetLastError());
-      if (h->escalate_dfl) {
-        std::vector<unsigned long long> red2(3 * np);
-        CK(cudaMemcpyAsync(red2.data(), h->d_red.p, 3 * np * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
-                           h->stream));
-        CK(cudaStreamSynchronize(h->stream));
-        for (int k = 0; k < np; ++k)
-          if (active[k]) {
-            double dm, xm;
-            memcpy(&dm, &red2[k], 8);
-            memcpy(&xm, &red2[np + k], 8);
-            b.resid[k] = xm > 0 ? dm / xm : dm;
-          }
+      for (int k = 0; k < np; ++k) {
+        b.fallback[k] = active[k];
+        if (active[k] && !h->escalate_dfl) b.resid[k] = 0.0;  // direct FP64 solve, no correction measured
       }
-      for (int k = 0; k < np; ++k) b.fallback[k] = active[k];
     }
     CK(cudaEventRecord(h->ev[5], h->stream));
+    for (int k = 0; k < np; ++k)
+      if (!(b.resid[k] <= tol_accept)) b.err[k] = FDMGPU_ERR_NOT_CONVERGED;
   }
   if (b.probs[0].P.nlm_abs > 0) {
     launch_taull(h->d_probs.p, h->pl, h->dims, h->pl.X64, h->stream);

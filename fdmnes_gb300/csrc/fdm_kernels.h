@@ -107,7 +107,9 @@ size_t gmres_state_bytes();
 int gmres_max_dim();
 void launch_copy_rhs(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s);
 int launch_dfl_escalation(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
-                           dfl* D, int iters, cudaStream_t s, cudaEvent_t ev_f0 = nullptr, cudaEvent_t ev_f1 = nullptr);
+                           dfl* D, cudaStream_t s, cudaEvent_t ev_f0 = nullptr, cudaEvent_t ev_f1 = nullptr);
+int launch_dfl_refine_step(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
+                           dfl* D, cudaStream_t s);
 void launch_resid_update(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s);
 void launch_copy_rhs32(const Prob* probs, const LaunchDims& d, const float* src, float* dst, const int* mask,
                        cudaStream_t s);

@@ -551,7 +551,7 @@ void launch_csr_nnz(const Prob* probs, const int* rowptr, const LaunchDims& d, i
 }
 
 int launch_dfl_escalation(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
-                          dfl* D, int iters, cudaStream_t s, cudaEvent_t ev_f0, cudaEvent_t ev_f1) {
+                          dfl* D, cudaStream_t s, cudaEvent_t ev_f0, cudaEvent_t ev_f1) {
   const int np = d.nprob;
   dfl* envd = reinterpret_cast<dfl*>(pl.env64);
   int nk = 0;
@@ -563,18 +563,23 @@ int launch_dfl_escalation(const StepPlan& sp, const Prob* probs, const Pools& pl
   if (ev_f1) cudaEventRecord(ev_f1, s);
   nk += launch_backward<dfl>(sp, envd, D, probs, tb, np, pl.active, s);
   k_dfl_to_x<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, D, pl.X64, pl.Xs, pl.cs, 1, pl.dmax, pl.xmax, pl.active);
-  ++nk;
-  for (int it = 0; it < iters; ++it) {
-    launch_residual(probs, pl, d, 1, s);
-    k_rhs_to_dfl<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, pl.B64, pl.Y32, pl.rs, D, 0, pl.active);
-    nk += 2;
-    nk += launch_forward<dfl>(sp, envd, D, probs, tb, np, pl.active, pl.piv, s);
-    nk += launch_backward<dfl>(sp, envd, D, probs, tb, np, pl.active, s);
-    k_dfl_to_x<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, D, pl.X64, pl.Xs, pl.cs, 0, pl.dmax, pl.xmax,
-                                                          pl.active);
-    ++nk;
-  }
-  return nk;
+  return nk + 1;
+}
+
+// One refinement step with the double-float factors: residual, solve, x += d;
+// dmax / xmax receive max|d| and max|x| of each active problem.
+int launch_dfl_refine_step(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
+                           dfl* D, cudaStream_t s) {
+  const int np = d.nprob;
+  dfl* envd = reinterpret_cast<dfl*>(pl.env64);
+  int nk = 0;
+  launch_residual(probs, pl, d, 1, s);
+  k_rhs_to_dfl<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, pl.B64, pl.Y32, pl.rs, D, 0, pl.active);
+  nk += 2;
+  nk += launch_forward<dfl>(sp, envd, D, probs, tb, np, pl.active, pl.piv, s);
+  nk += launch_backward<dfl>(sp, envd, D, probs, tb, np, pl.active, s);
+  k_dfl_to_x<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, D, pl.X64, pl.Xs, pl.cs, 0, pl.dmax, pl.xmax, pl.active);
+  return nk + 1;
 }
 
 void launch_copy_rhs(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s) {

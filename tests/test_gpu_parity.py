@@ -206,3 +206,21 @@ def test_two_sites_in_one_batch(solver_mod, oracle_lib):
                 assert rel(mixed_T[k], oracle_lib.taull(ga, ea, Xo)) < 1e-8
     sa.close()
     sb.close()
+
+
+def test_unreachable_tolerance_is_reported(solver_mod, golden):
+    """A refinement tolerance below what double-float arithmetic can reach
+    (1e-17) is reported per energy as not converged, after escalation, and the
+    solution is still the escalated one (1e-8 of the oracle)."""
+    from fdmnes_gb300 import abi
+    grid, energies = golden
+    sv = solver_mod.FdmSolver(grid)
+    sv.set_tolerance(1e-17, 1e-17)
+    X, info = sv.mat_solve_args(abi.EnergyArgs(energies[0]), "mixed")
+    assert not info["converged"]
+    assert info["n_fallback"] == 1
+    assert rel(X, energies[0]["smr"]) < 1e-8
+    sv.set_tolerance(0.0, 0.0)
+    X, info = sv.mat_solve_args(abi.EnergyArgs(energies[0]), "mixed")
+    assert info["converged"]
+    sv.close()
