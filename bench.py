@@ -330,7 +330,8 @@ def run_gpu(args):
                    "energies": n_all, "energies_per_gpu": n_e, "e_step_ev": step / world, "nligne": [min(r.nligne for _, r in items), max(r.nligne for _, r in items)],
                    "nrhs": [min(e.nlmso for e, _ in items), max(e.nlmso for e, _ in items)],
                    "l2": "working set ~100 GB per step, far above the 126 MB L2 (no flush needed)",
-                   "refine_tol": TOL, "refine_tol_accept": TOL_ACCEPT},
+                   "refine_tol": TOL, "refine_tol_accept": TOL_ACCEPT,
+                   "autotune": {"mixed": sv.tuning("mixed"), "fp64": sv.tuning("fp64")}},
         "roofline": roof_main,
         "roofline_other": [roof_res, roof_fac],
         "cpu_baseline": cb and {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},

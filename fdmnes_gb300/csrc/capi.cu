@@ -94,6 +94,14 @@ struct Batch {
 struct fdmgpu_handle {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t stream2 = nullptr;  // escalation overlapped with the refinement of the other problems
+  int overlap_escalation = 0;  // measured slower on the 401-energy Cu spectrum: off by default
+  cudaEvent_t ev_join = nullptr;
+  cudaEvent_t ev_esc[2 * 16] = {};  // factor start / end of up to 16 overlapped escalation batches
+  DevBuf<int> d_esc_mask;
+  int* h_esc_mask = nullptr;  // pinned, 16 slots of nprob ints
+  size_t h_esc_mask_cap = 0;
+  DevBuf<unsigned long long> d_red_esc, d_red_tmp;
   // static structure
   fdmgpu_grid g{};
   StaticDev S{};
@@ -126,6 +134,9 @@ struct fdmgpu_handle {
   int refine_recur = 0;   // classical refinement with the residual updated by recurrence (1)
   int escalate_dfl = 1;   // escalation by a double-float (1) or an FP64 (0) factorisation
   int gmres_m = 12;       // Krylov dimension of one GMRES cycle
+  int autotune = 1;         // time the trailing-update layouts on each new plan
+  int trail_threads[2] = {0, 0};        // chosen layout per precision (FP64, FP32); 0: built-in default
+  double trail_ms[2][2] = {{0, 0}, {0, 0}};  // trial device ms [precision][64 | 128 threads]
   double tol = 0.0;         // refinement stop: max|dx|/max|x| (0: the default of the residual mode)
   double tol_accept = 0.0;  // accepted without escalation when refinement stalls (0: default)
   int64_t ncols = 0;      // right-hand-side columns of the batch (sum of nrt * TS)
@@ -566,14 +577,45 @@ void record_asm(fdmgpu_handle* h) {
   }
 }
 
-void record_factor(fdmgpu_handle* h) {
+void record_factor_window(fdmgpu_handle* h, int threads, int k_begin, int k_end) {
   cudaStream_t s = h->stream;
   const Pools& pl = h->pl;
   const int np = h->dims.nprob;
   if (h->batch.precision == FDMGPU_PREC_FP64)
-    launch_factor<double>(h->sp, pl.env64, pl.X64, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-10, nullptr, s);
+    launch_factor<double>(h->sp, pl.env64, pl.X64, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-10, nullptr, s,
+                          threads, k_begin, k_end);
   else
-    launch_factor<float>(h->sp, pl.env32, pl.Y32, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-30, pl.piv, s);
+    launch_factor<float>(h->sp, pl.env32, pl.Y32, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-30, pl.piv, s,
+                         threads, k_begin, k_end);
+}
+
+void record_factor(fdmgpu_handle* h) {
+  record_factor_window(h, h->trail_threads[h->batch.precision == FDMGPU_PREC_FP64 ? 0 : 1], 0, -1);
+}
+
+void record_asm(fdmgpu_handle* h);
+
+// Autotuner: on a new plan, time the trailing update of the factor with 64
+// threads per tile pair (8x8 accumulators each) and with 128 (8x4) on eight
+// factorisation steps from the middle of the band of this batch, and keep the
+// faster.  The trial overwrites the band, which the run assembles again.
+fdmgpu_status tune_trailing(fdmgpu_handle* h) {
+  const int pi = h->batch.precision == FDMGPU_PREC_FP64 ? 0 : 1;
+  const int k0 = h->sp.ntmax / 3, k1 = std::min(h->sp.ntmax, k0 + 8);
+  const int variants[2] = {64, 128};
+  for (int v = 0; v < 2; ++v) {
+    record_asm(h);
+    CK(cudaEventRecord(h->ev[0], h->stream));
+    record_factor_window(h, variants[v], k0, k1);
+    CK(cudaEventRecord(h->ev[1], h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, h->ev[0], h->ev[1]));
+    h->trail_ms[pi][v] = t;
+  }
+  CK(cudaGetLastError());
+  h->trail_threads[pi] = h->trail_ms[pi][1] < h->trail_ms[pi][0] ? 128 : 64;
+  return FDMGPU_OK;
 }
 
 void record_solve(fdmgpu_handle* h) {
@@ -686,6 +728,10 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
                         h->d_nb_coef.p, h->d_rvol.p, h->d_poidsa.p, h->d_poidso.p, h->d_Kar.p, h->d_YsoT.p,
                         h->d_Ylmato.p, h->d_R32.p, h->d_act_df.p, h->d_act_rec.p, h->d_sites.p};
   for (const void* q : ptrs) ps = mix(ps, (uint64_t)(uintptr_t)q);
+  if (replan && h->autotune) {
+    st = tune_trailing(h);
+    if (st) return st;
+  }
   if (replan || ps != h->ptr_sig) {
     h->ptr_sig = ps;
     st = capture(h, record_asm, &h->g_asm, &h->nk_asm);
@@ -718,6 +764,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   b.err.assign(np, 0);
   float ms_refine = 0;
   bool esc_timed = false;
+  double esc_ms_overlap = -1.0, esc_flops_overlap = 0.0;
   if (b.precision == FDMGPU_PREC_MIXED) {
     // Per problem: classical refinement x += LU^-1 r while it contracts (a step
     // counts as slow when the correction does not halve); after two slow steps
@@ -741,6 +788,63 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
     }
     std::vector<unsigned long long> red(3 * np);
     std::vector<int> jd(np, 0);
+    // Overlapped escalation: a problem whose refinement stalls above
+    // tol_accept is factorised again in double-float arithmetic on stream2
+    // at once, while the others keep refining on the main stream.  Each such
+    // batch has its own mask; its refinement maxima go to d_red_esc (zeroed
+    // once per run: every problem escalates at most once), the initial
+    // solve's to d_red_tmp.
+    const bool overlap = h->overlap_escalation && h->escalate_dfl && !h->refine_gmres && !h->refine_recur;
+    std::vector<int> escalated(np, 0);
+    int n_esc_batches = 0;
+    double esc_flops_timed = 0.0;
+    auto escalate_now = [&](const std::vector<int>& which) -> fdmgpu_status {
+      // one pinned + device mask slot per batch, so that the upload does not
+      // wait for the previous batch; from the 16th batch on, slot 15 is
+      // reused after stream2 has drained
+      const int slot = std::min(n_esc_batches, 15);
+      if (n_esc_batches >= 15) CK(cudaStreamSynchronize(h->stream2));
+      int* hmask = h->h_esc_mask + (size_t)np * slot;
+      int* mask = h->d_esc_mask.p + (size_t)np * slot;
+      std::copy(which.begin(), which.end(), hmask);
+      CK(cudaEventRecord(h->ev_join, h->stream));
+      CK(cudaStreamWaitEvent(h->stream2, h->ev_join, 0));
+      CK(cudaMemcpyAsync(mask, hmask, np * sizeof(int), cudaMemcpyHostToDevice, h->stream2));
+      Pools pe = h->pl;
+      pe.active = mask;
+      pe.dmax = h->d_red_tmp.p;
+      pe.xmax = h->d_red_tmp.p + np;
+      pe.amax = h->d_red_tmp.p + 2 * np;
+      dfl* D = reinterpret_cast<dfl*>(h->pl.V);
+      const bool timed = n_esc_batches < 16;
+      nkern += launch_dfl_escalation(h->sp, h->d_probs.p, pe, h->tb, h->dims, D, h->stream2,
+                                     timed ? h->ev_esc[2 * n_esc_batches] : nullptr,
+                                     timed ? h->ev_esc[2 * n_esc_batches + 1] : nullptr);
+      pe.dmax = h->d_red_esc.p;
+      pe.xmax = h->d_red_esc.p + np;
+      pe.amax = h->d_red_esc.p + 2 * np;
+      nkern += launch_dfl_refine_step(h->sp, h->d_probs.p, pe, h->tb, h->dims, D, h->stream2);
+      for (int k = 0; k < np; ++k)
+        if (which[k]) {
+          escalated[k] = 1;
+          if (timed) esc_flops_timed += b.probs[k].flops_factor;
+        }
+      ++n_esc_batches;
+      return FDMGPU_OK;
+    };
+    if (overlap) {
+      if (h->d_red_esc.reserve(3 * (size_t)np) != cudaSuccess || h->d_red_tmp.reserve(3 * (size_t)np) != cudaSuccess ||
+          h->d_esc_mask.reserve(16 * (size_t)np) != cudaSuccess)
+        return fail(FDMGPU_ERR_NOMEM, "escalation buffers");
+      if (h->h_esc_mask_cap < 16 * (size_t)np) {
+        CK(cudaStreamSynchronize(h->stream2));
+        if (h->h_esc_mask) cudaFreeHost(h->h_esc_mask);
+        h->h_esc_mask = nullptr;
+        CK(cudaMallocHost(&h->h_esc_mask, 16 * (size_t)np * sizeof(int)));
+        h->h_esc_mask_cap = 16 * (size_t)np;
+      }
+      CK(cudaMemsetAsync(h->d_red_esc.p, 0, 3 * np * sizeof(unsigned long long), h->stream));
+    }
     CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
     if (h->refine_gmres)
       CK(cudaMemsetAsync(h->d_active_gm.p, 0, np * sizeof(int), h->stream));
@@ -807,6 +911,19 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
         }
         prev[k] = r;
       }
+      if (overlap) {
+        std::vector<int> which(np, 0);
+        int nw = 0;
+        for (int k = 0; k < np; ++k)
+          if (!active[k] && !escalated[k] && b.iters[k] == it && !(b.resid[k] <= tol_accept)) {
+            which[k] = 1;
+            ++nw;
+          }
+        if (nw) {
+          st = escalate_now(which);
+          if (st) return st;
+        }
+      }
       if (nact == 0) break;
       CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
       if (h->refine_recur) {
@@ -826,11 +943,75 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
       }
     }
     // Precision escalation: problems whose refinement missed tol_accept are
-    // factorised again in FP64 (their FP64 band is still intact) and solved.
+    // factorised again in double-float (or FP64) arithmetic and solved.
     int nfail = 0;
     for (int k = 0; k < np; ++k) {
       active[k] = !(b.resid[k] <= tol_accept);
       nfail += active[k];
+    }
+    if (overlap) {
+      std::vector<int> which(np, 0);
+      int nw = 0;
+      for (int k = 0; k < np; ++k)
+        if (active[k] && !escalated[k]) {
+          which[k] = 1;
+          ++nw;
+        }
+      if (nw) {
+        st = escalate_now(which);
+        if (st) return st;
+      }
+      if (n_esc_batches > 0) {
+        CK(cudaEventRecord(h->ev_join, h->stream2));
+        CK(cudaStreamWaitEvent(h->stream, h->ev_join, 0));
+        std::vector<unsigned long long> red2(3 * np);
+        CK(cudaMemcpyAsync(red2.data(), h->d_red_esc.p, 3 * np * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                           h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        std::vector<int> act2(np, 0);
+        int more = 0;
+        for (int k = 0; k < np; ++k)
+          if (escalated[k]) {
+            double dm, xm;
+            memcpy(&dm, &red2[k], 8);
+            memcpy(&xm, &red2[np + k], 8);
+            b.resid[k] = xm > 0 ? dm / xm : dm;
+            act2[k] = !(b.resid[k] <= tol_accept);
+            more += act2[k];
+          }
+        // rare: further double-float steps on the main stream
+        dfl* D = reinterpret_cast<dfl*>(h->pl.V);
+        for (int step = 1; step < 3 && more; ++step) {
+          CK(cudaMemcpyAsync(h->d_active.p, act2.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+          CK(cudaMemsetAsync(h->pl.dmax, 0, 3 * np * sizeof(unsigned long long), h->stream));
+          nkern += launch_dfl_refine_step(h->sp, h->d_probs.p, h->pl, h->tb, h->dims, D, h->stream);
+          CK(cudaMemcpyAsync(red2.data(), h->d_red.p, 3 * np * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                             h->stream));
+          CK(cudaStreamSynchronize(h->stream));
+          more = 0;
+          for (int k = 0; k < np; ++k)
+            if (act2[k]) {
+              double dm, xm;
+              memcpy(&dm, &red2[k], 8);
+              memcpy(&xm, &red2[np + k], 8);
+              b.resid[k] = xm > 0 ? dm / xm : dm;
+              act2[k] = !(b.resid[k] <= tol_accept);
+              more += act2[k];
+            }
+        }
+        for (int k = 0; k < np; ++k) b.fallback[k] = escalated[k];
+        // the escalation factor time of the timed batches (they overlap the refinement)
+        float tsum = 0;
+        for (int i = 0; i < std::min(n_esc_batches, 16); ++i) {
+          float t = 0;
+          CK(cudaEventElapsedTime(&t, h->ev_esc[2 * i], h->ev_esc[2 * i + 1]));
+          tsum += t;
+        }
+        esc_ms_overlap = tsum;
+        esc_flops_overlap = esc_flops_timed;
+        esc_timed = true;
+      }
+      nfail = 0;  // handled above
     }
     if (nfail > 0) {
       CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
@@ -921,7 +1102,10 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
       CK(cudaMemcpyAsync(nnz.data(), h->d_nnz.p, np * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
       CK(cudaStreamSynchronize(h->stream));
       for (int k = 0; k < np; ++k) info->flops_residual += 2.0 * nnz[k] * b.probs[k].P.nlmso;
-      if (esc_timed) {
+      if (esc_timed && esc_ms_overlap >= 0) {
+        info->ms_escalate_factor = esc_ms_overlap;
+        info->flops_escalate_factor = esc_flops_overlap;
+      } else if (esc_timed) {
         CK(cudaEventElapsedTime(&t, h->ev[8], h->ev[9]));
         info->ms_escalate_factor = t;
         for (int k = 0; k < np; ++k)
@@ -975,6 +1159,9 @@ fdmgpu_status fdmgpu_create(const fdmgpu_grid* g, fdmgpu_handle** out) {
   h->g = *g;
   CK(cudaGetDevice(&h->device));
   CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&h->stream2, cudaStreamNonBlocking));
+  CK(cudaEventCreateWithFlags(&h->ev_join, cudaEventDisableTiming));
+  for (auto& e : h->ev_esc) CK(cudaEventCreate(&e));
   for (auto& e : h->ev) CK(cudaEventCreate(&e));
   // derived neighbour descriptors of the interstitial points
   const int nv = g->nvois;
@@ -1158,6 +1345,14 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   for (auto& e : h->ev)
     if (e) cudaEventDestroy(e);
   if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->stream2) cudaStreamDestroy(h->stream2);
+  if (h->ev_join) cudaEventDestroy(h->ev_join);
+  for (auto& e : h->ev_esc)
+    if (e) cudaEventDestroy(e);
+  h->d_esc_mask.release();
+  if (h->h_esc_mask) cudaFreeHost(h->h_esc_mask);
+  h->d_red_esc.release();
+  h->d_red_tmp.release();
   delete h;
 }
 
@@ -1187,10 +1382,30 @@ fdmgpu_status fdmgpu_set_tolerance(fdmgpu_handle* h, double tol, double tol_acce
   return FDMGPU_OK;
 }
 
+fdmgpu_status fdmgpu_set_autotune(fdmgpu_handle* h, int32_t on) {
+  if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
+  h->autotune = on != 0;
+  if (!h->autotune) h->trail_threads[0] = h->trail_threads[1] = 0;
+  h->plan_sig = 0;
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_get_tuning(fdmgpu_handle* h, int32_t precision, int32_t* trailing_threads, double* ms64,
+                                double* ms128) {
+  if (!h || (precision != FDMGPU_PREC_FP64 && precision != FDMGPU_PREC_MIXED))
+    return fail(FDMGPU_ERR_ARG, "null handle or unknown precision");
+  const int pi = precision == FDMGPU_PREC_FP64 ? 0 : 1;
+  if (trailing_threads) *trailing_threads = h->trail_threads[pi];
+  if (ms64) *ms64 = h->trail_ms[pi][0];
+  if (ms128) *ms128 = h->trail_ms[pi][1];
+  return FDMGPU_OK;
+}
+
 fdmgpu_status fdmgpu_set_escalation(fdmgpu_handle* h, int32_t mode) {
-  if (!h || (mode != FDMGPU_ESCALATE_FP64 && mode != FDMGPU_ESCALATE_DF64))
+  if (!h || (mode != FDMGPU_ESCALATE_FP64 && mode != FDMGPU_ESCALATE_DF64 && mode != FDMGPU_ESCALATE_DF64_OVERLAP))
     return fail(FDMGPU_ERR_ARG, "unknown escalation mode");
-  h->escalate_dfl = mode == FDMGPU_ESCALATE_DF64;
+  h->escalate_dfl = mode != FDMGPU_ESCALATE_FP64;
+  h->overlap_escalation = mode == FDMGPU_ESCALATE_DF64_OVERLAP;
   return FDMGPU_OK;
 }
 

@@ -11,6 +11,8 @@
 //   k_trailing  A(I,J) -= L(I,K) U(K,J) and Y(I,R) -= L(I,K) Y(K,R).
 // The backward substitution (the reference's resolution loop, :348-358) is
 // k_bwd_diag + k_bwd_update; k_fwd_* are used by the refinement solves.
+#include <algorithm>
+
 #include "fdm_internal.cuh"
 #include "fdm_kernels.h"
 
@@ -78,8 +80,10 @@ __global__ void __launch_bounds__(GEMM_THREADS) k_panel(T* env, T* rhs, const Pr
   }
 }
 
-template <typename T>
-__global__ void __launch_bounds__(MMThreads<T>::value) k_trailing(T* env, T* rhs, const Prob* probs, Tables tb, int K,
+// NT: threads per tile pair (64: 8x8 accumulators per thread; 128: 8x4),
+// chosen per batch plan by the autotuner in the host code.
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT) k_trailing(T* env, T* rhs, const Prob* probs, Tables tb, int K,
                                                        int fuse_rhs, const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -104,7 +108,7 @@ __global__ void __launch_bounds__(MMThreads<T>::value) k_trailing(T* env, T* rhs
     B = rhs_ptr(rhs, P, K, c - nJ);
     C = rhs_ptr(rhs, P, I, c - nJ);
   }
-  tile_mm64<T, true>(C, A, B, (const int*)nullptr, As, Bs);
+  tile_mm64<T, true, false, NT>(C, A, B, (const int*)nullptr, As, Bs);
 }
 
 // Forward substitution, unit lower L: Y(K,R) <- L(K,K)^-1 P Y(K,R).
@@ -256,7 +260,8 @@ void setup_factor_kernels() {
   const int bytes = (int)smem_bytes<T>();
   cudaFuncSetAttribute(k_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes_panel<T>());
-  cudaFuncSetAttribute(k_trailing<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_trailing<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_trailing<T, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_fwd_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_fwd_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_bwd_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -269,10 +274,13 @@ void setup_factor_kernels() {
 
 template <typename T>
 int launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
-                  const int* active, int* err, double piv_thr, int* piv, cudaStream_t s) {
+                  const int* active, int* err, double piv_thr, int* piv, cudaStream_t s, int trail_threads,
+                  int k_begin, int k_end) {
+  if (trail_threads != 64 && trail_threads != 128) trail_threads = MMThreads<T>::value;
   const size_t sm = smem_bytes<T>();
   int nk = 0;
-  for (int K = 0; K < sp.ntmax; ++K) {
+  if (k_end < 0 || k_end > sp.ntmax) k_end = sp.ntmax;
+  for (int K = std::max(k_begin, 0); K < k_end; ++K) {
     k_diag<T><<<dim3(1, nprob), NTHREADS, sm, s>>>(env, probs, tb, K, active, err, piv_thr, piv);
     ++nk;
     const int np = fuse_rhs ? sp.panel_rhs[K] : sp.panel[K];
@@ -283,7 +291,10 @@ int launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables 
     }
     const int nt = fuse_rhs ? sp.trail_rhs[K] : sp.trail[K];
     if (nt > 0) {
-      k_trailing<T><<<dim3(nt, nprob), MMThreads<T>::value, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
+      if (trail_threads == 128)
+        k_trailing<T, 128><<<dim3(nt, nprob), 128, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
+      else
+        k_trailing<T, 64><<<dim3(nt, nprob), 64, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
       ++nk;
     }
   }
@@ -356,16 +367,16 @@ template void launch_backward_t<float>(const StepPlan&, const float*, float*, co
 template void setup_factor_kernels<float>();
 template void setup_factor_kernels<dfl>();
 template int launch_factor<dfl>(const StepPlan&, dfl*, dfl*, const Prob*, Tables, int, int, const int*, int*,
-                                 double, int*, cudaStream_t);
+                                 double, int*, cudaStream_t, int, int, int);
 template int launch_forward<dfl>(const StepPlan&, const dfl*, dfl*, const Prob*, Tables, int, const int*,
                                   const int*, cudaStream_t);
 template int launch_backward<dfl>(const StepPlan&, const dfl*, dfl*, const Prob*, Tables, int, const int*,
                                    cudaStream_t);
 template void setup_factor_kernels<double>();
 template int launch_factor<float>(const StepPlan&, float*, float*, const Prob*, Tables, int, int, const int*,
-                                   int*, double, int*, cudaStream_t);
+                                   int*, double, int*, cudaStream_t, int, int, int);
 template int launch_factor<double>(const StepPlan&, double*, double*, const Prob*, Tables, int, int,
-                                    const int*, int*, double, int*, cudaStream_t);
+                                    const int*, int*, double, int*, cudaStream_t, int, int, int);
 template int launch_forward<float>(const StepPlan&, const float*, float*, const Prob*, Tables, int,
                                     const int*, const int*, cudaStream_t);
 template int launch_forward<double>(const StepPlan&, const double*, double*, const Prob*, Tables, int,

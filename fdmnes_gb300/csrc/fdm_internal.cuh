@@ -364,18 +364,20 @@ __device__ __forceinline__ T mac_finish(T acc) { return acc; }
 template <>
 __device__ __forceinline__ dfl mac_finish<dfl>(dfl acc) { return df_fast_two_sum(acc.hi, acc.lo); }
 
-// Threads of the tile-product kernels.  Double-float accumulators take two
-// registers each, so that type uses 128 threads with 8 x 4 accumulators per
-// thread (half the registers, twice the warps) instead of 64 threads with 8 x 8.
+// Threads of the tile-product kernels: 64 threads with 8 x 8 accumulators per
+// thread (FP64), or 128 threads with 8 x 4 (FP32 and double-float: twice the
+// warps per tile for the same registers, which hides the latency of the
+// staging loads and of the dependent double-float operations).
 template <typename T> struct MMThreads { static constexpr int value = GEMM_THREADS; };
 template <> struct MMThreads<dfl> { static constexpr int value = 128; };
+template <> struct MMThreads<float> { static constexpr int value = 128; };
 
 // TA: use the transpose of A (C (-)= A^T * P B).  Thread (tx, ty) owns rows
 // {4ty + i, 32 + 4ty + i} (i < 4) and columns {4tx + j, 32 + 4tx + j} (64
 // threads) or {4tx + j} (128 threads), j < 4.
-template <typename T, bool SUB, bool TA = false>
+template <typename T, bool SUB, bool TA = false, int NT = MMThreads<T>::value>
 __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const int* perm, T* As, T* Bs) {
-  constexpr int NT = MMThreads<T>::value;
+  static_assert(NT == 64 || NT == 128, "tile_mm64 runs on 64 or 128 threads");
   constexpr int CW = NT == 128 ? 4 : 8;  // columns per thread
   const int t = threadIdx.x;
   // stage: As[r][k] = A[r][k] (A[k][r] when TA; stride SPA), Bs[r][c] = B[perm ? perm[r] : r][c] (stride SP)

@@ -21,7 +21,8 @@ struct StepPlan {
 template <typename T> void setup_factor_kernels();
 template <typename T>
 int launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
-                   const int* active, int* err, double piv_thr, int* piv, cudaStream_t s);
+                  const int* active, int* err, double piv_thr, int* piv, cudaStream_t s, int trail_threads = 0,
+                  int k_begin = 0, int k_end = -1);
 template <typename T>
 int launch_forward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, Tables tb, int nprob,
                     const int* active, const int* piv, cudaStream_t s);

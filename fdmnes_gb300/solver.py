@@ -63,6 +63,10 @@ def load_library(path: str = LIB_PATH):
     L.fdmgpu_set_escalation.restype = C.c_int
     L.fdmgpu_set_tolerance.argtypes = [vp, C.c_double, C.c_double]
     L.fdmgpu_set_tolerance.restype = C.c_int
+    L.fdmgpu_set_autotune.argtypes = [vp, C.c_int32]
+    L.fdmgpu_set_autotune.restype = C.c_int
+    L.fdmgpu_get_tuning.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.fdmgpu_get_tuning.restype = C.c_int
     L.fdmgpu_set_residual_mode.restype = C.c_int
     L.fdmgpu_batch_begin.argtypes = [vp, C.c_int32, C.c_int32]
     L.fdmgpu_batch_add.argtypes = [vp, vp, C.c_int32]
@@ -117,12 +121,21 @@ class FdmSolver:
         _check(self.lib.fdmgpu_set_refinement(self.h, {"classic": 0, "gmres": 1, "recurrence": 2}[mode], krylov_dim))
 
     def set_escalation(self, mode: str = "df64"):
-        """Re-solve arithmetic for energies the FP32 factors cannot refine: 'df64' or 'fp64'."""
-        _check(self.lib.fdmgpu_set_escalation(self.h, {"fp64": 0, "df64": 1}[mode]))
+        """Re-solve of energies the FP32 factors cannot refine: 'df64' (default), 'df64_overlap' or 'fp64'."""
+        _check(self.lib.fdmgpu_set_escalation(self.h, {"fp64": 0, "df64": 1, "df64_overlap": 2}[mode]))
 
     def set_tolerance(self, tol: float = 0.0, tol_accept: float = 0.0):
         """Refinement stop (max|dx|/max|x|) and the stalled-but-accepted level; 0 = default."""
         _check(self.lib.fdmgpu_set_tolerance(self.h, tol, tol_accept))
+
+    def set_autotune(self, on: bool = True):
+        _check(self.lib.fdmgpu_set_autotune(self.h, 1 if on else 0))
+
+    def tuning(self, precision: str = "mixed") -> dict:
+        """Trailing-update layout chosen by the autotuner and its two trial times."""
+        t, a, b = C.c_int32(0), C.c_double(0), C.c_double(0)
+        _check(self.lib.fdmgpu_get_tuning(self.h, PREC[precision], C.byref(t), C.byref(a), C.byref(b)))
+        return {"trailing_threads": t.value, "trial_ms_64": a.value, "trial_ms_128": b.value}
 
     def close(self):
         if getattr(self, "h", None):

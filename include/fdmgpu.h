@@ -67,8 +67,11 @@ typedef enum {
 /* Re-solve of an energy whose mixed precision refinement missed its tolerance. */
 typedef enum {
   FDMGPU_ESCALATE_FP64 = 0,    /* FP64 profile LU (no pivoting, as the reference)       */
-  FDMGPU_ESCALATE_DF64 = 1     /* double-float LU of the equilibrated matrix with
-                                  tile-local pivoting + 2 refinement steps (default)   */
+  FDMGPU_ESCALATE_DF64 = 1,    /* double-float LU of the equilibrated matrix with
+                                  tile-local pivoting + refinement, after the FP32
+                                  refinement of every energy has ended (default)        */
+  FDMGPU_ESCALATE_DF64_OVERLAP = 2 /* the same, started on a second stream as soon as an
+                                  energy stalls, while the others keep refining         */
 } fdmgpu_escalation;
 
 /* Energy-independent arguments of mat_solve (source/mat_solve_gaussian.f90:17-67). */
@@ -213,6 +216,16 @@ fdmgpu_status fdmgpu_set_escalation(fdmgpu_handle* h, int32_t mode);
  * residual, 1e-9 with FP64), else solved again by escalation.  0 selects the
  * default.  No counterpart in the reference. */
 fdmgpu_status fdmgpu_set_tolerance(fdmgpu_handle* h, double tol, double tol_accept);
+
+/* Autotuner (on by default): when a batch needs a new plan, the trailing
+ * update of the factor is timed on this batch with 64 threads per 64x64 tile
+ * pair (8x8 accumulators per thread) and with 128 (8x4), over eight steps
+ * from the middle of the band, and the faster layout is used for the plan.
+ * fdmgpu_get_tuning reports the layout chosen for a precision (0 before the
+ * first plan) and the two trial times.  No counterpart in the reference. */
+fdmgpu_status fdmgpu_set_autotune(fdmgpu_handle* h, int32_t on);
+fdmgpu_status fdmgpu_get_tuning(fdmgpu_handle* h, int32_t precision, int32_t* trailing_threads, double* ms64,
+                                double* ms128);
 
 /* Counterpart of getSolverParams (source/mat_solve_gaussian.f90:376-389,
  * source/mat_solve_mumps.f90:705-736): solver name "GPU" and group size 1. */

@@ -224,3 +224,42 @@ def test_unreachable_tolerance_is_reported(solver_mod, golden):
     X, info = sv.mat_solve_args(abi.EnergyArgs(energies[0]), "mixed")
     assert info["converged"]
     sv.close()
+
+
+def test_autotuner_layouts_agree(solver_mod):
+    """The autotuner times the two trailing-update layouts (64 threads with
+    8x8 accumulators, 128 with 8x4) on a new plan and keeps the faster; both
+    sum every element in the same k order, so the spectra are bit-identical."""
+    from fdmnes_gb300 import cluster as CL, xanes
+    st = CL.small_cu_structure()
+    items = xanes.spectrum_inputs(st, [3.0, 20.0, 30.0])
+    sv = solver_mod.FdmSolver(st)
+    for prec in ("fp64", "mixed"):
+        T1, _ = sv.spectrum(items, prec)
+        tun = sv.tuning(prec)
+        assert tun["trailing_threads"] in (64, 128)
+        assert tun["trial_ms_64"] > 0 and tun["trial_ms_128"] > 0
+        sv.set_autotune(False)   # built-in layout
+        T2, _ = sv.spectrum(items, prec)
+        sv.set_autotune(True)
+        assert all(np.array_equal(a, b) for a, b in zip(T1, T2)), prec
+    sv.close()
+
+
+def test_overlapped_escalation_gives_the_same_spectrum(solver_mod):
+    """Escalation on a second stream while the other energies refine gives
+    the same result bits as escalation after the refinement (the same
+    arithmetic per energy).  An acceptance level below the df64 residual's
+    floor (1e-11) sends every energy to escalation."""
+    from fdmnes_gb300 import cluster as CL, xanes
+    st = CL.cu_structure()
+    items = xanes.spectrum_inputs(st, [2.0, 26.0, 30.0, 34.0])
+    sv = solver_mod.FdmSolver(st)
+    sv.set_tolerance(1e-12, 1e-11)
+    out = {}
+    for mode in ("df64", "df64_overlap"):
+        sv.set_escalation(mode)
+        out[mode], info = sv.spectrum(items, "mixed")
+    assert info["n_fallback"] >= 1
+    assert all(np.array_equal(a, b) for a, b in zip(out["df64"], out["df64_overlap"]))
+    sv.close()

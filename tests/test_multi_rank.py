@@ -56,3 +56,43 @@ def test_gather_over_two_gloo_ranks(tmp_path):
     assert r0 == r1
     assert [v[0] for v in r0] == [k * k for k in range(7)]
     assert [v[1] for v in r0] == [k % 2 for k in range(7)]
+
+
+def test_weak_scaling_shards_cover_the_finer_spectrum():
+    """N ranks solve an N times finer spectrum, dealt round-robin: every energy
+    exactly once, the same work per rank (within one energy)."""
+    from fdmnes_gb300 import cluster as CL
+    for world in (1, 2, 4, 8):
+        all_e = CL.energy_grid(-5.0, 35.0, 0.1 / world)
+        parts = [shard.energy_shard(len(all_e), r, world) for r in range(world)]
+        assert sorted(sum(parts, [])) == list(range(len(all_e)))
+        sizes = [len(p) for p in parts]
+        assert max(sizes) - min(sizes) <= 1
+        assert abs(max(sizes) - 401) <= 1
+
+
+def _failing_worker(rank, world, port, out_dir):
+    import datetime
+    import torch.distributed as dist
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world, timeout=datetime.timedelta(seconds=5))
+    if rank == 1:
+        # a rank that fails between steps: it leaves without joining the gather
+        dist.destroy_process_group()
+        return
+    outcome = "gathered"
+    try:
+        shard.gather_by_energy({0: 1.0}, 2)
+    except Exception as exc:  # the collective times out or the peer is gone
+        outcome = "failed: " + type(exc).__name__
+    with open(os.path.join(out_dir, "r0.txt"), "w") as f:
+        f.write(outcome)
+
+
+def test_a_failed_rank_is_detected_on_the_host(tmp_path):
+    """The surviving rank's gather ends with an error (5 s process-group
+    timeout or the closed connection) instead of waiting forever."""
+    port = _free_port()
+    mp.spawn(_failing_worker, args=(2, port, str(tmp_path)), nprocs=2, join=True)
+    assert (tmp_path / "r0.txt").read_text().startswith("failed")
