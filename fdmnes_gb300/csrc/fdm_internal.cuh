@@ -333,6 +333,12 @@ __device__ __forceinline__ void ld4<float>(const float* p, float* v) {
   v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
 }
 template <>
+__device__ __forceinline__ void ld4<dfl>(const dfl* p, dfl* v) {
+  const float4 a = *reinterpret_cast<const float4*>(p);
+  const float4 b = *reinterpret_cast<const float4*>(p + 2);
+  v[0] = dfl(a.x, a.y); v[1] = dfl(a.z, a.w); v[2] = dfl(b.x, b.y); v[3] = dfl(b.z, b.w);
+}
+template <>
 __device__ __forceinline__ void ld4<double>(const double* p, double* v) {
   const double2 a = *reinterpret_cast<const double2*>(p);
   const double2 b = *reinterpret_cast<const double2*>(p + 2);
