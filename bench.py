@@ -285,7 +285,7 @@ def run_gpu(args):
         for ei, ri in items:
             sv.spectrum_add(ei, ri)
         sv.spectrum_run()
-        out = [sv.taull(k) for k in range(n_e)]
+        out = sv.taull_all()
         barrier_sync()
         e2e_times.append(time.perf_counter() - t0)
         if s == 0:

@@ -772,11 +772,11 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   if (b.precision == FDMGPU_PREC_MIXED) {
     // Per problem: classical refinement x += LU^-1 r while it contracts (a step
     // counts as slow when the correction does not halve); after two slow steps
-    // the problem switches to GMRES-IR cycles (when enabled); two slow GMRES
-    // cycles stop it.  A batched classical step costs about 1/300 of an FP64
-    // re-factorisation per problem, so slow convergence is preferred to
-    // escalation.  Stop at max|dx|/max|x| <= tol; results above tol_accept go
-    // to the FP64 escalation below.
+    // the problem switches to GMRES-IR cycles (when enabled) or stops; two
+    // slow GMRES cycles stop it.  A batched classical step costs a few percent
+    // of a re-factorisation per problem, so slow convergence is preferred to
+    // escalation.  Stop at max|dx|/max|x| <= tol; problems that stop above
+    // tol_accept go to the escalation below (double-float by default).
     const int max_iter = 40;
     const double tol = h->tol > 0 ? h->tol : 1e-10;
     const double tol_accept = h->tol_accept > 0 ? h->tol_accept : (h->residual_df64 ? 1e-7 : 1e-9);
@@ -1479,6 +1479,17 @@ fdmgpu_status fdmgpu_batch_taull(fdmgpu_handle* h, int32_t k, double* taull, int
   if (nlm) *nlm = P.nlm_abs;
   if (!taull) return FDMGPU_OK;
   CK(cudaMemcpy(taull, h->d_taull.p + 2 * P.taull, sizeof(double) * 2 * P.nlm_abs * P.nlm_abs,
+                cudaMemcpyDeviceToHost));
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_batch_taull_all(fdmgpu_handle* h, double* taull, int64_t capacity) {
+  if (!h || !h->batch.ran || h->batch.probs.empty()) return fail(FDMGPU_ERR_ARG, "no batch result");
+  int64_t n = 0;
+  for (auto& hp : h->batch.probs) n += (int64_t)hp.P.nlm_abs * hp.P.nlm_abs;
+  if (!taull || capacity < 2 * n) return fail(FDMGPU_ERR_ARG, "Taull buffer too small");
+  // the pool holds the energies' Taull contiguously in add order
+  CK(cudaMemcpy(taull, h->d_taull.p + 2 * h->batch.probs[0].P.taull, sizeof(double) * 2 * n,
                 cudaMemcpyDeviceToHost));
   return FDMGPU_OK;
 }

@@ -77,6 +77,8 @@ def load_library(path: str = LIB_PATH):
     L.fdmgpu_batch_stats.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double),
                                      C.POINTER(C.c_int32), C.POINTER(C.c_int32)]
     L.fdmgpu_batch_vjp.argtypes = [vp, vp, vp, C.POINTER(C.c_double)]
+    L.fdmgpu_batch_taull_all.argtypes = [vp, vp, C.c_int64]
+    L.fdmgpu_batch_taull_all.restype = C.c_int
     L.fdmgpu_batch_add_site.argtypes = [vp, vp, vp, C.c_int32]
     L.fdmgpu_batch_add_site.restype = C.c_int
     L.fdmgpu_update_grid_values.argtypes = [vp, vp]
@@ -210,6 +212,21 @@ class FdmSolver:
         _check(self.lib.fdmgpu_batch_taull(self.h, k, out.ctypes.data, C.byref(nl)))
         return out.view(np.complex128).reshape((nl.value, nl.value), order="F").copy()
 
+    def taull_all(self) -> List[np.ndarray]:
+        """Taull of every energy of the last batch, in one device-to-host copy."""
+        sizes = []
+        for k in range(len(self._batch_args)):
+            nl = C.c_int32(0)
+            _check(self.lib.fdmgpu_batch_taull(self.h, k, None, C.byref(nl)))
+            sizes.append(nl.value)
+        out = np.zeros(2 * sum(n * n for n in sizes))
+        _check(self.lib.fdmgpu_batch_taull_all(self.h, out.ctypes.data, out.size))
+        res, o = [], 0
+        for n in sizes:
+            res.append(out[o:o + 2 * n * n].view(np.complex128).reshape((n, n), order="F").copy())
+            o += 2 * n * n
+        return res
+
     def solution(self, k: int, nlmso: int, nligne: int) -> np.ndarray:
         smr = np.zeros((nlmso, nligne), order="F")
         _check(self.lib.fdmgpu_batch_solution(self.h, k, smr.ctypes.data))
@@ -262,4 +279,4 @@ class FdmSolver:
         for ei, ri in items:
             self.spectrum_add(ei, ri, iaabs)
         info = self.spectrum_run()
-        return [self.taull(k) for k in range(len(items))], info
+        return self.taull_all(), info

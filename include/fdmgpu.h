@@ -255,6 +255,9 @@ fdmgpu_status fdmgpu_batch_run(fdmgpu_handle* h, fdmgpu_info* info);
 fdmgpu_status fdmgpu_batch_rerun(fdmgpu_handle* h, fdmgpu_info* info);
 /* Taull of energy k (0-based, in add order): writes nlm*nlm complex values. */
 fdmgpu_status fdmgpu_batch_taull(fdmgpu_handle* h, int32_t k, double* taull, int32_t* nlm);
+/* Taull of every energy in one copy: nlm_k*nlm_k complex values per energy,
+ * concatenated in add order (capacity counts doubles). */
+fdmgpu_status fdmgpu_batch_taull_all(fdmgpu_handle* h, double* taull, int64_t capacity);
 /* Solution of energy k (nlmso, nligne) column-major into smr (host). */
 fdmgpu_status fdmgpu_batch_solution(fdmgpu_handle* h, int32_t k, double* smr);
 /* Per-energy diagnostics of the last run: refinement (outer) iterations,

@@ -103,6 +103,8 @@ def test_spectrum_mixed_vs_fp64_cross_section(solver_mod):
     T64, _ = sv.spectrum(items, "fp64")
     Tm, info = sv.spectrum(items, "mixed")
     assert xanes.convolved_relative_error(energies, Tm, T64) < 1e-6
+    # one-copy readout equals the per-energy readout
+    assert all(np.array_equal(a, sv.taull(k)) for k, a in enumerate(sv.taull_all()))
     # a replay of the same batch is bit-identical
     info2 = sv.spectrum_rerun()
     Tm2 = [sv.taull(k) for k in range(len(items))]
@@ -262,4 +264,25 @@ def test_overlapped_escalation_gives_the_same_spectrum(solver_mod):
         out[mode], info = sv.spectrum(items, "mixed")
     assert info["n_fallback"] >= 1
     assert all(np.array_equal(a, b) for a, b in zip(out["df64"], out["df64_overlap"]))
+    sv.close()
+
+
+def test_every_refinement_and_escalation_mode(solver_mod):
+    """Each documented mode of the mixed path meets the metric's bar against
+    the FP64 path on full Cu energies that include escalated ones: classical,
+    GMRES-IR and recurrence refinement; double-float and FP64 escalation."""
+    from fdmnes_gb300 import cluster as CL, xanes
+    st = CL.cu_structure()
+    energies = [2.0, 14.0, 26.0, 30.0, 34.0]
+    items = xanes.spectrum_inputs(st, energies)
+    sv = solver_mod.FdmSolver(st)
+    T64, _ = sv.spectrum(items, "fp64")
+    sv.set_tolerance(1e-8, 1e-6)
+    for refine, esc in (("classic", "df64"), ("gmres", "df64"), ("recurrence", "df64"), ("classic", "fp64")):
+        sv.set_refinement(refine, 12)
+        sv.set_escalation(esc)
+        T, info = sv.spectrum(items, "mixed")
+        err = max(rel(a, b) for a, b in zip(T, T64))
+        assert err < 1e-5, (refine, esc, err)
+        assert xanes.convolved_relative_error(energies, T, T64) < 1e-6, (refine, esc)
     sv.close()
