@@ -30,6 +30,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -58,7 +59,7 @@ class ClockSampler:
 
     def __init__(self):
         self.proc = None
-        self.path = os.path.join(HERE, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"fdm_clocks_{os.getpid()}.csv")
 
     def start(self):
         try:
