@@ -270,6 +270,47 @@ void launch_lambda_dot(const Prob* probs, const Pools& pl, const LaunchDims& d, 
   k_lambda_sum<<<d.nprob, 256, 0, s>>>(probs, rowpart, out);
 }
 
+// Transposed CSR (the CSR of A^T) of every problem, for the transposed
+// residual of a mixed batch's adjoint.  Counts per column, then one warp per
+// problem fills the rows in order, so each column lists its rows ascending
+// (deterministic sums).  Within one row the columns are distinct, so the
+// lanes of a warp never share a cursor.
+__global__ void k_csc_count(const Prob* probs, const int* rowptr, const int* col, int* colcnt) {
+  const Prob P = probs[blockIdx.y];
+  const int p = blockIdx.x * 8 + threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (p >= P.nt * TS) return;
+  const int k0 = rowptr[P.rowv + p], k1 = min(rowptr[P.rowv + p + 1], (int)P.csr_cap);
+  for (int k = k0 + lane; k < k1; k += 32) atomicAdd(&colcnt[P.rowv + col[P.csr + k] + 1], 1);
+}
+
+__global__ void k_csc_fill(const Prob* probs, int np, const int* rowptr, const int* col, const float2* val2,
+                           int* cursor, int* cscrow, float2* cscval2) {
+  const int e = blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32, lane = threadIdx.x % 32;
+  if (e >= np) return;
+  const Prob P = probs[e];
+  for (int p = 0; p < P.nt * TS; ++p) {
+    const int k0 = rowptr[P.rowv + p], k1 = min(rowptr[P.rowv + p + 1], (int)P.csr_cap);
+    for (int k = k0 + lane; k < k1; k += 32) {
+      const int c = col[P.csr + k];
+      const int pos = cursor[P.rowv + c]++;
+      if (pos < P.csr_cap) {
+        cscrow[P.csr + pos] = p;
+        cscval2[P.csr + pos] = val2[P.csr + k];
+      }
+    }
+    __syncwarp();
+  }
+}
+
+void launch_csc_build(const Prob* probs, const Pools& pl, const LaunchDims& d, int* colptr, int* cursor, int* cscrow,
+                      float2* cscval2, cudaStream_t s) {
+  cudaMemsetAsync(colptr, 0, d.rowv_total * sizeof(int), s);
+  k_csc_count<<<dim3((d.max_rows + 7) / 8, d.nprob), 256, 0, s>>>(probs, pl.rowptr, pl.col, colptr);
+  launch_csr_scan(probs, colptr, d, s);
+  cudaMemcpyAsync(cursor, colptr, d.rowv_total * sizeof(int), cudaMemcpyDeviceToDevice, s);
+  k_csc_fill<<<(d.nprob + 3) / 4, 128, 0, s>>>(probs, d.nprob, pl.rowptr, pl.col, pl.val2, cursor, cscrow, cscval2);
+}
+
 void launch_taull_vjp(const Prob* probs, const LaunchDims& d, const double* X, const double* gT, double* scratch,
                       double* G, int* err, cudaStream_t s) {
   const size_t sm = (size_t)d.max_nlmso * (sizeof(double2) + sizeof(int));

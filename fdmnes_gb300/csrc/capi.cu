@@ -123,6 +123,9 @@ struct fdmgpu_handle {
   DevBuf<double> d_dpool;
   DevBuf<double> d_env64, d_B64, d_X64, d_rs, d_cs, d_val, d_taull, d_tscratch, d_smr;
   DevBuf<double> d_gT, d_lam, d_gpart, d_grad;  // adjoint
+  DevBuf<double> d_G;                            // adjoint of a mixed batch: cotangent of X
+  DevBuf<float2> d_lams, d_cscval2;              // Lambda as double-float pairs; A^T values
+  DevBuf<int> d_colptr, d_cursor, d_cscrow;      // CSR of A^T
   DevBuf<float> d_env32, d_Y32, d_R32;
   DevBuf<int> d_act_df, d_act_rec;
   DevBuf<float2> d_val2, d_Xs;
@@ -1354,6 +1357,12 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   for (auto& e : h->ev_esc)
     if (e) cudaEventDestroy(e);
   h->d_esc_mask.release();
+  h->d_G.release();
+  h->d_lams.release();
+  h->d_colptr.release();
+  h->d_cursor.release();
+  h->d_cscrow.release();
+  h->d_cscval2.release();
   if (h->h_esc_mask) cudaFreeHost(h->h_esc_mask);
   h->d_red_esc.release();
   h->d_red_tmp.release();
@@ -1531,13 +1540,97 @@ fdmgpu_status fdmgpu_mat_solve(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t
   return st2 ? st2 : st;
 }
 
+// Adjoint solve of a mixed batch: A^T Lambda = G with the batch's factors of the
+// equilibrated matrix Ah = R A C (FP32 with tile-local pivots, or the
+// double-float factors of the escalated problems):  Ah^T mu = C G, Lambda = R mu,
+// refined with the transposed double-float residual C (G - A^T Lambda) from the
+// CSR of A^T.  With Lambda = 0 the first residual is C G itself.
+static fdmgpu_status vjp_mixed(fdmgpu_handle* h, int64_t nrhs) {
+  Batch& b = h->batch;
+  const int np = h->dims.nprob;
+  cudaStream_t s = h->stream;
+  int64_t csr = 0;
+  for (auto& hp : b.probs) csr = std::max<int64_t>(csr, hp.P.csr + hp.P.csr_cap);
+  const int64_t rowv = h->dims.rowv_total;
+  if (h->d_G.reserve(nrhs) != cudaSuccess || h->d_lams.reserve(nrhs) != cudaSuccess ||
+      h->d_colptr.reserve(rowv) != cudaSuccess || h->d_cursor.reserve(rowv) != cudaSuccess ||
+      h->d_cscrow.reserve(csr) != cudaSuccess || h->d_cscval2.reserve(csr) != cudaSuccess)
+    return fail(FDMGPU_ERR_NOMEM, "device allocation of the mixed adjoint pools failed");
+  CK(cudaMemsetAsync(h->d_G.p, 0, nrhs * sizeof(double), s));
+  CK(cudaMemsetAsync(h->d_lams.p, 0, nrhs * sizeof(float2), s));
+  launch_taull_vjp(h->d_probs.p, h->dims, h->pl.X64, h->d_gT.p, h->pl.tscratch, h->d_G.p, h->pl.err, s);
+  launch_csc_build(h->d_probs.p, h->pl, h->dims, h->d_colptr.p, h->d_cursor.p, h->d_cscrow.p, h->d_cscval2.p, s);
+  // residual: rows of A^T, scaled by C; update: Lambda += R * correction
+  Pools pa = h->pl;
+  pa.rowptr = h->d_colptr.p;
+  pa.col = h->d_cscrow.p;
+  pa.val2 = h->d_cscval2.p;
+  pa.B64 = h->d_G.p;
+  pa.rs = h->pl.cs;
+  pa.X64 = h->d_lam.p;
+  pa.Xs = h->d_lams.p;
+  pa.cs = h->pl.rs;
+  pa.active = h->d_active.p;
+  dfl* D = reinterpret_cast<dfl*>(h->pl.V);
+  dfl* envd = reinterpret_cast<dfl*>(h->pl.env64);
+  const double tol = h->tol > 0 ? h->tol : 1e-10;
+  std::vector<int> active(np, 1), slow(np, 0), m32(np), mdf(np);
+  std::vector<double> prev(np, 1e300);
+  std::vector<unsigned long long> red(3 * np);
+  for (int it = 1; it <= 30; ++it) {
+    int nact = 0;
+    for (int k = 0; k < np; ++k) {
+      m32[k] = active[k] && !b.fallback[k];
+      mdf[k] = active[k] && b.fallback[k];
+      nact += active[k];
+    }
+    if (!nact) break;
+    CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->d_act_rec.p, m32.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(h->d_act_df.p, mdf.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(h->pl.dmax, 0, 3 * np * sizeof(unsigned long long), s));
+    launch_residual(h->d_probs.p, pa, h->dims, 1, s);
+    // FP32 factors
+    launch_forward_t<float>(h->sp, h->pl.env32, h->pl.Y32, h->d_probs.p, h->tb, np, h->d_act_rec.p, s);
+    launch_backward_t<float>(h->sp, h->pl.env32, h->pl.Y32, h->d_probs.p, h->tb, np, h->d_act_rec.p, h->pl.piv, s);
+    Pools pu = pa;
+    pu.active = h->d_act_rec.p;
+    launch_update_x(h->d_probs.p, pu, h->dims, 0, s);
+    // double-float factors of the escalated problems
+    launch_rhs_to_dfl(h->d_probs.p, h->dims, nullptr, h->pl.Y32, h->pl.cs, D, 0, h->d_act_df.p, s);
+    launch_forward_t<dfl>(h->sp, envd, D, h->d_probs.p, h->tb, np, h->d_act_df.p, s);
+    launch_backward_t<dfl>(h->sp, envd, D, h->d_probs.p, h->tb, np, h->d_act_df.p, h->pl.piv, s);
+    launch_dfl_to_x(h->d_probs.p, h->dims, D, h->d_lam.p, h->d_lams.p, h->pl.rs, 0, h->pl.dmax, h->pl.xmax,
+                    h->d_act_df.p, s);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(red.data(), h->d_red.p, 3 * np * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (int k = 0; k < np; ++k) {
+      if (!active[k]) continue;
+      double dm, xm;
+      memcpy(&dm, &red[k], 8);
+      memcpy(&xm, &red[np + k], 8);
+      const double r = xm > 0 ? dm / xm : dm;
+      if (!std::isfinite(r) || r <= tol) {
+        active[k] = 0;
+      } else {
+        slow[k] = (it > 1 && r > 0.5 * prev[k]) ? slow[k] + 1 : 0;
+        if (slow[k] >= 2) active[k] = 0;
+      }
+      prev[k] = r;
+    }
+  }
+  return FDMGPU_OK;
+}
+
 fdmgpu_status fdmgpu_batch_vjp(fdmgpu_handle* h, const double* gtaull, double* grad_vr, double* ms) {
   if (!h || !gtaull || !grad_vr) return fail(FDMGPU_ERR_ARG, "null argument");
   Batch& b = h->batch;
   if (!b.ran) return fail(FDMGPU_ERR_ARG, "vjp needs a batch that has run");
-  if (b.precision != FDMGPU_PREC_FP64)
-    return fail(FDMGPU_ERR_UNSUPPORTED, "vjp needs the factors of an FP64 batch");
   if (b.sites.size() > 1) return fail(FDMGPU_ERR_UNSUPPORTED, "vjp of a batch over several sites");
+  if (b.precision == FDMGPU_PREC_MIXED && (h->refine_gmres || !h->escalate_dfl))
+    return fail(FDMGPU_ERR_UNSUPPORTED, "vjp of a mixed batch needs classical or recurrence refinement and "
+                                        "double-float escalation");
   const int np = h->dims.nprob;
   for (int k = 0; k < np; ++k) {
     if (b.probs[k].P.nlm_abs <= 0) return fail(FDMGPU_ERR_ARG, "vjp needs an absorber (iaabs > 0) in every energy");
@@ -1567,9 +1660,14 @@ fdmgpu_status fdmgpu_batch_vjp(fdmgpu_handle* h, const double* gtaull, double* g
   CK(cudaMemcpyAsync(h->d_gT.p, gT.data(), ntaull * sizeof(double), cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(h->d_lam.p, 0, nrhs * sizeof(double), s));
   CK(cudaMemsetAsync(h->d_grad.p, 0, (size_t)h->g.npoint * nspin * sizeof(double), s));
-  launch_taull_vjp(h->d_probs.p, h->dims, h->pl.X64, h->d_gT.p, h->pl.tscratch, h->d_lam.p, h->pl.err, s);
-  launch_forward_t<double>(h->sp, h->pl.env64, h->d_lam.p, h->d_probs.p, h->tb, np, nullptr, s);
-  launch_backward_t<double>(h->sp, h->pl.env64, h->d_lam.p, h->d_probs.p, h->tb, np, nullptr, nullptr, s);
+  if (b.precision == FDMGPU_PREC_FP64) {
+    launch_taull_vjp(h->d_probs.p, h->dims, h->pl.X64, h->d_gT.p, h->pl.tscratch, h->d_lam.p, h->pl.err, s);
+    launch_forward_t<double>(h->sp, h->pl.env64, h->d_lam.p, h->d_probs.p, h->tb, np, nullptr, s);
+    launch_backward_t<double>(h->sp, h->pl.env64, h->d_lam.p, h->d_probs.p, h->tb, np, nullptr, nullptr, s);
+  } else {
+    fdmgpu_status st = vjp_mixed(h, nrhs);
+    if (st) return st;
+  }
   launch_grad_vr(h->S, h->d_probs.p, h->pl.ipool, h->dims, nspin, h->pl.X64, h->d_lam.p, h->d_gpart.p,
                  h->d_grad.p, s);
   CK(cudaGetLastError());

@@ -359,6 +359,10 @@ template void launch_forward_t<double>(const StepPlan&, const double*, double*, 
                                        cudaStream_t);
 template void launch_backward_t<double>(const StepPlan&, const double*, double*, const Prob*, Tables, int,
                                         const int*, const int*, cudaStream_t);
+template void launch_forward_t<dfl>(const StepPlan&, const dfl*, dfl*, const Prob*, Tables, int, const int*,
+                                    cudaStream_t);
+template void launch_backward_t<dfl>(const StepPlan&, const dfl*, dfl*, const Prob*, Tables, int, const int*,
+                                     const int*, cudaStream_t);
 template void launch_forward_t<float>(const StepPlan&, const float*, float*, const Prob*, Tables, int, const int*,
                                       cudaStream_t);
 template void launch_backward_t<float>(const StepPlan&, const float*, float*, const Prob*, Tables, int, const int*,

@@ -122,6 +122,13 @@ void launch_taull_vjp(const Prob* probs, const LaunchDims& d, const double* X, c
                       double* G, int* err, cudaStream_t s);
 void launch_grad_vr(const StaticDev& S, const Prob* probs, const int* ipool, const LaunchDims& d, int nspin,
                     const double* X, const double* Lam, double* part, double* grad, cudaStream_t s);
+void launch_csr_scan(const Prob* probs, int* ptr, const LaunchDims& d, cudaStream_t s);
+void launch_rhs_to_dfl(const Prob* probs, const LaunchDims& d, const double* B, const float* Y, const double* scale,
+                       dfl* D, int from_b, const int* mask, cudaStream_t s);
+void launch_dfl_to_x(const Prob* probs, const LaunchDims& d, const dfl* D, double* X, float2* Xs, const double* scale,
+                     int first, unsigned long long* dmax, unsigned long long* xmax, const int* mask, cudaStream_t s);
+void launch_csc_build(const Prob* probs, const Pools& pl, const LaunchDims& d, int* colptr, int* cursor, int* cscrow,
+                      float2* cscval2, cudaStream_t s);
 void launch_lambda_dot(const Prob* probs, const Pools& pl, const LaunchDims& d, const double* Lam, double* rowpart,
                        double* out, cudaStream_t s);
 void launch_taull(const Prob* probs, const Pools& pl, const LaunchDims& d, const double* X, cudaStream_t s);

@@ -449,6 +449,10 @@ void launch_csr(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims&
                                                              pl.err);
 }
 
+void launch_csr_scan(const Prob* probs, int* ptr, const LaunchDims& d, cudaStream_t s) {
+  k_csr_scan<<<dim3(1, d.nprob), 1024, 0, s>>>(probs, ptr);
+}
+
 void launch_residual(const Prob* probs, const Pools& pl, const LaunchDims& d, int df64, cudaStream_t s) {
   if (df64)
     k_residual_df<<<dim3((d.max_rows + 7) / 8, d.nprob), 256, 0, s>>>(probs, pl.rowptr, pl.col, pl.val2, pl.B64,
@@ -580,6 +584,16 @@ int launch_dfl_refine_step(const StepPlan& sp, const Prob* probs, const Pools& p
   nk += launch_backward<dfl>(sp, envd, D, probs, tb, np, pl.active, s);
   k_dfl_to_x<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, D, pl.X64, pl.Xs, pl.cs, 0, pl.dmax, pl.xmax, pl.active);
   return nk + 1;
+}
+
+void launch_rhs_to_dfl(const Prob* probs, const LaunchDims& d, const double* B, const float* Y, const double* scale,
+                       dfl* D, int from_b, const int* mask, cudaStream_t s) {
+  k_rhs_to_dfl<<<dim3(d.max_rhs_tiles, d.nprob), 256, 0, s>>>(probs, B, Y, scale, D, from_b, mask);
+}
+
+void launch_dfl_to_x(const Prob* probs, const LaunchDims& d, const dfl* D, double* X, float2* Xs, const double* scale,
+                     int first, unsigned long long* dmax, unsigned long long* xmax, const int* mask, cudaStream_t s) {
+  k_dfl_to_x<<<dim3(d.max_rhs_tiles, d.nprob), 256, 0, s>>>(probs, D, X, Xs, scale, first, dmax, xmax, mask);
 }
 
 void launch_copy_rhs(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s) {

@@ -3,14 +3,15 @@
 The role of the reference's fitting loop (source/minim.f90), restricted to one
 structural parameter: theta moves the first coordination shell of the
 absorber radially.  Loss L(theta) = sum_E (sigma_E(theta) - target_E)^2 with
-sigma the dipole absorption -Im Tr Taull(L=1).  Each step runs the FP64
-batched spectrum, one vector-Jacobian product (cotangent 2 (sigma - target))
+sigma the dipole absorption -Im Tr Taull(L=1).  Each step runs the batched
+spectrum (FP64, or mixed precision with ``--precision mixed``), one
+vector-Jacobian product (cotangent 2 (sigma - target))
 and the two adjoint dot products that give dL/dtheta
 (``gradients``); the step length follows Barzilai-Borwein.  The grid's
 membership (which points lie inside atoms) can change between steps, so the
 handle is rebuilt for every theta.
 
-Usage:  python -m fdmnes_gb300.fit [--energies N] [--steps K] [--offset A]
+Usage:  python -m fdmnes_gb300.fit [--energies N] [--steps K] [--offset A] [--precision P]
 """
 from __future__ import annotations
 
@@ -34,12 +35,12 @@ def sigma_spectrum(st: CL.Structure, energies: Sequence[float]) -> np.ndarray:
 
 
 def loss_grad(build: Callable[[float], CL.Structure], theta: float, energies: Sequence[float],
-              target: np.ndarray, h: float = 1e-4):
-    """L(theta) and dL/dtheta through the adjoint (FP64)."""
+              target: np.ndarray, h: float = 1e-4, precision: str = "fp64"):
+    """L(theta) and dL/dtheta through the adjoint of the batch of ``precision``."""
     st = build(theta)
     sv = FdmSolver(st)
     items = xanes.spectrum_inputs(st, energies)
-    T, _ = sv.spectrum(items, "fp64")
+    T, _ = sv.spectrum(items, precision)
     sig = np.array([xanes.absorption(t) for t in T])
     r = sig - target
     sv.vjp([xanes.absorption_cotangent(t, 2.0 * rk) for t, rk in zip(T, r)])
@@ -53,14 +54,14 @@ def loss_grad(build: Callable[[float], CL.Structure], theta: float, energies: Se
 
 
 def fit(build: Callable[[float], CL.Structure], energies: Sequence[float], target: np.ndarray,
-        theta0: float = 0.0, steps: int = 20, step0: float = 1e-3) -> List[dict]:
+        theta0: float = 0.0, steps: int = 20, step0: float = 1e-3, precision: str = "fp64") -> List[dict]:
     """Barzilai-Borwein gradient descent on theta; returns the per-step history."""
     hist = []
     theta, alpha = theta0, None
     prev = None
     for k in range(steps):
         t0 = time.time()
-        L, g = loss_grad(build, theta, energies, target)
+        L, g = loss_grad(build, theta, energies, target, precision=precision)
         hist.append({"step": k, "theta": theta, "loss": L, "grad": g, "s": time.time() - t0})
         if prev is not None:
             dth, dg = theta - prev[0], g - prev[1]
@@ -79,11 +80,12 @@ def main():
     ap.add_argument("--energies", type=int, default=41)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--offset", type=float, default=0.03, help="shell displacement of the target (A)")
+    ap.add_argument("--precision", choices=("fp64", "mixed"), default="fp64")
     args = ap.parse_args()
     B.build()
     energies = CL.energy_grid(-5.0, 35.0, 40.0 / (args.energies - 1))
     target = sigma_spectrum(cu_shell_structure(args.offset), energies)
-    hist = fit(cu_shell_structure, energies, target, 0.0, args.steps)
+    hist = fit(cu_shell_structure, energies, target, 0.0, args.steps, precision=args.precision)
     for hrow in hist:
         print(json.dumps(hrow), flush=True)
 

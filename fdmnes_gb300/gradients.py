@@ -1,4 +1,4 @@
-"""Gradients of a spectrum loss through the adjoint of the batched FP64 solve.
+"""Gradients of a spectrum loss through the adjoint of the batched solve.
 
 L = sum_E w_E sigma(E) with sigma the dipole absorption -Im Tr Taull(L=1)
 (``xanes.absorption``).  Two parameter families:
@@ -10,6 +10,10 @@ L = sum_E w_E sigma(E) with sigma the dipole absorption -Im Tr Taull(L=1)
   taken by central differences of the assembly only
   (``fdmgpu_batch_adjoint_dot`` at theta +- h).  The structure (grid
   membership, row numbering) must not change within +- h.
+
+``precision`` selects the forward batch: "fp64" (FP64 factors and solves) or
+"mixed" (FP32 factors with double-float refinement; the adjoint then runs on
+the same factors, refined to the handle's tolerance).
 """
 from __future__ import annotations
 
@@ -21,13 +25,14 @@ from . import cluster as CL
 from . import xanes
 
 
-def spectrum_loss(sv, items, weights) -> Tuple[float, list]:
-    T, _ = sv.spectrum(items, "fp64")
+def spectrum_loss(sv, items, weights, precision: str = "fp64") -> Tuple[float, list]:
+    T, _ = sv.spectrum(items, precision)
     return float(sum(w * xanes.absorption(t) for w, t in zip(weights, T))), T
 
 
 def loss_and_gradients(sv, build_structure: Callable[[float], CL.Structure], theta: float,
-                       energies: Sequence[float], weights: Sequence[float], h: float = 1e-4):
+                       energies: Sequence[float], weights: Sequence[float], h: float = 1e-4,
+                       precision: str = "fp64"):
     """L(theta), dL/dVr and dL/dtheta.
 
     build_structure(theta) returns the Structure at parameter theta; sv must hold
@@ -36,7 +41,7 @@ def loss_and_gradients(sv, build_structure: Callable[[float], CL.Structure], the
     """
     st0 = sv.st
     items = xanes.spectrum_inputs(st0, energies)
-    L, T = spectrum_loss(sv, items, weights)
+    L, T = spectrum_loss(sv, items, weights, precision)
     grad_vr, ms = sv.vjp([xanes.absorption_cotangent(t, w) for t, w in zip(T, weights)])
     dots = []
     for sgn in (1.0, -1.0):

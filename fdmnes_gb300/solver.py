@@ -247,7 +247,8 @@ class FdmSolver:
     def vjp(self, g_taull: Sequence[np.ndarray]) -> Tuple[np.ndarray, float]:
         """Gradient of L with respect to the grid potential Vr, given the
         cotangents g_taull[k] = dL/d(Im Taull_k) (nlm x nlm real) of the energies
-        of the last FP64 batch.  Returns (dL/dVr of shape (npoint, nspin), device ms)."""
+        of the last batch (FP64 or mixed).  Returns (dL/dVr of shape
+        (npoint, nspin), device ms)."""
         flat = np.concatenate([np.asarray(g, dtype=np.float64).ravel(order="F") for g in g_taull])
         g = self.st.grid
         grad = np.zeros((g.npoint, self.st.nspin), order="F")

@@ -268,14 +268,18 @@ fdmgpu_status fdmgpu_batch_stats(fdmgpu_handle* h, int32_t k, int32_t* iters, do
                                  int32_t* fallback, int32_t* inner_iters);
 
 /*
- * Vector-Jacobian product of the last FP64 batch: given the cotangent
+ * Vector-Jacobian product of the last batch: given the cotangent
  * gtaull = dL/d(Im Taull) of every energy (nlm*nlm reals per energy,
  * column-major, concatenated in add order), writes dL/dVr into grad_vr
  * (npoint, nspin), column-major like Vr.  It reuses the batch's factors
  * (transposed solves A^T Lambda = dL/dX) and its solutions; Vr enters the FDM
- * matrix on the diagonal of the grid rows (source/mat.f90:1151-1156).  Points
- * inside atoms get 0.  ms (may be NULL) receives the device time.  No
- * counterpart in the reference.
+ * matrix on the diagonal of the grid rows (source/mat.f90:1151-1156).  After
+ * an FP64 batch the FP64 factors solve A^T directly; after a mixed batch the
+ * FP32 (or, for escalated energies, double-float) factors of the equilibrated
+ * matrix are refined with a double-float transposed residual (classical or
+ * recurrence refinement with double-float escalation).  Points inside atoms
+ * get 0.  ms (may be NULL) receives the device time.  No counterpart in the
+ * reference.
  */
 fdmgpu_status fdmgpu_batch_vjp(fdmgpu_handle* h, const double* gtaull, double* grad_vr, double* ms);
 

@@ -1,4 +1,4 @@
-"""Adjoint (vector-Jacobian product) of the batched FP64 spectrum.
+"""Adjoint (vector-Jacobian product) of the batched spectrum.
 
 L = sum_E w_E sigma(E), sigma = -Im Tr Taull(L=1).  fdmgpu_batch_vjp returns
 dL/dVr at every grid point; it is checked against central finite differences
@@ -6,6 +6,11 @@ of the same FP64 GPU spectrum, Vr(i) +- h with h = 1e-4 Ry, on the small Cu
 cluster.  Bar: relative difference <= 1e-5.  The FD quotient's own rounding
 error is about 1e-13 |L| / h, i.e. ~6e-6 absolute for |L| ~ 6e3 at h = 1e-4
 Ry, against derivatives of 2..7; measured differences are 1e-7..3e-6.
+
+The mixed-precision batch's adjoint (FP32 or double-float transposed solves,
+refined with a double-float transposed residual) is checked against the FP64
+adjoint, and the shell-distance gradient (adjoint through the solve, central
+differences of the assembly only) against central differences of the loss.
 """
 import numpy as np
 import pytest
@@ -75,10 +80,62 @@ def test_vjp_is_linear_in_the_cotangent(setup):
     assert np.allclose(sum(wk * p for wk, p in zip(w, parts)), g2, rtol=1e-12, atol=1e-12 * np.abs(g2).max())
 
 
-def test_vjp_needs_fp64_factors(setup):
+def test_mixed_vjp_matches_fp64_vjp(setup):
+    """The adjoint of a mixed batch (FP32 factors refined with the transposed
+    double-float residual) gives the FP64 batch's gradient to 1e-8 of its
+    largest component on the small cluster."""
     from fdmnes_gb300 import xanes
-    from fdmnes_gb300.solver import FdmError
     st, sv, items, w, loss = setup
-    T, _ = sv.spectrum(items, "mixed")
-    with pytest.raises(FdmError):
-        sv.vjp([xanes.absorption_cotangent(t) for t in T])
+    T, _ = sv.spectrum(items, "fp64")
+    g64, _ = sv.vjp([xanes.absorption_cotangent(t, wk) for t, wk in zip(T, w)])
+    Tm, _ = sv.spectrum(items, "mixed")
+    gm, _ = sv.vjp([xanes.absorption_cotangent(t, wk) for t, wk in zip(Tm, w)])
+    assert np.abs(gm - g64).max() <= 1e-8 * np.abs(g64).max()
+
+
+def test_mixed_vjp_with_escalated_energies():
+    """Full Cu energies at the benchmark's tolerances (1e-8, acceptance 1e-6):
+    two of the four stall in FP32 refinement above the acceptance level
+    (condition numbers up to 1e10) and are re-factorised in double-float, so
+    their adjoint runs on the double-float factors.  The gradient matches the
+    FP64 adjoint to 1e-6 of its largest component (3e-8 measured)."""
+    from fdmnes_gb300 import build, cluster as CL, xanes
+    from fdmnes_gb300.solver import FdmSolver
+    build.build()
+    st = CL.cu_structure()
+    items = xanes.spectrum_inputs(st, [2.0, 26.0, 30.0, 34.0])
+    sv = FdmSolver(st)
+    T, _ = sv.spectrum(items, "fp64")
+    g64, _ = sv.vjp([xanes.absorption_cotangent(t) for t in T])
+    sv.set_tolerance(1e-8, 1e-6)
+    Tm, info = sv.spectrum(items, "mixed")
+    assert info["n_fallback"] >= 1
+    gm, _ = sv.vjp([xanes.absorption_cotangent(t) for t in Tm])
+    assert np.abs(gm - g64).max() <= 1e-6 * np.abs(g64).max()
+    sv.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_shell_gradient_matches_central_differences(precision):
+    """dL/dtheta for theta the first-shell distance of the small Cu cluster:
+    Lambda^T (dB/dtheta - dA/dtheta X) against central differences of the FP64
+    loss, both with h = 1e-4 A (grid membership unchanged within +- h).
+    Bar 1e-5 relative; 5e-7 measured for the FP64 adjoint.  The mixed batch
+    runs at the benchmark's tolerances (1e-8, acceptance 1e-6)."""
+    from fdmnes_gb300 import build, gradients as G, xanes
+    from fdmnes_gb300.solver import FdmSolver
+    build.build()
+    energies, w = [3.0, 12.0, 27.0], [1.0, -0.7, 0.4]
+    sv = FdmSolver(G.cu_shell_structure(0.0))
+    sv.set_tolerance(1e-8, 1e-6)
+    L, _, _, dth, _ = G.loss_and_gradients(sv, G.cu_shell_structure, 0.0, energies, w, h=H, precision=precision)
+    sv.close()
+    Ls = []
+    for sgn in (1.0, -1.0):
+        st = G.cu_shell_structure(sgn * H)
+        s2 = FdmSolver(st)
+        Ls.append(G.spectrum_loss(s2, xanes.spectrum_inputs(st, energies), w)[0])
+        s2.close()
+    fd = (Ls[0] - Ls[1]) / (2 * H)
+    assert np.isfinite(L)
+    assert abs(dth - fd) <= TOL * abs(fd), (dth, fd)
