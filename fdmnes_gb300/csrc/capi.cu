@@ -1578,30 +1578,37 @@ static fdmgpu_status vjp_mixed(fdmgpu_handle* h, int64_t nrhs) {
   std::vector<double> prev(np, 1e300);
   std::vector<unsigned long long> red(3 * np);
   for (int it = 1; it <= 30; ++it) {
-    int nact = 0;
+    int n32 = 0, ndf = 0;
     for (int k = 0; k < np; ++k) {
       m32[k] = active[k] && !b.fallback[k];
       mdf[k] = active[k] && b.fallback[k];
-      nact += active[k];
+      n32 += m32[k];
+      ndf += mdf[k];
     }
-    if (!nact) break;
+    if (!n32 && !ndf) break;
     CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->d_act_rec.p, m32.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(h->d_act_df.p, mdf.data(), np * sizeof(int), cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(h->pl.dmax, 0, 3 * np * sizeof(unsigned long long), s));
     launch_residual(h->d_probs.p, pa, h->dims, 1, s);
-    // FP32 factors
-    launch_forward_t<float>(h->sp, h->pl.env32, h->pl.Y32, h->d_probs.p, h->tb, np, h->d_act_rec.p, s);
-    launch_backward_t<float>(h->sp, h->pl.env32, h->pl.Y32, h->d_probs.p, h->tb, np, h->d_act_rec.p, h->pl.piv, s);
-    Pools pu = pa;
-    pu.active = h->d_act_rec.p;
-    launch_update_x(h->d_probs.p, pu, h->dims, 0, s);
+    // FP32 factors (the step launches of a factor kind none of the active
+    // problems use are skipped)
+    if (n32) {
+      launch_forward_t<float>(h->sp, h->pl.env32, h->pl.Y32, h->d_probs.p, h->tb, np, h->d_act_rec.p, s);
+      launch_backward_t<float>(h->sp, h->pl.env32, h->pl.Y32, h->d_probs.p, h->tb, np, h->d_act_rec.p, h->pl.piv,
+                               s);
+      Pools pu = pa;
+      pu.active = h->d_act_rec.p;
+      launch_update_x(h->d_probs.p, pu, h->dims, 0, s);
+    }
     // double-float factors of the escalated problems
-    launch_rhs_to_dfl(h->d_probs.p, h->dims, nullptr, h->pl.Y32, h->pl.cs, D, 0, h->d_act_df.p, s);
-    launch_forward_t<dfl>(h->sp, envd, D, h->d_probs.p, h->tb, np, h->d_act_df.p, s);
-    launch_backward_t<dfl>(h->sp, envd, D, h->d_probs.p, h->tb, np, h->d_act_df.p, h->pl.piv, s);
-    launch_dfl_to_x(h->d_probs.p, h->dims, D, h->d_lam.p, h->d_lams.p, h->pl.rs, 0, h->pl.dmax, h->pl.xmax,
-                    h->d_act_df.p, s);
+    if (ndf) {
+      launch_rhs_to_dfl(h->d_probs.p, h->dims, nullptr, h->pl.Y32, h->pl.cs, D, 0, h->d_act_df.p, s);
+      launch_forward_t<dfl>(h->sp, envd, D, h->d_probs.p, h->tb, np, h->d_act_df.p, s);
+      launch_backward_t<dfl>(h->sp, envd, D, h->d_probs.p, h->tb, np, h->d_act_df.p, h->pl.piv, s);
+      launch_dfl_to_x(h->d_probs.p, h->dims, D, h->d_lam.p, h->d_lams.p, h->pl.rs, 0, h->pl.dmax, h->pl.xmax,
+                      h->d_act_df.p, s);
+    }
     CK(cudaGetLastError());
     CK(cudaMemcpyAsync(red.data(), h->d_red.p, 3 * np * sizeof(unsigned long long), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
