@@ -766,6 +766,34 @@ class EnergyInputs:
     ispin: int = 1
 
 
+def boundary_radial(st: Structure, enervide: float, lmaxa: np.ndarray) -> Dict[tuple, np.ndarray]:
+    """Radial solutions u_L(r) of every atom at its boundary points (Sch_radial,
+    then f_interp2 as in cal_phiato), keyed by (spin block, atom index 0-based,
+    L) for every spin block of the structure and L <= lmaxa[ia]."""
+    cl, g = st.cluster, st.grid
+    out: Dict[tuple, np.ndarray] = {}
+    ur_cache: Dict[tuple, np.ndarray] = {}
+    for isp in range(1, st.nspin + 1):
+        dvs = st.spin_shift(isp)
+        ecs = enervide - (st.V0bd + dvs)
+        for ia in range(cl.natome):
+            ipr = int(cl.itype[ia])
+            r = st.radial_r[ipr]
+            Vrad = st.radial_V[ipr] + dvs
+            nb = int(g.nbord[ia])
+            rr = st.rrel[:nb, ia]
+            idx = np.searchsorted(r, rr, side="right")   # first r(i) > rrel, 0-based
+            idx = np.clip(idx, 2, len(r) - 1)
+            for L in range(int(lmaxa[ia]) + 1):
+                key = (isp, ipr, L)
+                if key not in ur_cache:
+                    ur_cache[key] = sch_radial(r, Vrad, enervide, ecs, L, float(cl.zproto[ipr]) +
+                                               (1.0 if ipr == 0 else 0.0))
+                u = ur_cache[key]
+                out[(isp, ia, L)] = f_interp2(rr, r[idx - 2], r[idx - 1], r[idx], u[idx - 2], u[idx - 1], u[idx])
+    return out
+
+
 def energy_inputs(st: Structure, energy_ev: float, e_fermi_ev: float = -5.0, ispin: int = 1) -> EnergyInputs:
     """Per-energy inputs: l cut-offs, atomic boundary functions, Bessel/Neumann."""
     cl, g = st.cluster, st.grid
@@ -792,28 +820,11 @@ def energy_inputs(st: Structure, energy_ev: float, e_fermi_ev: float = -5.0, isp
     # calcMatRow read it at min(ispin, nspin) (source/mat.f90:1144,1296-1304).
     nspinp = st.nspin
     phiato = np.zeros((g.nbtm, nlmagm, nspinp, 1, 1, natome, 1), order="F")
-    ur_cache: Dict[tuple, np.ndarray] = {}
-    for isp in range(1, nspinp + 1):
-        dvs = st.spin_shift(isp)
-        ecs = enervide - (st.V0bd + dvs)
-        for ia in range(natome):
-            ipr = int(cl.itype[ia])
-            r = st.radial_r[ipr]
-            Vrad = st.radial_V[ipr] + dvs
-            nb = int(g.nbord[ia])
-            rr = st.rrel[:nb, ia]
-            idx = np.searchsorted(r, rr, side="right")   # first r(i) > rrel, 0-based
-            idx = np.clip(idx, 2, len(r) - 1)
-            for L in range(int(lmaxa[ia]) + 1):
-                key = (isp, ipr, L)
-                if key not in ur_cache:
-                    ur_cache[key] = sch_radial(r, Vrad, enervide, ecs, L, float(cl.zproto[ipr]) +
-                                               (1.0 if ipr == 0 else 0.0))
-                u = ur_cache[key]
-                phi = f_interp2(rr, r[idx - 2], r[idx - 1], r[idx], u[idx - 2], u[idx - 1], u[idx])
-                for m in range(-L, L + 1):
-                    lm = L * L + L + m
-                    phiato[:nb, lm, isp - 1, 0, 0, ia, 0] = phi * st.Ylmato[:nb, lm, ia]
+    for (isp, ia, L), phi in boundary_radial(st, enervide, lmaxa).items():
+        nb = int(g.nbord[ia])
+        for m in range(-L, L + 1):
+            lm = L * L + L + m
+            phiato[:nb, lm, isp - 1, 0, 0, ia, 0] = phi * st.Ylmato[:nb, lm, ia]
     # phiso, non-Rydberg, real branch
     konder = math.sqrt(ecin_out)
     fnorm = math.sqrt(konder / math.pi)
@@ -827,7 +838,7 @@ def energy_inputs(st: Structure, energy_ev: float, e_fermi_ev: float = -5.0, isp
 
 
 # ---------------------------------------------------------------------------
-# newind (source/mat.f90:1761-1921), regular solution, nspino = 1
+# newind (source/mat.f90:1761-1921), regular solution, nspino = 1 or 2
 # ---------------------------------------------------------------------------
 
 @dataclasses.dataclass
@@ -890,6 +901,9 @@ def newind(st: Structure, nlmsa: np.ndarray, nlmso: int, nspino: int = 1) -> Row
                 lb2[ii - 1] = max(lb2[ii - 1], ianew[ia - 1] + n_ato_ri * nlmsa[ia - 1])
             elif ia == -2:
                 lb2[ii - 1] = nligne
+        if nspino == 2:      # the point's spin-1 row has the same span
+            lb1[ii - 2] = lb1[ii - 1]
+            lb2[ii - 2] = lb2[ii - 1]
     for ia in range(natome):
         lb11 = ianew[ia] + 1
         lb22 = ianew[ia] + n_ato_ri * nlmsa[ia]
@@ -910,6 +924,8 @@ def newind(st: Structure, nlmsa: np.ndarray, nlmso: int, nspino: int = 1) -> Row
         ii = new[i]
         if ii != 0:
             newinv[ii - 1] = i
+            if nspino == 2:
+                newinv[ii - 2] = i
     for ia in range(natome):
         newinv[ianew[ia]:ianew[ia] + n_ato_ri * nlmsa[ia]] = -(ia + 1)
     return RowIndex(nligne=nligne, nligneso=nligne - nlmso, new=new.astype(np.int32),

@@ -35,6 +35,10 @@ def lib():
         L.oracle_cbessneur.argtypes = [C.c_double, C.c_double, C.c_int, vp, vp]
         L.oracle_invcomp.argtypes = [C.c_int, vp]
         L.oracle_taull.argtypes = [vp, vp, C.c_int, vp, vp, C.POINTER(C.c_int32)]
+        L.oracle_mat_solve_c.argtypes = [vp, vp, vp, vp, C.POINTER(C.c_int64), C.POINTER(C.c_double),
+                                         C.POINTER(C.c_double), C.POINTER(C.c_int32)]
+        L.oracle_assemble_dense_c.argtypes = [vp, vp, vp, vp]
+        L.oracle_taull_c.argtypes = [vp, vp, C.c_int, vp, vp, C.c_int, vp, C.POINTER(C.c_int32)]
         _lib = L
     return _lib
 
@@ -107,3 +111,45 @@ def invcomp(a):
     if st != 0:
         raise RuntimeError("oracle_invcomp: singular")
     return a
+
+
+def mat_solve_c(grid_args, energy_args):
+    """Complex solution smr + i smi (nlmso, nligne), Fortran-ordered, plus nnz."""
+    n, m = energy_args.nligne, energy_args.nlmso
+    smr = np.zeros((m, n), order="F")
+    smi = np.zeros((m, n), order="F")
+    nnz = C.c_int64(0)
+    tf, tt = C.c_double(0), C.c_double(0)
+    bad = C.c_int32(0)
+    st = lib().oracle_mat_solve_c(C.addressof(grid_args.s), C.addressof(energy_args.s), smr.ctypes.data,
+                                  smi.ctypes.data, C.byref(nnz), C.byref(tf), C.byref(tt), C.byref(bad))
+    if st != 0:
+        raise RuntimeError(f"oracle_mat_solve_c failed with status {st} (row {bad.value})")
+    return smr + 1j * smi, dict(nnz=nnz.value, time_fill=tf.value, time_tria=tt.value)
+
+
+def assemble_dense_c(grid_args, energy_args):
+    n, m = energy_args.nligne, energy_args.nlmso
+    A = np.zeros((n, n), dtype=np.complex128, order="F")
+    B = np.zeros((m, n), dtype=np.complex128, order="F")
+    st = lib().oracle_assemble_dense_c(C.addressof(grid_args.s), C.addressof(energy_args.s), A.ctypes.data,
+                                       B.ctypes.data)
+    if st != 0:
+        raise RuntimeError(f"oracle_assemble_dense_c failed with status {st}")
+    return A, B
+
+
+def taull_c(grid_args, energy_args, x, iaabs=1, symmetrise=True):
+    """Taull (nlm, nsp, nlm, nsp) of a complex-basis solution x (nlmso, nligne)."""
+    nsp = int(grid_args.d["nspino"])
+    nl = C.c_int32(0)
+    out = np.zeros(2 * (64 * nsp) ** 2)
+    smr = np.asfortranarray(x.real)
+    smi = np.asfortranarray(x.imag)
+    st = lib().oracle_taull_c(C.addressof(grid_args.s), C.addressof(energy_args.s), iaabs, smr.ctypes.data,
+                              smi.ctypes.data, int(bool(symmetrise)), out.ctypes.data, C.byref(nl))
+    if st != 0:
+        raise RuntimeError(f"oracle_taull_c failed with status {st}")
+    k = nl.value
+    t = out[:2 * (k * nsp) ** 2].view(np.complex128).reshape((k, nsp, k, nsp), order="F")
+    return t.copy()

@@ -32,66 +32,11 @@
 
 #include "../include/fdmgpu.h"
 
+#include "oracle_ctx.h"
+
 namespace {
 
-typedef std::complex<double> cdouble;
-
-// Fortran-style accessors (1-based indices).
-struct I2 {
-  const int32_t* p; int64_t ld;
-  int32_t operator()(int64_t i, int64_t j) const { return p[(i - 1) + (j - 1) * ld]; }
-};
-struct D2 {
-  const double* p; int64_t ld;
-  double operator()(int64_t i, int64_t j) const { return p[(i - 1) + (j - 1) * ld]; }
-};
-
-struct Ctx {
-  const fdmgpu_grid* g;
-  const fdmgpu_energy* e;
-  I2 ivois, isvois, ibord, isbord;
-  D2 poidsa, Ylmso, Kar;
-  int64_t ld_ylmato1, ld_ylmato2;
-  int nspino;
-  int ispin;
-};
-
-inline double Ylmato(const Ctx& c, int ib, int lm, int ia) {
-  return c.g->Ylmato[(ib - 1) + (int64_t)(lm - 1) * c.g->nbtm + (int64_t)(ia - 1) * c.g->nbtm * c.g->nlmmax];
-}
-// phiato(ib, Lm, isp, isol, i_RI, ia, 1), dims (nphiato1, nlmagm, nspinp, nspino, n_RI, natome, nphiato7)
-inline double Phiato(const Ctx& c, int ib, int lm, int isp, int isol, int iri, int ia) {
-  const fdmgpu_energy* e = c.e;
-  int64_t d1 = e->nphiato1, d2 = e->nlmagm, d3 = e->nspinp, d4 = c.nspino, d5 = e->n_RI;
-  int64_t off = (ib - 1) + d1 * ((lm - 1) + d2 * ((isp - 1) + d3 * ((isol - 1) + d4 * ((iri - 1) + d5 * (ia - 1)))));
-  return e->phiato[off];
-}
-// Besselr / Neumanr (nsort_r, 0:lmaxso, nspinr)
-inline double Bes(const Ctx& c, const double* a, int ib, int L, int isp) {
-  const fdmgpu_energy* e = c.e;
-  return a[(ib - 1) + (int64_t)e->nsort_r * (L + (int64_t)(e->lmaxso + 1) * (isp - 1))];
-}
-inline int Lato(const Ctx& c, int lm, int ia) { return c.g->lato[(lm - 1) + (int64_t)c.g->nlmsam * (ia - 1 + (int64_t)c.g->natome * (c.e->igrph - 1))]; }
-inline int Mato(const Ctx& c, int lm, int ia) { return c.g->mato[(lm - 1) + (int64_t)c.g->nlmsam * (ia - 1 + (int64_t)c.g->natome * (c.e->igrph - 1))]; }
-inline int Iato(const Ctx& c, int lm, int ia) { return c.g->iato[(lm - 1) + (int64_t)c.g->nlmsam * (ia - 1 + (int64_t)c.g->natome * (c.e->igrph - 1))]; }
-inline int Lso(const Ctx& c, int lm) { return c.g->lso[(lm - 1) + (int64_t)c.g->nso1 * (c.e->igrph - 1)]; }
-inline int Mso(const Ctx& c, int lm) { return c.g->mso[(lm - 1) + (int64_t)c.g->nso1 * (c.e->igrph - 1)]; }
-inline int Iso(const Ctx& c, int lm) { return c.g->iso[(lm - 1) + (int64_t)c.g->nso1 * (c.e->igrph - 1)]; }
-
-Ctx make_ctx(const fdmgpu_grid* g, const fdmgpu_energy* e) {
-  Ctx c;
-  c.g = g; c.e = e;
-  c.ivois = {g->ivois, g->npsom};
-  c.isvois = {g->isvois, g->npsom};
-  c.ibord = {g->ibord, g->nbtm};
-  c.isbord = {g->isbord, g->nbtm};
-  c.poidsa = {g->poidsa, g->nbm};
-  c.Ylmso = {g->Ylmso, g->nsort};
-  c.Kar = {g->Kar, 64};
-  c.nspino = g->nspino;
-  c.ispin = e->ispin;
-  return c;
-}
+using namespace oracle;
 
 // One row of the matrix (abvr over lb1..lb2, stored at abvr[k - lb1]) and the
 // right-hand side smr(:, ii).  Real path of calcMatRow, source/mat.f90:1034-1632.
@@ -232,40 +177,19 @@ int check_supported(const fdmgpu_grid* g, const fdmgpu_energy* e) {
 
 }  // namespace
 
-extern "C" {
+namespace oracle {
 
-// Dense assembly of A (nligne x nligne, column-major) and B = smr (nlmso x nligne),
-// row by row with calcMatRow.  Used by the dense-LU known-answer test.
-int oracle_assemble_dense(const fdmgpu_grid* g, const fdmgpu_energy* e, double* A, double* smr) {
-  int st = check_supported(g, e);
-  if (st) return st;
-  Ctx c = make_ctx(g, e);
-  const int n = e->nligne;
-  std::vector<double> row;
-  for (int ii = 1; ii <= n; ++ii) {
-    const int l1 = e->lb1[ii - 1], l2 = e->lb2[ii - 1];
-    row.assign(l2 - l1 + 1, 0.0);
-    calc_mat_row(c, ii, row.data(), l1, smr + (int64_t)(ii - 1) * e->nlmso);
-    for (int k = l1; k <= l2; ++k) A[(int64_t)(ii - 1) + (int64_t)(k - 1) * n] = row[k - l1];
-  }
-  return 0;
-}
-
-// Gaussian profile solve, source/mat_solve_gaussian.f90:5-372 (real branch).
-// smr (nlmso, nligne) is zero on entry and holds the solution on return.
-int oracle_mat_solve(const fdmgpu_grid* g, const fdmgpu_energy* e, double* smr, int64_t* nnz_out,
-                     double* time_fill, double* time_tria, int32_t* bad_row) {
-  int st = check_supported(g, e);
-  if (st) return st;
-  Ctx c = make_ctx(g, e);
+int64_t symbolic_profile(const Ctx& c, std::vector<int32_t>& ind, std::vector<int32_t>& nb_not_zero,
+                         std::vector<int64_t>& lbz) {
+  const fdmgpu_grid* g = c.g;
+  const fdmgpu_energy* e = c.e;
   const int nligne = e->nligne, nlmso = e->nlmso, nspino = g->nspino;
   const int nligneso = e->nligneso;
   const int* newinv = e->newinv;
   const int* new_ = e->new_;
-  // Symbolic phase (:67-165): lower-part nonzero columns of each row after elimination.
   std::vector<char> colnz(nligne + 1, 0);
-  std::vector<int32_t> nb_not_zero(nligne + 1, 0);
-  std::vector<int64_t> lbz(nligne + 1, 0);
+  nb_not_zero.assign(nligne + 1, 0);
+  lbz.assign(nligne + 1, 0);
   std::vector<int32_t> ind_inv;
   int64_t nb_tot = 0;
   for (int pass = 1; pass <= 2; ++pass) {
@@ -319,11 +243,46 @@ int oracle_mat_solve(const fdmgpu_grid* g, const fdmgpu_energy* e, double* smr, 
       }
     }
   }
-  std::vector<int32_t> ind(nb_tot);
+  ind.assign(nb_tot, 0);
   for (int64_t lk = 1; lk <= nb_tot; ++lk) ind[lk - 1] = ind_inv[nb_tot + 1 - lk - 1];
   ind_inv.clear();
   lbz[1] = 0;
   for (int ii = 2; ii <= nligne; ++ii) lbz[ii] = lbz[ii - 1] + nb_not_zero[ii - 1];
+  return nb_tot;
+}
+
+}  // namespace oracle
+
+extern "C" {
+
+// Dense assembly of A (nligne x nligne, column-major) and B = smr (nlmso x nligne),
+// row by row with calcMatRow.  Used by the dense-LU known-answer test.
+int oracle_assemble_dense(const fdmgpu_grid* g, const fdmgpu_energy* e, double* A, double* smr) {
+  int st = check_supported(g, e);
+  if (st) return st;
+  Ctx c = make_ctx(g, e);
+  const int n = e->nligne;
+  std::vector<double> row;
+  for (int ii = 1; ii <= n; ++ii) {
+    const int l1 = e->lb1[ii - 1], l2 = e->lb2[ii - 1];
+    row.assign(l2 - l1 + 1, 0.0);
+    calc_mat_row(c, ii, row.data(), l1, smr + (int64_t)(ii - 1) * e->nlmso);
+    for (int k = l1; k <= l2; ++k) A[(int64_t)(ii - 1) + (int64_t)(k - 1) * n] = row[k - l1];
+  }
+  return 0;
+}
+
+// Gaussian profile solve, source/mat_solve_gaussian.f90:5-372 (real branch).
+// smr (nlmso, nligne) is zero on entry and holds the solution on return.
+int oracle_mat_solve(const fdmgpu_grid* g, const fdmgpu_energy* e, double* smr, int64_t* nnz_out,
+                     double* time_fill, double* time_tria, int32_t* bad_row) {
+  int st = check_supported(g, e);
+  if (st) return st;
+  Ctx c = make_ctx(g, e);
+  const int nligne = e->nligne, nlmso = e->nlmso;
+  std::vector<int32_t> ind, nb_not_zero;
+  std::vector<int64_t> lbz;
+  const int64_t nb_tot = symbolic_profile(c, ind, nb_not_zero, lbz);
   if (nnz_out) *nnz_out = nb_tot;
 
   // Filling, elimination and normalisation (:177-317).
@@ -380,7 +339,7 @@ int oracle_mat_solve(const fdmgpu_grid* g, const fdmgpu_energy* e, double* smr, 
   return 0;
 }
 
-// newind, source/mat.f90:1761-1921, regular solution (n_ato_RI = 1).
+// newind, source/mat.f90:1761-1921, regular solution (n_ato_RI = 1), nspino 1 or 2.
 // xyz4: (npsom) distance of each point; new_ has npoint+1 entries (index 0..npoint).
 int oracle_newind(const fdmgpu_grid* g, const double* xyz4, const double* distai, const int32_t* nlmsa, int nlmso,
                   int32_t nligne, int32_t* new_, int32_t* newinv, int32_t* ianew, int32_t* lb1, int32_t* lb2) {
@@ -422,6 +381,10 @@ int oracle_newind(const fdmgpu_grid* g, const double* xyz4, const double* distai
         lb2[r - 1] = nligne;
       }
     }
+    if (nspino == 2) {  // the point's spin-1 row has the same span (mat.f90:1841-1844)
+      lb1[r - 2] = lb1[r - 1];
+      lb2[r - 2] = lb2[r - 1];
+    }
   }
   I2 ibord{g->ibord, g->nbtm};
   for (int ia = 1; ia <= natome; ++ia) {
@@ -442,7 +405,10 @@ int oracle_newind(const fdmgpu_grid* g, const double* xyz4, const double* distai
   for (int r = 0; r < nligne; ++r) newinv[r] = 0;
   for (int i = 1; i <= npoint; ++i) {
     const int r = new_[i];
-    if (r != 0) newinv[r - 1] = i;
+    if (r != 0) {
+      newinv[r - 1] = i;
+      if (nspino == 2) newinv[r - 2] = i;
+    }
   }
   for (int ia = 1; ia <= natome; ++ia)
     for (int Lm = 1; Lm <= n_ato_RI * nlmsa[ia - 1]; ++Lm) newinv[ianew[ia - 1] + Lm - 1] = -ia;

@@ -1,0 +1,140 @@
+"""Known-answer tests that pin the complex (Cal_comp) branch of the oracle.
+
+The reference ships no tests or outputs and cannot be compiled here, so the
+complex restatement (oracle/oracle_complex.cpp) is pinned by relations that
+the reference's equations must satisfy:
+
+K1  the Gaussian profile solve equals a dense LU solve of the same assembled
+    complex matrix (with and without spin-orbit);
+K2  the complex machinery on real inputs (Cal_comp with the real basis and
+    real harmonics) gives a zero imaginary part and the real branch's solution;
+K3  the outgoing-wave (Hankel) basis gives the same Taull as the real basis
+    renormalised by (I + iS)^-1 (source/mat.f90:312-343) - two different
+    matrices, one physical answer;
+K4  spin-orbit with the coupling switched off (gradvr = 0, no relativistic
+    terms, spin-diagonal atomic solutions) decouples into two copies of the
+    complex-harmonic problem, bit for bit;
+K5  complex harmonics give Taull_c = U Taull_r U^H, U the unitary map of Yc
+    (source/mat.f90:1733-1754) from the real harmonics.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from fdmnes_gb300 import abi, cluster as CL, complex_path as CP
+
+E = 12.0
+
+
+@pytest.fixture(scope="module")
+def cu():
+    st = CL.small_cu_structure()
+    ga = abi.GridArgs(st)
+    ei = CL.energy_inputs(st, E)
+    ri = CL.newind(st, ei.nlmsa, ei.nlmso)
+    ea = abi.EnergyArgs(st, ei, ri)
+    X, _ = oracle.mat_solve(ga, ea)
+    return st, ga, ea, X
+
+
+@pytest.fixture(scope="module")
+def pt():
+    return CP.pt_so_structure()
+
+
+def _dense_rel(ga, ea):
+    X, _ = oracle.mat_solve_c(ga, ea)
+    A, B = oracle.assemble_dense_c(ga, ea)
+    Xd = np.linalg.solve(A, B.T).T
+    return np.abs(X - Xd).max() / np.abs(Xd).max()
+
+
+def test_k1_dense_lu_complex_harmonics(pt):
+    ga = abi.GridArgs(CP.grid_dict(pt, False))
+    ea = abi.EnergyArgs(CP.energy_dict(pt, E, spinorbit=False, ylm_comp=True))
+    assert _dense_rel(ga, ea) < 1e-12
+
+
+def test_k1_dense_lu_spin_orbit(pt):
+    """Spin-orbit with the relativistic and gradient terms and a model coupling
+    (nligne 1826, 200 right-hand sides); measured 2.5e-11."""
+    ga = abi.GridArgs(CP.grid_dict(pt, True))
+    ea = abi.EnergyArgs(CP.energy_dict(pt, E, spinorbit=True))
+    assert _dense_rel(ga, ea) < 1e-9
+
+
+def test_k2_complex_machinery_on_real_inputs(cu):
+    st, ga, ea, Xr = cu
+    d = dict(ea.d)
+    d.update(Cal_comp=1)
+    Xc, _ = oracle.mat_solve_c(ga, abi.EnergyArgs(d))
+    assert np.abs(Xc.imag).max() == 0.0
+    # the outer rows associate poidso*Y*Y differently in the two branches
+    assert np.abs(Xc.real - Xr).max() <= 1e-12 * np.abs(Xr).max()
+
+
+def test_k3_outgoing_basis_equals_renormalised_real_basis(cu):
+    st, ga, ea, Xr = cu
+    Tr = oracle.taull(ga, ea, Xr)
+    ea3 = abi.EnergyArgs(CP.energy_dict(st, E, spinorbit=False, ylm_comp=False))
+    X3, _ = oracle.mat_solve_c(ga, ea3)
+    T3 = oracle.taull_c(ga, ea3, X3, symmetrise=True)[:, 0, :, 0]
+    assert np.abs(T3 - Tr).max() <= 1e-11 * np.abs(Tr).max()
+
+
+def test_k4_spin_orbit_without_coupling_decouples(pt):
+    g = pt.grid
+    ga1 = abi.GridArgs(CP.grid_dict(pt, False))
+    ea1 = abi.EnergyArgs(CP.energy_dict(pt, E, spinorbit=False, ylm_comp=True))
+    X1, _ = oracle.mat_solve_c(ga1, ea1)
+    T1 = oracle.taull_c(ga1, ea1, X1, symmetrise=False)[:, 0, :, 0]
+    ga2 = abi.GridArgs(CP.grid_dict(pt, True))
+    ea2 = abi.EnergyArgs(CP.energy_dict(pt, E, spinorbit=True, relativistic=False, so_coupling=0.0,
+                                        gradvr=np.zeros((g.npoint, 3, 2), order="F")))
+    X2, _ = oracle.mat_solve_c(ga2, ea2)
+    T2 = oracle.taull_c(ga2, ea2, X2, symmetrise=False)
+    assert np.array_equal(T2[:, 0, :, 0], T1)
+    assert np.array_equal(T2[:, 1, :, 1], T1)
+    assert np.abs(T2[:, 0, :, 1]).max() == 0.0 and np.abs(T2[:, 1, :, 0]).max() == 0.0
+
+
+def test_k5_complex_harmonics_are_a_unitary_change_of_basis(cu):
+    st, ga, _, _ = cu
+    ear = abi.EnergyArgs(CP.energy_dict(st, E, spinorbit=False, ylm_comp=False))
+    eac = abi.EnergyArgs(CP.energy_dict(st, E, spinorbit=False, ylm_comp=True))
+    Tr = oracle.taull_c(ga, ear, oracle.mat_solve_c(ga, ear)[0], symmetrise=False)[:, 0, :, 0]
+    Tc = oracle.taull_c(ga, eac, oracle.mat_solve_c(ga, eac)[0], symmetrise=False)[:, 0, :, 0]
+    n = Tc.shape[0]
+    lmax = int(round(np.sqrt(n))) - 1
+    U = np.zeros((n, n), complex)
+    for L in range(lmax + 1):
+        for m in range(-L, L + 1):
+            e1 = np.zeros(n)
+            e2 = np.zeros(n)
+            e1[L * L + L + m] = 1.0
+            e2[L * L + L - m] = 1.0
+            U[L * L + L + m] = CP.yc(m, e1, e2)
+    assert np.allclose(U @ U.conj().T, np.eye(n), atol=1e-15)
+    assert np.abs(Tc - U @ Tr @ U.conj().T).max() <= 1e-12 * np.abs(Tc).max()
+
+
+def test_newind_spin_orbit_matches_oracle(pt):
+    """Row numbering with interleaved spin rows (nspino = 2): the package's
+    newind and the oracle's agree, and both spin rows of a point share its
+    span and its point (source/mat.f90:1841-1844,1883)."""
+    ga = abi.GridArgs(CP.grid_dict(pt, True))
+    ei = CL.energy_inputs(pt, E)
+    nlmsa = (2 * (ei.lmaxa + 1) ** 2).astype(np.int32)
+    nlmso = 2 * (ei.lmaxso + 1) ** 2
+    ri = CL.newind(pt, nlmsa, nlmso, 2)
+    g = pt.grid
+    new, newinv, ianew, lb1, lb2 = oracle.newind(ga, g.xyz[3], pt.distai, nlmsa, nlmso, ri.nligne, g.npoint,
+                                                 pt.natome)
+    assert np.array_equal(new, ri.new) and np.array_equal(newinv, ri.newinv)
+    assert np.array_equal(ianew, ri.ianew)
+    assert np.array_equal(lb1, ri.lb1) and np.array_equal(lb2, ri.lb2)
+    inter = np.nonzero(ri.new[1:])[0] + 1
+    rows = ri.new[inter]
+    assert np.array_equal(ri.newinv[rows - 1], inter) and np.array_equal(ri.newinv[rows - 2], inter)
+    assert np.array_equal(ri.lb1[rows - 2], ri.lb1[rows - 1])
+    assert np.array_equal(ri.lb2[rows - 2], ri.lb2[rows - 1])
