@@ -70,12 +70,15 @@ struct HostProb {
   double flops_factor = 0, flops_solve = 0;
   std::vector<int> in_i;
   std::vector<double> in_d;
+  // offsets inside in_d of the Vr, gradvr, phiato, Bessel and Neumann blocks
+  int64_t rel_grad = 0, rel_phi = 0, rel_bes = 0, rel_neu = 0;
   int nlmsa_max = 0;
   uint64_t sig = 0;
 };
 
 struct Batch {
   int precision = FDMGPU_PREC_FP64;
+  int cplx = -1;   // complex (1) or real (0) problems; -1 before the first energy
   int max_energies = 0;
   std::vector<HostProb> probs;
   // results
@@ -112,8 +115,9 @@ struct fdmgpu_handle {
   std::vector<int> numia_h, isrt_h, ibord_h, nbordf_h;
   std::vector<int> lato_h, mato_h;
   DevBuf<int> d_inter_pt, d_nb_kind, d_nb_idx, d_numia, d_nbord, d_nbordf, d_ibord, d_isbord, d_isrt, d_lato, d_mato,
-      d_lso, d_mso;
-  DevBuf<double> d_nb_coef, d_rvol, d_clapl, d_poidsa, d_poidso, d_Kar, d_YsoT, d_Ylmato;
+      d_lso, d_mso, d_iato, d_iso;
+  DevBuf<double> d_nb_coef, d_rvol, d_clapl, d_poidsa, d_poidso, d_Kar, d_YsoT, d_Ylmato, d_cgrad;
+  bool chars_c1 = false;  // every character the grid uses is 1 (Kar) with Kari = 0: what the complex path needs
   // batch pools
   Batch batch;
   DevBuf<Prob> d_probs;
@@ -174,8 +178,41 @@ uint64_t mix(uint64_t h, uint64_t v) {
   return h;
 }
 
+// Complex problems (Cal_comp): the complex outgoing basis with real energies,
+// complex or real harmonics, optionally spin-orbit (nspino = 2, two spin
+// blocks) and the relativistic terms; C1 characters; regular solution.
+fdmgpu_status check_energy_c(const fdmgpu_handle* h, const fdmgpu_energy* e) {
+  const fdmgpu_grid& g = h->g;
+  if (e->E_comp || e->irregular || e->Repres_comp || e->Base_hexa || e->Basereel || e->n_RI != 1 ||
+      e->n_ato_RI != 1 || e->nphiato7 != 2)
+    return fail(FDMGPU_ERR_UNSUPPORTED,
+                "this build's complex path: Cal_comp with real energies (E_comp false), the complex basis "
+                "(Basereel false), regular solution, complex phiato (nphiato7 = 2)");
+  if (!h->chars_c1) return fail(FDMGPU_ERR_UNSUPPORTED, "the complex path needs the C1 characters (Kar = 1, Kari = 0)");
+  if (e->Spinorbite != (g.nspino == 2)) return fail(FDMGPU_ERR_ARG, "Spinorbite must match the grid's nspino");
+  if (e->Spinorbite && (g.nspin != 2 || e->nspinp != 2 || e->nspinr != 2))
+    return fail(FDMGPU_ERR_UNSUPPORTED, "spin-orbit needs two spin blocks (nspin = nspinp = nspinr = 2)");
+  if (!e->Spinorbite && e->nspinr != 1) return fail(FDMGPU_ERR_ARG, "nspinr must be 1 without spin-orbit");
+  if (e->nligne <= 0 || e->nlmso <= 0 || e->nligneso != e->nligne - e->nlmso)
+    return fail(FDMGPU_ERR_ARG, "inconsistent nligne / nlmso / nligneso");
+  if ((int64_t)2 * e->nligne > (int64_t)1 << 30) return fail(FDMGPU_ERR_ARG, "nligne too large");
+  if (e->lmaxso < 0 || g.nspino * (e->lmaxso + 1) * (e->lmaxso + 1) < e->nlmso || e->nsort_r < g.nsort)
+    return fail(FDMGPU_ERR_ARG, "Bessel arrays too small for nlmso");
+  if (e->nlmso > g.nso1) return fail(FDMGPU_ERR_ARG, "nlmso exceeds the outer harmonic tables");
+  if (e->ispin < 1 || e->nspinp < std::min(e->ispin, g.nspin) || e->nphiato1 < g.nbtm)
+    return fail(FDMGPU_ERR_ARG, "phiato too small (nspinp or nphiato1)");
+  if (!e->new_ || !e->newinv || !e->lb1 || !e->lb2 || !e->ianew || !e->nlmsa || !e->Vr || !e->phiato ||
+      !e->Besselr || !e->Neumanr || ((e->Relativiste || e->Spinorbite) && !e->gradvr))
+    return fail(FDMGPU_ERR_ARG, "null array argument");
+  if ((e->Relativiste || e->Spinorbite) && e->nicm < g.npoint) return fail(FDMGPU_ERR_ARG, "gradvr too small (nicm)");
+  for (int Lm = 1; Lm <= e->nlmso; ++Lm)
+    if (F2(g.lso, g.nso1, Lm, 1) > e->lmaxso) return fail(FDMGPU_ERR_ARG, "outer harmonic above lmaxso");
+  return FDMGPU_OK;
+}
+
 fdmgpu_status check_energy(const fdmgpu_handle* h, const fdmgpu_energy* e) {
   if (!e) return fail(FDMGPU_ERR_ARG, "null energy arguments");
+  if (e->Cal_comp) return check_energy_c(h, e);
   if (e->Cal_comp || e->E_comp || e->Spinorbite || e->Relativiste || e->Repres_comp || e->Ylm_comp || e->irregular ||
       e->Base_hexa || e->n_RI != 1 || e->n_ato_RI != 1 || e->nphiato7 != 1 || h->g.nspino != 1 || !e->Basereel)
     return fail(FDMGPU_ERR_UNSUPPORTED,
@@ -196,14 +233,19 @@ fdmgpu_status check_energy(const fdmgpu_handle* h, const fdmgpu_energy* e) {
 
 // Band tile plan of one problem from newind's lb1/lb2.
 fdmgpu_status plan_problem(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& hp) {
-  const int n = e->nligne;
+  // a complex problem is planned as its real-equivalent system: complex row ii
+  // becomes rows 2ii-1 and 2ii, each spanning the columns 2 lb1 - 1 .. 2 lb2
+  const bool cplx = e->Cal_comp != 0;
+  const int n = cplx ? 2 * e->nligne : e->nligne;
+  auto lb1 = [&](int ii) { return cplx ? 2 * e->lb1[(ii + 1) / 2 - 1] - 1 : e->lb1[ii - 1]; };
+  auto lb2 = [&](int ii) { return cplx ? 2 * e->lb2[(ii + 1) / 2 - 1] : e->lb2[ii - 1]; };
   const int nt = (n + TS - 1) / TS;
   const int npad = nt * TS;
   std::vector<int> fl(npad), lu(npad);
   for (int p = 0; p < npad; ++p) {
     if (p < n) {
       const int ii = n - p;
-      const int l1 = e->lb1[ii - 1], l2 = e->lb2[ii - 1];
+      const int l1 = lb1(ii), l2 = lb2(ii);
       if (l1 < 1 || l2 > n || l1 > ii || l2 < ii) return fail(FDMGPU_ERR_ARG, "lb1/lb2 do not bracket the diagonal");
       fl[p] = n - l2;
       lu[p] = n - l1;
@@ -281,10 +323,19 @@ fdmgpu_status plan_problem(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& h
   P.nlmagm = e->nlmagm;
   P.ispin = e->ispin;
   P.enervide = e->Enervide;
+  P.cplx = cplx ? 1 : 0;
+  P.nligne_c = e->nligne;
+  P.so = e->Spinorbite ? 1 : 0;
+  P.rel = e->Relativiste ? 1 : 0;
+  P.ylmc = e->Ylm_comp ? 1 : 0;
+  P.nspinp = e->nspinp;
+  P.nspinr = std::max(1, e->nspinr);
+  P.nspin = g.nspin;
   // signature of the plan
   uint64_t s = mix(0, (uint64_t)n);
   s = mix(s, (uint64_t)e->nlmso);
-  for (int i = 0; i < n; i += 7) s = mix(s, (uint64_t)e->lb1[i] * 131 + (uint64_t)e->lb2[i]);
+  s = mix(s, (uint64_t)(P.cplx * 8 + P.so * 4 + P.rel * 2 + P.ylmc));
+  for (int i = 0; i < e->nligne; i += 7) s = mix(s, (uint64_t)e->lb1[i] * 131 + (uint64_t)e->lb2[i]);
   for (int ia = 0; ia < g.natome; ++ia) s = mix(s, (uint64_t)e->nlmsa[ia] * 1000003u + (uint64_t)e->ianew[ia]);
   hp.sig = s;
   return FDMGPU_OK;
@@ -301,6 +352,38 @@ void pack_inputs(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& hp) {
   hp.in_i.insert(hp.in_i.end(), e->nlmsa, e->nlmsa + g.natome);
   hp.nlmsa_max = 0;
   for (int ia = 0; ia < g.natome; ++ia) hp.nlmsa_max = std::max(hp.nlmsa_max, e->nlmsa[ia]);
+  if (e->Cal_comp) {
+    // Vr (npoint, nspin) | gradvr (npoint, 3, nspin) | phiato real part, imaginary part
+    // (nbtm, nlmagm, nspinp, nspino, natome) | Bessel, Neumann [nspinr][nsort][lmaxso+1]
+    hp.in_d.insert(hp.in_d.end(), e->Vr, e->Vr + (int64_t)g.npoint * g.nspin);
+    hp.rel_grad = (int64_t)hp.in_d.size();
+    for (int isp = 1; isp <= g.nspin; ++isp)
+      for (int k = 1; k <= 3; ++k)
+        for (int i = 1; i <= g.npoint; ++i)
+          hp.in_d.push_back(e->gradvr ? e->gradvr[(i - 1) + (int64_t)e->nicm * ((k - 1) + 3 * (int64_t)(isp - 1))]
+                                      : 0.0);
+    hp.rel_phi = (int64_t)hp.in_d.size();
+    const int64_t d1 = e->nphiato1, d2 = e->nlmagm, d3 = e->nspinp, d4 = g.nspino, d5 = e->n_RI, d6 = g.natome;
+    for (int part = 0; part < 2; ++part)
+      for (int ia = 1; ia <= g.natome; ++ia)
+        for (int isol = 1; isol <= g.nspino; ++isol)
+          for (int isp = 1; isp <= e->nspinp; ++isp)
+            for (int lm = 1; lm <= e->nlmagm; ++lm) {
+              const double* src =
+                  e->phiato + d1 * ((lm - 1) + d2 * ((isp - 1) + d3 * ((isol - 1) + d4 * (0 + d5 * ((ia - 1) + d6 * part)))));
+              hp.in_d.insert(hp.in_d.end(), src, src + g.nbtm);
+            }
+    const int nl = e->lmaxso + 1;
+    for (int which = 0; which < 2; ++which) {
+      (which == 0 ? hp.rel_bes : hp.rel_neu) = (int64_t)hp.in_d.size();
+      const double* a = which == 0 ? e->Besselr : e->Neumanr;
+      for (int isp = 1; isp <= std::max(1, e->nspinr); ++isp)
+        for (int ib = 0; ib < g.nsort; ++ib)
+          for (int L = 0; L < nl; ++L)
+            hp.in_d.push_back(a[ib + (int64_t)e->nsort_r * (L + (int64_t)nl * (isp - 1))]);
+    }
+    return;
+  }
   // doubles: Vr(:, ispp)
   const int ispp = std::min(e->ispin, g.nspin);
   hp.in_d.insert(hp.in_d.end(), e->Vr + (int64_t)g.npoint * (ispp - 1), e->Vr + (int64_t)g.npoint * ispp);
@@ -318,9 +401,12 @@ void pack_inputs(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& hp) {
     }
   // Bessel / Neumann (nsort_r, 0:lmaxso, ispq = 1) -> [ib][L]
   const int nl = e->lmaxso + 1;
+  hp.rel_grad = g.npoint;
+  hp.rel_phi = g.npoint;
   for (int which = 0; which < 2; ++which) {
     const double* a = which == 0 ? e->Besselr : e->Neumanr;
     const size_t b0 = hp.in_d.size();
+    (which == 0 ? hp.rel_bes : hp.rel_neu) = (int64_t)b0;
     hp.in_d.resize(b0 + (size_t)g.nsort * nl);
     for (int ib = 0; ib < g.nsort; ++ib)
       for (int L = 0; L < nl; ++L) hp.in_d[b0 + (size_t)ib * nl + L] = a[ib + (int64_t)e->nsort_r * L];
@@ -443,6 +529,8 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
       h->d_taull.reserve(2 * (size_t)std::max<int64_t>(taull, 1)) != cudaSuccess ||
       h->d_tscratch.reserve(2 * (size_t)std::max<int64_t>(scratch, 1)) != cudaSuccess)
     return fail(FDMGPU_ERR_NOMEM, "device allocation of the batch pools failed");
+  const bool cplx = h->batch.cplx == 1;
+  if (cplx && h->d_piv.reserve(rowv) != cudaSuccess) return fail(FDMGPU_ERR_NOMEM, "device allocation of the pivots");
   if (mixed) {
     if (h->d_env32.reserve((size_t)env * TS2) != cudaSuccess || h->d_Y32.reserve(rhs) != cudaSuccess ||
         h->d_rs.reserve(rowv) != cudaSuccess || h->d_cs.reserve(rowv) != cudaSuccess ||
@@ -475,6 +563,7 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   pl.amax = h->d_red.p + 2 * np;
   pl.taull = h->d_taull.p;
   pl.tscratch = h->d_tscratch.p;
+  if (cplx) pl.piv = h->d_piv.p;
   if (mixed) {
     pl.env32 = h->d_env32.p;
     pl.Y32 = h->d_Y32.p;
@@ -514,9 +603,10 @@ fdmgpu_status upload_inputs(fdmgpu_handle* h) {
     hp.P.in_nlmsa = hp.P.in_ianew + g.natome;
     ni += hp.in_i.size();
     hp.P.in_vr = nd;
-    hp.P.in_phi = nd + g.npoint;
-    hp.P.in_bes = hp.P.in_phi + (int64_t)g.nbtm * hp.P.nlmagm * g.natome;
-    hp.P.in_neu = hp.P.in_bes + (int64_t)g.nsort * (hp.P.lmaxso + 1);
+    hp.P.in_grad = nd + hp.rel_grad;
+    hp.P.in_phi = nd + hp.rel_phi;
+    hp.P.in_bes = nd + hp.rel_bes;
+    hp.P.in_neu = nd + hp.rel_neu;
     nd += hp.in_d.size();
   }
   if (ni > h->h_pinned_i_cap) {
@@ -569,7 +659,10 @@ void record_asm(fdmgpu_handle* h) {
   cudaMemsetAsync(pl.env64, 0, env * sizeof(double), s);
   cudaMemsetAsync(pl.B64, 0, rhs * sizeof(double), s);
   cudaMemsetAsync(pl.err, 0, np * sizeof(int), s);
-  launch_assemble(h->d_sites.p, probs, pl, h->tb, h->dims, s);
+  if (h->batch.cplx == 1)
+    launch_assemble_c(h->d_sites.p, probs, pl, h->tb, h->dims, 0, s);
+  else
+    launch_assemble(h->d_sites.p, probs, pl, h->tb, h->dims, s);
   if (h->batch.precision == FDMGPU_PREC_FP64) {
     cudaMemcpyAsync(pl.X64, pl.B64, rhs * sizeof(double), cudaMemcpyDeviceToDevice, s);
   } else {
@@ -584,9 +677,12 @@ void record_factor_window(fdmgpu_handle* h, int threads, int k_begin, int k_end)
   cudaStream_t s = h->stream;
   const Pools& pl = h->pl;
   const int np = h->dims.nprob;
+  // the real-equivalent form of a complex problem pivots inside the diagonal
+  // tiles (the real part of a complex pivot can vanish); real problems keep
+  // the reference's elimination order
   if (h->batch.precision == FDMGPU_PREC_FP64)
-    launch_factor<double>(h->sp, pl.env64, pl.X64, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-10, nullptr, s,
-                          threads, k_begin, k_end);
+    launch_factor<double>(h->sp, pl.env64, pl.X64, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-10,
+                          h->batch.cplx == 1 ? pl.piv : nullptr, s, threads, k_begin, k_end);
   else
     launch_factor<float>(h->sp, pl.env32, pl.Y32, h->d_probs.p, h->tb, np, 1, nullptr, pl.err, 1e-30, pl.piv, s,
                          threads, k_begin, k_end);
@@ -1071,8 +1167,15 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
       if (!(b.resid[k] <= tol_accept)) b.err[k] = FDMGPU_ERR_NOT_CONVERGED;
   }
   if (b.probs[0].P.nlm_abs > 0) {
-    launch_taull(h->d_probs.p, h->pl, h->dims, h->pl.X64, h->stream);
-    nkern += 1;
+    if (b.cplx == 1) {
+      int mx = 0;
+      for (auto& hp : b.probs) mx = std::max(mx, hp.P.nlm_abs);
+      launch_taull_c(h->d_sites.p, h->d_probs.p, h->pl, h->dims, mx, h->stream);
+      nkern += 2;
+    } else {
+      launch_taull(h->d_probs.p, h->pl, h->dims, h->pl.X64, h->stream);
+      nkern += 1;
+    }
   }
   std::vector<int> err(np);
   CK(cudaMemcpyAsync(err.data(), h->d_err.p, np * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
@@ -1159,7 +1262,7 @@ void fdmgpu_get_solver_params(int32_t* mpi_host_num_for_mumps, char solver[6]) {
 fdmgpu_status fdmgpu_create(const fdmgpu_grid* g, fdmgpu_handle** out) {
   if (!g || !out) return fail(FDMGPU_ERR_ARG, "null argument");
   *out = nullptr;
-  if (g->nspino != 1 || g->ngrph < 1) return fail(FDMGPU_ERR_UNSUPPORTED, "nspino = 1 only in this build");
+  if ((g->nspino != 1 && g->nspino != 2) || g->ngrph < 1) return fail(FDMGPU_ERR_ARG, "nspino must be 1 or 2");
   if (g->npoint <= 0 || g->npsom < g->npoint || g->nvois <= 0 || g->natome < 0)
     return fail(FDMGPU_ERR_ARG, "inconsistent grid sizes");
   fdmgpu_handle* h = new fdmgpu_handle();
@@ -1230,6 +1333,20 @@ fdmgpu_status fdmgpu_create(const fdmgpu_grid* g, fdmgpu_handle** out) {
     h->nb_atoms_h.push_back(atoms);
   }
   h->nbordf_h.assign(g->nbordf, g->nbordf + g->natome);
+  // the complex path folds no characters: every one the grid uses must be 1
+  h->chars_c1 = g->ngrph == 1 && g->Kar && g->Kari;
+  for (int i = 1; h->chars_c1 && i <= g->npoint; ++i)
+    for (int iv = 1; iv <= nv && h->chars_c1; ++iv) {
+      const int is = std::abs(F2(g->isvois, g->npsom, i, iv));
+      for (int sp = 0; sp < g->nspino; ++sp)
+        if (is < 1 || is > 64 || g->Kar[is - 1 + 64 * sp] != 1.0 || g->Kari[is - 1 + 64 * sp] != 0.0) h->chars_c1 = false;
+    }
+  for (int ia = 1; h->chars_c1 && ia <= g->natome; ++ia)
+    for (int ib = 1; ib <= g->nbord[ia - 1] && h->chars_c1; ++ib) {
+      const int is = std::abs(F2(g->isbord, g->nbtm, ib, ia));
+      for (int sp = 0; sp < g->nspino; ++sp)
+        if (is < 1 || is > 64 || g->Kar[is - 1 + 64 * sp] != 1.0 || g->Kari[is - 1 + 64 * sp] != 0.0) h->chars_c1 = false;
+    }
   cudaStream_t s = h->stream;
   auto up_i = [&](DevBuf<int>& b, const int32_t* p, size_t n) {
     return upload(b, std::vector<int>(p, p + n), s);
@@ -1252,6 +1369,12 @@ fdmgpu_status fdmgpu_create(const fdmgpu_grid* g, fdmgpu_handle** out) {
   e = e ? e : up_i(h->d_mato, g->mato, (size_t)g->nlmsam * g->natome);
   e = e ? e : up_i(h->d_lso, g->lso, g->nso1);
   e = e ? e : up_i(h->d_mso, g->mso, g->nso1);
+  // spin and gradient tables are read by the complex path only; absent ones read as 1 and 0
+  e = e ? e : (g->iato ? up_i(h->d_iato, g->iato, (size_t)g->nlmsam * g->natome)
+                       : upload(h->d_iato, std::vector<int>((size_t)g->nlmsam * g->natome, 1), s));
+  e = e ? e : (g->iso ? up_i(h->d_iso, g->iso, g->nso1) : upload(h->d_iso, std::vector<int>(g->nso1, 1), s));
+  e = e ? e : (g->cgrad ? up_d(h->d_cgrad, g->cgrad, g->nvois)
+                        : upload(h->d_cgrad, std::vector<double>(g->nvois, 0.0), s));
   e = e ? e : up_d(h->d_rvol, g->rvol, g->nim);
   e = e ? e : up_d(h->d_clapl, g->clapl, g->nvois + 1);
   e = e ? e : up_d(h->d_poidsa, g->poidsa, (size_t)g->nbm * g->natome);
@@ -1302,6 +1425,11 @@ fdmgpu_status fdmgpu_create(const fdmgpu_grid* g, fdmgpu_handle** out) {
   S.mato = h->d_mato.p;
   S.lso = h->d_lso.p;
   S.mso = h->d_mso.p;
+  S.iato = h->d_iato.p;
+  S.iso = h->d_iso.p;
+  S.cgrad = h->d_cgrad.p;
+  S.nspino = g->nspino;
+  S.nspin = g->nspin;
   setup_factor_kernels<float>();
   setup_factor_kernels<double>();
   setup_factor_kernels<dfl>();
@@ -1321,12 +1449,13 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   DevBuf<int>* ib[] = {&h->d_inter_pt, &h->d_nb_kind, &h->d_nb_idx, &h->d_numia, &h->d_nbord, &h->d_nbordf,
                        &h->d_ibord,    &h->d_isbord,  &h->d_isrt,   &h->d_lato,  &h->d_mato,  &h->d_lso,
                        &h->d_mso,      &h->d_J0,      &h->d_J1,     &h->d_Imax,  &h->d_Imin,  &h->d_ipool,
-                       &h->d_rowptr,   &h->d_col,     &h->d_err,    &h->d_active, &h->d_piv};
+                       &h->d_rowptr,   &h->d_col,     &h->d_err,    &h->d_active, &h->d_piv,   &h->d_iato,
+                       &h->d_iso};
   for (auto* b : ib) b->release();
   DevBuf<double>* db[] = {&h->d_nb_coef, &h->d_rvol, &h->d_clapl, &h->d_poidsa, &h->d_poidso, &h->d_Kar,
                           &h->d_YsoT,    &h->d_Ylmato, &h->d_dpool, &h->d_env64, &h->d_B64,  &h->d_X64,
                           &h->d_rs,      &h->d_cs,   &h->d_val,   &h->d_taull,  &h->d_tscratch, &h->d_smr,
-                          &h->d_gT,      &h->d_lam,  &h->d_gpart, &h->d_grad};
+                          &h->d_gT,      &h->d_lam,  &h->d_gpart, &h->d_grad,  &h->d_cgrad};
   for (auto* b : db) b->release();
   h->d_env32.release();
   h->d_val2.release();
@@ -1427,6 +1556,7 @@ fdmgpu_status fdmgpu_batch_begin(fdmgpu_handle* h, int32_t precision, int32_t ma
   if (precision != FDMGPU_PREC_FP64 && precision != FDMGPU_PREC_MIXED)
     return fail(FDMGPU_ERR_ARG, "unknown precision");
   h->batch.probs.clear();
+  h->batch.cplx = -1;
   h->batch.sites.assign(1, h);
   h->batch.precision = precision;
   h->batch.max_energies = max_energies;
@@ -1445,6 +1575,11 @@ fdmgpu_status fdmgpu_batch_add_site(fdmgpu_handle* h, fdmgpu_handle* site, const
   if (b.max_energies > 0 && (int)b.probs.size() >= b.max_energies) return fail(FDMGPU_ERR_ARG, "batch is full");
   int si = (int)(std::find(b.sites.begin(), b.sites.end(), site) - b.sites.begin());
   if (si == (int)b.sites.size()) b.sites.push_back(site);
+  const int cplx = e->Cal_comp ? 1 : 0;
+  if (b.cplx >= 0 && b.cplx != cplx) return fail(FDMGPU_ERR_ARG, "a batch holds either real or complex problems");
+  if (cplx && b.precision != FDMGPU_PREC_FP64)
+    return fail(FDMGPU_ERR_UNSUPPORTED, "complex problems are solved in FP64 in this build");
+  if (cplx && b.sites.size() > 1) return fail(FDMGPU_ERR_UNSUPPORTED, "complex problems of several sites in one batch");
   HostProb hp;
   st = plan_problem(site, e, hp);
   if (st) return st;
@@ -1454,11 +1589,32 @@ fdmgpu_status fdmgpu_batch_add_site(fdmgpu_handle* h, fdmgpu_handle* site, const
     hp.P.iaabs = iaabs;
     hp.P.nlm_abs = e->nlmsa[iaabs - 1];
     hp.P.ianew_abs = e->ianew[iaabs - 1];
-    for (int lm = 1; lm <= hp.P.nlm_abs; ++lm) {
-      const int L = F2(g.lato, g.nlmsam, lm, iaabs), m = F2(g.mato, g.nlmsam, lm, iaabs);
-      if (L * L + L + 1 + m != lm) return fail(FDMGPU_ERR_UNSUPPORTED, "Taull needs the C1 harmonic order");
+    if (cplx) {
+      // every (L, m, spin) up to the absorber's lmax once, so that Taull is dense
+      // in (L^2 + L + m, spin) on both sides
+      const int nsp = g.nspino;
+      int lmax = 0;
+      std::vector<int> seen;
+      for (int lm = 1; lm <= hp.P.nlm_abs; ++lm) lmax = std::max(lmax, F2(g.lato, g.nlmsam, lm, iaabs));
+      const int nlmq = (lmax + 1) * (lmax + 1);
+      if (hp.P.nlm_abs != nsp * nlmq) return fail(FDMGPU_ERR_UNSUPPORTED, "Taull needs complete absorber harmonic tables");
+      seen.assign(nsp * nlmq, 0);
+      for (int lm = 1; lm <= hp.P.nlm_abs; ++lm) {
+        const int L = F2(g.lato, g.nlmsam, lm, iaabs), m = F2(g.mato, g.nlmsam, lm, iaabs);
+        const int is = nsp == 2 ? F2(g.iato, g.nlmsam, lm, iaabs) : 1;
+        if (m < -L || m > L || is < 1 || is > nsp || seen[(L * L + L + m) + nlmq * (is - 1)]++)
+          return fail(FDMGPU_ERR_UNSUPPORTED, "Taull needs complete absorber harmonic tables");
+      }
+      if ((int64_t)hp.P.nlm_abs * hp.P.nlm_abs > (int64_t)e->nlmso * (e->nlmso + 2 * hp.P.nlm_abs))
+        return fail(FDMGPU_ERR_UNSUPPORTED, "absorber harmonics exceed the Taull scratch");
+    } else {
+      for (int lm = 1; lm <= hp.P.nlm_abs; ++lm) {
+        const int L = F2(g.lato, g.nlmsam, lm, iaabs), m = F2(g.mato, g.nlmsam, lm, iaabs);
+        if (L * L + L + 1 + m != lm) return fail(FDMGPU_ERR_UNSUPPORTED, "Taull needs the C1 harmonic order");
+      }
     }
   }
+  b.cplx = cplx;
   hp.sig = mix(hp.sig, (uint64_t)hp.P.nlm_abs * 7919u + (uint64_t)hp.P.ianew_abs);
   hp.sig = mix(hp.sig, (uint64_t)si * 104729u + 1u);
   pack_inputs(site, e, hp);
@@ -1528,16 +1684,29 @@ fdmgpu_status fdmgpu_batch_stats(fdmgpu_handle* h, int32_t k, int32_t* iters, do
 
 fdmgpu_status fdmgpu_mat_solve(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t precision, double* smr, double* smi,
                                fdmgpu_info* info) {
-  (void)smi;
-  if (!h || !smr) return fail(FDMGPU_ERR_ARG, "null argument");
+  if (!h || !smr || !e) return fail(FDMGPU_ERR_ARG, "null argument");
+  if (e->Cal_comp && !smi) return fail(FDMGPU_ERR_ARG, "a complex problem needs smi");
   fdmgpu_status st = fdmgpu_batch_begin(h, precision, 1);
   if (st) return st;
   st = fdmgpu_batch_add(h, e, 0);
   if (st) return st;
   st = fdmgpu_batch_run(h, info);
   if (st && st != FDMGPU_ERR_NOT_CONVERGED) return st;
-  fdmgpu_status st2 = fdmgpu_batch_solution(h, 0, smr);
-  return st2 ? st2 : st;
+  if (!e->Cal_comp) {
+    fdmgpu_status st2 = fdmgpu_batch_solution(h, 0, smr);
+    return st2 ? st2 : st;
+  }
+  // real-equivalent solution: row 2ii-1 holds Re x(ii), row 2ii Im x(ii)
+  const int64_t n = e->nligne, m = e->nlmso;
+  std::vector<double> xe((size_t)(2 * n * m));
+  fdmgpu_status st2 = fdmgpu_batch_solution(h, 0, xe.data());
+  if (st2) return st2;
+  for (int64_t ii = 0; ii < n; ++ii)
+    for (int64_t l = 0; l < m; ++l) {
+      smr[l + m * ii] = xe[(size_t)(l + m * (2 * ii))];
+      smi[l + m * ii] = xe[(size_t)(l + m * (2 * ii + 1))];
+    }
+  return st;
 }
 
 // Adjoint solve of a mixed batch: A^T Lambda = G with the batch's factors of the

@@ -59,6 +59,15 @@ struct Prob {
   int64_t in_neu;     // offset of Neumann n(ib, L), [nsort][lmaxso+1]
   int64_t taull;      // offset of Taull (complex) for this problem
   int64_t scratch;    // offset of the complex nlmso x (nlmso + nlm_abs) Taull scratch
+  // complex (Cal_comp) problems, stored as the real-equivalent system: complex
+  // row ii (1-based) becomes rows 2ii-1 (real part) and 2ii (imaginary part)
+  // of an order-2n real system, each complex entry a the 2x2 block
+  // [Re a, -Im a; Im a, Re a]; n above is then 2 nligne.
+  int cplx;           // 0 real, 1 complex
+  int nligne_c;       // complex order (nligne)
+  int so, rel, ylmc;  // Spinorbite, Relativiste, Ylm_comp
+  int nspinp, nspinr, nspin;
+  int64_t in_grad;    // offset of gradvr(npoint, 3, nspin) in the double pool
 };
 
 // Per tile-row / tile-column tables of a problem, at Prob::trow.
@@ -104,6 +113,10 @@ struct StaticDev {
   const int* mato;
   const int* lso;          // (nso1)
   const int* mso;
+  const int* iato;         // (nlmsam, natome) spin of each atom harmonic (spin-orbit)
+  const int* iso;          // (nso1) spin of each outer harmonic
+  const double* cgrad;     // (nvois) gradient coefficients
+  int nspino, nspin;
 };
 
 // -------------------------------------------------------------------------

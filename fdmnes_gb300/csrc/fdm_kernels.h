@@ -95,6 +95,11 @@ struct LaunchDims {
 
 void launch_assemble(const StaticDev* sites, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
                      cudaStream_t s);
+// Complex problems in their real-equivalent form (complex.cu).
+void launch_assemble_c(const StaticDev* sites, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
+                       int basereel, cudaStream_t s);
+void launch_taull_c(const StaticDev* sites, const Prob* probs, const Pools& pl, const LaunchDims& d, int max_nlm,
+                    cudaStream_t s);
 void launch_equilibrate_convert(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s);
 void launch_csr(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s);
 // X64 = cs * Y32 (first solve) or X64 += cs * Y32 (refinement), with max reductions.

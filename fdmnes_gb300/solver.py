@@ -165,6 +165,24 @@ class FdmSolver:
         d["converged"] = st == 0
         return smr, d
 
+    def mat_solve_complex(self, ea: abi.EnergyArgs, precision: str = "fp64") -> Tuple[np.ndarray, dict]:
+        """mat_solve of a complex (Cal_comp) problem: the solution smr + i smi
+        (nlmso, nligne) and diagnostics.  The handle's grid must carry the
+        problem's nspino (``complex_path.grid_dict``)."""
+        smr = np.zeros((ea.nlmso, ea.nligne), order="F")
+        smi = np.zeros((ea.nlmso, ea.nligne), order="F")
+        info = abi.FdmInfo()
+        _check(self.lib.fdmgpu_mat_solve(self.h, C.addressof(ea.s), PREC[precision], smr.ctypes.data,
+                                         smi.ctypes.data, C.addressof(info)))
+        return smr + 1j * smi, info_dict(info)
+
+    def taull_c(self, k: int, nspino: int) -> np.ndarray:
+        """Taull of a complex batch energy as (nlm, nspino, nlm, nspino), indexed
+        by L^2 + L + m and spin on both sides."""
+        t = self.taull(k)
+        n = t.shape[0] // nspino
+        return t.reshape((n, nspino, n, nspino), order="F").copy()
+
     def spectrum_begin(self, precision: str, n: int):
         _check(self.lib.fdmgpu_batch_begin(self.h, PREC[precision], n))
         self._batch_args = []

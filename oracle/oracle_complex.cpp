@@ -133,7 +133,7 @@ void calc_mat_row_c(const Ctx& c, int ii, cdouble* row, int lb1, cdouble* rhs) {
     const int isp = std::min(ispin, nspino);
     const double VmE = e->Vr[(i - 1) + (int64_t)g->npoint * (ispp - 1)] - e->Enervide;
     A(ii) = cdouble(VmE - g->clapl[0], e->E_comp ? -e->Eimag : 0.0);
-    if (e->Relativiste) A(ii) -= a2s4 * VmE * VmE;
+    if (e->Relativiste) A(ii) -= a2s4 * (VmE * VmE);   // a2s4 * VmE**2
     double bder = 0.0;
     if (e->Relativiste || e->Spinorbite) bder = -a2s4 / (1.0 - a2s4 * VmE);
     double cfvs_r[2] = {0.0, 0.0}, cfvs_i[2] = {0.0, 0.0};

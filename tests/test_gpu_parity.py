@@ -286,3 +286,64 @@ def test_every_refinement_and_escalation_mode(solver_mod):
         assert err < 1e-5, (refine, esc, err)
         assert xanes.convolved_relative_error(energies, T, T64) < 1e-6, (refine, esc)
     sv.close()
+
+
+def _complex_case(spinorbit: bool, energy: float = 12.0):
+    from fdmnes_gb300 import abi, complex_path as CP
+    st = CP.pt_so_structure()
+    ga = abi.GridArgs(CP.grid_dict(st, spinorbit))
+    ea = abi.EnergyArgs(CP.energy_dict(st, energy, spinorbit=spinorbit, ylm_comp=True))
+    return st, ga, ea
+
+
+@pytest.mark.parametrize("spinorbit", [False, True])
+def test_complex_fp64_matches_oracle(solver_mod, spinorbit):
+    """Complex problems (Cal_comp: complex harmonics; with spin-orbit two
+    interleaved spin rows per point and the relativistic and gradient terms)
+    solved on the GPU in their real-equivalent form with tile-local pivoting,
+    against the oracle's complex Gaussian solve, and Taull against the
+    oracle's.  Bar 1e-9 relative (the spin-orbit matrices' own conditioning
+    puts the dense-LU cross-check of the oracle at 2.5e-11)."""
+    import oracle
+    st, ga, ea = _complex_case(spinorbit)
+    X0, _ = oracle.mat_solve_c(ga, ea)
+    T0 = oracle.taull_c(ga, ea, X0)
+    sv = solver_mod.FdmSolver(ga.d)
+    X, _ = sv.mat_solve_complex(ea, "fp64")
+    assert rel(X, X0) < 1e-9
+    nsp = 2 if spinorbit else 1
+    sv.spectrum_begin("fp64", 1)
+    sv.spectrum_add_args(ea)
+    sv.spectrum_run()
+    T = sv.taull_c(0, nsp)
+    assert np.abs(T - T0).max() <= 1e-9 * np.abs(T0).max()
+    sv.close()
+
+
+def test_complex_batch_of_energies(solver_mod):
+    """Several spin-orbit energies in one batch (different orders and outer
+    harmonics per energy) agree with one-by-one oracle solves."""
+    import oracle
+    from fdmnes_gb300 import abi, complex_path as CP
+    st = CP.pt_so_structure()
+    ga = abi.GridArgs(CP.grid_dict(st, True))
+    eas = [abi.EnergyArgs(CP.energy_dict(st, E, spinorbit=True)) for E in (3.0, 20.0)]
+    sv = solver_mod.FdmSolver(ga.d)
+    sv.spectrum_begin("fp64", len(eas))
+    for ea in eas:
+        sv.spectrum_add_args(ea)
+    sv.spectrum_run()
+    for k, ea in enumerate(eas):
+        X0, _ = oracle.mat_solve_c(ga, ea)
+        T0 = oracle.taull_c(ga, ea, X0)
+        assert np.abs(sv.taull_c(k, 2) - T0).max() <= 1e-9 * np.abs(T0).max()
+    sv.close()
+
+
+def test_complex_mixed_precision_is_rejected(solver_mod):
+    """Complex problems are solved in FP64 in this build: the mixed path says so."""
+    st, ga, ea = _complex_case(True)
+    sv = solver_mod.FdmSolver(ga.d)
+    with pytest.raises(solver_mod.FdmError):
+        sv.mat_solve_complex(ea, "mixed")
+    sv.close()
