@@ -194,7 +194,11 @@ void fdmgpu_destroy(fdmgpu_handle* h);
  * source/mat_solve_mumps.f90:5-261): assemble the FDM matrix and the right-hand
  * sides of one energy on the GPU, factorise, solve, and write the solution into
  * smr (nlmso, nligne) column-major (and smi when Cal_comp).  Synchronous.
- * smr/smi are host pointers.  info may be NULL. */
+ * smr/smi are host pointers.  info may be NULL.
+ * Complex problems (Cal_comp: complex harmonics, spin-orbit with nspino = 2,
+ * relativistic terms; real energies, complex basis, C1 characters) are
+ * solved in FP64 as their real-equivalent system with tile-local pivoting;
+ * precision must be FDMGPU_PREC_FP64 for them and smi must be given. */
 fdmgpu_status fdmgpu_mat_solve(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t precision,
                                double* smr, double* smi, fdmgpu_info* info);
 
@@ -253,12 +257,16 @@ fdmgpu_status fdmgpu_batch_run(fdmgpu_handle* h, fdmgpu_info* info);
  * copies): the device-resident timing of a spectrum.  No counterpart in the
  * reference. */
 fdmgpu_status fdmgpu_batch_rerun(fdmgpu_handle* h, fdmgpu_info* info);
-/* Taull of energy k (0-based, in add order): writes nlm*nlm complex values. */
+/* Taull of energy k (0-based, in add order): writes nlm*nlm complex values,
+ * column-major, indexed by Lm0 - 1 = L^2 + L + m on both sides.  For a complex
+ * batch nlm = nspino * (lmax + 1)^2 and the index is (Lm0 - 1) + (lmax + 1)^2
+ * (spin - 1), the reference's Taull(Lm0, spin, Lm0', spin'). */
 fdmgpu_status fdmgpu_batch_taull(fdmgpu_handle* h, int32_t k, double* taull, int32_t* nlm);
 /* Taull of every energy in one copy: nlm_k*nlm_k complex values per energy,
  * concatenated in add order (capacity counts doubles). */
 fdmgpu_status fdmgpu_batch_taull_all(fdmgpu_handle* h, double* taull, int64_t capacity);
-/* Solution of energy k (nlmso, nligne) column-major into smr (host). */
+/* Solution of energy k (nlmso, nligne) column-major into smr (host).  For a
+ * complex batch (nlmso, 2 nligne): column 2ii-1 holds Re x(ii), 2ii Im x(ii). */
 fdmgpu_status fdmgpu_batch_solution(fdmgpu_handle* h, int32_t k, double* smr);
 /* Per-energy diagnostics of the last run: refinement (outer) iterations,
  * final relative correction max|dx|/max|x|, whether the energy was solved
