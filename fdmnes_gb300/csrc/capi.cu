@@ -186,7 +186,7 @@ fdmgpu_status check_energy_c(const fdmgpu_handle* h, const fdmgpu_energy* e) {
   if (e->E_comp || e->irregular || e->Repres_comp || e->Base_hexa || e->Basereel || e->n_RI != 1 ||
       e->n_ato_RI != 1 || e->nphiato7 != 2)
     return fail(FDMGPU_ERR_UNSUPPORTED,
-                "this build's complex path: Cal_comp with real energies (E_comp false), the complex basis "
+                "the library's complex path: Cal_comp with real energies (E_comp false), the complex basis "
                 "(Basereel false), regular solution, complex phiato (nphiato7 = 2)");
   if (!h->chars_c1) return fail(FDMGPU_ERR_UNSUPPORTED, "the complex path needs the C1 characters (Kar = 1, Kari = 0)");
   if (e->Spinorbite != (g.nspino == 2)) return fail(FDMGPU_ERR_ARG, "Spinorbite must match the grid's nspino");
@@ -216,7 +216,7 @@ fdmgpu_status check_energy(const fdmgpu_handle* h, const fdmgpu_energy* e) {
   if (e->Cal_comp || e->E_comp || e->Spinorbite || e->Relativiste || e->Repres_comp || e->Ylm_comp || e->irregular ||
       e->Base_hexa || e->n_RI != 1 || e->n_ato_RI != 1 || e->nphiato7 != 1 || h->g.nspino != 1 || !e->Basereel)
     return fail(FDMGPU_ERR_UNSUPPORTED,
-                "this build provides the real-arithmetic regular solution (Cal_comp = E_comp = Spinorbite = "
+                "the library provides the real-arithmetic regular solution (Cal_comp = E_comp = Spinorbite = "
                 "Relativiste = irregular = false, Basereel = true, nspino = 1)");
   if (e->nligne <= 0 || e->nlmso <= 0 || e->nligneso != e->nligne - e->nlmso)
     return fail(FDMGPU_ERR_ARG, "inconsistent nligne / nlmso / nligneso");
@@ -301,16 +301,21 @@ fdmgpu_status plan_problem(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& h
   hp.flops_factor = ff;
   hp.flops_solve = 2.0 * e->nlmso * (double)(nnzL + nnzU + n);
   hp.nnz_profile = nnzL + nnzU + n;
-  // CSR capacity: structural nonzeros of calcMatRow
+  // CSR capacity: structural nonzeros of calcMatRow (a grid point has nspino
+  // rows, each reaching both spin rows of its interstitial neighbours); in the
+  // real-equivalent form every complex entry is a 2x2 block
   const fdmgpu_grid& g = h->g;
-  int64_t cap = (npad - n);
+  const int nso = g.nspino;
+  int64_t cap = 0;
   for (size_t k = 0; k < h->inter_pt_h.size(); ++k) {
-    cap += 1 + h->n_inter_h[k] + (h->has_outer_h[k] ? e->nlmso : 0);
-    for (int ia : h->nb_atoms_h[k]) cap += e->nlmsa[ia - 1];
+    int64_t row = 1 + (int64_t)nso * h->n_inter_h[k] + (h->has_outer_h[k] ? e->nlmso : 0);
+    for (int ia : h->nb_atoms_h[k]) row += e->nlmsa[ia - 1];
+    cap += nso * row;
   }
   cap += (int64_t)e->nlmso * (e->nlmso + g.nsortf);
   for (int ia = 1; ia <= g.natome; ++ia) cap += (int64_t)e->nlmsa[ia - 1] * (h->nbordf_h[ia - 1] + e->nlmsa[ia - 1]);
-  hp.nnz_cap = cap;
+  if (cplx) cap *= 4;
+  hp.nnz_cap = cap + (npad - n);
   // descriptor (offsets filled later)
   Prob& P = hp.P;
   memset(&P, 0, sizeof(P));
@@ -1578,7 +1583,7 @@ fdmgpu_status fdmgpu_batch_add_site(fdmgpu_handle* h, fdmgpu_handle* site, const
   const int cplx = e->Cal_comp ? 1 : 0;
   if (b.cplx >= 0 && b.cplx != cplx) return fail(FDMGPU_ERR_ARG, "a batch holds either real or complex problems");
   if (cplx && b.precision != FDMGPU_PREC_FP64)
-    return fail(FDMGPU_ERR_UNSUPPORTED, "complex problems are solved in FP64 in this build");
+    return fail(FDMGPU_ERR_UNSUPPORTED, "the library solves complex problems in FP64");
   if (cplx && b.sites.size() > 1) return fail(FDMGPU_ERR_UNSUPPORTED, "complex problems of several sites in one batch");
   HostProb hp;
   st = plan_problem(site, e, hp);

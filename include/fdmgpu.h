@@ -36,7 +36,7 @@ extern "C" {
 typedef enum {
   FDMGPU_OK = 0,
   FDMGPU_ERR_ARG = 1,          /* invalid argument / inconsistent sizes          */
-  FDMGPU_ERR_UNSUPPORTED = 2,  /* flag combination not provided by this build     */
+  FDMGPU_ERR_UNSUPPORTED = 2,  /* flag combination the library does not provide   */
   FDMGPU_ERR_CUDA = 3,         /* CUDA runtime error (message via fdmgpu_last_error) */
   FDMGPU_ERR_ZERO_PIVOT = 4,   /* |pivot| below threshold: the reference stops here */
   FDMGPU_ERR_NOT_CONVERGED = 5,/* mixed precision refinement did not converge      */

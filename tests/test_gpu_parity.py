@@ -341,7 +341,7 @@ def test_complex_batch_of_energies(solver_mod):
 
 
 def test_complex_mixed_precision_is_rejected(solver_mod):
-    """Complex problems are solved in FP64 in this build: the mixed path says so."""
+    """The library solves complex problems in FP64: the mixed path says so."""
     st, ga, ea = _complex_case(True)
     sv = solver_mod.FdmSolver(ga.d)
     with pytest.raises(solver_mod.FdmError):
