@@ -138,3 +138,22 @@ def test_newind_spin_orbit_matches_oracle(pt):
     assert np.array_equal(ri.newinv[rows - 1], inter) and np.array_equal(ri.newinv[rows - 2], inter)
     assert np.array_equal(ri.lb1[rows - 2], ri.lb1[rows - 1])
     assert np.array_equal(ri.lb2[rows - 2], ri.lb2[rows - 1])
+
+
+def test_gradpot_is_exact_on_linear_potentials(pt):
+    """gradvr (source/potential.f90:5436-5477) on V = a.r + b returns a at every
+    point whose 12 neighbours lie inside the grid, axis k of neighbour pair iv
+    being 1 + ((iv - 1) / 2) mod 3 as the spin-orbit terms of calcMatRow assume;
+    the second spin block carries its own potential."""
+    import dataclasses
+    g = pt.grid
+    xyz = g.xyz[:3, :g.npoint]
+    a = np.array([0.3, -0.7, 1.1])
+    V = (a[:, None] * xyz).sum(0) + 0.5
+    st = dataclasses.replace(pt, Vr=np.asfortranarray(np.stack([V, 2.0 * V], 1)))
+    gv = CP.gradpot(st, g.cgrad, g.ivois)
+    nb = g.ivois[:g.npoint, :12]
+    inner = np.all((nb >= 1) & (nb <= g.npoint), axis=1)
+    assert inner.sum() > 100
+    assert np.abs(gv[inner, :, 0] - a).max() < 1e-13
+    assert np.abs(gv[inner, :, 1] - 2.0 * a).max() < 1e-13
