@@ -46,3 +46,18 @@ def test_solver_module_fails_loudly_without_library(tmp_path):
     from fdmnes_gb300 import solver
     with pytest.raises(RuntimeError):
         solver.load_library(str(tmp_path / "missing.so"))
+
+
+def test_create_rejects_bad_grids_before_device_work(lib_path):
+    """fdmgpu_create checks nspino (1, or 2 with spin-orbit) and the grid sizes
+    before it touches a device, so the checks run on a host without a GPU."""
+    from fdmnes_gb300 import abi, cluster as CL
+    lib = C.CDLL(lib_path)
+    lib.fdmgpu_create.argtypes = [C.c_void_p, C.c_void_p]
+    lib.fdmgpu_create.restype = C.c_int
+    d = abi.grid_dict(CL.small_cu_structure())
+    h = C.c_void_p()
+    for bad in ({"nspino": 3}, {"nspino": 0}, {"npoint": 0}, {"ngrph": 0}):
+        ga = abi.GridArgs(dict(d, **bad))
+        assert lib.fdmgpu_create(C.addressof(ga.s), C.byref(h)) == 1, bad
+        assert not h.value
