@@ -41,3 +41,16 @@ def golden():
 
 def rel(a, b):
     return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+@pytest.fixture(scope="session")
+def golden_complex():
+    """Complex spin-orbit golden problem: grid and energy arguments (dicts of
+    arrays and scalars) and the oracle's solution and Taull."""
+    d = np.load(os.path.join(GOLDEN, "golden_complex.npz"))
+
+    def part(pre):
+        out = {k[len(pre):]: d[k] for k in d.files if k.startswith(pre)}
+        return {k: (v.item() if v.ndim == 0 else v) for k, v in out.items()}
+
+    return part("g_"), part("e_"), d["smr"] + 1j * d["smi"], d["taull"]

@@ -4,6 +4,10 @@
   (fcc Cu absorber, FDM radius 1.4 A, grid step 0.25 A, C1) at two energies,
   with the oracle's solution smr and Taull.  The GPU parity tests load these
   arrays, so both machines solve bit-identical inputs.
+* golden_complex.npz - the complex (Cal_comp) mat_solve arguments of a small
+  spin-orbit problem (fcc Pt absorber, FDM radius 1.2 A, nspino = 2, complex
+  harmonics, relativistic terms) at 6 eV with the oracle's solution
+  smr + i smi and its Taull (nlm, 2, nlm, 2).
 * kat_special.npz   - known-answer values of the special functions used by the
   inputs: spherical Bessel/Neumann functions from scipy (times sqrt(k/pi), as
   source/sphere.f90:7356 normalises them) and real spherical harmonics from
@@ -20,7 +24,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 sys.path.insert(0, ROOT)
 
-from fdmnes_gb300 import abi, cluster as CL  # noqa: E402
+from fdmnes_gb300 import abi, cluster as CL, complex_path as CP  # noqa: E402
 import oracle  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
@@ -50,6 +54,20 @@ def make_problem():
         A, B = oracle.assemble_dense(ga, ea)
         out[f"e{k}_dense_solution"] = np.linalg.solve(A, B.T).T
     np.savez_compressed(os.path.join(OUT, "golden_problem.npz"), **out)
+
+
+def make_complex():
+    st = CL.build_structure(CL.pt_cluster(0.5), 0.25, 1.2, 15.0, nspin=2)
+    gd = CP.grid_dict(st, True)
+    ga = abi.GridArgs(gd)
+    ed = CP.energy_dict(st, 6.0, spinorbit=True)
+    ea = abi.EnergyArgs(ed)
+    X, _ = oracle.mat_solve_c(ga, ea)
+    T = oracle.taull_c(ga, ea, X)
+    out = {"g_" + k: np.asarray(v) for k, v in gd.items()}
+    out.update({"e_" + k: np.asarray(v) for k, v in ed.items()})
+    out["smr"], out["smi"], out["taull"] = X.real.copy(), X.imag.copy(), T
+    np.savez_compressed(os.path.join(OUT, "golden_complex.npz"), **out)
 
 
 def make_special():
@@ -84,5 +102,6 @@ def make_special():
 if __name__ == "__main__":
     oracle.build()
     make_problem()
+    make_complex()
     make_special()
     print("written", sorted(f for f in os.listdir(OUT) if f.endswith(".npz")))

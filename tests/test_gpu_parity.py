@@ -347,3 +347,20 @@ def test_complex_mixed_precision_is_rejected(solver_mod):
     with pytest.raises(solver_mod.FdmError):
         sv.mat_solve_complex(ea, "mixed")
     sv.close()
+
+
+def test_complex_golden_fixture(solver_mod, golden_complex):
+    """The committed spin-orbit fixture: the GPU solves the stored inputs (the
+    same bits on every machine) and matches the stored oracle solution and
+    Taull to 1e-9."""
+    from fdmnes_gb300 import abi
+    g, e, X0, T0 = golden_complex
+    ea = abi.EnergyArgs(e)
+    sv = solver_mod.FdmSolver(g)
+    X, _ = sv.mat_solve_complex(ea, "fp64")
+    assert rel(X, X0) < 1e-9
+    sv.spectrum_begin("fp64", 1)
+    sv.spectrum_add_args(ea)
+    sv.spectrum_run()
+    assert np.abs(sv.taull_c(0, 2) - T0).max() <= 1e-9 * np.abs(T0).max()
+    sv.close()

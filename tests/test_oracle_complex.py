@@ -157,3 +157,15 @@ def test_gradpot_is_exact_on_linear_potentials(pt):
     assert inner.sum() > 100
     assert np.abs(gv[inner, :, 0] - a).max() < 1e-13
     assert np.abs(gv[inner, :, 1] - 2.0 * a).max() < 1e-13
+
+
+def test_oracle_reproduces_the_complex_golden_fixture(golden_complex):
+    """The committed spin-orbit fixture (tests/golden/make_golden.py) is
+    reproduced by the oracle on its stored inputs: the oracle's complex branch
+    has not drifted since the fixture was written."""
+    g, e, X0, T0 = golden_complex
+    ga, ea = abi.GridArgs(g), abi.EnergyArgs(e)
+    X, _ = oracle.mat_solve_c(ga, ea)
+    assert np.abs(X - X0).max() <= 1e-12 * np.abs(X0).max()
+    T = oracle.taull_c(ga, ea, X)
+    assert np.abs(T - T0).max() <= 1e-12 * np.abs(T0).max()
