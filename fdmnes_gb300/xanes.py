@@ -38,6 +38,13 @@ def absorption(taull: np.ndarray) -> float:
     return float(-np.imag(np.trace(taull[1:4, 1:4])))
 
 
+def absorption_so(taull4: np.ndarray) -> float:
+    """Spin-orbit counterpart of ``absorption``: -Im of the trace of the L = 1
+    block summed over both spins, for Taull shaped (nlm, 2, nlm, 2) as
+    ``FdmSolver.taull_c`` returns it."""
+    return float(-np.imag(sum(np.trace(taull4[1:4, s, 1:4, s]) for s in range(taull4.shape[1]))))
+
+
 def absorption_cotangent(taull: np.ndarray, g_sigma: float = 1.0) -> np.ndarray:
     """dL/d(Im Taull) for L = g_sigma * absorption(taull): -g_sigma on the L = 1 diagonal."""
     g = np.zeros(taull.shape, dtype=np.float64)

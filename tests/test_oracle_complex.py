@@ -96,6 +96,9 @@ def test_k4_spin_orbit_without_coupling_decouples(pt):
     assert np.array_equal(T2[:, 0, :, 0], T1)
     assert np.array_equal(T2[:, 1, :, 1], T1)
     assert np.abs(T2[:, 0, :, 1]).max() == 0.0 and np.abs(T2[:, 1, :, 0]).max() == 0.0
+    # the dipole cross-section of the two decoupled spins is twice the spinless one
+    from fdmnes_gb300 import xanes
+    assert abs(xanes.absorption_so(T2) - 2.0 * xanes.absorption(T1)) <= 1e-14 * abs(xanes.absorption(T1))
 
 
 def test_k5_complex_harmonics_are_a_unitary_change_of_basis(cu):
