@@ -1808,6 +1808,7 @@ fdmgpu_status fdmgpu_batch_vjp(fdmgpu_handle* h, const double* gtaull, double* g
   if (!h || !gtaull || !grad_vr) return fail(FDMGPU_ERR_ARG, "null argument");
   Batch& b = h->batch;
   if (!b.ran) return fail(FDMGPU_ERR_ARG, "vjp needs a batch that has run");
+  if (b.cplx == 1) return fail(FDMGPU_ERR_UNSUPPORTED, "vjp of a complex batch (the adjoint is the real-basis one)");
   if (b.sites.size() > 1) return fail(FDMGPU_ERR_UNSUPPORTED, "vjp of a batch over several sites");
   if (b.precision == FDMGPU_PREC_MIXED && (h->refine_gmres || !h->escalate_dfl))
     return fail(FDMGPU_ERR_UNSUPPORTED, "vjp of a mixed batch needs classical or recurrence refinement and "

@@ -286,7 +286,8 @@ fdmgpu_status fdmgpu_batch_stats(fdmgpu_handle* h, int32_t k, int32_t* iters, do
  * FP32 (or, for escalated energies, double-float) factors of the equilibrated
  * matrix are refined with a double-float transposed residual (classical or
  * recurrence refinement with double-float escalation).  Points inside atoms
- * get 0.  ms (may be NULL) receives the device time.  No counterpart in the
+ * get 0.  ms (may be NULL) receives the device time.  Real-basis batches only
+ * (a complex batch returns FDMGPU_ERR_UNSUPPORTED).  No counterpart in the
  * reference.
  */
 fdmgpu_status fdmgpu_batch_vjp(fdmgpu_handle* h, const double* gtaull, double* grad_vr, double* ms);
