@@ -364,3 +364,26 @@ def test_complex_golden_fixture(solver_mod, golden_complex):
     sv.spectrum_run()
     assert np.abs(sv.taull_c(0, 2) - T0).max() <= 1e-9 * np.abs(T0).max()
     sv.close()
+
+
+def test_complex_thirteen_atoms(solver_mod):
+    """Spin-orbit on a 13-atom Pt cluster (coarse 0.45 A grid, FDM radius
+    3.0 A): every atom's harmonic block, the interleaved spin rows and the
+    relativistic and gradient terms on the GPU against the oracle.  Bar 1e-6:
+    the matrix's conditioning already separates the oracle's own profile solve
+    from a dense LU of the same matrix by 4.8e-9."""
+    import oracle
+    from fdmnes_gb300 import abi, cluster as CL, complex_path as CP
+    st = CL.build_structure(CL.pt_cluster(2.8), 0.45, 3.0, 15.0, nspin=2)
+    ga = abi.GridArgs(CP.grid_dict(st, True))
+    ea = abi.EnergyArgs(CP.energy_dict(st, 8.0, spinorbit=True))
+    X0, _ = oracle.mat_solve_c(ga, ea)
+    T0 = oracle.taull_c(ga, ea, X0)
+    sv = solver_mod.FdmSolver(ga.d)
+    X, _ = sv.mat_solve_complex(ea, "fp64")
+    assert rel(X, X0) < 1e-6
+    sv.spectrum_begin("fp64", 1)
+    sv.spectrum_add_args(ea)
+    sv.spectrum_run()
+    assert np.abs(sv.taull_c(0, 2) - T0).max() <= 1e-6 * np.abs(T0).max()
+    sv.close()

@@ -172,3 +172,21 @@ def test_oracle_reproduces_the_complex_golden_fixture(golden_complex):
     assert np.abs(X - X0).max() <= 1e-12 * np.abs(X0).max()
     T = oracle.taull_c(ga, ea, X)
     assert np.abs(T - T0).max() <= 1e-12 * np.abs(T0).max()
+
+
+def test_k4_thirteen_atoms():
+    """K4 on a 13-atom Pt cluster (coarse 0.45 A grid, FDM radius 3.0 A): with
+    the spin-orbit coupling off, every atom's interleaved spin rows and the
+    spin-doubled outer rows reproduce the complex-harmonic problem bit for bit
+    on both spins (nligne 2722 with spin-orbit)."""
+    st = CL.build_structure(CL.pt_cluster(2.8), 0.45, 3.0, 15.0, nspin=2)
+    assert st.natome == 13
+    g = st.grid
+    ga1 = abi.GridArgs(CP.grid_dict(st, False))
+    ea1 = abi.EnergyArgs(CP.energy_dict(st, 8.0, spinorbit=False, ylm_comp=True))
+    T1 = oracle.taull_c(ga1, ea1, oracle.mat_solve_c(ga1, ea1)[0], symmetrise=False)[:, 0, :, 0]
+    ga2 = abi.GridArgs(CP.grid_dict(st, True))
+    ea2 = abi.EnergyArgs(CP.energy_dict(st, 8.0, spinorbit=True, relativistic=False, so_coupling=0.0,
+                                        gradvr=np.zeros((g.npoint, 3, 2), order="F")))
+    T2 = oracle.taull_c(ga2, ea2, oracle.mat_solve_c(ga2, ea2)[0], symmetrise=False)
+    assert np.array_equal(T2[:, 0, :, 0], T1) and np.array_equal(T2[:, 1, :, 1], T1)
