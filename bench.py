@@ -229,6 +229,7 @@ def run_gpu(args):
     # convolved error ~3e-9); the library default (1e-10) is kept for parity
     TOL, TOL_ACCEPT = 1e-8, 1e-6
     sv.set_tolerance(TOL, TOL_ACCEPT)
+    sv.set_factor_mode(args.factor_mode)
 
     def barrier_sync():
         torch.cuda.synchronize()
@@ -331,7 +332,7 @@ def run_gpu(args):
                    "energies": n_all, "energies_per_gpu": n_e, "e_step_ev": step / world, "nligne": [min(r.nligne for _, r in items), max(r.nligne for _, r in items)],
                    "nrhs": [min(e.nlmso for e, _ in items), max(e.nlmso for e, _ in items)],
                    "l2": "working set ~100 GB per step, far above the 126 MB L2 (no flush needed)",
-                   "refine_tol": TOL, "refine_tol_accept": TOL_ACCEPT,
+                   "refine_tol": TOL, "refine_tol_accept": TOL_ACCEPT, "factor_mode": args.factor_mode,
                    "autotune": {"mixed": sv.tuning("mixed"), "fp64": sv.tuning("fp64")}},
         "roofline": roof_main,
         "roofline_other": [roof_res, roof_fac],
@@ -361,6 +362,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--energies", type=int, default=401,
                     help="energies of the spectrum over -5..35 eV (401: step 0.1 eV; 41: step 1 eV)")
+    ap.add_argument("--factor-mode", default="fp32", choices=["fp32", "wide_atom"],
+                    help="accumulation of the FP32 factor (wide_atom: double-float sums at the atom-harmonic steps)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

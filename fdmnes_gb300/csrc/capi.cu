@@ -64,6 +64,7 @@ struct HostProb {
   Prob P;
   std::vector<int> J0, J1, Imax, Imin;  // nt + 1
   std::vector<int64_t> strip;           // nt + 1
+  std::vector<unsigned char> wide;      // nt + 1: tile row holds atom-harmonic rows
   int64_t ntiles = 0;
   int64_t nnz_cap = 0;
   int64_t nnz_profile = 0;
@@ -142,6 +143,8 @@ struct fdmgpu_handle {
   int escalate_dfl = 1;   // escalation by a double-float (1) or an FP64 (0) factorisation
   int gmres_m = 12;       // Krylov dimension of one GMRES cycle
   int autotune = 1;         // time the trailing-update layouts on each new plan
+  int factor_mode = 0;      // FDMGPU_FACTOR_*: wide accumulation at the atom-harmonic steps of the FP32 factor
+  DevBuf<unsigned char> d_wide;
   int trail_threads[2] = {0, 0};        // chosen layout per precision (FP64, FP32); 0: built-in default
   double trail_ms[2][2] = {{0, 0}, {0, 0}};  // trial device ms [precision][64 | 128 threads]
   double tol = 0.0;         // refinement stop: max|dx|/max|x| (0: the default of the residual mode)
@@ -277,6 +280,13 @@ fdmgpu_status plan_problem(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& h
   }
   hp.strip[nt] = off;
   hp.ntiles = off;
+  // tile rows holding atom-harmonic rows (newind marks them with -ia)
+  hp.wide.assign(nt + 1, 0);
+  for (int p = 0; p < n; ++p) {
+    const int ii = n - p;
+    const int ic = cplx ? (ii + 1) / 2 : ii;
+    if (e->newinv[ic - 1] < 0) hp.wide[p / TS] = 1;
+  }
   for (int K = 0; K < nt; ++K) {
     int im = K;
     while (im + 1 < nt && hp.J0[im + 1] <= K) ++im;
@@ -436,6 +446,10 @@ void build_step_plan(fdmgpu_handle* h) {
   sp.bwd.assign(N, 0);
   sp.tfwd.assign(N, 0);
   sp.tbwd.assign(N, 0);
+  sp.wide_any.assign(N, 0);
+  if (h->tb.wide)
+    for (auto& hp : pr)
+      for (int K = 0; K < hp.P.nt; ++K) sp.wide_any[K] |= hp.wide[K];
   for (auto& hp : pr) {
     for (int K = 0; K < hp.P.nt; ++K) {
       const int nI = hp.Imax[K] - K, nJ = hp.J1[K] - K, nR = hp.P.nrt;
@@ -457,6 +471,7 @@ void build_step_plan(fdmgpu_handle* h) {
 struct Layout {
   int64_t env = 0, rhs = 0, rowv = 0, csr = 0, taull = 0, scratch = 0;
   std::vector<int> J0, J1, Imax, Imin;
+  std::vector<unsigned char> wide;
   std::vector<int64_t> strip;
 };
 
@@ -503,6 +518,7 @@ void layout_batch(fdmgpu_handle* h, Layout& L) {
     Imax.insert(Imax.end(), hp.Imax.begin(), hp.Imax.end());
     Imin.insert(Imin.end(), hp.Imin.begin(), hp.Imin.end());
     strip.insert(strip.end(), hp.strip.begin(), hp.strip.end());
+    L.wide.insert(L.wide.end(), hp.wide.begin(), hp.wide.end());
     d.max_rows = std::max(d.max_rows, P.nt * TS);
     d.max_tiles = std::max<int>(d.max_tiles, (int)hp.ntiles);
     d.max_rhs_tiles = std::max(d.max_rhs_tiles, P.nt * P.nrt);
@@ -528,6 +544,7 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   CK(upload(h->d_Imax, Imax, s));
   CK(upload(h->d_Imin, Imin, s));
   CK(upload(h->d_strip, strip, s));
+  CK(upload(h->d_wide, L.wide, s));
   if (h->d_env64.reserve((size_t)env * TS2) != cudaSuccess || h->d_B64.reserve(rhs) != cudaSuccess ||
       h->d_X64.reserve(rhs) != cudaSuccess || h->d_err.reserve(np) != cudaSuccess ||
       h->d_active.reserve(np) != cudaSuccess || h->d_red.reserve(3 * (size_t)np) != cudaSuccess ||
@@ -556,6 +573,7 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   h->tb.Imax = h->d_Imax.p;
   h->tb.Imin = h->d_Imin.p;
   h->tb.strip = h->d_strip.p;
+  h->tb.wide = (mixed && h->factor_mode == FDMGPU_FACTOR_WIDE_ATOM) ? h->d_wide.p : nullptr;
   Pools& pl = h->pl;
   pl = Pools();
   pl.env64 = h->d_env64.p;
@@ -813,6 +831,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   cudaGetLastError();  // clear a stale error of an earlier call on this thread
   sig = mix(sig, (uint64_t)h->residual_df64);
   sig = mix(sig, (uint64_t)(h->refine_gmres * 1000 + h->gmres_m));
+  sig = mix(sig, (uint64_t)h->factor_mode + 77u);
   const bool replan = sig != h->plan_sig || b.precision != h->plan_prec || !h->g_asm;
   Layout lay;
   layout_batch(h, lay);
@@ -834,7 +853,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
                         h->d_piv.p,   h->d_val2.p,  h->d_Xs.p,    h->d_valS.p,  h->d_V.p,    h->d_W.p,
                         h->d_gstate.p, h->d_inner.p, h->d_jdone.p, h->d_notconv.p, h->d_active_gm.p,
                         h->d_nb_coef.p, h->d_rvol.p, h->d_poidsa.p, h->d_poidso.p, h->d_Kar.p, h->d_YsoT.p,
-                        h->d_Ylmato.p, h->d_R32.p, h->d_act_df.p, h->d_act_rec.p, h->d_sites.p};
+                        h->d_Ylmato.p, h->d_R32.p, h->d_act_df.p, h->d_act_rec.p, h->d_sites.p, h->d_wide.p};
   for (const void* q : ptrs) ps = mix(ps, (uint64_t)(uintptr_t)q);
   if (replan && h->autotune) {
     st = tune_trailing(h);
@@ -1479,6 +1498,7 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   h->d_act_df.release();
   h->d_act_rec.release();
   h->d_strip.release();
+  h->d_wide.release();
   h->d_probs.release();
   h->d_red.release();
   if (h->h_pinned_i) cudaFreeHost(h->h_pinned_i);
@@ -1526,6 +1546,13 @@ fdmgpu_status fdmgpu_set_tolerance(fdmgpu_handle* h, double tol, double tol_acce
     return fail(FDMGPU_ERR_ARG, "tolerances must satisfy 0 <= tol <= tol_accept < 1 (0 selects the default)");
   h->tol = tol;
   h->tol_accept = tol_accept;
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_set_factor_mode(fdmgpu_handle* h, int32_t mode) {
+  if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
+  if (mode != FDMGPU_FACTOR_FP32 && mode != FDMGPU_FACTOR_WIDE_ATOM) return fail(FDMGPU_ERR_ARG, "unknown factor mode");
+  h->factor_mode = mode;
   return FDMGPU_OK;
 }
 

@@ -12,6 +12,7 @@
 // The backward substitution (the reference's resolution loop, :348-358) is
 // k_bwd_diag + k_bwd_update; k_fwd_* are used by the refinement solves.
 #include <algorithm>
+#include <type_traits>
 
 #include "fdm_internal.cuh"
 #include "fdm_kernels.h"
@@ -81,13 +82,19 @@ __global__ void __launch_bounds__(GEMM_THREADS) k_panel(T* env, T* rhs, const Pr
 }
 
 // NT: threads per tile pair (64: 8x8 accumulators per thread; 128: 8x4),
-// chosen per batch plan by the autotuner in the host code.
-template <typename T, int NT>
+// chosen per batch plan by the autotuner in the host code.  WIDE (FP32 only):
+// double-float accumulation of the products; each FP32 problem's step runs in
+// exactly one of the two instantiations, as tb.wide marks it.
+template <typename T, int NT, bool WIDE = false>
 __global__ void __launch_bounds__(NT) k_trailing(T* env, T* rhs, const Prob* probs, Tables tb, int K,
                                                        int fuse_rhs, const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
   if (K >= P.nt || (active && !active[e])) return;
+  if (std::is_same<T, float>::value) {
+    const bool w = tb.wide && tb.wide[P.trow + K];
+    if (w != WIDE) return;
+  }
   const int nI = tb.Imax[P.trow + K] - K;
   const int nJ = tb.J1[P.trow + K] - K;
   const int nC = nJ + (fuse_rhs ? P.nrt : 0);
@@ -108,7 +115,10 @@ __global__ void __launch_bounds__(NT) k_trailing(T* env, T* rhs, const Prob* pro
     B = rhs_ptr(rhs, P, K, c - nJ);
     C = rhs_ptr(rhs, P, I, c - nJ);
   }
-  tile_mm64<T, true, false, NT>(C, A, B, (const int*)nullptr, As, Bs);
+  if constexpr (WIDE)
+    tile_mm64<T, true, false, NT, facc>(C, A, B, (const int*)nullptr, As, Bs);
+  else
+    tile_mm64<T, true, false, NT>(C, A, B, (const int*)nullptr, As, Bs);
 }
 
 // Forward substitution, unit lower L: Y(K,R) <- L(K,K)^-1 P Y(K,R).
@@ -262,6 +272,10 @@ void setup_factor_kernels() {
   cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes_panel<T>());
   cudaFuncSetAttribute(k_trailing<T, 64>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_trailing<T, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if constexpr (std::is_same<T, float>::value) {
+    cudaFuncSetAttribute(k_trailing<T, 64, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    cudaFuncSetAttribute(k_trailing<T, 128, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  }
   cudaFuncSetAttribute(k_fwd_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_fwd_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_bwd_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -296,6 +310,16 @@ int launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables 
       else
         k_trailing<T, 64><<<dim3(nt, nprob), 64, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
       ++nk;
+      // the problems whose step K is marked wide run in the wide instantiation
+      if constexpr (std::is_same<T, float>::value) {
+        if (tb.wide && K < (int)sp.wide_any.size() && sp.wide_any[K]) {
+          if (trail_threads == 128)
+            k_trailing<T, 128, true><<<dim3(nt, nprob), 128, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
+          else
+            k_trailing<T, 64, true><<<dim3(nt, nprob), 64, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
+          ++nk;
+        }
+      }
     }
   }
   return nk;

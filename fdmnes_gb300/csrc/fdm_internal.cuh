@@ -77,6 +77,8 @@ struct Tables {
   const int64_t* strip;  // tile offset of row block I's strip
   const int* Imax;    // last row block with a stored tile in column K
   const int* Imin;    // first row block whose strip reaches column K
+  const unsigned char* wide;  // per tile row: the FP32 factor accumulates step K's trailing
+                              // update in double-float (nullptr: never)
 };
 
 template <typename T>
@@ -383,6 +385,42 @@ __device__ __forceinline__ T mac_finish(T acc) { return acc; }
 template <>
 __device__ __forceinline__ dfl mac_finish<dfl>(dfl acc) { return df_fast_two_sum(acc.hi, acc.lo); }
 
+// Wide accumulation of FP32 products: the exact product (p + e, e by FMA) is
+// added to an unnormalised double-float sum with Knuth's two-sum (about 8
+// FP32 operations per multiply-add).  Used by the FP32 factor at the steps
+// whose multipliers are large (the atom-harmonic tiles), where FP32 sums
+// next to them lose the factor's accuracy.
+struct facc {
+  float hi, lo;
+};
+template <typename A>
+__device__ __forceinline__ A acc_zero() { return A(0); }
+template <>
+__device__ __forceinline__ facc acc_zero<facc>() { return facc{0.0f, 0.0f}; }
+__device__ __forceinline__ void mac(facc& acc, float a, float b) {
+  const float p = a * b;
+  const float e = fmaf(a, b, -p);
+  const float s = acc.hi + p;
+  const float bb = s - acc.hi;
+  const float err = (acc.hi - (s - bb)) + (p - bb);
+  acc.hi = s;
+  acc.lo += err + e;
+}
+// c - acc (sub) or acc, rounded once more to the storage type.
+template <typename T, typename A>
+__device__ __forceinline__ T acc_apply(T c, A acc, bool sub) {
+  const T v = mac_finish(acc);
+  return sub ? c - v : v;
+}
+template <>
+__device__ __forceinline__ float acc_apply<float, facc>(float c, facc a, bool sub) {
+  if (!sub) return a.hi + a.lo;
+  const float s = c - a.hi;            // two-sum of c and -hi
+  const float t = s - c;
+  const float err = (c - (s - t)) + (-a.hi - t);
+  return s + (err - a.lo);
+}
+
 // Threads of the tile-product kernels: 64 threads with 8 x 8 accumulators per
 // thread (FP64), or 128 threads with 8 x 4 (FP32 and double-float: twice the
 // warps per tile for the same registers, which hides the latency of the
@@ -394,7 +432,7 @@ template <> struct MMThreads<float> { static constexpr int value = 128; };
 // TA: use the transpose of A (C (-)= A^T * P B).  Thread (tx, ty) owns rows
 // {4ty + i, 32 + 4ty + i} (i < 4) and columns {4tx + j, 32 + 4tx + j} (64
 // threads) or {4tx + j} (128 threads), j < 4.
-template <typename T, bool SUB, bool TA = false, int NT = MMThreads<T>::value>
+template <typename T, bool SUB, bool TA = false, int NT = MMThreads<T>::value, typename Acc = T>
 __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const int* perm, T* As, T* Bs) {
   static_assert(NT == 64 || NT == 128, "tile_mm64 runs on 64 or 128 threads");
   constexpr int CW = NT == 128 ? 4 : 8;  // columns per thread
@@ -416,11 +454,11 @@ __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const in
   }
   __syncthreads();
   const int tx = t % (NT / 8), ty = t / (NT / 8);
-  T acc[8][CW];
+  Acc acc[8][CW];
 #pragma unroll
   for (int i = 0; i < 8; ++i)
 #pragma unroll
-    for (int j = 0; j < CW; ++j) acc[i][j] = T(0);
+    for (int j = 0; j < CW; ++j) acc[i][j] = acc_zero<Acc>();
 #pragma unroll 2
   for (int k = 0; k < TS; ++k) {
     T a[8], b[CW];
@@ -444,10 +482,7 @@ __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const in
     for (int h = 0; h < CW / 4; ++h) {
       T* cp = C + row * TS + 32 * h + 4 * tx;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        const T v = mac_finish(acc[i][4 * h + j]);
-        cp[j] = SUB ? cp[j] - v : v;
-      }
+      for (int j = 0; j < 4; ++j) cp[j] = acc_apply<T, Acc>(cp[j], acc[i][4 * h + j], SUB);
     }
   }
 }

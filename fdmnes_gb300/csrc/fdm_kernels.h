@@ -16,6 +16,7 @@ struct StepPlan {
   std::vector<int> trail, trail_rhs;   // trailing tiles (+ RHS tiles) of step K
   std::vector<int> fwd, bwd;           // forward / backward update tiles of step K
   std::vector<int> tfwd, tbwd;         // the same for the transposed solves (U^T, then L^T)
+  std::vector<int> wide_any;           // step K of some problem accumulates wide (FP32 factor)
 };
 
 template <typename T> void setup_factor_kernels();

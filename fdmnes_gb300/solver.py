@@ -65,6 +65,8 @@ def load_library(path: str = LIB_PATH):
     L.fdmgpu_set_tolerance.restype = C.c_int
     L.fdmgpu_set_autotune.argtypes = [vp, C.c_int32]
     L.fdmgpu_set_autotune.restype = C.c_int
+    L.fdmgpu_set_factor_mode.argtypes = [vp, C.c_int32]
+    L.fdmgpu_set_factor_mode.restype = C.c_int
     L.fdmgpu_get_tuning.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.fdmgpu_get_tuning.restype = C.c_int
     L.fdmgpu_set_residual_mode.restype = C.c_int
@@ -129,6 +131,11 @@ class FdmSolver:
     def set_tolerance(self, tol: float = 0.0, tol_accept: float = 0.0):
         """Refinement stop (max|dx|/max|x|) and the stalled-but-accepted level; 0 = default."""
         _check(self.lib.fdmgpu_set_tolerance(self.h, tol, tol_accept))
+
+    def set_factor_mode(self, mode: str = "fp32"):
+        """Accumulation of the mixed path's FP32 factor: 'fp32' (default) or
+        'wide_atom' (double-float sums at the atom-harmonic steps)."""
+        _check(self.lib.fdmgpu_set_factor_mode(self.h, {"fp32": 0, "wide_atom": 1}[mode]))
 
     def set_autotune(self, on: bool = True):
         _check(self.lib.fdmgpu_set_autotune(self.h, 1 if on else 0))

@@ -176,6 +176,16 @@ typedef struct fdmgpu_info {
   double ms_escalate_factor, flops_escalate_factor;
 } fdmgpu_info;
 
+/* Accumulation of the FP32 factor of the mixed path. */
+typedef enum {
+  FDMGPU_FACTOR_FP32 = 0,      /* FP32 sums throughout (default)                          */
+  FDMGPU_FACTOR_WIDE_ATOM = 1  /* double-float sums in the trailing update of the steps
+                                  whose tile row holds atom-harmonic rows; those steps'
+                                  multipliers are large, and FP32 sums next to them cost
+                                  the factor the accuracy that keeps the refinement from
+                                  escalating (not yet measured on the GPU)               */
+} fdmgpu_factor_mode;
+
 /* Library version string. */
 const char* fdmgpu_version(void);
 
@@ -220,6 +230,10 @@ fdmgpu_status fdmgpu_set_escalation(fdmgpu_handle* h, int32_t mode);
  * residual, 1e-9 with FP64), else solved again by escalation.  0 selects the
  * default.  No counterpart in the reference. */
 fdmgpu_status fdmgpu_set_tolerance(fdmgpu_handle* h, double tol, double tol_accept);
+
+/* Accumulation mode of the FP32 factor (fdmgpu_factor_mode), for the
+ * batches planned after the call.  No counterpart in the reference. */
+fdmgpu_status fdmgpu_set_factor_mode(fdmgpu_handle* h, int32_t mode);
 
 /* Autotuner (on by default): when a batch needs a new plan, the trailing
  * update of the factor is timed on this batch with 64 threads per 64x64 tile

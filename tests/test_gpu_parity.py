@@ -387,3 +387,27 @@ def test_complex_thirteen_atoms(solver_mod):
     sv.spectrum_run()
     assert np.abs(sv.taull_c(0, 2) - T0).max() <= 1e-6 * np.abs(T0).max()
     sv.close()
+
+
+def test_wide_accumulation_at_atom_steps(solver_mod):
+    """FDMGPU_FACTOR_WIDE_ATOM (double-float sums in the FP32 factor's trailing
+    update at the steps whose tile row holds atom-harmonic rows) on full Cu
+    energies: the spectrum meets the mixed path's bar against FP64, and no
+    more energies need escalation than with FP32 sums (a faulty wide update
+    would push even the 2 eV energy into escalation)."""
+    from fdmnes_gb300 import cluster as CL, xanes
+    st = CL.cu_structure()
+    energies = [2.0, 22.0, 26.0, 30.0, 34.0]
+    items = xanes.spectrum_inputs(st, energies)
+    sv = solver_mod.FdmSolver(st)
+    T64, _ = sv.spectrum(items, "fp64")
+    sv.set_tolerance(1e-8, 1e-6)
+    fallbacks = {}
+    for mode in ("fp32", "wide_atom"):
+        sv.set_factor_mode(mode)
+        T, info = sv.spectrum(items, "mixed")
+        fallbacks[mode] = info["n_fallback"]
+        assert max(rel(a, b) for a, b in zip(T, T64)) < 1e-5, mode
+        assert xanes.convolved_relative_error(energies, T, T64) < 1e-6, mode
+    assert fallbacks["wide_atom"] <= fallbacks["fp32"], fallbacks
+    sv.close()
