@@ -23,8 +23,14 @@ of that case on top of a :class:`cluster.Structure`:
   ``source/sphere.f90:413``) is upstream of the solve and not restated: these
   are model inputs with the reference's structure.
 
-Energies are real (``E_comp`` false, ``Eimag`` = 0): the reference's default
-FDM path zeroes the broadening before the solve (``source/lecture.f90:5410``).
+Energies are real (``E_comp`` false, ``Eimag`` = 0) unless ``eimag_ry`` is
+given: the reference's default FDM path zeroes the broadening before the solve
+(``source/lecture.f90:5410``).  With ``eimag_ry`` > 0 the outer functions are
+the complex-argument j_l, n_l of ``cbessneu`` at k = sqrt(Ecinetic + i Eimag)
+(``phiso``, ``source/mat.f90:778-785,978-990``) and the grid diagonal carries
+-i Eimag (``E_comp``); ``phiato`` stays the real-energy model.  This is the
+regular solution of the reference's complex-energy mode only: its irregular
+solution and Tau_RI (``FDM_comp``) are not generated.
 """
 from __future__ import annotations
 
@@ -44,6 +50,23 @@ def yc(m: int, y1: np.ndarray, y2: np.ndarray) -> np.ndarray:
     if m < 0:
         return (y2 - 1j * y1) * s
     return (y1 + 1j * y2) * ((-1) ** m) * s
+
+
+def cbessneu(fnorm: complex, z: np.ndarray, lmax: int):
+    """fnorm * j_l(z), fnorm * n_l(z) for complex z by upward recursion
+    (source/sphere.f90:7226-7254); z: (n,) -> two (n, lmax + 1) arrays."""
+    z = np.asarray(z, dtype=np.complex128)
+    bs = np.zeros((len(z), lmax + 1), dtype=np.complex128)
+    nm = np.zeros_like(bs)
+    nm[:, 0] = -fnorm * np.cos(z) / z
+    bs[:, 0] = fnorm * np.sin(z) / z
+    if lmax >= 1:
+        nm[:, 1] = nm[:, 0] / z - bs[:, 0]
+        bs[:, 1] = bs[:, 0] / z + nm[:, 0]
+    for L in range(2, lmax + 1):
+        nm[:, L] = (2 * L - 1) * nm[:, L - 1] / z - nm[:, L - 2]
+        bs[:, L] = (2 * L - 1) * bs[:, L - 1] / z - bs[:, L - 2]
+    return bs, nm
 
 
 def gradpot(st: CL.Structure, cgrad: np.ndarray, ivois: np.ndarray, iord: int = 4) -> np.ndarray:
@@ -127,7 +150,7 @@ def _so_weight(L: int, m: int, isol: int, ispo: int, so_coupling: float) -> floa
 
 def energy_dict(st: CL.Structure, energy_ev: float, spinorbit: bool, ylm_comp: bool = True,
                 relativistic: Optional[bool] = None, so_coupling: float = 0.1, basereel: bool = False,
-                gradvr: Optional[np.ndarray] = None, e_fermi_ev: float = -5.0) -> dict:
+                gradvr: Optional[np.ndarray] = None, e_fermi_ev: float = -5.0, eimag_ry: float = 0.0) -> dict:
     """Per-energy arguments of one complex mat_solve call.
 
     spinorbit: nspino = 2 (needs nspin = 2), with the relativistic terms unless
@@ -176,6 +199,22 @@ def energy_dict(st: CL.Structure, energy_ev: float, spinorbit: bool, ylm_comp: b
     nspinr = st.nspin if spinorbit else 1
     bes = np.asfortranarray(np.repeat(ei.besselr, nspinr, axis=2))
     neu = np.asfortranarray(np.repeat(ei.neumanr, nspinr, axis=2))
+    ecomp = {}
+    if eimag_ry > 0.0:
+        # phiso with E_comp: k = sqrt(Ecinetic + i Eimag), fnorm = sqrt(k / pi)
+        konde = np.sqrt(complex(ei.ecinetic_out, eimag_ry))
+        fnormc = np.sqrt(konde / np.pi)
+        zc = konde * g.xyz[3, g.isrt - 1]
+        bc, nc = cbessneu(fnormc, zc, ei.lmaxso)
+        arrs = []
+        for a in (bc, nc):
+            out = np.zeros((2, g.nsort, ei.lmaxso + 1, nspinr), order="F")
+            for isp in range(nspinr):
+                out[0, :, :, isp] = a.real
+                out[1, :, :, isp] = a.imag
+            arrs.append(out)
+        ecomp = dict(E_comp=1, Eimag=eimag_ry, nsort_c=g.nsort, nsort_r=0, Bessel=arrs[0], Neuman=arrs[1],
+                     Besselr=None, Neumanr=None)
     if gradvr is None:
         gradvr = gradpot(st, g.cgrad, g.ivois)
     d = abi.energy_dict(st, ei, ri)
@@ -183,6 +222,7 @@ def energy_dict(st: CL.Structure, energy_ev: float, spinorbit: bool, ylm_comp: b
              nspinr=nspinr, nicm=g.npoint, Cal_comp=1, E_comp=0, Basereel=int(basereel), Relativiste=int(relativistic),
              Spinorbite=int(spinorbit), Ylm_comp=int(ylm_comp), ispin=1, phiato=phi, Besselr=bes, Neumanr=neu,
              gradvr=np.asfortranarray(gradvr), new_=ri.new, newinv=ri.newinv, lb1=ri.lb1, lb2=ri.lb2, ianew=ri.ianew)
+    d.update(ecomp)
     return d
 
 

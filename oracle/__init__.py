@@ -39,6 +39,7 @@ def lib():
                                          C.POINTER(C.c_double), C.POINTER(C.c_int32)]
         L.oracle_assemble_dense_c.argtypes = [vp, vp, vp, vp]
         L.oracle_taull_c.argtypes = [vp, vp, C.c_int, vp, vp, C.c_int, vp, C.POINTER(C.c_int32)]
+        L.oracle_cbessneu.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, vp, vp]
         _lib = L
     return _lib
 
@@ -153,3 +154,12 @@ def taull_c(grid_args, energy_args, x, iaabs=1, symmetrise=True):
     k = nl.value
     t = out[:2 * (k * nsp) ** 2].view(np.complex128).reshape((k, nsp, k, nsp), order="F")
     return t.copy()
+
+
+def cbessneu(fnorm, z, lmax):
+    """Complex fnorm * j_l(z), fnorm * n_l(z), l = 0..lmax, for complex z."""
+    b = np.zeros(lmax + 1, dtype=np.complex128)
+    nm = np.zeros(lmax + 1, dtype=np.complex128)
+    lib().oracle_cbessneu(float(np.real(fnorm)), float(np.imag(fnorm)), float(np.real(z)), float(np.imag(z)),
+                          int(lmax), b.ctypes.data, nm.ctypes.data)
+    return b, nm

@@ -18,6 +18,7 @@
 //     outer-sphere rows                                             :1405-1511
 //     atom rows                                                     :1515-1632
 //   Yc (complex harmonic from two real ones)  source/mat.f90:1733-1754
+//   cbessneu (complex-argument j_l, n_l)       source/sphere.f90:7226-7254
 //   mat_solve (Gaussian), complex branch       source/mat_solve_gaussian.f90:196-358
 //   Taull of the complex basis                 source/mat.f90:354-405 (Basereel false)
 //     and the symmetrisation                   source/mat.f90:594-644
@@ -348,6 +349,25 @@ int check_supported_c(const fdmgpu_grid* g, const fdmgpu_energy* e) {
 }  // namespace
 
 extern "C" {
+
+// cbessneu, source/sphere.f90:7226-7254: fnorm*j_l(z), fnorm*n_l(z) for complex
+// z and fnorm by upward recursion, l = 0..lmax; outputs interleaved re/im.
+void oracle_cbessneu(double fnorm_re, double fnorm_im, double z_re, double z_im, int lmax, double* bessel_ri,
+                     double* neuman_ri) {
+  const cdouble fnorm(fnorm_re, fnorm_im), z(z_re, z_im);
+  cdouble* bs = reinterpret_cast<cdouble*>(bessel_ri);
+  cdouble* nm = reinterpret_cast<cdouble*>(neuman_ri);
+  nm[0] = -fnorm * std::cos(z) / z;
+  bs[0] = fnorm * std::sin(z) / z;
+  if (lmax == 0) return;
+  nm[1] = nm[0] / z - bs[0];
+  bs[1] = bs[0] / z + nm[0];
+  for (int L = 2; L <= lmax; ++L) {
+    const double L1 = 2 * L - 1;
+    nm[L] = L1 * nm[L - 1] / z - nm[L - 2];
+    bs[L] = L1 * bs[L - 1] / z - bs[L - 2];
+  }
+}
 
 // Dense complex assembly: A (nligne x nligne) and B = smr + i smi (nlmso x
 // nligne), both column-major complex interleaved.

@@ -190,3 +190,42 @@ def test_k4_thirteen_atoms():
                                         gradvr=np.zeros((g.npoint, 3, 2), order="F")))
     T2 = oracle.taull_c(ga2, ea2, oracle.mat_solve_c(ga2, ea2)[0], symmetrise=False)
     assert np.array_equal(T2[:, 0, :, 0], T1) and np.array_equal(T2[:, 1, :, 1], T1)
+
+
+def test_cbessneu_matches_scipy_for_complex_arguments():
+    """cbessneu (source/sphere.f90:7226-7254), the complex-energy outer
+    functions of phiso, against scipy's spherical_jn / spherical_yn of complex
+    argument times the complex sqrt(k / pi), for the orders the upward
+    recursion resolves (l up to about |z| + 3: beyond, j_l falls below the
+    recursion's cancellation, in the reference's algorithm as here); the
+    package's numpy restatement gives the oracle's values."""
+    from scipy import special
+    k = np.sqrt(1.9 + 0.05j)
+    f = np.sqrt(k / np.pi)
+    for z, lmax in ((0.8 + 0.02j, 3), (3.7 + 0.21j, 7), (9.0 + 0.4j, 12)):
+        b, n = oracle.cbessneu(f, z, lmax)
+        bj = f * np.array([special.spherical_jn(L, z) for L in range(lmax + 1)])
+        by = f * np.array([special.spherical_yn(L, z) for L in range(lmax + 1)])
+        assert np.all(np.abs(b - bj) <= 1e-11 * np.abs(bj)), z
+        assert np.all(np.abs(n - by) <= 1e-12 * np.abs(by)), z
+        bp, np_ = CP.cbessneu(f, np.array([z]), lmax)
+        assert np.allclose(bp[0], b, rtol=1e-10, atol=0) and np.allclose(np_[0], n, rtol=1e-10, atol=0)
+
+
+@pytest.mark.parametrize("spinorbit", [False, True])
+def test_k6_complex_energy_is_continuous_at_real_energies(pt, spinorbit):
+    """K6: the complex-energy regular system (E_comp: complex-argument
+    Hankel functions, -i Eimag on the grid diagonal) tends to the real-energy
+    system as Eimag -> 0 (5.6e-13 at Eimag = 1e-12 Ry), departs linearly (the
+    same slope at 1e-8 and 1e-6 Ry), and its profile solve matches a dense LU
+    at a finite broadening."""
+    ga = abi.GridArgs(CP.grid_dict(pt, spinorbit))
+    X0, _ = oracle.mat_solve_c(ga, abi.EnergyArgs(CP.energy_dict(pt, E, spinorbit=spinorbit)))
+    diff = {}
+    for eim in (1e-12, 1e-8, 1e-6):
+        X, _ = oracle.mat_solve_c(ga, abi.EnergyArgs(CP.energy_dict(pt, E, spinorbit=spinorbit, eimag_ry=eim)))
+        diff[eim] = np.abs(X - X0).max() / np.abs(X0).max()
+    assert diff[1e-12] < 1e-10
+    assert abs(diff[1e-8] / 1e-8 - diff[1e-6] / 1e-6) <= 0.05 * diff[1e-6] / 1e-6
+    ea = abi.EnergyArgs(CP.energy_dict(pt, E, spinorbit=spinorbit, eimag_ry=0.037))
+    assert _dense_rel(ga, ea) < (1e-9 if spinorbit else 1e-12)
