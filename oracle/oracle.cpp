@@ -1,6 +1,6 @@
 // oracle.cpp - CPU restatement of the FDMNES FDM assembly + Gaussian solve.
 //
-// TEST INFRASTRUCTURE ONLY.  This file is the checker that the GPU path is
+// TEST INFRASTRUCTURE ONLY.  This file is the CPU model that the GPU path is
 // compared against; nothing in the product links, imports or calls it.  Only
 // tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.
 //

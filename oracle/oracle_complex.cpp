@@ -1,7 +1,7 @@
 // oracle_complex.cpp - CPU restatement of the complex (Cal_comp) branch of the
 // FDMNES FDM assembly and Gaussian solve.
 //
-// TEST INFRASTRUCTURE ONLY, like oracle.cpp: the checker, never the product.
+// TEST INFRASTRUCTURE ONLY, like oracle.cpp: compared against, never part of the product.
 //
 // Parity status: unpinned against the reference binary (no Fortran compiler
 // on either machine); pinned by known-answer tests instead: a dense complex
