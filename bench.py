@@ -40,6 +40,8 @@ sys.path.insert(0, HERE)
 
 E_MIN, E_MAX, E_STEP = -5.0, 35.0, 0.1
 METRIC = "FDM energy-points/sec on 1 GB300, mixed+batched vs plain FP64, at <=1e-6 rel error"
+WORKLOAD_CU401 = ("Cu fcc a=3.61 A, 13-atom cluster, FDM radius 3.0 A, step 0.25 A, C1, "
+                  "401 energies -5..35 eV step 0.1 eV, batched mixed precision")
 
 
 def _peaks():
@@ -101,6 +103,8 @@ _W = {}
 
 def _oracle_init():
     sys.path.insert(0, HERE)
+    import oracle
+    oracle.use_timed_build(True)  # the -O3 build of the restatement (the reference's level)
     from fdmnes_gb300 import abi, cluster as CL
     st = CL.cu_structure()
     _W["st"], _W["ga"] = st, abi.GridArgs(st)
@@ -121,12 +125,21 @@ def _oracle_worker(args):
     return time.perf_counter() - t0
 
 
-def cpu_baseline(n_energies: int):
-    """Oracle restatement on the host cores, one energy per process (spawned)."""
+def cpu_energy_sample(n_energies: int, offset: int = 0):
+    """n energies spread over the 401-point grid -5..35 eV (step 0.1 eV),
+    shifted by `offset` grid points so that successive samples cover different
+    energies of the spectrum."""
+    grid = np.round(np.arange(401) * E_STEP + E_MIN, 10)
+    idx = (np.round(np.linspace(0, 400, n_energies)).astype(int) + offset) % 401
+    return grid[idx]
+
+
+def cpu_baseline(n_energies: int, offset: int = 0):
+    """Oracle restatement (-O3 build) on the host cores, one energy per process (spawned)."""
     import oracle
     oracle.build()
     cores = min(os.cpu_count() or 1, n_energies)
-    energies = np.linspace(E_MIN, E_MAX, n_energies)
+    energies = cpu_energy_sample(n_energies, offset)
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores, initializer=_oracle_init) as pool:
         per = pool.map(_oracle_worker, [(float(e),) for e in energies], chunksize=1)
@@ -134,8 +147,9 @@ def cpu_baseline(n_energies: int):
     # (source/fdm.f90:3484-3497): a spectrum of n energies takes the slowest rank's time
     wall = max(per)
     return {"value": n_energies / wall, "unit": "energies/s", "cores": cores, "kind": "port",
-            "sample": f"{n_energies} Cu energies {E_MIN}..{E_MAX} eV, one per process; "
-                      f"single-energy solve {min(per):.2f}-{max(per):.2f} s",
+            "build": "C++ restatement of mat_solve_gaussian + calcMatRow + Taull, g++ -O3",
+            "sample": f"{n_energies} of the 401 Cu energies {E_MIN}..{E_MAX} eV (grid offset {offset}), "
+                      f"one per process; single-energy solve {min(per):.2f}-{max(per):.2f} s",
             "wall_s": wall}
 
 
@@ -180,10 +194,12 @@ def run_reference(args):
     if rank != 0:
         return
     n = max(1, min(os.cpu_count() or 1, 16))
-    cfg = {"workload": "Cu fcc 13 atoms, R=3.0 A, h=0.25 A, C1, real, energies -5..35 eV", "sample_energies": n}
+    cfg = {"workload": WORKLOAD_CU401, "energies": 401, "sample_energies_per_step": n,
+           "sample": "each step solves n energies of the 401-point spectrum, one per host core; successive "
+                     "steps take successive grid offsets"}
     times = []
     for step in range(args.warmup + args.steps):
-        cb = cpu_baseline(n)
+        cb = cpu_baseline(n, offset=step)
         if step >= args.warmup:
             times.append(cb)
     v = statistics.median([c["value"] for c in times])
@@ -191,7 +207,7 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * n / v, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": cfg,
             "cpu_baseline": {"value": v, "unit": "energies/s", "cores": times[0]["cores"], "kind": "port",
-                             "sample": times[0]["sample"]},
+                             "build": times[0]["build"], "sample": times[0]["sample"]},
             "e2e": {"value": v, "unit": "energies/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -299,7 +315,10 @@ def run_gpu(args):
 
     peaks, peak_kind = _peaks()
     last = infos[-1]
-    FP32_PIPE_TFLOPS = 73.1  # FP32 FMA rate probed on this GB300 pool (2 flops per FMA)
+    # FP32 / FP64 FMA pipe rates of this GPU, measured here (fdmgpu_measure_pipe_peaks)
+    from fdmnes_gb300.solver import measure_pipe_peaks
+    pipes = measure_pipe_peaks()
+    FP32_PIPE_TFLOPS = pipes["fp32_tflops"]
 
     def roof(flops, ms, kernel, note):
         ach = flops / (ms / 1000.0) / 1e12 if ms > 0 else 0.0

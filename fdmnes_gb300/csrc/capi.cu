@@ -144,6 +144,7 @@ struct fdmgpu_handle {
   int gmres_m = 12;       // Krylov dimension of one GMRES cycle
   int autotune = 1;         // time the trailing-update layouts on each new plan
   int factor_mode = 0;      // FDMGPU_FACTOR_*: wide accumulation at the atom-harmonic steps of the FP32 factor
+  int tile_engine = FDMGPU_ENGINE_SIMT;  // FDMGPU_ENGINE_*: FP32 tile updates on the FP32 pipes or the tensor cores
   DevBuf<unsigned char> d_wide;
   int trail_threads[2] = {0, 0};        // chosen layout per precision (FP64, FP32); 0: built-in default
   double trail_ms[2][2] = {{0, 0}, {0, 0}};  // trial device ms [precision][64 | 128 threads]
@@ -450,9 +451,15 @@ void build_step_plan(fdmgpu_handle* h) {
   if (h->tb.wide)
     for (auto& hp : pr)
       for (int K = 0; K < hp.P.nt; ++K) sp.wide_any[K] |= hp.wide[K];
+  sp.trail_tc.assign(N, 0);
+  sp.fwd_tc.assign(N, 0);
+  sp.bwd_tc.assign(N, 0);
   for (auto& hp : pr) {
     for (int K = 0; K < hp.P.nt; ++K) {
       const int nI = hp.Imax[K] - K, nJ = hp.J1[K] - K, nR = hp.P.nrt;
+      sp.trail_tc[K] = std::max(sp.trail_tc[K], tc_items(nI, nJ + nR));
+      sp.fwd_tc[K] = std::max(sp.fwd_tc[K], tc_items(nI, nR));
+      sp.bwd_tc[K] = std::max(sp.bwd_tc[K], tc_items(K - hp.Imin[K], nR));
       sp.panel[K] = std::max(sp.panel[K], nI + nJ);
       sp.panel_rhs[K] = std::max(sp.panel_rhs[K], nI + nJ + nR);
       sp.trail[K] = std::max(sp.trail[K], nI * nJ);
@@ -574,6 +581,9 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   h->tb.Imin = h->d_Imin.p;
   h->tb.strip = h->d_strip.p;
   h->tb.wide = (mixed && h->factor_mode == FDMGPU_FACTOR_WIDE_ATOM) ? h->d_wide.p : nullptr;
+  // real mixed batches may run their FP32 tile updates on the tensor cores
+  h->sp.tc = (mixed && !cplx && h->tile_engine == FDMGPU_ENGINE_TCGEN05) ? 1 : 0;
+  h->sp.tc_err = h->d_err.p;
   Pools& pl = h->pl;
   pl = Pools();
   pl.env64 = h->d_env64.p;
@@ -832,6 +842,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   sig = mix(sig, (uint64_t)h->residual_df64);
   sig = mix(sig, (uint64_t)(h->refine_gmres * 1000 + h->gmres_m));
   sig = mix(sig, (uint64_t)h->factor_mode + 77u);
+  sig = mix(sig, (uint64_t)h->tile_engine + 191u);
   const bool replan = sig != h->plan_sig || b.precision != h->plan_prec || !h->g_asm;
   Layout lay;
   layout_batch(h, lay);
@@ -1457,6 +1468,7 @@ fdmgpu_status fdmgpu_create(const fdmgpu_grid* g, fdmgpu_handle** out) {
   setup_factor_kernels<float>();
   setup_factor_kernels<double>();
   setup_factor_kernels<dfl>();
+  setup_tc_kernels();
   *out = h;
   return FDMGPU_OK;
 }
@@ -1553,6 +1565,13 @@ fdmgpu_status fdmgpu_set_factor_mode(fdmgpu_handle* h, int32_t mode) {
   if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
   if (mode != FDMGPU_FACTOR_FP32 && mode != FDMGPU_FACTOR_WIDE_ATOM) return fail(FDMGPU_ERR_ARG, "unknown factor mode");
   h->factor_mode = mode;
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_set_tile_engine(fdmgpu_handle* h, int32_t engine) {
+  if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
+  if (engine != FDMGPU_ENGINE_SIMT && engine != FDMGPU_ENGINE_TCGEN05) return fail(FDMGPU_ERR_ARG, "unknown tile engine");
+  h->tile_engine = engine;
   return FDMGPU_OK;
 }
 

@@ -305,7 +305,10 @@ int launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables 
     }
     const int nt = fuse_rhs ? sp.trail_rhs[K] : sp.trail[K];
     if (nt > 0) {
-      if (trail_threads == 128)
+      if (std::is_same<T, float>::value && sp.tc && fuse_rhs)
+        launch_tc_update(0, sp.trail_tc[K], nprob, reinterpret_cast<float*>(env), reinterpret_cast<float*>(rhs),
+                         probs, tb, K, active, err, s);
+      else if (trail_threads == 128)
         k_trailing<T, 128><<<dim3(nt, nprob), 128, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
       else
         k_trailing<T, 64><<<dim3(nt, nprob), 64, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
@@ -334,7 +337,11 @@ int launch_forward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, 
     k_fwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active, piv);
     ++nk;
     if (sp.fwd[K] > 0) {
-      k_fwd_update<T><<<dim3(sp.fwd[K], nprob), MMThreads<T>::value, sm, s>>>(env, rhs, probs, tb, K, active);
+      if (std::is_same<T, float>::value && sp.tc)
+        launch_tc_update(1, sp.fwd_tc[K], nprob, reinterpret_cast<float*>(const_cast<T*>(env)),
+                         reinterpret_cast<float*>(rhs), probs, tb, K, active, sp.tc_err, s);
+      else
+        k_fwd_update<T><<<dim3(sp.fwd[K], nprob), MMThreads<T>::value, sm, s>>>(env, rhs, probs, tb, K, active);
       ++nk;
     }
   }
@@ -350,7 +357,11 @@ int launch_backward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs,
     k_bwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
     ++nk;
     if (sp.bwd[K] > 0) {
-      k_bwd_update<T><<<dim3(sp.bwd[K], nprob), MMThreads<T>::value, sm, s>>>(env, rhs, probs, tb, K, active);
+      if (std::is_same<T, float>::value && sp.tc)
+        launch_tc_update(2, sp.bwd_tc[K], nprob, reinterpret_cast<float*>(const_cast<T*>(env)),
+                         reinterpret_cast<float*>(rhs), probs, tb, K, active, sp.tc_err, s);
+      else
+        k_bwd_update<T><<<dim3(sp.bwd[K], nprob), MMThreads<T>::value, sm, s>>>(env, rhs, probs, tb, K, active);
       ++nk;
     }
   }

@@ -17,7 +17,21 @@ struct StepPlan {
   std::vector<int> fwd, bwd;           // forward / backward update tiles of step K
   std::vector<int> tfwd, tbwd;         // the same for the transposed solves (U^T, then L^T)
   std::vector<int> wide_any;           // step K of some problem accumulates wide (FP32 factor)
+  // FP32 tile updates on the tensor cores (tc_update.cu): work items (two tile
+  // rows x up to four tile columns) of the trailing update with the fused
+  // right-hand sides, and of the forward / backward solve updates
+  int tc = 0;
+  std::vector<int> trail_tc, fwd_tc, bwd_tc;
+  int* tc_err = nullptr;               // per-problem status word of the solve updates (mbarrier timeout)
 };
+
+// Split-TF32 tcgen05 tile updates (tc_update.cu).  mode 0: factor trailing
+// update C -= L U with the fused right-hand sides; 1: forward solve update
+// Y(I) -= L(I,K) Y(K); 2: backward solve update Y(I) -= U(I,K) Y(K).
+void setup_tc_kernels();
+void launch_tc_update(int mode, int items, int nprob, float* env, float* rhs, const Prob* probs, Tables tb, int K,
+                      const int* active, int* err, cudaStream_t s);
+int tc_items(int nI, int nC);
 
 template <typename T> void setup_factor_kernels();
 template <typename T>

@@ -128,22 +128,56 @@ __global__ void __launch_bounds__(NOALLOC_THREADS)
 constexpr int MAX_DEVICES = 64;
 std::mutex g_scratch_mu;
 double2* g_scratch_addr[MAX_DEVICES] = {};
+unsigned long long g_scratch_ctx[MAX_DEVICES] = {};  // context the address belongs to
+
+// Unique id of the calling thread's current CUDA context (0 when it cannot be
+// read).  A device reset destroys the primary context and the next one may
+// load this library's device image at another address; the id tells the two
+// apart (a context's address can be reused, its id is not).
+typedef int (*ctx_get_current_fn)(void**);
+typedef int (*ctx_get_id_fn)(void*, unsigned long long*);
+unsigned long long current_context_id() {
+  static ctx_get_current_fn get_current = nullptr;
+  static ctx_get_id_fn get_id = nullptr;
+  static bool looked_up = false;
+  if (!looked_up) {
+    void* f1 = nullptr;
+    void* f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) == cudaSuccess &&
+        q1 == cudaDriverEntryPointSuccess &&
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) == cudaSuccess &&
+        q2 == cudaDriverEntryPointSuccess) {
+      get_current = reinterpret_cast<ctx_get_current_fn>(f1);
+      get_id = reinterpret_cast<ctx_get_id_fn>(f2);
+    }
+    looked_up = true;
+  }
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
 
 }  // namespace
 
-// Address of this device's scratch array, looked up once per device with that
-// device current (the lookup may load this library's device code).
+// Address of this device's scratch array, looked up with that device current
+// once per device and CUDA context (the lookup may load this library's device
+// code).  After a device reset the new context's address is looked up again.
 cudaError_t taull_noalloc_scratch(double2** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= MAX_DEVICES) return cudaErrorInvalidDevice;
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_addr[dev]) {
+  const unsigned long long ctx = current_context_id();
+  if (!g_scratch_addr[dev] || ctx == 0 || ctx != g_scratch_ctx[dev]) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_taull_scratch);
     if (e != cudaSuccess) return e;
     g_scratch_addr[dev] = static_cast<double2*>(p);
+    // the id is read after the lookup: the lookup makes the context current
+    g_scratch_ctx[dev] = current_context_id();
   }
   *out = g_scratch_addr[dev];
   return cudaSuccess;

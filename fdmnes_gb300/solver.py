@@ -67,6 +67,10 @@ def load_library(path: str = LIB_PATH):
     L.fdmgpu_set_autotune.restype = C.c_int
     L.fdmgpu_set_factor_mode.argtypes = [vp, C.c_int32]
     L.fdmgpu_set_factor_mode.restype = C.c_int
+    L.fdmgpu_measure_pipe_peaks.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
+    L.fdmgpu_measure_pipe_peaks.restype = C.c_int
+    L.fdmgpu_set_tile_engine.argtypes = [vp, C.c_int32]
+    L.fdmgpu_set_tile_engine.restype = C.c_int
     L.fdmgpu_get_tuning.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.fdmgpu_get_tuning.restype = C.c_int
     L.fdmgpu_set_residual_mode.restype = C.c_int
@@ -97,6 +101,13 @@ def load_library(path: str = LIB_PATH):
 def _check(st: int):
     if st != 0:
         raise FdmError(st, load_library().fdmgpu_last_error().decode())
+
+
+def measure_pipe_peaks() -> dict:
+    """FP32 and FP64 FMA rates of the current GPU in TFLOP/s (measured)."""
+    f32, f64 = C.c_double(0), C.c_double(0)
+    _check(load_library().fdmgpu_measure_pipe_peaks(C.byref(f32), C.byref(f64)))
+    return {"fp32_tflops": f32.value, "fp64_tflops": f64.value}
 
 
 def info_dict(info: abi.FdmInfo) -> dict:
@@ -136,6 +147,11 @@ class FdmSolver:
         """Accumulation of the mixed path's FP32 factor: 'fp32' (default) or
         'wide_atom' (double-float sums at the atom-harmonic steps)."""
         _check(self.lib.fdmgpu_set_factor_mode(self.h, {"fp32": 0, "wide_atom": 1}[mode]))
+
+    def set_tile_engine(self, engine: str = "tcgen05"):
+        """FP32 tile updates of mixed batches on the FP32 pipes ("simt") or on
+        the tensor cores as split-TF32 products ("tcgen05")."""
+        _check(self.lib.fdmgpu_set_tile_engine(self.h, {"simt": 0, "tcgen05": 1}[engine]))
 
     def set_autotune(self, on: bool = True):
         _check(self.lib.fdmgpu_set_autotune(self.h, 1 if on else 0))

@@ -186,6 +186,16 @@ typedef enum {
                                   escalating (not yet measured on the GPU)               */
 } fdmgpu_factor_mode;
 
+/* Arithmetic units of the FP32 tile updates of the mixed path (the trailing
+ * update of the factor, source/mat_solve_gaussian.f90:231-262 in tile form,
+ * and the forward / backward updates of the refinement solves). */
+typedef enum {
+  FDMGPU_ENGINE_SIMT = 0,      /* FP32 FMA pipes, register-blocked 64x64x64 products     */
+  FDMGPU_ENGINE_TCGEN05 = 1    /* tensor cores (tcgen05.mma kind::tf32), operands split
+                                  hi + lo into TF32 pairs, three products per tile pair:
+                                  the accuracy of FP32 products, FP32 accumulation       */
+} fdmgpu_tile_engine;
+
 /* Library version string. */
 const char* fdmgpu_version(void);
 
@@ -235,6 +245,12 @@ fdmgpu_status fdmgpu_set_tolerance(fdmgpu_handle* h, double tol, double tol_acce
  * batches planned after the call.  No counterpart in the reference. */
 fdmgpu_status fdmgpu_set_factor_mode(fdmgpu_handle* h, int32_t mode);
 
+/* Tile engine of the FP32 updates (fdmgpu_tile_engine) for the real mixed
+ * batches planned after the call; steps that accumulate wide
+ * (FDMGPU_FACTOR_WIDE_ATOM) stay on the FP32 pipes.  No counterpart in the
+ * reference. */
+fdmgpu_status fdmgpu_set_tile_engine(fdmgpu_handle* h, int32_t engine);
+
 /* Autotuner (on by default): when a batch needs a new plan, the trailing
  * update of the factor is timed on this batch with 64 threads per 64x64 tile
  * pair (8x8 accumulators per thread) and with 128 (8x4), over eight steps
@@ -244,6 +260,12 @@ fdmgpu_status fdmgpu_set_factor_mode(fdmgpu_handle* h, int32_t mode);
 fdmgpu_status fdmgpu_set_autotune(fdmgpu_handle* h, int32_t on);
 fdmgpu_status fdmgpu_get_tuning(fdmgpu_handle* h, int32_t precision, int32_t* trailing_threads, double* ms64,
                                 double* ms128);
+
+/* Measured FMA rates of the current GPU's FP32 and FP64 pipes (TFLOP/s, 2
+ * flops per FMA), the roofline peaks of the kernels that run on them.
+ * Allocates a few bytes of device memory; takes ~0.1 s.  No counterpart in
+ * the reference. */
+fdmgpu_status fdmgpu_measure_pipe_peaks(double* fp32_tflops, double* fp64_tflops);
 
 /* Counterpart of getSolverParams (source/mat_solve_gaussian.f90:376-389,
  * source/mat_solve_mumps.f90:705-736): solver name "GPU" and group size 1. */
@@ -364,8 +386,10 @@ fdmgpu_status fdmgpu_batch_adjoint_dot(fdmgpu_handle* h, const fdmgpu_energy* co
  * example by issuing them all on one stream.
  *
  * The first call on each device looks up the array's address, with that
- * device current.  That lookup can load the library's device code.  A caller
- * that captures streams should make one call on each device before capture.
+ * device current, and so does the first call after the device's context was
+ * replaced (cudaDeviceReset): the address is kept per CUDA context.  That
+ * lookup can load the library's device code.  A caller that captures streams
+ * should make one call on each device before capture.
  */
 #define FDMGPU_TAULL_NOALLOC_SCRATCH_BYTES (2 * 1024 * 1024)
 #define FDMGPU_TAULL_NOALLOC_MAX_NLMSO 512

@@ -13,7 +13,19 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+# the same sources at -O3 (the reference's build level), for the timed CPU baseline only
+LIB_TIMED_PATH = os.path.join(HERE, "_build", "liboracle_timed.so")
 _lib = None
+_use_timed = False
+
+
+def use_timed_build(on: bool = True) -> None:
+    """Route this process's oracle calls to the -O3 build (bench.py's CPU
+    baseline).  Must be called before the first oracle call of the process."""
+    global _use_timed
+    if _lib is not None and on != _use_timed:
+        raise RuntimeError("oracle library already loaded")
+    _use_timed = on
 
 
 def build() -> str:
@@ -24,9 +36,10 @@ def build() -> str:
 def lib():
     global _lib
     if _lib is None:
-        if not os.path.exists(LIB_PATH):
+        path = LIB_TIMED_PATH if _use_timed else LIB_PATH
+        if not os.path.exists(path):
             build()
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(path)
         vp = C.c_void_p
         L.oracle_mat_solve.argtypes = [vp, vp, vp, C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                        C.POINTER(C.c_double), C.POINTER(C.c_int32)]

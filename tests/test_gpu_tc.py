@@ -1,0 +1,102 @@
+"""The FP32 tile updates on the tensor cores (split-TF32 tcgen05.mma).
+
+The mixed path factors in FP32 and refines in FP64; with
+FDMGPU_ENGINE_TCGEN05 its trailing update and its refinement-solve updates
+run as three TF32 products of hi/lo operand pairs.  Parity bars are those of
+the FP32-pipe engine: the refined solution equals the oracle's to 1e-8
+(double-float residual) or 1e-10 (FP64 residual).  The products must be as
+accurate as FP32 products: per energy, the refinement needs at most a few
+more steps than with the FP32-pipe updates (a TF32-only product, ~1e-3
+relative, would stall the refinement of these matrices, whose equilibrated
+condition numbers reach 1e6-4e7).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def solver_mod():
+    from fdmnes_gb300 import build
+    build.build()
+    from fdmnes_gb300 import solver
+    return solver
+
+
+def test_golden_mixed_tcgen05_matches_oracle(solver_mod, golden):
+    from fdmnes_gb300 import abi
+    grid, energies = golden
+    sv = solver_mod.FdmSolver(grid)
+    sv.set_tile_engine("tcgen05")
+    for mode, tol in (("df64", 1e-8), ("fp64", 1e-10)):
+        sv.set_residual(mode)
+        for e in energies:
+            X, info = sv.mat_solve_args(abi.EnergyArgs(e), "mixed")
+            assert info["converged"]
+            assert rel(X, e["smr"]) < tol, (mode, rel(X, e["smr"]))
+    sv.close()
+
+
+def test_small_cluster_tcgen05_batch(solver_mod, oracle_lib):
+    from fdmnes_gb300 import abi, cluster as CL
+    st = CL.small_cu_structure()
+    ga = abi.GridArgs(st)
+    energies = (-5.0, 3.0, 12.0, 27.0, 35.0)
+    items, refs = [], []
+    for E in energies:
+        ei = CL.energy_inputs(st, E)
+        ri = CL.newind(st, ei.nlmsa, ei.nlmso)
+        ea = abi.EnergyArgs(st, ei, ri)
+        Xo, _ = oracle_lib.mat_solve(ga, ea)
+        refs.append(oracle_lib.taull(ga, ea, Xo))
+        items.append((ei, ri))
+    sv = solver_mod.FdmSolver(st)
+    sv.set_tile_engine("tcgen05")
+    T, info = sv.spectrum(items, "mixed")
+    for k, To in enumerate(refs):
+        assert rel(T[k], To) < 1e-8, (energies[k], rel(T[k], To))
+    sv.close()
+
+
+def test_full_cu_tcgen05_refines_like_fp32_pipes(solver_mod):
+    """Nine energies of the 13-atom Cu spectrum: the tensor-core engine gives
+    the FP64 cross-section to <= 1e-6 (convolved) and needs about as many
+    refinement steps per energy as the FP32-pipe engine."""
+    from fdmnes_gb300 import cluster as CL, xanes
+    st = CL.cu_structure()
+    energies = np.linspace(-5.0, 35.0, 9)
+    items = xanes.spectrum_inputs(st, energies)
+    sv = solver_mod.FdmSolver(st)
+    T64, _ = sv.spectrum(items, "fp64")
+    sv.set_tolerance(1e-8, 1e-6)
+    its = {}
+    for engine in ("simt", "tcgen05"):
+        sv.set_tile_engine(engine)
+        Tm, info = sv.spectrum(items, "mixed")
+        err = xanes.convolved_relative_error(energies, Tm, T64)
+        assert err < 1e-6, (engine, err)
+        its[engine] = [sv.stats(k)[0] for k in range(len(items))]
+    for k in range(len(items)):
+        assert its["tcgen05"][k] <= its["simt"][k] + 3, (energies[k], its)
+    sv.close()
+
+
+def test_tcgen05_with_wide_atom_steps(solver_mod):
+    """Steps marked for wide accumulation stay on the FP32 pipes while the
+    others run on the tensor cores, in the same launch sequence."""
+    from fdmnes_gb300 import cluster as CL, xanes
+    st = CL.cu_structure()
+    energies = np.array([8.0, 26.0, 34.0])
+    items = xanes.spectrum_inputs(st, energies)
+    sv = solver_mod.FdmSolver(st)
+    T64, _ = sv.spectrum(items, "fp64")
+    sv.set_tolerance(1e-8, 1e-6)
+    sv.set_factor_mode("wide_atom")
+    sv.set_tile_engine("tcgen05")
+    Tm, info = sv.spectrum(items, "mixed")
+    assert xanes.convolved_relative_error(energies, Tm, T64) < 1e-6
+    assert max(rel(a, b) for a, b in zip(Tm, T64)) < 1e-5
+    sv.close()

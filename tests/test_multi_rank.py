@@ -96,3 +96,55 @@ def test_a_failed_rank_is_detected_on_the_host(tmp_path):
     port = _free_port()
     mp.spawn(_failing_worker, args=(2, port, str(tmp_path)), nprocs=2, join=True)
     assert (tmp_path / "r0.txt").read_text().startswith("failed")
+
+
+def _fdm_worker(rank, world, port, energies, out_dir):
+    """Rank `rank` solves its round-robin share of a small Cu spectrum (the
+    oracle's FDM solve and Taull on the CPU, the per-rank work of the
+    reference's energy loop) and gathers every energy's Taull."""
+    import pickle
+    import torch.distributed as dist
+    import oracle
+    from fdmnes_gb300 import abi, cluster as CL
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    st = CL.small_cu_structure()
+    ga = abi.GridArgs(st)
+    local = {}
+    for k in shard.energy_shard(len(energies), rank, world):
+        ei = CL.energy_inputs(st, energies[k])
+        ri = CL.newind(st, ei.nlmsa, ei.nlmso)
+        ea = abi.EnergyArgs(st, ei, ri)
+        X, _ = oracle.mat_solve(ga, ea)
+        local[k] = oracle.taull(ga, ea, X)
+    res = shard.gather_by_energy(local, len(energies))
+    with open(os.path.join(out_dir, f"fdm{rank}.pkl"), "wb") as f:
+        pickle.dump(res, f)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_sharded_fdm_spectrum_equals_single_process(tmp_path):
+    """Two gloo ranks, each solving its round-robin share of a 5-energy FDM
+    spectrum, gather the same Taull, bit for bit, as one process solving all
+    energies."""
+    import pickle
+    import numpy as np
+    import oracle
+    from fdmnes_gb300 import abi, cluster as CL
+    oracle.build()
+    energies = [-5.0, 2.0, 9.0, 21.0, 35.0]
+    port = _free_port()
+    mp.spawn(_fdm_worker, args=(2, port, energies, str(tmp_path)), nprocs=2, join=True)
+    r0 = pickle.load(open(tmp_path / "fdm0.pkl", "rb"))
+    r1 = pickle.load(open(tmp_path / "fdm1.pkl", "rb"))
+    st = CL.small_cu_structure()
+    ga = abi.GridArgs(st)
+    for k, E in enumerate(energies):
+        ei = CL.energy_inputs(st, E)
+        ri = CL.newind(st, ei.nlmsa, ei.nlmso)
+        ea = abi.EnergyArgs(st, ei, ri)
+        X, _ = oracle.mat_solve(ga, ea)
+        T = oracle.taull(ga, ea, X)
+        assert np.array_equal(r0[k], T) and np.array_equal(r1[k], T), E

@@ -107,3 +107,31 @@ def test_noalloc_rejects_sizes_beyond_the_scratch(torch_cuda):
     assert f(smr.data_ptr(), 8, 16, 12, 8, out.data_ptr(), None, None) == 1  # absorber rows past nligne
     assert f(None, 8, 16, 0, 8, out.data_ptr(), None, None) == 1
     sv.close()
+
+
+def test_noalloc_reports_a_singular_normalisation(torch_cuda):
+    """nlmso = 2 with the outer block S = [[0, 1], [-1, 0]]: norm = I + iS is
+    singular, and the kernel's status word reads FDMGPU_ERR_ZERO_PIVOT (a
+    division by zero in the back substitution, no fault).  A regular call
+    afterwards reports FDMGPU_OK again."""
+    from fdmnes_gb300 import cluster as CL
+    from fdmnes_gb300.solver import FdmSolver
+    sv = FdmSolver(CL.small_cu_structure())
+    f = _bind(sv.lib)
+    # smr (nlmso = 2, nligne = 4) column-major: columns 1-2 the absorber rows,
+    # columns 3-4 the outer rows, S(i, j) = smr(i, outer row j)
+    smr = np.array([[1.0, 0.5, 0.0, 1.0],
+                    [0.25, 1.0, -1.0, 0.0]])
+    d_smr = torch_cuda.from_numpy(smr.ravel(order="F").copy()).to("cuda")
+    out = torch_cuda.zeros(2 * 2 * 2, dtype=torch_cuda.float64, device="cuda")
+    status = torch_cuda.full((1,), -1, dtype=torch_cuda.int32, device="cuda")
+    stream = torch_cuda.cuda.current_stream().cuda_stream
+    assert f(d_smr.data_ptr(), 2, 4, 0, 2, out.data_ptr(), status.data_ptr(), stream) == 0
+    torch_cuda.cuda.synchronize()
+    assert int(status.item()) == 4  # FDMGPU_ERR_ZERO_PIVOT
+    smr[:, 2:] = [[0.0, 0.5], [-0.25, 0.0]]  # I + iS regular
+    d_smr = torch_cuda.from_numpy(smr.ravel(order="F").copy()).to("cuda")
+    assert f(d_smr.data_ptr(), 2, 4, 0, 2, out.data_ptr(), status.data_ptr(), stream) == 0
+    torch_cuda.cuda.synchronize()
+    assert int(status.item()) == 0
+    sv.close()
