@@ -77,12 +77,30 @@ def grid_dict(st: CL.Structure) -> dict:
         Ylmato=st.Ylmato, Ylmso=st.Ylmso, Kar=kar, Kari=np.zeros((64, 1), order="F"))
 
 
+class FdmRadial(C.Structure):
+    _fields_ = [("ntype", C.c_int32), ("nr_max", C.c_int32), ("nspin", C.c_int32), ("nr", P_I32),
+                ("r", P_F64), ("V", P_F64), ("dv_spin", P_F64), ("z_origin", P_F64), ("itype", P_I32),
+                ("rrel", P_F64), ("rsort", P_F64), ("v0bd", C.c_double)]
+
+
+class RadialArgs:
+    """An FdmRadial struct from a Structure (cluster.radial_tables)."""
+
+    def __init__(self, st):
+        self.keep: List = []
+        self.d = CL.radial_tables(st)
+        self.s = _fill(FdmRadial, self.d, self.keep)
+
+
 def energy_dict(st: CL.Structure, ei: CL.EnergyInputs, ri: CL.RowIndex) -> dict:
-    """The per-call mat_solve arguments of one energy (real path) as plain arrays."""
+    """The per-call mat_solve arguments of one energy (real path) as plain arrays.
+    Inputs left None (phiato, Bessel, Neumann) are passed as NULL: the library
+    generates them on the device."""
     g = st.grid
+    nspinp = ei.phiato.shape[2] if ei.phiato is not None else st.nspin
     return dict(
         nligne=ri.nligne, nligneso=ri.nligneso, nlmso=ei.nlmso, lmaxso=ei.lmaxso, nlmagm=ei.nlmagm,
-        nphiato1=g.nbtm, nphiato7=1, nspinp=ei.phiato.shape[2], n_RI=1, n_ato_RI=1, nspinr=1, nsort_r=g.nsort, nsort_c=0,
+        nphiato1=g.nbtm, nphiato7=1, nspinp=nspinp, n_RI=1, n_ato_RI=1, nspinr=1, nsort_r=g.nsort, nsort_c=0,
         igrph=1, ispin=ei.ispin, nicm=1, Cal_comp=0, E_comp=0, Basereel=1, Base_hexa=0, irregular=0,
         Relativiste=0, Spinorbite=0, Repres_comp=0, Ylm_comp=0, Test_reg=0,
         Enervide=ei.enervide, Eimag=ei.eimag, new_=ri.new, newinv=ri.newinv, lb1=ri.lb1, lb2=ri.lb2,

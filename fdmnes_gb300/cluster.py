@@ -760,9 +760,9 @@ class EnergyInputs:
     nlmsa: np.ndarray          # (natome,)
     nlmso: int
     nlmagm: int
-    phiato: np.ndarray         # (nbtm, nlmagm, nspinp=nspin, nspino=1, n_RI=1, natome, nphiato7=1) F
-    besselr: np.ndarray        # (nsort, 0:lmaxso, nspinr=1) F
-    neumanr: np.ndarray
+    phiato: Optional[np.ndarray]   # (nbtm, nlmagm, nspinp=nspin, nspino=1, n_RI=1, natome, nphiato7=1) F
+    besselr: Optional[np.ndarray]  # (nsort, 0:lmaxso, nspinr=1) F; None: generated on the device
+    neumanr: Optional[np.ndarray]
     ispin: int = 1
 
 
@@ -794,8 +794,34 @@ def boundary_radial(st: Structure, enervide: float, lmaxa: np.ndarray) -> Dict[t
     return out
 
 
-def energy_inputs(st: Structure, energy_ev: float, e_fermi_ev: float = -5.0, ispin: int = 1) -> EnergyInputs:
-    """Per-energy inputs: l cut-offs, atomic boundary functions, Bessel/Neumann."""
+def radial_tables(st: Structure) -> dict:
+    """The structure's radial data in the layout of fdmgpu_radial: per atom type
+    the radial mesh and spherical potential, the spin shifts, the charge of the
+    expansion at the origin (Z, plus one for the absorber's type, as
+    boundary_radial uses), atom types (1-based), boundary distances and the
+    radii of the outer points."""
+    cl, g = st.cluster, st.grid
+    ntype = len(st.radial_r)
+    nr = np.array([len(r) for r in st.radial_r], dtype=np.int32)
+    nr_max = int(nr.max())
+    r = np.zeros((nr_max, ntype), order="F")
+    V = np.zeros((nr_max, ntype), order="F")
+    for t in range(ntype):
+        r[:nr[t], t] = st.radial_r[t]
+        V[:nr[t], t] = st.radial_V[t]
+    return dict(ntype=ntype, nr_max=nr_max, nspin=st.nspin, nr=nr, r=r, V=V,
+                dv_spin=np.array([st.spin_shift(i) for i in range(1, st.nspin + 1)]),
+                z_origin=np.array([float(cl.zproto[t]) + (1.0 if t == 0 else 0.0) for t in range(ntype)]),
+                itype=(np.asarray(cl.itype, dtype=np.int32) + 1), rrel=st.rrel,
+                rsort=np.ascontiguousarray(g.xyz[3, g.isrt - 1]), v0bd=st.V0bd)
+
+
+def energy_inputs(st: Structure, energy_ev: float, e_fermi_ev: float = -5.0, ispin: int = 1,
+                  functions: bool = True) -> EnergyInputs:
+    """Per-energy inputs: l cut-offs, atomic boundary functions, Bessel/Neumann.
+    With functions=False only the cut-offs and sizes are formed (phiato,
+    besselr and neumanr are None): the library then generates them on the
+    device from the structure's radial tables (radial_tables)."""
     cl, g = st.cluster, st.grid
     enervide = (energy_ev + e_fermi_ev) / RYDB
     dv = st.spin_shift(ispin)
@@ -815,6 +841,10 @@ def energy_inputs(st: Structure, energy_ev: float, e_fermi_ev: float = -5.0, isp
     nlmso = (lmaxso + 1) ** 2
     lmax_g = int(lmaxat.max())
     nlmagm = (lmax_g + 1) ** 2
+    if not functions:
+        return EnergyInputs(energy_ev=energy_ev, enervide=enervide, eimag=0.0, ecinetic_out=ecin_out,
+                            lmaxa=lmaxa, lmaxso=lmaxso, nlmsa=nlmsa, nlmso=nlmso, nlmagm=nlmagm,
+                            phiato=None, besselr=None, neumanr=None, ispin=ispin)
     # radial solutions per prototype, spin and L, then cal_phiato per atom.
     # phiato holds every spin block (nspinp = nspin): the grid rows of
     # calcMatRow read it at min(ispin, nspin) (source/mat.f90:1144,1296-1304).

@@ -73,6 +73,7 @@ struct HostProb {
   std::vector<double> in_d;
   // offsets inside in_d of the Vr, gradvr, phiato, Bessel and Neumann blocks
   int64_t rel_grad = 0, rel_phi = 0, rel_bes = 0, rel_neu = 0;
+  int64_t gen_phi = 0, gen_bes = 0;   // generated inputs: doubles of phiato and of one Bessel table
   int nlmsa_max = 0;
   uint64_t sig = 0;
 };
@@ -164,6 +165,25 @@ struct fdmgpu_handle {
   int plan_prec = -1;
   cudaGraphExec_t g_asm = nullptr, g_fac = nullptr, g_sol = nullptr, g_res = nullptr, g_iter = nullptr;
   int64_t nk_asm = 0, nk_fac = 0, nk_sol = 0, nk_res = 0, nk_iter = 0;  // kernel nodes per graph
+  // classical refinement driven on the device: the stopping rule of every
+  // step is evaluated by k_refine_check and a while node repeats the step
+  cudaGraphExec_t g_loop = nullptr;
+  int64_t nk_loop_body = 0;
+  DevBuf<double> d_xs;  // cross-section inputs and outputs of fdmgpu_batch_xanes
+  // radial tables of this grid's atom types (fdmgpu_set_radial) for inputs
+  // generated on the device
+  bool has_radial = false;
+  RadialDev rad{};
+  int rad_ntype = 0, rad_nr_max = 0;
+  double rad_v0bd = 0.0, rad_dv_max = 0.0;
+  std::vector<int> rad_itype;           // host copy, 0-based
+  DevBuf<int> d_rad_i;                  // nr | itype | iidx
+  DevBuf<double> d_rad_d;               // r | mcl0 | gm | gp | f2 | V | dv | z | rrel | rsort
+  DevBuf<RadialDev> d_rads;             // per batch site
+  DevBuf<double> d_radU;                // radial solutions of a batch
+  GenDims gdims;
+  DevBuf<RefineState> d_rstate;
+  DevBuf<RefineCtl> d_rctl;
   StepPlan sp;
   LaunchDims dims;
   Tables tb{};
@@ -227,11 +247,25 @@ fdmgpu_status check_energy(const fdmgpu_handle* h, const fdmgpu_energy* e) {
   if (e->lmaxso < 0 || (e->lmaxso + 1) * (e->lmaxso + 1) < e->nlmso || e->nsort_r < h->g.nsort)
     return fail(FDMGPU_ERR_ARG, "Bessel arrays too small for nlmso");
   if (e->nlmso > h->g.nso1) return fail(FDMGPU_ERR_ARG, "nlmso exceeds the outer harmonic tables");
-  if (e->ispin < 1 || e->nspinp < std::min(e->ispin, h->g.nspin))
+  const bool gen = !e->phiato && !e->Besselr && !e->Neumanr;
+  if (gen && !h->has_radial)
+    return fail(FDMGPU_ERR_ARG, "phiato / Besselr / Neumanr are NULL but the grid has no radial tables "
+                                "(fdmgpu_set_radial)");
+  if (e->ispin < 1 || (!gen && e->nspinp < std::min(e->ispin, h->g.nspin)))
     return fail(FDMGPU_ERR_ARG, "phiato must hold spin block min(ispin, nspin) (nspinp too small)");
-  if (!e->new_ || !e->newinv || !e->lb1 || !e->lb2 || !e->ianew || !e->nlmsa || !e->Vr || !e->phiato ||
-      !e->Besselr || !e->Neumanr)
+  if (!e->new_ || !e->newinv || !e->lb1 || !e->lb2 || !e->ianew || !e->nlmsa || !e->Vr ||
+      (!gen && (!e->phiato || !e->Besselr || !e->Neumanr)))
     return fail(FDMGPU_ERR_ARG, "null array argument");
+  if (gen) {
+    // the generated phiato holds the atoms' harmonics up to their type's cut-off
+    for (int ia = 0; ia < h->g.natome; ++ia) {
+      const int l = (int)std::lround(std::sqrt((double)e->nlmsa[ia])) - 1;
+      if ((l + 1) * (l + 1) != e->nlmsa[ia] || e->nlmsa[ia] > e->nlmagm)
+        return fail(FDMGPU_ERR_ARG, "nlmsa must be (lmax + 1)^2 <= nlmagm with generated inputs");
+    }
+    if (e->Enervide - h->rad_v0bd - h->rad_dv_max <= 0.0)
+      return fail(FDMGPU_ERR_ARG, "generated inputs need a positive kinetic energy");
+  }
   return FDMGPU_OK;
 }
 
@@ -403,6 +437,23 @@ void pack_inputs(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& hp) {
   // doubles: Vr(:, ispp)
   const int ispp = std::min(e->ispin, g.nspin);
   hp.in_d.insert(hp.in_d.end(), e->Vr + (int64_t)g.npoint * (ispp - 1), e->Vr + (int64_t)g.npoint * ispp);
+  if (!e->phiato) {
+    // generated on the device: only their sizes here; upload_inputs places
+    // them after every uploaded block
+    hp.P.gen = 1;
+    for (int t = 0; t < MAX_GEN_TYPES; ++t) hp.P.gen_lmax[t] = -1;
+    for (int ia = 0; ia < g.natome; ++ia) {
+      const int t = h->rad_itype[ia];
+      const int l = (int)std::lround(std::sqrt((double)e->nlmsa[ia])) - 1;
+      hp.P.gen_lmax[t] = std::max(hp.P.gen_lmax[t], l);
+    }
+    hp.gen_phi = (int64_t)g.nbtm * e->nlmagm * g.natome;
+    hp.gen_bes = (int64_t)g.nsort * (e->lmaxso + 1);
+    hp.rel_grad = g.npoint;
+    hp.rel_phi = hp.rel_bes = hp.rel_neu = -1;
+    return;
+  }
+  hp.P.gen = 0;
   // phiato(ib, Lm, isp, isol=1, iRI=1, ia, 1) -> (nbtm, nlmagm, natome)
   const int isp = std::min(e->ispin, g.nspin);  // calcMatRow reads phiato at min(ispin, nspin)
   const int64_t d1 = e->nphiato1, d2 = e->nlmagm, d3 = e->nspinp, d4 = g.nspino, d5 = e->n_RI;
@@ -450,7 +501,7 @@ void build_step_plan(fdmgpu_handle* h) {
   sp.wide_any.assign(N, 0);
   if (h->tb.wide)
     for (auto& hp : pr)
-      for (int K = 0; K < hp.P.nt; ++K) sp.wide_any[K] |= hp.wide[K];
+      for (int K = 0; K < hp.P.nt; ++K) sp.wide_any[K] |= (h->factor_mode == FDMGPU_FACTOR_WIDE_ALL) ? 1 : hp.wide[K];
   sp.trail_tc.assign(N, 0);
   sp.fwd_tc.assign(N, 0);
   sp.bwd_tc.assign(N, 0);
@@ -525,7 +576,10 @@ void layout_batch(fdmgpu_handle* h, Layout& L) {
     Imax.insert(Imax.end(), hp.Imax.begin(), hp.Imax.end());
     Imin.insert(Imin.end(), hp.Imin.begin(), hp.Imin.end());
     strip.insert(strip.end(), hp.strip.begin(), hp.strip.end());
-    L.wide.insert(L.wide.end(), hp.wide.begin(), hp.wide.end());
+    if (h->factor_mode == FDMGPU_FACTOR_WIDE_ALL)
+      L.wide.insert(L.wide.end(), hp.wide.size(), (unsigned char)1);
+    else
+      L.wide.insert(L.wide.end(), hp.wide.begin(), hp.wide.end());
     d.max_rows = std::max(d.max_rows, P.nt * TS);
     d.max_tiles = std::max<int>(d.max_tiles, (int)hp.ntiles);
     d.max_rhs_tiles = std::max(d.max_rhs_tiles, P.nt * P.nrt);
@@ -580,9 +634,10 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   h->tb.Imax = h->d_Imax.p;
   h->tb.Imin = h->d_Imin.p;
   h->tb.strip = h->d_strip.p;
-  h->tb.wide = (mixed && h->factor_mode == FDMGPU_FACTOR_WIDE_ATOM) ? h->d_wide.p : nullptr;
+  h->tb.wide = (mixed && h->factor_mode != FDMGPU_FACTOR_FP32) ? h->d_wide.p : nullptr;
   // real mixed batches may run their FP32 tile updates on the tensor cores
-  h->sp.tc = (mixed && !cplx && h->tile_engine == FDMGPU_ENGINE_TCGEN05) ? 1 : 0;
+  h->sp.tc = (mixed && !cplx && h->tile_engine != FDMGPU_ENGINE_SIMT) ? 1 : 0;
+  h->sp.tc_solve = (mixed && !cplx && h->tile_engine == FDMGPU_ENGINE_TCGEN05) ? 1 : 0;
   h->sp.tc_err = h->d_err.p;
   Pools& pl = h->pl;
   pl = Pools();
@@ -642,15 +697,33 @@ fdmgpu_status upload_inputs(fdmgpu_handle* h) {
     hp.P.in_neu = nd + hp.rel_neu;
     nd += hp.in_d.size();
   }
+  // device-generated phiato / Bessel / Neumann after the uploaded doubles
+  const size_t nd_up = nd;
+  GenDims& gd = h->gdims;
+  gd = GenDims();
+  for (auto& hp : pr) {
+    if (!hp.P.gen) continue;
+    const fdmgpu_handle* sh = h->batch.sites[hp.P.site];
+    hp.P.in_phi = nd;
+    hp.P.in_bes = nd + hp.gen_phi;
+    hp.P.in_neu = nd + hp.gen_phi + hp.gen_bes;
+    nd += hp.gen_phi + 2 * hp.gen_bes;
+    ++gd.nprob_gen;
+    gd.ntype_max = std::max(gd.ntype_max, sh->rad_ntype);
+    for (int t = 0; t < MAX_GEN_TYPES; ++t) gd.lmax1 = std::max(gd.lmax1, hp.P.gen_lmax[t] + 1);
+    gd.natome_max = std::max(gd.natome_max, sh->g.natome);
+    gd.nsort_max = std::max(gd.nsort_max, sh->g.nsort);
+    gd.nr_max = std::max(gd.nr_max, sh->rad_nr_max);
+  }
   if (ni > h->h_pinned_i_cap) {
     if (h->h_pinned_i) cudaFreeHost(h->h_pinned_i);
     CK(cudaMallocHost(&h->h_pinned_i, ni * sizeof(int)));
     h->h_pinned_i_cap = ni;
   }
-  if (nd > h->h_pinned_d_cap) {
+  if (nd_up > h->h_pinned_d_cap) {
     if (h->h_pinned_d) cudaFreeHost(h->h_pinned_d);
-    CK(cudaMallocHost(&h->h_pinned_d, nd * sizeof(double)));
-    h->h_pinned_d_cap = nd;
+    CK(cudaMallocHost(&h->h_pinned_d, nd_up * sizeof(double)));
+    h->h_pinned_d_cap = nd_up;
   }
   CK(cudaStreamSynchronize(h->stream));  // the pinned buffers may still feed a previous copy
   size_t oi = 0, od = 0;
@@ -665,11 +738,17 @@ fdmgpu_status upload_inputs(fdmgpu_handle* h) {
   if (h->d_ipool.reserve(ni) != cudaSuccess || h->d_dpool.reserve(nd) != cudaSuccess)
     return fail(FDMGPU_ERR_NOMEM, "device allocation of the input pools failed");
   CK(cudaMemcpyAsync(h->d_ipool.p, h->h_pinned_i, ni * sizeof(int), cudaMemcpyHostToDevice, h->stream));
-  CK(cudaMemcpyAsync(h->d_dpool.p, h->h_pinned_d, nd * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  CK(cudaMemcpyAsync(h->d_dpool.p, h->h_pinned_d, nd_up * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   CK(upload(h->d_probs, P, h->stream));
   std::vector<StaticDev> sites;
   for (auto* sh : h->batch.sites) sites.push_back(sh->S);
   CK(upload(h->d_sites, sites, h->stream));
+  std::vector<RadialDev> rads;
+  for (auto* sh : h->batch.sites) rads.push_back(sh->rad);
+  CK(upload(h->d_rads, rads, h->stream));
+  if (gd.nprob_gen > 0 &&
+      h->d_radU.reserve((size_t)h->batch.probs.size() * gd.ntype_max * gd.lmax1 * gd.nr_max) != cudaSuccess)
+    return fail(FDMGPU_ERR_NOMEM, "radial solution scratch");
   h->pl.ipool = h->d_ipool.p;
   h->pl.dpool = h->d_dpool.p;
   return FDMGPU_OK;
@@ -692,10 +771,13 @@ void record_asm(fdmgpu_handle* h) {
   cudaMemsetAsync(pl.env64, 0, env * sizeof(double), s);
   cudaMemsetAsync(pl.B64, 0, rhs * sizeof(double), s);
   cudaMemsetAsync(pl.err, 0, np * sizeof(int), s);
-  if (h->batch.cplx == 1)
+  if (h->batch.cplx == 1) {
     launch_assemble_c(h->d_sites.p, probs, pl, h->tb, h->dims, 0, s);
-  else
+  } else {
+    launch_generate_inputs(probs, h->d_rads.p, h->d_sites.p, h->d_ipool.p, h->dims, h->gdims, h->d_radU.p,
+                           h->d_dpool.p, s);
     launch_assemble(h->d_sites.p, probs, pl, h->tb, h->dims, s);
+  }
   if (h->batch.precision == FDMGPU_PREC_FP64) {
     cudaMemcpyAsync(pl.X64, pl.B64, rhs * sizeof(double), cudaMemcpyDeviceToDevice, s);
   } else {
@@ -801,6 +883,66 @@ void record_iter(fdmgpu_handle* h) {
   if (h->refine_recur) launch_resid_update(probs, pl, h->dims, s);
 }
 
+size_t count_kernel_nodes(cudaGraph_t graph) {
+  size_t nn = 0;
+  if (cudaGraphGetNodes(graph, nullptr, &nn) != cudaSuccess) return 0;
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (nn && cudaGraphGetNodes(graph, nodes.data(), &nn) != cudaSuccess) return 0;
+  size_t nk = 0;
+  for (auto nd : nodes) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++nk;
+  }
+  return nk;
+}
+
+// The refinement loop as one graph: the stopping rule of the first step (whose
+// residual and solves the caller launches, so the first residual can be timed)
+// followed by a while node whose body is one more step plus its stopping rule.
+fdmgpu_status capture_refine_loop(fdmgpu_handle* h) {
+  if (h->g_loop) {
+    cudaGraphExecDestroy(h->g_loop);
+    h->g_loop = nullptr;
+  }
+  const int np = h->dims.nprob;
+  cudaGraph_t g = nullptr;
+  CK(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle cond;
+  fdmgpu_status st = FDMGPU_OK;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&cond, g, 0, 0);
+  cudaGraphNode_t first = nullptr, loop = nullptr;
+  size_t nn = 1;
+  cudaGraphNodeParams cp = {};
+  if (e == cudaSuccess) e = cudaStreamBeginCaptureToGraph(h->stream, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    launch_refine_check(h->d_rstate.p, h->d_active.p, h->pl, h->d_rctl.p, np, cond, 1, h->stream);
+    e = cudaStreamEndCapture(h->stream, &g);
+  }
+  if (e == cudaSuccess) e = cudaGraphGetNodes(g, &first, &nn);
+  if (e == cudaSuccess) {
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = cond;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    e = cudaGraphAddNode(&loop, g, &first, nullptr, 1, &cp);
+  }
+  if (e == cudaSuccess) {
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    e = cudaStreamBeginCaptureToGraph(h->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+      record_residual(h);
+      record_iter(h);
+      launch_refine_check(h->d_rstate.p, h->d_active.p, h->pl, h->d_rctl.p, np, cond, 1, h->stream);
+      e = cudaStreamEndCapture(h->stream, &body);
+    }
+    if (e == cudaSuccess) h->nk_loop_body = (int64_t)count_kernel_nodes(body);
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&h->g_loop, g, 0);
+  if (e != cudaSuccess) st = fail(FDMGPU_ERR_CUDA, std::string("refinement loop graph: ") + cudaGetErrorString(e));
+  cudaGraphDestroy(g);
+  return st;
+}
+
 fdmgpu_status capture(fdmgpu_handle* h, void (*rec)(fdmgpu_handle*), cudaGraphExec_t* out, int64_t* nkernels) {
   if (*out) {
     cudaGraphExecDestroy(*out);
@@ -843,6 +985,11 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   sig = mix(sig, (uint64_t)(h->refine_gmres * 1000 + h->gmres_m));
   sig = mix(sig, (uint64_t)h->factor_mode + 77u);
   sig = mix(sig, (uint64_t)h->tile_engine + 191u);
+  for (auto& hp : b.probs) {
+    sig = mix(sig, (uint64_t)hp.P.gen * 31u);
+    if (hp.P.gen)
+      for (int t = 0; t < MAX_GEN_TYPES; ++t) sig = mix(sig, (uint64_t)(hp.P.gen_lmax[t] + 2) * 7u + t);
+  }
   const bool replan = sig != h->plan_sig || b.precision != h->plan_prec || !h->g_asm;
   Layout lay;
   layout_batch(h, lay);
@@ -864,7 +1011,8 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
                         h->d_piv.p,   h->d_val2.p,  h->d_Xs.p,    h->d_valS.p,  h->d_V.p,    h->d_W.p,
                         h->d_gstate.p, h->d_inner.p, h->d_jdone.p, h->d_notconv.p, h->d_active_gm.p,
                         h->d_nb_coef.p, h->d_rvol.p, h->d_poidsa.p, h->d_poidso.p, h->d_Kar.p, h->d_YsoT.p,
-                        h->d_Ylmato.p, h->d_R32.p, h->d_act_df.p, h->d_act_rec.p, h->d_sites.p, h->d_wide.p};
+                        h->d_Ylmato.p, h->d_R32.p, h->d_act_df.p, h->d_act_rec.p, h->d_sites.p, h->d_wide.p,
+                        h->d_rads.p,  h->d_radU.p};
   for (const void* q : ptrs) ps = mix(ps, (uint64_t)(uintptr_t)q);
   if (replan && h->autotune) {
     st = tune_trailing(h);
@@ -882,6 +1030,10 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
       st = capture(h, record_residual, &h->g_res, &h->nk_res);
       if (st) return st;
       st = capture(h, record_iter, &h->g_iter, &h->nk_iter);
+      if (st) return st;
+      if (h->d_rstate.reserve(np) != cudaSuccess || h->d_rctl.reserve(1) != cudaSuccess)
+        return fail(FDMGPU_ERR_NOMEM, "refinement state");
+      st = capture_refine_loop(h);
       if (st) return st;
     }
     h->plan_sig = sig;
@@ -987,7 +1139,32 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
     if (h->refine_gmres)
       CK(cudaMemsetAsync(h->d_active_gm.p, 0, np * sizeof(int), h->stream));
     CK(cudaEventRecord(h->ev[4], h->stream));
-    for (int it = 1; it <= max_iter; ++it) {
+    // Classical refinement: the whole loop runs on the device (one graph with
+    // a while node, k_refine_check deciding after every step); the host reads
+    // the per-problem outcome once at the end.
+    const bool dev_loop = !h->refine_gmres && !h->refine_recur && !overlap;
+    if (dev_loop) {
+      const RefineCtl c0{0, max_iter, tol, np, 0};
+      CK(cudaMemcpyAsync(h->d_rctl.p, &c0, sizeof c0, cudaMemcpyHostToDevice, h->stream));
+      launch_refine_init(h->d_rstate.p, h->d_active.p, np, h->stream);
+      CK(cudaEventRecord(h->ev[6], h->stream));
+      CK(cudaGraphLaunch(h->g_res, h->stream));
+      CK(cudaEventRecord(h->ev[7], h->stream));
+      CK(cudaGraphLaunch(h->g_iter, h->stream));
+      CK(cudaGraphLaunch(h->g_loop, h->stream));
+      std::vector<RefineState> rs(np);
+      RefineCtl c1;
+      CK(cudaMemcpyAsync(rs.data(), h->d_rstate.p, np * sizeof(RefineState), cudaMemcpyDeviceToHost, h->stream));
+      CK(cudaMemcpyAsync(&c1, h->d_rctl.p, sizeof c1, cudaMemcpyDeviceToHost, h->stream));
+      CK(cudaStreamSynchronize(h->stream));
+      nkern += 2 + h->nk_res + h->nk_iter + (int64_t)std::max(c1.it - 1, 0) * h->nk_loop_body;
+      for (int k = 0; k < np; ++k) {
+        b.iters[k] = rs[k].iters;
+        b.resid[k] = rs[k].resid;
+        active[k] = rs[k].active;
+      }
+    }
+    for (int it = 1; it <= max_iter && !dev_loop; ++it) {
       if (it == 1) CK(cudaEventRecord(h->ev[6], h->stream));
       CK(cudaGraphLaunch(h->g_res, h->stream));
       if (it == 1) CK(cudaEventRecord(h->ev[7], h->stream));
@@ -1480,6 +1657,14 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   if (h->g_fac) cudaGraphExecDestroy(h->g_fac);
   if (h->g_sol) cudaGraphExecDestroy(h->g_sol);
   if (h->g_iter) cudaGraphExecDestroy(h->g_iter);
+  if (h->g_loop) cudaGraphExecDestroy(h->g_loop);
+  h->d_rstate.release();
+  h->d_rctl.release();
+  h->d_xs.release();
+  h->d_rad_i.release();
+  h->d_rad_d.release();
+  h->d_rads.release();
+  h->d_radU.release();
   if (h->g_res) cudaGraphExecDestroy(h->g_res);
   h->d_nnz.release();
   DevBuf<int>* ib[] = {&h->d_inter_pt, &h->d_nb_kind, &h->d_nb_idx, &h->d_numia, &h->d_nbord, &h->d_nbordf,
@@ -1563,14 +1748,117 @@ fdmgpu_status fdmgpu_set_tolerance(fdmgpu_handle* h, double tol, double tol_acce
 
 fdmgpu_status fdmgpu_set_factor_mode(fdmgpu_handle* h, int32_t mode) {
   if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
-  if (mode != FDMGPU_FACTOR_FP32 && mode != FDMGPU_FACTOR_WIDE_ATOM) return fail(FDMGPU_ERR_ARG, "unknown factor mode");
+  if (mode != FDMGPU_FACTOR_FP32 && mode != FDMGPU_FACTOR_WIDE_ATOM && mode != FDMGPU_FACTOR_WIDE_ALL)
+    return fail(FDMGPU_ERR_ARG, "unknown factor mode");
   h->factor_mode = mode;
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_set_radial(fdmgpu_handle* h, const fdmgpu_radial* rd) {
+  if (!h || !rd) return fail(FDMGPU_ERR_ARG, "null argument");
+  const fdmgpu_grid& g = h->g;
+  if (g.nspino != 1) return fail(FDMGPU_ERR_UNSUPPORTED, "generated inputs are provided for the real path (nspino = 1)");
+  if (rd->ntype < 1 || rd->ntype > MAX_GEN_TYPES || rd->nr_max < 4 || rd->nspin < 1 || !rd->nr || !rd->r || !rd->V ||
+      !rd->dv_spin || !rd->z_origin || !rd->itype || !rd->rrel || !rd->rsort)
+    return fail(FDMGPU_ERR_ARG, "radial tables: bad sizes or null arrays (1 <= ntype <= 8)");
+  const int T = rd->ntype, NR = rd->nr_max, nb = g.nbtm, na = g.natome;
+  std::vector<int> ih(T + na + (size_t)nb * na, 0);
+  std::vector<double> dh((size_t)6 * NR * T + rd->nspin + T + (size_t)nb * na + g.nsort, 0.0);
+  double* r = dh.data();
+  double* mcl0 = r + (size_t)NR * T;
+  double* gm = mcl0 + (size_t)NR * T;
+  double* gp = gm + (size_t)NR * T;
+  double* f2 = gp + (size_t)NR * T;
+  double* V = f2 + (size_t)NR * T;
+  double* dv = V + (size_t)NR * T;
+  double* z = dv + rd->nspin;
+  double* rrel = z + T;
+  double* rsort = rrel + (size_t)nb * na;
+  h->rad_dv_max = -1e300;
+  for (int i = 0; i < rd->nspin; ++i) {
+    dv[i] = rd->dv_spin[i];
+    h->rad_dv_max = std::max(h->rad_dv_max, dv[i]);
+  }
+  for (int t = 0; t < T; ++t) {
+    const int n = rd->nr[t];
+    if (n < 4 || n > NR) return fail(FDMGPU_ERR_ARG, "radial mesh size out of range");
+    ih[t] = n;
+    z[t] = rd->z_origin[t];
+    const double* rt = rd->r + (size_t)NR * t;
+    for (int i = 0; i < n; ++i) {
+      if (!(rt[i] > 0.0) || (i > 0 && !(rt[i] > rt[i - 1]))) return fail(FDMGPU_ERR_ARG, "radial mesh must increase");
+      r[(size_t)NR * t + i] = rt[i];
+      V[(size_t)NR * t + i] = rd->V[(size_t)NR * t + i];
+    }
+    // three-point Laplacian coefficients of the mesh (coef_sch_rad,
+    // source/sphere.f90:324-396), with the mesh extended geometrically past
+    // both ends
+    for (int i = 0; i < n; ++i) {
+      const double rp = i + 1 < n ? rt[i + 1] : rt[n - 1] * rt[n - 1] / rt[n - 2];
+      const double rm = i > 0 ? rt[i - 1] : rt[0] * rt[0] / rt[1];
+      const double drr = 0.5 * (rp - rm);
+      const double cm = 1.0 / ((rt[i] - rm) * drr), cp = 1.0 / ((rp - rt[i]) * drr);
+      const double c0 = -cm - cp;
+      mcl0[(size_t)NR * t + i] = -c0;
+      gm[(size_t)NR * t + i] = -cm;
+      gp[(size_t)NR * t + i] = -cp;
+      f2[(size_t)NR * t + i] = 1.0 / (rt[i] * rt[i]);
+    }
+  }
+  h->rad_itype.assign(na, 0);
+  for (int ia = 0; ia < na; ++ia) {
+    const int t = rd->itype[ia] - 1;
+    if (t < 0 || t >= T) return fail(FDMGPU_ERR_ARG, "itype out of range");
+    ih[T + ia] = t;
+    h->rad_itype[ia] = t;
+    const double* rt = rd->r + (size_t)NR * t;
+    const int n = rd->nr[t];
+    for (int ib = 0; ib < g.nbord[ia] && ib < nb; ++ib) {
+      const double x = rd->rrel[ib + (size_t)nb * ia];
+      rrel[ib + (size_t)nb * ia] = x;
+      // first mesh point beyond x, kept inside [2, n - 1] (cal_phiato's stencil)
+      int k = (int)(std::upper_bound(rt, rt + n, x) - rt);
+      k = std::min(std::max(k, 2), n - 1);
+      ih[T + na + ib + (size_t)nb * ia] = k;
+    }
+  }
+  for (int ib = 0; ib < g.nsort; ++ib) rsort[ib] = rd->rsort[ib];
+  cudaStream_t s = h->stream;
+  CK(upload(h->d_rad_i, ih, s));
+  CK(upload(h->d_rad_d, dh, s));
+  CK(cudaStreamSynchronize(s));
+  RadialDev R{};
+  R.ntype = T;
+  R.nr_max = NR;
+  R.nspin = rd->nspin;
+  R.nr = h->d_rad_i.p;
+  R.itype = h->d_rad_i.p + T;
+  R.iidx = h->d_rad_i.p + T + na;
+  const double* b = h->d_rad_d.p;
+  R.r = b;
+  R.mcl0 = b + (size_t)NR * T;
+  R.gm = b + (size_t)2 * NR * T;
+  R.gp = b + (size_t)3 * NR * T;
+  R.f2 = b + (size_t)4 * NR * T;
+  R.V = b + (size_t)5 * NR * T;
+  R.dv_spin = b + (size_t)6 * NR * T;
+  R.z_origin = R.dv_spin + rd->nspin;
+  R.rrel = R.z_origin + T;
+  R.rsort = R.rrel + (size_t)nb * na;
+  R.v0bd = rd->v0bd;
+  h->rad = R;
+  h->rad_ntype = T;
+  h->rad_nr_max = NR;
+  h->rad_v0bd = rd->v0bd;
+  h->has_radial = true;
+  h->plan_sig = 0;
   return FDMGPU_OK;
 }
 
 fdmgpu_status fdmgpu_set_tile_engine(fdmgpu_handle* h, int32_t engine) {
   if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
-  if (engine != FDMGPU_ENGINE_SIMT && engine != FDMGPU_ENGINE_TCGEN05) return fail(FDMGPU_ERR_ARG, "unknown tile engine");
+  if (engine != FDMGPU_ENGINE_SIMT && engine != FDMGPU_ENGINE_TCGEN05 && engine != FDMGPU_ENGINE_TCGEN05_FACTOR)
+    return fail(FDMGPU_ERR_ARG, "unknown tile engine");
   h->tile_engine = engine;
   return FDMGPU_OK;
 }
@@ -2038,6 +2326,66 @@ fdmgpu_status fdmgpu_batch_adjoint_dot(fdmgpu_handle* h, const fdmgpu_energy* co
   CK(cudaStreamSynchronize(s));
   for (int k = 0; k < np; ++k)
     if (err[k]) return fail((fdmgpu_status)err[k], "assembly of energy " + std::to_string(k) + " failed");
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_batch_inputs(fdmgpu_handle* h, int32_t k, double* phiato, double* besselr, double* neumanr) {
+  if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
+  Batch& b = h->batch;
+  if (k < 0 || k >= (int)b.probs.size() || !b.ran) return fail(FDMGPU_ERR_ARG, "no such energy in the last run");
+  const HostProb& hp = b.probs[k];
+  if (hp.P.cplx) return fail(FDMGPU_ERR_UNSUPPORTED, "real problems only");
+  const fdmgpu_grid& g = b.sites[hp.P.site]->g;
+  const size_t nphi = (size_t)g.nbtm * hp.P.nlmagm * g.natome, nb = (size_t)g.nsort * (hp.P.lmaxso + 1);
+  cudaStream_t s = h->stream;
+  if (phiato) CK(cudaMemcpyAsync(phiato, h->d_dpool.p + hp.P.in_phi, nphi * sizeof(double), cudaMemcpyDeviceToHost, s));
+  // [ib][L] on the device -> (nsort, 0:lmaxso) column-major
+  std::vector<double> t(nb);
+  for (int w = 0; w < 2; ++w) {
+    double* out = w == 0 ? besselr : neumanr;
+    if (!out) continue;
+    CK(cudaMemcpyAsync(t.data(), h->d_dpool.p + (w == 0 ? hp.P.in_bes : hp.P.in_neu), nb * sizeof(double),
+                       cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const int nl = hp.P.lmaxso + 1;
+    for (int ib = 0; ib < g.nsort; ++ib)
+      for (int L = 0; L < nl; ++L) out[ib + (size_t)g.nsort * L] = t[(size_t)ib * nl + L];
+  }
+  CK(cudaStreamSynchronize(s));
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_batch_xanes(fdmgpu_handle* h, const double* energies_ev, const double* half_width,
+                                 int32_t width_per_input, const double* weight, double* sigma, double* sigma_conv,
+                                 double* tensor) {
+  if (!h || !energies_ev || !half_width || !sigma) return fail(FDMGPU_ERR_ARG, "null argument");
+  Batch& b = h->batch;
+  const int n = (int)b.probs.size();
+  if (!b.ran || n == 0) return fail(FDMGPU_ERR_ARG, "run a batch first");
+  if (b.probs[0].P.nlm_abs < 4) return fail(FDMGPU_ERR_ARG, "the absorber needs its p harmonics (lmax >= 1)");
+  if (b.cplx == 1 && tensor) return fail(FDMGPU_ERR_UNSUPPORTED, "the Cartesian tensor is formed for real batches only");
+  for (int k = 1; k < n; ++k)
+    if (!(energies_ev[k] > energies_ev[k - 1])) return fail(FDMGPU_ERR_ARG, "energies must increase, one problem each");
+  if (sigma_conv && n < 2) return fail(FDMGPU_ERR_ARG, "the convolution needs two energies");
+  // E | width | weight | sigma | conv | tensor
+  if (h->d_xs.reserve((size_t)n * 14) != cudaSuccess) return fail(FDMGPU_ERR_NOMEM, "cross-section buffers");
+  double* dE = h->d_xs.p;
+  double* dW = dE + n;
+  double* dw = dW + n;
+  double* dS = dw + n;
+  double* dC = dS + n;
+  double* dT = dC + n;
+  cudaStream_t s = h->stream;
+  CK(cudaMemcpyAsync(dE, energies_ev, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dW, half_width, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (weight) CK(cudaMemcpyAsync(dw, weight, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  launch_dipole(h->d_probs.p, h->pl.taull, weight ? dw : nullptr, n, dS, tensor ? dT : nullptr, s);
+  if (sigma_conv) launch_lorentz(dE, dS, dW, width_per_input != 0, n, dC, s);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(sigma, dS, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (sigma_conv) CK(cudaMemcpyAsync(sigma_conv, dC, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (tensor) CK(cudaMemcpyAsync(tensor, dT, 9 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
   return FDMGPU_OK;
 }
 

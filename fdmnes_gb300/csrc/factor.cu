@@ -337,7 +337,7 @@ int launch_forward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, 
     k_fwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active, piv);
     ++nk;
     if (sp.fwd[K] > 0) {
-      if (std::is_same<T, float>::value && sp.tc)
+      if (std::is_same<T, float>::value && sp.tc_solve)
         launch_tc_update(1, sp.fwd_tc[K], nprob, reinterpret_cast<float*>(const_cast<T*>(env)),
                          reinterpret_cast<float*>(rhs), probs, tb, K, active, sp.tc_err, s);
       else
@@ -357,7 +357,7 @@ int launch_backward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs,
     k_bwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
     ++nk;
     if (sp.bwd[K] > 0) {
-      if (std::is_same<T, float>::value && sp.tc)
+      if (std::is_same<T, float>::value && sp.tc_solve)
         launch_tc_update(2, sp.bwd_tc[K], nprob, reinterpret_cast<float*>(const_cast<T*>(env)),
                          reinterpret_cast<float*>(rhs), probs, tb, K, active, sp.tc_err, s);
       else

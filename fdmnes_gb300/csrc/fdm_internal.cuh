@@ -68,6 +68,31 @@ struct Prob {
   int so, rel, ylmc;  // Spinorbite, Relativiste, Ylm_comp
   int nspinp, nspinr, nspin;
   int64_t in_grad;    // offset of gradvr(npoint, 3, nspin) in the double pool
+  // inputs generated on the device (radial.cu) instead of uploaded: phiato,
+  // Bessel and Neumann of the real path, from the site's radial tables
+  int gen;
+  int gen_lmax[8];    // l cut-off per atom type at this energy
+};
+constexpr int MAX_GEN_TYPES = 8;
+
+// Energy-independent radial tables of a site for the generated inputs
+// (device pointers; per atom type t the mesh and coefficients at t * nr_max).
+struct RadialDev {
+  int ntype, nr_max, nspin;
+  const int* nr;           // (ntype) mesh points
+  const double* r;         // (nr_max, ntype) radial mesh (bohr)
+  const double* mcl0;      // -clapl0 of the three-point Laplacian on the mesh
+  const double* gm;        // -claplm
+  const double* gp;        // -claplp
+  const double* f2;        // 1 / r^2
+  const double* V;         // spherical potential of the type (Ry), spin-independent part
+  const double* dv_spin;   // (nspin) spin shift of the potential (Ry)
+  const double* z_origin;  // (ntype) charge of the expansion at the origin
+  const int* itype;        // (natome) type of each atom, 0-based
+  const double* rrel;      // (nbtm, natome) distance of each boundary point to its atom
+  const int* iidx;         // (nbtm, natome) first mesh index with r > rrel (clipped to [2, nr-1])
+  const double* rsort;     // (nsort) radius of each outer point (bohr)
+  double v0bd;             // interstitial level subtracted from the energy for the kinetic energy
 };
 
 // Per tile-row / tile-column tables of a problem, at Prob::trow.

@@ -20,7 +20,8 @@ struct StepPlan {
   // FP32 tile updates on the tensor cores (tc_update.cu): work items (two tile
   // rows x up to four tile columns) of the trailing update with the fused
   // right-hand sides, and of the forward / backward solve updates
-  int tc = 0;
+  int tc = 0;        // trailing update of the FP32 factor on the tensor cores
+  int tc_solve = 0;  // forward / backward updates of the FP32 solves on the tensor cores
   std::vector<int> trail_tc, fwd_tc, bwd_tc;
   int* tc_err = nullptr;               // per-problem status word of the solve updates (mbarrier timeout)
 };
@@ -107,6 +108,40 @@ struct LaunchDims {
   int max_nlmsa = 0;       // max harmonics of one atom over the batch
   int64_t rowv_total = 0;  // entries of the per-row vectors (sum of npad + 1)
 };
+
+// Device-side stopping rule of the classical refinement (refine.cu).
+struct RefineState {   // per problem
+  int active, slow, iters, pad;
+  double prev, resid;
+};
+struct RefineCtl {     // per batch
+  int it;              // refinement steps done
+  int max_iter;
+  double tol;
+  int nact;            // problems still active after the last step
+  int pad;
+};
+void launch_refine_init(RefineState* rs, int* active, int np, cudaStream_t s);
+void launch_refine_check(RefineState* rs, int* active, const Pools& pl, RefineCtl* ctl, int np,
+                         cudaGraphConditionalHandle cond, int use_cond, cudaStream_t s);
+
+// Generated per-energy inputs (radial.cu).
+struct GenDims {
+  int nprob_gen = 0;   // problems with generated inputs
+  int ntype_max = 0;
+  int lmax1 = 1;       // max l cut-off + 1 over the generated problems and types
+  int natome_max = 0;
+  int nsort_max = 0;
+  int nr_max = 0;
+};
+void launch_generate_inputs(const Prob* probs, const RadialDev* rads, const StaticDev* sites, const int* ipool,
+                            const LaunchDims& d, const GenDims& g, double* U, double* dpool, cudaStream_t s);
+
+// Dipole absorption and tensor per energy, Lorentzian convolution (xsection.cu).
+void launch_dipole(const Prob* probs, const double* taull, const double* weight, int nprob, double* sigma,
+                   double* tensor, cudaStream_t s);
+void launch_lorentz(const double* E, const double* x, const double* width, int width_per_input, int n, double* out,
+                    cudaStream_t s);
 
 void launch_assemble(const StaticDev* sites, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
                      cudaStream_t s);

@@ -606,3 +606,73 @@ void launch_solution_out(const Prob& P, const double* X, double* smr_dev, cudaSt
 }
 
 }  // namespace fdm
+
+namespace fdm {
+
+// Stopping rule of the classical refinement, evaluated on the device after
+// every step (one block): problem k stops when r = max|dx|/max|x| <= tol or r
+// is not finite, or after two consecutive steps that do not halve r; the loop
+// ends when no problem is active or ctl->it reaches ctl->max_iter.  With a
+// conditional handle, the while node of the refinement graph reads the
+// decision, so no step needs the host.
+__global__ void __launch_bounds__(1024) k_refine_check(RefineState* rs, int* active, const unsigned long long* dmax,
+                                                       const unsigned long long* xmax, RefineCtl* ctl, int np,
+                                                       cudaGraphConditionalHandle cond, int use_cond) {
+  __shared__ int nact;
+  if (threadIdx.x == 0) nact = 0;
+  __syncthreads();
+  const int it = ctl->it + 1;
+  const double tol = ctl->tol;
+  for (int k = threadIdx.x; k < np; k += blockDim.x) {
+    RefineState s = rs[k];
+    if (!s.active) continue;
+    const double dm = __longlong_as_double((long long)dmax[k]);
+    const double xm = __longlong_as_double((long long)xmax[k]);
+    const double r = xm > 0 ? dm / xm : dm;
+    s.iters = it;
+    s.resid = r;
+    if (!isfinite(r) || r <= tol) {
+      s.active = 0;
+    } else {
+      s.slow = (it > 1 && r > 0.5 * s.prev) ? s.slow + 1 : 0;
+      if (s.slow >= 2)
+        s.active = 0;
+      else
+        atomicAdd(&nact, 1);
+    }
+    s.prev = r;
+    rs[k] = s;
+    active[k] = s.active;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ctl->it = it;
+    ctl->nact = nact;
+    if (use_cond) cudaGraphSetConditional(cond, (nact > 0 && it < ctl->max_iter) ? 1u : 0u);
+  }
+}
+
+__global__ void k_refine_init(RefineState* rs, int* active, int np) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= np) return;
+  RefineState s;
+  s.active = 1;
+  s.slow = 0;
+  s.iters = 0;
+  s.pad = 0;
+  s.prev = 1e300;
+  s.resid = __longlong_as_double(0x7ff8000000000000ll);
+  rs[k] = s;
+  active[k] = 1;
+}
+
+void launch_refine_init(RefineState* rs, int* active, int np, cudaStream_t s) {
+  k_refine_init<<<(np + 255) / 256, 256, 0, s>>>(rs, active, np);
+}
+
+void launch_refine_check(RefineState* rs, int* active, const Pools& pl, RefineCtl* ctl, int np,
+                         cudaGraphConditionalHandle cond, int use_cond, cudaStream_t s) {
+  k_refine_check<<<1, 1024, 0, s>>>(rs, active, pl.dmax, pl.xmax, ctl, np, cond, use_cond);
+}
+
+}  // namespace fdm

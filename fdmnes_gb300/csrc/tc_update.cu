@@ -184,44 +184,93 @@ __device__ __forceinline__ bool decode(float* env, float* rhs, const Prob& P, co
   return true;
 }
 
-// Stage K half `kh` of the operands: A rows (m < 128) and B rows (n < 64 nc),
-// split into hi and lo images.
-__device__ __forceinline__ void stage(const Work& w, int kh, unsigned char* sAhi, unsigned char* sAlo,
-                                     unsigned char* sBhi, unsigned char* sBlo) {
+// Operands of one K half in registers: thread t holds the A chunks
+// q = t + 128 i (i < 8: row r, four consecutive k) and the B units
+// q = t + 128 j (j < 16: column n, four consecutive k), read from global
+// memory before any of them is written to shared memory, so that all the
+// loads of a half are in flight together.
+struct Regs {
+  float4 a[8];
+  float b[16][4];
+};
+
+__device__ __forceinline__ void load_half(const Work& w, int kh, Regs& R) {
   const int t = threadIdx.x;
-  // A: 128 rows x 8 float4 chunks; lanes 0-7 of a quarter-warp fill one core matrix
-#pragma unroll 2
-  for (int q = t; q < 128 * (KH / 4); q += THREADS) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int q = t + THREADS * i;
     const int kq = (q >> 3) & 7, r = ((q >> 6) << 3) | (q & 7);
     const float* a = w.A[r >> 6];
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (a) v = __ldg(reinterpret_cast<const float4*>(a + (r & 63) * TS + kh * KH + 4 * kq));
+    R.a[i] = a ? __ldg(reinterpret_cast<const float4*>(a + (r & 63) * TS + kh * KH + 4 * kq))
+               : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  const int nn = w.nc * TS;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int q = t + THREADS * j;
+    if (q < nn * (KH / 4)) {
+      const int n = q % nn, kq = q / nn;
+      const float* b = w.B[n >> 6] + (kh * KH + 4 * kq) * TS + (n & 63);
+      R.b[j][0] = __ldg(b);
+      R.b[j][1] = __ldg(b + TS);
+      R.b[j][2] = __ldg(b + 2 * TS);
+      R.b[j][3] = __ldg(b + 3 * TS);
+    }
+  }
+}
+
+// Split the registers into hi and lo TF32 parts and write the K-major images.
+// A: lanes 0-7 of a quarter warp fill one 128-byte core matrix; B: one thread
+// writes one 16-byte core-matrix row (4 consecutive k of column n), lanes with
+// consecutive n hit distinct bank groups.
+__device__ __forceinline__ void store_half(const Work& w, const Regs& R, unsigned char* sAhi, unsigned char* sAlo,
+                                           unsigned char* sBhi, unsigned char* sBlo) {
+  const int t = threadIdx.x;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int q = t + THREADS * i;
+    const int kq = (q >> 3) & 7, r = ((q >> 6) << 3) | (q & 7);
     uint4 hi, lo;
-    split(v.x, hi.x, lo.x);
-    split(v.y, hi.y, lo.y);
-    split(v.z, hi.z, lo.z);
-    split(v.w, hi.w, lo.w);
+    split(R.a[i].x, hi.x, lo.x);
+    split(R.a[i].y, hi.y, lo.y);
+    split(R.a[i].z, hi.z, lo.z);
+    split(R.a[i].w, hi.w, lo.w);
     const uint32_t off = img_off(r, 4 * kq);
     *reinterpret_cast<uint4*>(sAhi + off) = hi;
     *reinterpret_cast<uint4*>(sAlo + off) = lo;
   }
-  // B: row n of the operand is column n % 64 of tile n / 64 (B tiles are
-  // row-major in k); one thread gathers 4 consecutive k of one column (lanes
-  // read consecutive columns: coalesced) and writes one 16-byte core-matrix row
   const int nn = w.nc * TS;
-  for (int q = t; q < nn * (KH / 4); q += THREADS) {
-    const int n = q % nn, kq = q / nn;
-    const float* b = w.B[n >> 6] + (kh * KH + 4 * kq) * TS + (n & 63);
-    const float x0 = __ldg(b), x1 = __ldg(b + TS), x2 = __ldg(b + 2 * TS), x3 = __ldg(b + 3 * TS);
-    uint4 hi, lo;
-    split(x0, hi.x, lo.x);
-    split(x1, hi.y, lo.y);
-    split(x2, hi.z, lo.z);
-    split(x3, hi.w, lo.w);
-    const uint32_t off = img_off(n, 4 * kq);
-    *reinterpret_cast<uint4*>(sBhi + off) = hi;
-    *reinterpret_cast<uint4*>(sBlo + off) = lo;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int q = t + THREADS * j;
+    if (q < nn * (KH / 4)) {
+      const int n = q % nn, kq = q / nn;
+      uint4 hi, lo;
+      split(R.b[j][0], hi.x, lo.x);
+      split(R.b[j][1], hi.y, lo.y);
+      split(R.b[j][2], hi.z, lo.z);
+      split(R.b[j][3], hi.w, lo.w);
+      const uint32_t off = img_off(n, 4 * kq);
+      *reinterpret_cast<uint4*>(sBhi + off) = hi;
+      *reinterpret_cast<uint4*>(sBlo + off) = lo;
+    }
   }
+}
+
+// One thread issues the 4 k-steps x 3 products of a half and commits them.
+__device__ __forceinline__ void issue_half(uint32_t tmem, uint32_t idesc, int kh, const unsigned char* sAhi,
+                                           const unsigned char* sAlo, const unsigned char* sBhi,
+                                           const unsigned char* sBlo, uint32_t bar) {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t ahi = smem_u32(sAhi), alo = smem_u32(sAlo), bhi = smem_u32(sBhi), blo = smem_u32(sBlo);
+#pragma unroll
+  for (int s = 0; s < KH / 8; ++s) {
+    const uint32_t ko = s * 2 * 128;  // 8 TF32 = two core matrices along K
+    mma_tf32(tmem, sdesc(alo + ko, LBO, SBO), sdesc(bhi + ko, LBO, SBO), idesc, (kh | s) ? 1u : 0u);
+    mma_tf32(tmem, sdesc(ahi + ko, LBO, SBO), sdesc(blo + ko, LBO, SBO), idesc, 1u);
+    mma_tf32(tmem, sdesc(ahi + ko, LBO, SBO), sdesc(bhi + ko, LBO, SBO), idesc, 1u);
+  }
+  mma_commit(bar);
 }
 
 template <int MODE>
@@ -245,6 +294,8 @@ __global__ void __launch_bounds__(THREADS, 2) k_tc_update(float* env, float* rhs
   const uint32_t bar_a = smem_u32(bar);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
+  Regs R;
+  load_half(w, 0, R);  // in flight while the barrier and TMEM are set up
   if (threadIdx.x == 0) {
     mbar_init(bar_a, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -260,55 +311,61 @@ __global__ void __launch_bounds__(THREADS, 2) k_tc_update(float* env, float* rhs
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
   const uint32_t idesc = idesc_tf32(128, TS * w.nc);
-  bool ok = true;
 
-  for (int kh = 0; kh < 2; ++kh) {
-    stage(w, kh, sAhi, sAlo, sBhi, sBlo);
-    // make the generic-proxy writes of the images visible to the tensor core
+  // half 0: images, MMAs; half 1's loads are in flight while they run
+  store_half(w, R, sAhi, sAlo, sBhi, sBlo);
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic-proxy writes -> tensor core
+  __syncthreads();
+  if (threadIdx.x == 0) issue_half(tmem, idesc, 0, sAhi, sAlo, sBhi, sBlo, bar_a);
+  load_half(w, 1, R);
+  // the images are overwritten only once the half-0 MMAs have read them (a
+  // uniform decision: every thread sees the same outcome)
+  bool ok = __syncthreads_and(mbar_wait(bar_a, 0u)) != 0;
+  if (ok) {
+    store_half(w, R, sAhi, sAlo, sBhi, sBlo);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
-    if (threadIdx.x == 0) {
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t ahi = smem_u32(sAhi), alo = smem_u32(sAlo), bhi = smem_u32(sBhi), blo = smem_u32(sBlo);
-#pragma unroll
-      for (int s = 0; s < KH / 8; ++s) {
-        const uint32_t ko = s * 2 * 128;  // 8 TF32 = two core matrices along K
-        mma_tf32(tmem, sdesc(alo + ko, LBO, SBO), sdesc(bhi + ko, LBO, SBO), idesc, (kh | s) ? 1u : 0u);
-        mma_tf32(tmem, sdesc(ahi + ko, LBO, SBO), sdesc(blo + ko, LBO, SBO), idesc, 1u);
-        mma_tf32(tmem, sdesc(ahi + ko, LBO, SBO), sdesc(bhi + ko, LBO, SBO), idesc, 1u);
-      }
-      mma_commit(bar_a);
-    }
-    // the images are overwritten by the next half (and TMEM is read after the
-    // last one) only once the MMAs have completed
-    // (a uniform decision: every thread leaves the loop together)
-    ok = __syncthreads_and(mbar_wait(bar_a, (uint32_t)kh)) != 0;
-    if (!ok) break;
+    if (threadIdx.x == 0) issue_half(tmem, idesc, 1, sAhi, sAlo, sBhi, sBlo, bar_a);
   }
+  // epilogue: thread (warp, lane) owns accumulator row r = 32 warp + lane,
+  // row r % 64 of tile row r / 64; the first C tile is read while the last
+  // MMAs run
+  const int r = 32 * warp + lane;
+  const int h = r >> 6, row = r & 63;
+  float4 c4[16];
+  {
+    float* cp = w.C[h][0];
+    if (cp) {
+#pragma unroll
+      for (int j = 0; j < 16; ++j) c4[j] = __ldcs(reinterpret_cast<const float4*>(cp + row * TS) + j);
+    }
+  }
+  if (ok) ok = __syncthreads_and(mbar_wait(bar_a, 1u)) != 0;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-
   if (ok) {
-    // epilogue: thread (warp, lane) owns accumulator row r = 32 warp + lane,
-    // which is row r % 64 of tile row r / 64
-    const int r = 32 * warp + lane;
-    const int h = r >> 6, row = r & 63;
     for (int c = 0; c < w.nc; ++c) {
+      uint32_t v[64];
+      tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(c * TS), v);
+      tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(c * TS + 32), v + 32);
+      float* cp = w.C[h][c];
+      if (cp) {
+        float4* q = reinterpret_cast<float4*>(cp + row * TS);
 #pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        uint32_t v[32];
-        tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(c * TS + 32 * half), v);
-        float* cp = w.C[h][c];
-        if (cp) {
-          float4* q = reinterpret_cast<float4*>(cp + row * TS + 32 * half);
+        for (int j = 0; j < 16; ++j) {
+          float4 x = c4[j];
+          x.x -= __uint_as_float(v[4 * j + 0]);
+          x.y -= __uint_as_float(v[4 * j + 1]);
+          x.z -= __uint_as_float(v[4 * j + 2]);
+          x.w -= __uint_as_float(v[4 * j + 3]);
+          __stcs(q + j, x);
+        }
+      }
+      // next C tile of this row
+      if (c + 1 < w.nc) {
+        float* cn = w.C[h][c + 1];
+        if (cn) {
 #pragma unroll
-          for (int j = 0; j < 8; ++j) {
-            float4 x = q[j];
-            x.x -= __uint_as_float(v[4 * j + 0]);
-            x.y -= __uint_as_float(v[4 * j + 1]);
-            x.z -= __uint_as_float(v[4 * j + 2]);
-            x.w -= __uint_as_float(v[4 * j + 3]);
-            q[j] = x;
-          }
+          for (int j = 0; j < 16; ++j) c4[j] = __ldcs(reinterpret_cast<const float4*>(cn + row * TS) + j);
         }
       }
     }

@@ -69,6 +69,12 @@ def load_library(path: str = LIB_PATH):
     L.fdmgpu_set_factor_mode.restype = C.c_int
     L.fdmgpu_measure_pipe_peaks.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double)]
     L.fdmgpu_measure_pipe_peaks.restype = C.c_int
+    L.fdmgpu_batch_inputs.argtypes = [vp, C.c_int32, vp, vp, vp]
+    L.fdmgpu_batch_inputs.restype = C.c_int
+    L.fdmgpu_set_radial.argtypes = [vp, vp]
+    L.fdmgpu_set_radial.restype = C.c_int
+    L.fdmgpu_batch_xanes.argtypes = [vp, vp, vp, C.c_int32, vp, vp, vp, vp]
+    L.fdmgpu_batch_xanes.restype = C.c_int
     L.fdmgpu_set_tile_engine.argtypes = [vp, C.c_int32]
     L.fdmgpu_set_tile_engine.restype = C.c_int
     L.fdmgpu_get_tuning.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_double)]
@@ -146,12 +152,30 @@ class FdmSolver:
     def set_factor_mode(self, mode: str = "fp32"):
         """Accumulation of the mixed path's FP32 factor: 'fp32' (default) or
         'wide_atom' (double-float sums at the atom-harmonic steps)."""
-        _check(self.lib.fdmgpu_set_factor_mode(self.h, {"fp32": 0, "wide_atom": 1}[mode]))
+        _check(self.lib.fdmgpu_set_factor_mode(self.h, {"fp32": 0, "wide_atom": 1, "wide_all": 2}[mode]))
+
+    def set_radial(self):
+        """Upload the structure's radial tables, so that energies added with
+        functions=False inputs (cluster.energy_inputs(..., functions=False))
+        get phiato, Bessel and Neumann generated on the device."""
+        self.radial_args = abi.RadialArgs(self.st)
+        _check(self.lib.fdmgpu_set_radial(self.h, C.addressof(self.radial_args.s)))
+
+    def batch_inputs(self, k: int, nlmagm: int, lmaxso: int):
+        """phiato (nbtm, nlmagm, natome), Besselr and Neumanr (nsort, lmaxso+1)
+        of energy k of the last run as the device holds them."""
+        g = self.st.grid
+        phi = np.zeros((g.nbtm, nlmagm, self.st.natome), order="F")
+        bs = np.zeros((g.nsort, lmaxso + 1), order="F")
+        nm = np.zeros((g.nsort, lmaxso + 1), order="F")
+        _check(self.lib.fdmgpu_batch_inputs(self.h, k, phi.ctypes.data, bs.ctypes.data, nm.ctypes.data))
+        return phi, bs, nm
 
     def set_tile_engine(self, engine: str = "tcgen05"):
-        """FP32 tile updates of mixed batches on the FP32 pipes ("simt") or on
-        the tensor cores as split-TF32 products ("tcgen05")."""
-        _check(self.lib.fdmgpu_set_tile_engine(self.h, {"simt": 0, "tcgen05": 1}[engine]))
+        """FP32 tile updates of mixed batches on the FP32 pipes ("simt"), on
+        the tensor cores as split-TF32 products ("tcgen05"), or the factor's
+        trailing update only on the tensor cores ("tcgen05_factor")."""
+        _check(self.lib.fdmgpu_set_tile_engine(self.h, {"simt": 0, "tcgen05": 1, "tcgen05_factor": 2}[engine]))
 
     def set_autotune(self, on: bool = True):
         _check(self.lib.fdmgpu_set_autotune(self.h, 1 if on else 0))
@@ -267,6 +291,23 @@ class FdmSolver:
             res.append(out[o:o + 2 * n * n].view(np.complex128).reshape((n, n), order="F").copy())
             o += 2 * n * n
         return res
+
+    def xanes(self, energies, half_width=0.78, width_per_input: bool = False, weight=None,
+              tensor: bool = False):
+        """Dipole absorption sigma(E) of the last batch and its Lorentzian
+        convolution, computed on the device in FP64 (fdmgpu_batch_xanes).
+        Returns (sigma, sigma_conv) or (sigma, sigma_conv, tensor (n, 3, 3))."""
+        E = np.ascontiguousarray(energies, dtype=np.float64)
+        n = len(E)
+        hw = np.ascontiguousarray(np.broadcast_to(np.asarray(half_width, dtype=np.float64), (n,)))
+        w = None if weight is None else np.ascontiguousarray(weight, dtype=np.float64)
+        sig = np.zeros(n)
+        conv = np.zeros(n)
+        ten = np.zeros((n, 3, 3)) if tensor else None
+        _check(self.lib.fdmgpu_batch_xanes(self.h, E.ctypes.data, hw.ctypes.data, int(width_per_input),
+                                           None if w is None else w.ctypes.data, sig.ctypes.data,
+                                           conv.ctypes.data, None if ten is None else ten.ctypes.data))
+        return (sig, conv, ten) if tensor else (sig, conv)
 
     def solution(self, k: int, nlmso: int, nligne: int) -> np.ndarray:
         smr = np.zeros((nlmso, nligne), order="F")

@@ -53,21 +53,33 @@ def absorption_cotangent(taull: np.ndarray, g_sigma: float = 1.0) -> np.ndarray:
     return g
 
 
-def lorentzian_convolve(energies: np.ndarray, x: np.ndarray, half_width: float) -> np.ndarray:
+def dipole_tensor(taull: np.ndarray, weight: float = 1.0) -> np.ndarray:
+    """S(a, b) = -Im w (T(a,b) + T(b,a)) / 2 over the Cartesian components
+    a, b = x, y, z of the L = 1 real harmonics (0-based harmonic 3, 1, 2)."""
+    idx = [3, 1, 2]
+    T = taull[np.ix_(idx, idx)]
+    return -weight * 0.5 * np.imag(T + T.T)
+
+
+def lorentzian_convolve(energies: np.ndarray, x: np.ndarray, half_width, width_per_input: bool = False) -> np.ndarray:
+    """half_width: a number, or one width per energy (of the output energy,
+    or of the input bin when width_per_input, the reference's Gamma_var)."""
     E = np.asarray(energies, dtype=np.float64)
     x = np.asarray(x, dtype=np.float64)
     n = len(E)
     if n < 2:
         return x.copy()
+    bw = np.broadcast_to(np.asarray(half_width, dtype=np.float64), (n,))
+    bw = np.where(bw >= 0.0, np.maximum(bw, 1e-8), bw)
     e1 = np.empty(n)
     e2 = np.empty(n)
     e1[0] = 1.5 * E[0] - 0.5 * E[1]
     e1[1:] = 0.5 * (E[1:] + E[:-1])
     e2[:-1] = 0.5 * (E[1:] + E[:-1])
     e2[-1] = 1.5 * E[-1] - 0.5 * E[-2]
-    b = max(half_width, 1e-8)
     out = np.empty(n)
     for i in range(n):
+        b = bw if width_per_input else bw[i]
         lor = np.arctan((e1 - E[i]) / b) - np.arctan((e2 - E[i]) / b)
         out[i] = -np.sum(lor * x) / math.pi
     return out

@@ -179,11 +179,12 @@ typedef struct fdmgpu_info {
 /* Accumulation of the FP32 factor of the mixed path. */
 typedef enum {
   FDMGPU_FACTOR_FP32 = 0,      /* FP32 sums throughout (default)                          */
-  FDMGPU_FACTOR_WIDE_ATOM = 1  /* double-float sums in the trailing update of the steps
+  FDMGPU_FACTOR_WIDE_ATOM = 1, /* double-float sums in the trailing update of the steps
                                   whose tile row holds atom-harmonic rows; those steps'
                                   multipliers are large, and FP32 sums next to them cost
                                   the factor the accuracy that keeps the refinement from
-                                  escalating (not yet measured on the GPU)               */
+                                  escalating                                              */
+  FDMGPU_FACTOR_WIDE_ALL = 2   /* double-float sums in the trailing update of every step */
 } fdmgpu_factor_mode;
 
 /* Arithmetic units of the FP32 tile updates of the mixed path (the trailing
@@ -191,9 +192,11 @@ typedef enum {
  * and the forward / backward updates of the refinement solves). */
 typedef enum {
   FDMGPU_ENGINE_SIMT = 0,      /* FP32 FMA pipes, register-blocked 64x64x64 products     */
-  FDMGPU_ENGINE_TCGEN05 = 1    /* tensor cores (tcgen05.mma kind::tf32), operands split
+  FDMGPU_ENGINE_TCGEN05 = 1,   /* tensor cores (tcgen05.mma kind::tf32), operands split
                                   hi + lo into TF32 pairs, three products per tile pair:
                                   the accuracy of FP32 products, FP32 accumulation       */
+  FDMGPU_ENGINE_TCGEN05_FACTOR = 2 /* tensor cores for the factor's trailing update only;
+                                  the refinement solves on the FP32 pipes                */
 } fdmgpu_tile_engine;
 
 /* Library version string. */
@@ -244,6 +247,35 @@ fdmgpu_status fdmgpu_set_tolerance(fdmgpu_handle* h, double tol, double tol_acce
 /* Accumulation mode of the FP32 factor (fdmgpu_factor_mode), for the
  * batches planned after the call.  No counterpart in the reference. */
 fdmgpu_status fdmgpu_set_factor_mode(fdmgpu_handle* h, int32_t mode);
+
+/*
+ * Radial tables for per-energy inputs generated on the device (real path).
+ * With them, an energy whose phiato, Besselr and Neumanr are all NULL has
+ * those inputs computed on the GPU: the regular radial solution of each atom
+ * type by the three-point recursion of Sch_radial (source/sphere.f90:324-396,
+ * :519-523 start, :583-695 recursion), interpolated onto the atom's boundary
+ * points and multiplied by Ylmato as cal_phiato does (source/sphere.f90:
+ * 3225-3370, f_interp2 source/tools.f90:504-522), and the outer Bessel and
+ * Neumann values of phiso (source/mat.f90:739-1028, cbessneur
+ * source/sphere.f90:7356-7384) at k = sqrt(Enervide - v0bd - dv_spin(ispin)).
+ * The energy's nlmsa give each atom's l cut-off and nlmagm the layout.
+ * No counterpart in the reference, which computes them on the host per energy.
+ */
+typedef struct fdmgpu_radial {
+  int32_t ntype;          /* atom types (<= 8)                                              */
+  int32_t nr_max;         /* leading dimension of r and V                                    */
+  int32_t nspin;          /* spin blocks of dv_spin                                          */
+  const int32_t* nr;      /* (ntype) mesh points of each type                               */
+  const double* r;        /* (nr_max, ntype) radial mesh (bohr), increasing                 */
+  const double* V;        /* (nr_max, ntype) spherical potential of each type (Ry)          */
+  const double* dv_spin;  /* (nspin) spin shift of the potential (Ry)                       */
+  const double* z_origin; /* (ntype) charge of the expansion of u_L at the origin           */
+  const int32_t* itype;   /* (natome) type of each atom, 1-based                            */
+  const double* rrel;     /* (nbtm, natome) distance of each boundary point to its atom     */
+  const double* rsort;    /* (nsort) distance of each outer point to the absorber (bohr)    */
+  double v0bd;            /* interstitial level: kinetic energy = Enervide - v0bd - dv (Ry) */
+} fdmgpu_radial;
+fdmgpu_status fdmgpu_set_radial(fdmgpu_handle* h, const fdmgpu_radial* radial);
 
 /* Tile engine of the FP32 updates (fdmgpu_tile_engine) for the real mixed
  * batches planned after the call; steps that accumulate wide
@@ -310,6 +342,35 @@ fdmgpu_status fdmgpu_batch_solution(fdmgpu_handle* h, int32_t k, double* smr);
  * energy's status (FDMGPU_OK when it converged).  Any pointer may be NULL. */
 fdmgpu_status fdmgpu_batch_stats(fdmgpu_handle* h, int32_t k, int32_t* iters, double* residual,
                                  int32_t* fallback, int32_t* inner_iters);
+
+/* The per-energy inputs energy k of the last run was assembled from, as the
+ * device holds them: phiato (nbtm, nlmagm, natome) of its spin block and
+ * Besselr, Neumanr (nsort, 0:lmaxso), column-major.  Real problems; any
+ * pointer may be NULL.  For checking inputs generated on the device
+ * (fdmgpu_set_radial).  No counterpart in the reference. */
+fdmgpu_status fdmgpu_batch_inputs(fdmgpu_handle* h, int32_t k, double* phiato, double* besselr, double* neumanr);
+
+/*
+ * Dipole absorption of the last batch, in FP64 on the device, from the Taull
+ * already in device memory: the K-edge E1E1 channel of tens_ab
+ * (source/tensor.f90:1218-1264) and the Lorentzian convolution of the
+ * spectrum (source/convolution.f90:1612-1680).  One problem per energy, added
+ * in increasing energy order.
+ *   energies_ev (n)   photon energies of the batch's problems (add order);
+ *   half_width  (n)   Lorentzian half width per energy (the reference's bb);
+ *   width_per_input   0: the width of the output energy (bb(ie)), 1: of the
+ *                     input bin (Gamma_var);
+ *   weight      (n)   |radial integral|^2 per energy, or NULL for 1;
+ *   sigma       (n)   out: sigma(E) = -Im sum over the L = 1 block of w Taull
+ *                     (both spin blocks for a complex batch);
+ *   sigma_conv  (n)   out or NULL: the convolved spectrum;
+ *   tensor      (9n)  out or NULL (real batches): S(a, b) = -Im w (T(a,b) +
+ *                     T(b,a)) / 2 for a, b in x, y, z, row-major per energy.
+ * Host pointers.  Synchronous.
+ */
+fdmgpu_status fdmgpu_batch_xanes(fdmgpu_handle* h, const double* energies_ev, const double* half_width,
+                                 int32_t width_per_input, const double* weight, double* sigma, double* sigma_conv,
+                                 double* tensor);
 
 /*
  * Vector-Jacobian product of the last batch: given the cotangent

@@ -44,6 +44,8 @@ def lib():
         L.oracle_mat_solve.argtypes = [vp, vp, vp, C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                        C.POINTER(C.c_double), C.POINTER(C.c_int32)]
         L.oracle_assemble_dense.argtypes = [vp, vp, vp, vp]
+        L.oracle_assemble_csr.argtypes = [vp, vp, vp, vp, vp, vp]
+        L.oracle_assemble_csr_c.argtypes = [vp, vp, vp, vp, vp, vp]
         L.oracle_newind.argtypes = [vp, vp, vp, vp, C.c_int, C.c_int32, vp, vp, vp, vp, vp]
         L.oracle_cbessneur.argtypes = [C.c_double, C.c_double, C.c_int, vp, vp]
         L.oracle_invcomp.argtypes = [C.c_int, vp]
@@ -176,3 +178,35 @@ def cbessneu(fnorm, z, lmax):
     lib().oracle_cbessneu(float(np.real(fnorm)), float(np.imag(fnorm)), float(np.real(z)), float(np.imag(z)),
                           int(lmax), b.ctypes.data, nm.ctypes.data)
     return b, nm
+
+
+def assemble_csr(grid_args, energy_args, complex_=False):
+    """(scipy.sparse.csr_matrix A (nligne x nligne), B (nlmso, nligne) F-ordered)
+    assembled row by row with calcMatRow (real, or complex when complex_)."""
+    import scipy.sparse as sp
+    n, m = energy_args.nligne, energy_args.nlmso
+    f = lib().oracle_assemble_csr_c if complex_ else lib().oracle_assemble_csr
+    rowptr = np.zeros(n + 1, dtype=np.int64)
+    st = f(C.addressof(grid_args.s), C.addressof(energy_args.s), rowptr.ctypes.data, None, None, None)
+    if st != 0:
+        raise RuntimeError(f"oracle assembly failed with status {st}")
+    nnz = int(rowptr[-1])
+    col = np.zeros(nnz, dtype=np.int32)
+    dt = np.complex128 if complex_ else np.float64
+    val = np.zeros(nnz, dtype=dt)
+    B = np.zeros((m, n), dtype=dt, order="F")
+    st = f(C.addressof(grid_args.s), C.addressof(energy_args.s), rowptr.ctypes.data, col.ctypes.data,
+           val.ctypes.data, B.ctypes.data)
+    if st != 0:
+        raise RuntimeError(f"oracle assembly failed with status {st}")
+    return sp.csr_matrix((val, col, rowptr), shape=(n, n)), B
+
+
+def backward_error(A, B, X):
+    """Normwise backward error max_c ||b_c - A x_c||_inf / (||A||_inf ||x_c||_inf + ||b_c||_inf)
+    for X, B of shape (nrhs, n) (the smr layout) and a sparse or dense A."""
+    R = B.T - A @ X.T
+    nA = float(abs(A).sum(axis=1).max())
+    num = np.abs(R).max(axis=0)
+    den = nA * np.abs(X.T).max(axis=0) + np.abs(B.T).max(axis=0)
+    return float((num / den).max())

@@ -272,6 +272,39 @@ int oracle_assemble_dense(const fdmgpu_grid* g, const fdmgpu_energy* e, double* 
   return 0;
 }
 
+// Sparse assembly: the nonzeros of A in CSR form (rows ii = 1..nligne in
+// order, 0-based columns) and B = smr (nlmso x nligne), with calcMatRow.  With
+// colidx == nullptr only the row pointers are written (rowptr[nligne] = nnz),
+// so the caller can size the arrays.  Used by the backward-error checks of
+// problems too large for a dense copy.
+int oracle_assemble_csr(const fdmgpu_grid* g, const fdmgpu_energy* e, int64_t* rowptr, int32_t* colidx, double* val,
+                        double* smr) {
+  int st = check_supported(g, e);
+  if (st) return st;
+  Ctx c = make_ctx(g, e);
+  const int n = e->nligne;
+  std::vector<double> row;
+  std::vector<double> brow(e->nlmso);
+  rowptr[0] = 0;
+  for (int ii = 1; ii <= n; ++ii) {
+    const int l1 = e->lb1[ii - 1], l2 = e->lb2[ii - 1];
+    row.assign(l2 - l1 + 1, 0.0);
+    double* b = smr ? smr + (int64_t)(ii - 1) * e->nlmso : brow.data();
+    calc_mat_row(c, ii, row.data(), l1, b);
+    int64_t q = rowptr[ii - 1];
+    for (int k = l1; k <= l2; ++k) {
+      if (row[k - l1] == 0.0) continue;
+      if (colidx) {
+        colidx[q] = k - 1;
+        val[q] = row[k - l1];
+      }
+      ++q;
+    }
+    rowptr[ii] = q;
+  }
+  return 0;
+}
+
 // Gaussian profile solve, source/mat_solve_gaussian.f90:5-372 (real branch).
 // smr (nlmso, nligne) is zero on entry and holds the solution on return.
 int oracle_mat_solve(const fdmgpu_grid* g, const fdmgpu_energy* e, double* smr, int64_t* nnz_out,

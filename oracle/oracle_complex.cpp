@@ -388,6 +388,39 @@ int oracle_assemble_dense_c(const fdmgpu_grid* g, const fdmgpu_energy* e, double
   return 0;
 }
 
+// Sparse complex assembly in CSR form (see oracle_assemble_csr); values and
+// B complex interleaved.
+int oracle_assemble_csr_c(const fdmgpu_grid* g, const fdmgpu_energy* e, int64_t* rowptr, int32_t* colidx,
+                          double* val_ri, double* B_ri) {
+  int st = check_supported_c(g, e);
+  if (st) return st;
+  Ctx c = make_ctx(g, e);
+  cdouble* val = reinterpret_cast<cdouble*>(val_ri);
+  cdouble* B = reinterpret_cast<cdouble*>(B_ri);
+  const int n = e->nligne;
+  std::vector<cdouble> row;
+  std::vector<cdouble> brow(e->nlmso);
+  rowptr[0] = 0;
+  for (int ii = 1; ii <= n; ++ii) {
+    const int l1 = e->lb1[ii - 1], l2 = e->lb2[ii - 1];
+    row.assign(l2 - l1 + 1, 0.0);
+    cdouble* b = B ? B + (int64_t)(ii - 1) * e->nlmso : brow.data();
+    std::fill(brow.begin(), brow.end(), cdouble(0.0));
+    calc_mat_row_c(c, ii, row.data(), l1, b);
+    int64_t q = rowptr[ii - 1];
+    for (int k = l1; k <= l2; ++k) {
+      if (row[k - l1] == 0.0) continue;
+      if (colidx) {
+        colidx[q] = k - 1;
+        val[q] = row[k - l1];
+      }
+      ++q;
+    }
+    rowptr[ii] = q;
+  }
+  return 0;
+}
+
 // Gaussian profile solve, complex branch (source/mat_solve_gaussian.f90:196-358):
 // the row elimination of the real branch with the complex products written out
 // as the reference writes them, the division by the pivot through its

@@ -1,0 +1,85 @@
+"""Per-energy inputs generated on the device (fdmgpu_set_radial): phiato from
+the radial recursion of Sch_radial and cal_phiato's interpolation
+(source/sphere.f90:324-733,3186-3370), Bessel and Neumann of phiso
+(source/mat.f90:739-1028), against the host restatement in
+fdmnes_gb300/cluster.py (energy_inputs).  The device evaluates the same
+operations in the same order in FP64 without contraction; only pow, sin and
+cos may round differently in the last bit, so the inputs agree to 1e-13
+relative (max |diff| / max |ref|), and the solved Taull of the small cluster
+to 1e-11.  On the full 13-atom cluster (condition numbers ~1e10) the
+convolved cross-section is held to 1e-9."""
+import numpy as np
+import pytest
+
+from conftest import rel
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def solver_mod():
+    from fdmnes_gb300 import build
+    build.build()
+    from fdmnes_gb300 import solver
+    return solver
+
+
+def _items(st, energies, functions, ispin=1):
+    from fdmnes_gb300 import cluster as CL
+    out = []
+    for E in energies:
+        ei = CL.energy_inputs(st, float(E), ispin=ispin, functions=functions)
+        out.append((ei, CL.newind(st, ei.nlmsa, ei.nlmso)))
+    return out
+
+
+def test_generated_inputs_match_host(solver_mod):
+    from fdmnes_gb300 import cluster as CL
+    st = CL.small_cu_structure()
+    E = [-5.0, 3.0, 12.0, 27.0, 35.0]
+    host = _items(st, E, True)
+    sv = solver_mod.FdmSolver(st)
+    T_host, _ = sv.spectrum(host, "fp64")
+    sv.set_radial()
+    T_gen, _ = sv.spectrum(_items(st, E, False), "fp64")
+    for k, (ei, ri) in enumerate(host):
+        phi, bs, nm = sv.batch_inputs(k, ei.nlmagm, ei.lmaxso)
+        assert rel(phi, ei.phiato[:, :, 0, 0, 0, :, 0]) < 1e-13
+        assert rel(bs, ei.besselr[:, :, 0]) < 1e-13
+        assert rel(nm, ei.neumanr[:, :, 0]) < 1e-13
+        assert rel(T_gen[k], T_host[k]) < 1e-11, (E[k], rel(T_gen[k], T_host[k]))
+    sv.close()
+
+
+def test_generated_inputs_spin_blocks_and_types(solver_mod):
+    """Rutile (two atom types, two spin blocks): every type's radial solution
+    and every spin shift."""
+    from fdmnes_gb300 import cluster as CL
+    st = CL.build_structure(CL.rutile_cluster(2.0), 0.3, 2.4, 30.0, nspin=2, spin_split_ev=1.5)
+    sv = solver_mod.FdmSolver(st)
+    sv.set_radial()
+    for isp in (1, 2):
+        host = _items(st, [4.0, 22.0], True, ispin=isp)
+        T_host, _ = sv.spectrum(host, "fp64")
+        T_gen, _ = sv.spectrum(_items(st, [4.0, 22.0], False, ispin=isp), "fp64")
+        for k, (ei, ri) in enumerate(host):
+            phi, bs, nm = sv.batch_inputs(k, ei.nlmagm, ei.lmaxso)
+            assert rel(phi, ei.phiato[:, :, isp - 1, 0, 0, :, 0]) < 1e-13
+            assert rel(bs, ei.besselr[:, :, 0]) < 1e-13 and rel(nm, ei.neumanr[:, :, 0]) < 1e-13
+            assert rel(T_gen[k], T_host[k]) < 1e-9
+    sv.close()
+
+
+def test_generated_full_cu_spectrum(solver_mod):
+    from fdmnes_gb300 import cluster as CL, xanes
+    st = CL.cu_structure()
+    E = np.linspace(-5.0, 35.0, 9)
+    sv = solver_mod.FdmSolver(st)
+    T_host, _ = sv.spectrum(_items(st, E, True), "fp64")
+    sv.set_radial()
+    sv.set_tolerance(1e-8, 1e-6)
+    T_gen, _ = sv.spectrum(_items(st, E, False), "mixed")
+    assert xanes.convolved_relative_error(E, T_gen, T_host) < 1e-6
+    T_gen64, _ = sv.spectrum(_items(st, E, False), "fp64")
+    assert xanes.convolved_relative_error(E, T_gen64, T_host) < 1e-9
+    sv.close()
