@@ -207,11 +207,11 @@ uint64_t mix(uint64_t h, uint64_t v) {
 // blocks) and the relativistic terms; C1 characters; regular solution.
 fdmgpu_status check_energy_c(const fdmgpu_handle* h, const fdmgpu_energy* e) {
   const fdmgpu_grid& g = h->g;
-  if (e->E_comp || e->irregular || e->Repres_comp || e->Base_hexa || e->Basereel || e->n_RI != 1 ||
-      e->n_ato_RI != 1 || e->nphiato7 != 2)
+  if (e->irregular || e->Repres_comp || e->Base_hexa || e->Basereel || e->n_RI != 1 || e->n_ato_RI != 1 ||
+      e->nphiato7 != 2)
     return fail(FDMGPU_ERR_UNSUPPORTED,
-                "the library's complex path: Cal_comp with real energies (E_comp false), the complex basis "
-                "(Basereel false), regular solution, complex phiato (nphiato7 = 2)");
+                "the library's complex path: Cal_comp, real or complex energies (E_comp), the complex basis "
+                "(Basereel false), regular solution (n_RI = 1), complex phiato (nphiato7 = 2)");
   if (!h->chars_c1) return fail(FDMGPU_ERR_UNSUPPORTED, "the complex path needs the C1 characters (Kar = 1, Kari = 0)");
   if (e->Spinorbite != (g.nspino == 2)) return fail(FDMGPU_ERR_ARG, "Spinorbite must match the grid's nspino");
   if (e->Spinorbite && (g.nspin != 2 || e->nspinp != 2 || e->nspinr != 2))
@@ -220,13 +220,15 @@ fdmgpu_status check_energy_c(const fdmgpu_handle* h, const fdmgpu_energy* e) {
   if (e->nligne <= 0 || e->nlmso <= 0 || e->nligneso != e->nligne - e->nlmso)
     return fail(FDMGPU_ERR_ARG, "inconsistent nligne / nlmso / nligneso");
   if ((int64_t)2 * e->nligne > (int64_t)1 << 30) return fail(FDMGPU_ERR_ARG, "nligne too large");
-  if (e->lmaxso < 0 || g.nspino * (e->lmaxso + 1) * (e->lmaxso + 1) < e->nlmso || e->nsort_r < g.nsort)
+  if (e->lmaxso < 0 || g.nspino * (e->lmaxso + 1) * (e->lmaxso + 1) < e->nlmso ||
+      (e->E_comp ? e->nsort_c : e->nsort_r) < g.nsort)
     return fail(FDMGPU_ERR_ARG, "Bessel arrays too small for nlmso");
   if (e->nlmso > g.nso1) return fail(FDMGPU_ERR_ARG, "nlmso exceeds the outer harmonic tables");
   if (e->ispin < 1 || e->nspinp < std::min(e->ispin, g.nspin) || e->nphiato1 < g.nbtm)
     return fail(FDMGPU_ERR_ARG, "phiato too small (nspinp or nphiato1)");
   if (!e->new_ || !e->newinv || !e->lb1 || !e->lb2 || !e->ianew || !e->nlmsa || !e->Vr || !e->phiato ||
-      !e->Besselr || !e->Neumanr || ((e->Relativiste || e->Spinorbite) && !e->gradvr))
+      (e->E_comp ? (!e->Bessel || !e->Neuman) : (!e->Besselr || !e->Neumanr)) ||
+      ((e->Relativiste || e->Spinorbite) && !e->gradvr))
     return fail(FDMGPU_ERR_ARG, "null array argument");
   if ((e->Relativiste || e->Spinorbite) && e->nicm < g.npoint) return fail(FDMGPU_ERR_ARG, "gradvr too small (nicm)");
   for (int Lm = 1; Lm <= e->nlmso; ++Lm)
@@ -374,6 +376,8 @@ fdmgpu_status plan_problem(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& h
   P.ispin = e->ispin;
   P.enervide = e->Enervide;
   P.cplx = cplx ? 1 : 0;
+  P.ecomp = (cplx && e->E_comp) ? 1 : 0;
+  P.eimag = P.ecomp ? e->Eimag : 0.0;
   P.nligne_c = e->nligne;
   P.so = e->Spinorbite ? 1 : 0;
   P.rel = e->Relativiste ? 1 : 0;
@@ -426,11 +430,21 @@ void pack_inputs(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& hp) {
     const int nl = e->lmaxso + 1;
     for (int which = 0; which < 2; ++which) {
       (which == 0 ? hp.rel_bes : hp.rel_neu) = (int64_t)hp.in_d.size();
-      const double* a = which == 0 ? e->Besselr : e->Neumanr;
-      for (int isp = 1; isp <= std::max(1, e->nspinr); ++isp)
-        for (int ib = 0; ib < g.nsort; ++ib)
-          for (int L = 0; L < nl; ++L)
-            hp.in_d.push_back(a[ib + (int64_t)e->nsort_r * (L + (int64_t)nl * (isp - 1))]);
+      if (e->E_comp) {
+        // complex (2, nsort_c, 0:lmaxso, nspinr): the real block, then the imaginary block
+        const double* a = which == 0 ? e->Bessel : e->Neuman;
+        for (int part = 0; part < 2; ++part)
+          for (int isp = 1; isp <= std::max(1, e->nspinr); ++isp)
+            for (int ib = 0; ib < g.nsort; ++ib)
+              for (int L = 0; L < nl; ++L)
+                hp.in_d.push_back(a[2 * (ib + (int64_t)e->nsort_c * (L + (int64_t)nl * (isp - 1))) + part]);
+      } else {
+        const double* a = which == 0 ? e->Besselr : e->Neumanr;
+        for (int isp = 1; isp <= std::max(1, e->nspinr); ++isp)
+          for (int ib = 0; ib < g.nsort; ++ib)
+            for (int L = 0; L < nl; ++L)
+              hp.in_d.push_back(a[ib + (int64_t)e->nsort_r * (L + (int64_t)nl * (isp - 1))]);
+      }
     }
     return;
   }
@@ -1364,7 +1378,8 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
         launch_copy_rhs(h->d_probs.p, h->pl, h->dims, h->stream);
         nkern += 1;
         nkern += launch_factor<double>(h->sp, h->pl.env64, h->pl.X64, h->d_probs.p, h->tb, np, 1,
-                                       h->d_active.p, h->pl.err, 1e-10, nullptr, h->stream);
+                                       h->d_active.p, h->pl.err, 1e-10, b.cplx == 1 ? h->pl.piv : nullptr,
+                                       h->stream);
         nkern += launch_backward<double>(h->sp, h->pl.env64, h->pl.X64, h->d_probs.p, h->tb, np,
                                          h->d_active.p, h->stream);
       }
@@ -1916,8 +1931,6 @@ fdmgpu_status fdmgpu_batch_add_site(fdmgpu_handle* h, fdmgpu_handle* site, const
   if (si == (int)b.sites.size()) b.sites.push_back(site);
   const int cplx = e->Cal_comp ? 1 : 0;
   if (b.cplx >= 0 && b.cplx != cplx) return fail(FDMGPU_ERR_ARG, "a batch holds either real or complex problems");
-  if (cplx && b.precision != FDMGPU_PREC_FP64)
-    return fail(FDMGPU_ERR_UNSUPPORTED, "the library solves complex problems in FP64");
   if (cplx && b.sites.size() > 1) return fail(FDMGPU_ERR_UNSUPPORTED, "complex problems of several sites in one batch");
   HostProb hp;
   st = plan_problem(site, e, hp);

@@ -11,8 +11,9 @@
 // two rows of a block always share a tile).
 //
 // Restates the complex branch of calcMatRow (source/mat.f90:1034-1632) for
-// Cal_comp = true, E_comp = irregular = Repres_comp = false, C1 characters
-// (Kar = 1, Kari = 0):
+// Cal_comp = true, irregular = Repres_comp = false, C1 characters (Kar = 1,
+// Kari = 0), real energies or complex ones (E_comp: -i Eimag on the grid
+// diagonal, mat.f90:1151-1152, and the complex Bessel / Neumann of phiso):
 //   k_asmc_grid       grid rows with the relativistic and spin-orbit gradient
 //                     terms (mat.f90:1142-1402), one warp per point, both spin
 //                     rows of a point in turn
@@ -111,6 +112,13 @@ __device__ __forceinline__ double2 phic(const CIn& c, const Prob& P, const Stati
 __device__ __forceinline__ double besr(const CIn& c, const double* a, const StaticDev& S, int ib, int L, int isp) {
   return a[((int64_t)(isp - 1) * S.nsort + (ib - 1)) * c.nl + L];
 }
+// Complex Bessel / Neumann value: the imaginary block follows the real one
+// (complex energies); zero imaginary part for real energies.
+__device__ __forceinline__ double2 besc(const CIn& c, const Prob& P, const double* a, const StaticDev& S, int ib, int L,
+                                        int isp) {
+  const int64_t o = ((int64_t)(isp - 1) * S.nsort + (ib - 1)) * c.nl + L;
+  return make_double2(a[o], P.ecomp ? a[o + (int64_t)P.nspinr * S.nsort * c.nl] : 0.0);
+}
 __device__ __forceinline__ double ysot(const StaticDev& S, int ib, int lm0) {
   return S.YsoT[(int64_t)(ib - 1) * S.nlmomax + (lm0 - 1)];
 }
@@ -125,8 +133,10 @@ __device__ __forceinline__ double ylmato(const StaticDev& S, int ib, int lm0, in
 // Neumanr in the real basis (Basereel, kept for completeness).
 __device__ __forceinline__ double2 colfac(const CIn& c, const Prob& P, const StaticDev& S, int basereel, int ib, int L,
                                           int ispq) {
-  if (basereel) return make_double2(besr(c, c.neu, S, ib, L, ispq), 0.0);
-  return make_double2(besr(c, c.bes, S, ib, L, ispq), besr(c, c.neu, S, ib, L, ispq));
+  const double2 n = besc(c, P, c.neu, S, ib, L, ispq);
+  if (basereel) return n;
+  const double2 j = besc(c, P, c.bes, S, ib, L, ispq);
+  return make_double2(j.x - n.y, j.y + n.x);  // j + i n
 }
 
 __global__ void k_asmc_pad(const Prob* probs, double* env, Tables tb, int* err) {
@@ -167,7 +177,7 @@ __global__ void __launch_bounds__(256) k_asmc_grid(const StaticDev* sites, const
     const double VmE = c.vr[(i - 1) + (int64_t)S.npoint * (ispp - 1)] - P.enervide;
     double dr = VmE - S.clapl[0];
     if (P.rel) dr = dr - a2s4 * (VmE * VmE);
-    if (lane == 0) add_c(env, P, tb, ii, ii, make_double2(dr, 0.0), err, e);
+    if (lane == 0) add_c(env, P, tb, ii, ii, make_double2(dr, P.ecomp ? -P.eimag : 0.0), err, e);
     const double bder = (P.rel || P.so) ? -a2s4 / (1.0 - a2s4 * VmE) : 0.0;
     double cr[2] = {0.0, 0.0}, ci[2] = {0.0, 0.0};
     for (int iv = 0; iv < S.nvois; ++iv) {
@@ -233,8 +243,7 @@ __global__ void __launch_bounds__(256) k_asmc_grid(const StaticDev* sites, const
           const double2 cf = make_double2(cr[s - 1], ci[s - 1]);
           const double2 y = yso(P, S, ib, m, lm0);
           add_c(env, P, tb, ii, P.nligneso + Lm, c_mul(c_mul(colfac(c, P, S, basereel, ib, L, iq), y), cf), err, e);
-          const double bj = besr(c, c.bes, S, ib, L, iq);
-          const double2 g = c_mul(make_double2(y.x * bj, y.y * bj), cf);
+          const double2 g = c_mul(c_mul(y, besc(c, P, c.bes, S, ib, L, iq)), cf);
           add_rhs_c(B, P, ii, Lm, make_double2(-g.x, -g.y));
         }
         ispq = min(S.iso[P.nlmso - 1], P.nspinr);
@@ -295,8 +304,7 @@ __global__ void __launch_bounds__(256) k_asmc_outer(const StaticDev* sites, cons
       cd = c_mul(cb, yc(mp, ysot(S, ib, lmp0), ysot(S, ib, lmp0 - 2 * mp)));
     else
       cd = c_mul(cb, make_double2(ysot(S, ib, lmp0), 0.0));
-    const double bj = besr(c, c.bes, S, ib, L, iq);
-    cd = make_double2(cd.x * bj, cd.y * bj);
+    cd = c_mul(cd, besc(c, P, c.bes, S, ib, L, iq));
     sm = make_double2(sm.x - cd.x, sm.y - cd.y);
   }
   const int ii = P.nligneso + Lm;

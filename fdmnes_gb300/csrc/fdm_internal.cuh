@@ -72,6 +72,11 @@ struct Prob {
   // Bessel and Neumann of the real path, from the site's radial tables
   int gen;
   int gen_lmax[8];    // l cut-off per atom type at this energy
+  // complex energy (E_comp, regular solution): -i Eimag on the grid
+  // diagonal, complex Bessel / Neumann stored as real blocks then imaginary
+  // blocks, each [nspinr][nsort][lmaxso+1]
+  int ecomp;
+  double eimag;
 };
 constexpr int MAX_GEN_TYPES = 8;
 

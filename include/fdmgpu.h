@@ -220,8 +220,9 @@ void fdmgpu_destroy(fdmgpu_handle* h);
  * smr/smi are host pointers.  info may be NULL.
  * Complex problems (Cal_comp: complex harmonics, spin-orbit with nspino = 2,
  * relativistic terms; real energies, complex basis, C1 characters) are
- * solved in FP64 as their real-equivalent system with tile-local pivoting;
- * precision must be FDMGPU_PREC_FP64 for them and smi must be given. */
+ * solved as their real-equivalent system with tile-local pivoting, in FP64
+ * or in mixed precision (FP32 factor, double-float residual refinement);
+ * smi must be given. */
 fdmgpu_status fdmgpu_mat_solve(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t precision,
                                double* smr, double* smi, fdmgpu_info* info);
 

@@ -340,12 +340,48 @@ def test_complex_batch_of_energies(solver_mod):
     sv.close()
 
 
-def test_complex_mixed_precision_is_rejected(solver_mod):
-    """The library solves complex problems in FP64: the mixed path says so."""
-    st, ga, ea = _complex_case(True)
+@pytest.mark.parametrize("spinorbit", [False, True])
+def test_complex_mixed_precision_matches_oracle(solver_mod, spinorbit):
+    """Complex problems in mixed precision: the real-equivalent system factored
+    in FP32 with tile-local pivoting and refined against the double-float
+    residual, like the real path.  Bars as the real path's: 1e-8 with the
+    double-float residual, 1e-10 with the FP64 residual."""
+    import oracle
+    st, ga, ea = _complex_case(spinorbit)
+    X0, _ = oracle.mat_solve_c(ga, ea)
+    T0 = oracle.taull_c(ga, ea, X0)
     sv = solver_mod.FdmSolver(ga.d)
-    with pytest.raises(solver_mod.FdmError):
-        sv.mat_solve_complex(ea, "mixed")
+    for mode, tol in (("df64", 1e-8), ("fp64", 1e-10)):
+        sv.set_residual(mode)
+        X, info = sv.mat_solve_complex(ea, "mixed")
+        assert rel(X, X0) < tol, (mode, rel(X, X0))
+    sv.set_residual("df64")
+    nsp = 2 if spinorbit else 1
+    sv.spectrum_begin("mixed", 1)
+    sv.spectrum_add_args(ea)
+    sv.spectrum_run()
+    assert np.abs(sv.taull_c(0, nsp) - T0).max() <= 1e-8 * np.abs(T0).max()
+    sv.close()
+
+
+def test_complex_mixed_batch_matches_fp64(solver_mod):
+    """Spin-orbit energies of the 13-atom Pt cluster (coarse grid) in one
+    mixed batch against the FP64 batch: Taull to 1e-6 (the bar of that
+    cluster's FP64 parity, set by its conditioning)."""
+    from fdmnes_gb300 import abi, cluster as CL, complex_path as CP
+    st = CL.build_structure(CL.pt_cluster(2.8), 0.45, 3.0, 15.0, nspin=2)
+    ga = abi.GridArgs(CP.grid_dict(st, True))
+    eas = [abi.EnergyArgs(CP.energy_dict(st, E, spinorbit=True)) for E in (3.0, 8.0, 14.0)]
+    sv = solver_mod.FdmSolver(ga.d)
+    T = {}
+    for prec in ("fp64", "mixed"):
+        sv.spectrum_begin(prec, len(eas))
+        for ea in eas:
+            sv.spectrum_add_args(ea)
+        sv.spectrum_run()
+        T[prec] = [sv.taull_c(k, 2) for k in range(len(eas))]
+    for a, b in zip(T["mixed"], T["fp64"]):
+        assert np.abs(a - b).max() <= 1e-6 * np.abs(b).max()
     sv.close()
 
 
@@ -410,4 +446,36 @@ def test_wide_accumulation_at_atom_steps(solver_mod):
         assert max(rel(a, b) for a, b in zip(T, T64)) < 1e-5, mode
         assert xanes.convolved_relative_error(energies, T, T64) < 1e-6, mode
     assert fallbacks["wide_atom"] <= fallbacks["fp32"], fallbacks
+    sv.close()
+
+
+@pytest.mark.parametrize("spinorbit", [False, True])
+def test_complex_energy_matches_oracle(solver_mod, spinorbit):
+    """Complex energies (E_comp, the regular solution): E + i Eimag with Eimag =
+    0.5 eV, -i Eimag on the grid diagonal and the complex-argument Bessel /
+    Neumann of phiso at k = sqrt(Ekin + i Eimag).  FP64 against the oracle's
+    complex solve to 1e-9, mixed to 1e-8, and Taull of a batch of broadened
+    energies to 1e-9."""
+    import oracle
+    from fdmnes_gb300 import abi, complex_path as CP
+    st = CP.pt_so_structure()
+    ga = abi.GridArgs(CP.grid_dict(st, spinorbit))
+    eim = 0.5 / 13.605693122994
+    eas = [abi.EnergyArgs(CP.energy_dict(st, E, spinorbit=spinorbit, eimag_ry=eim)) for E in (3.0, 12.0, 25.0)]
+    sv = solver_mod.FdmSolver(ga.d)
+    nsp = 2 if spinorbit else 1
+    refs = []
+    for ea in eas:
+        X0, _ = oracle.mat_solve_c(ga, ea)
+        refs.append((X0, oracle.taull_c(ga, ea, X0)))
+    X, _ = sv.mat_solve_complex(eas[1], "fp64")
+    assert rel(X, refs[1][0]) < 1e-9
+    Xm, _ = sv.mat_solve_complex(eas[1], "mixed")
+    assert rel(Xm, refs[1][0]) < 1e-8
+    sv.spectrum_begin("fp64", len(eas))
+    for ea in eas:
+        sv.spectrum_add_args(ea)
+    sv.spectrum_run()
+    for k, (_, T0) in enumerate(refs):
+        assert np.abs(sv.taull_c(k, nsp) - T0).max() <= 1e-9 * np.abs(T0).max()
     sv.close()
