@@ -213,11 +213,22 @@ def run_reference(args):
 
 
 # ---------------------------------------------------------------- GPU arm
+def _traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu capture summary
+    (profiles/traffic.json, written from `ncu --metrics dram__bytes_read.sum,
+    dram__bytes_write.sum`), or None."""
+    try:
+        with open(os.path.join(HERE, "profiles", "traffic.json")) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
     from fdmnes_gb300 import build as B, cluster as CL, xanes
-    from fdmnes_gb300.solver import FdmSolver
+    from fdmnes_gb300.solver import FdmSolver, measure_pipe_peaks
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -238,14 +249,17 @@ def run_gpu(args):
     n_e = len(energies)
     n_all = len(all_energies)
     st = CL.cu_structure()
-    items = xanes.spectrum_inputs(st, energies)
+    items = xanes.spectrum_inputs(st, energies)                      # host-built phiato / Bessel / Neumann
+    items_gen = xanes.spectrum_inputs(st, energies, functions=False)  # generated on the device
     sv = FdmSolver(st)
+    sv.set_radial()
     # operating point for the metric's <= 1e-6 cross-section bar: refinement
-    # stops at max|dx|/max|x| <= 1e-8 and accepts stalls up to 1e-6 (measured
-    # convolved error ~3e-9); the library default (1e-10) is kept for parity
+    # stops at max|dx|/max|x| <= 1e-8 and accepts stalls up to 1e-6; the
+    # library default (1e-10) is kept for parity
     TOL, TOL_ACCEPT = 1e-8, 1e-6
     sv.set_tolerance(TOL, TOL_ACCEPT)
     sv.set_factor_mode(args.factor_mode)
+    sv.set_tile_engine(args.tile_engine)
 
     def barrier_sync():
         torch.cuda.synchronize()
@@ -259,20 +273,24 @@ def run_gpu(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    # plain FP64 reference spectrum (correctness path), once
+    # plain FP64 reference spectrum (the correctness path), once, on the same
+    # device-generated inputs, and its device-resident timing
     t0 = time.perf_counter()
-    T64, info64 = sv.spectrum(items, "fp64")
+    T64, info64 = sv.spectrum(items_gen, "fp64")
     fp64_wall = time.perf_counter() - t0
-    info64 = sv.spectrum_rerun()  # device-resident timing of the FP64 path
+    info64 = sv.spectrum_rerun()
     fp64_ms = info64["ms_assemble"] + info64["ms_factor"] + info64["ms_solve"]
+    sig64, conv64 = sv.xanes(energies, 0.78)
 
     # mixed precision spectrum: warm-up (plans, graphs), then timed reruns
     sv.spectrum_begin("mixed", n_e)
-    for ei, ri in items:
+    for ei, ri in items_gen:
         sv.spectrum_add(ei, ri)
     info = sv.spectrum_run()
-    Tm = [sv.taull(k) for k in range(n_e)]
-    err_conv = xanes.convolved_relative_error(energies, Tm, T64)
+    Tm = sv.taull_all()
+    sigm, convm = sv.xanes(energies, 0.78)
+    err_conv = float(np.abs(convm - conv64).max() / np.abs(conv64).max())
+    err_conv_host = xanes.convolved_relative_error(energies, Tm, T64)
     err_taull = max(float(np.abs(a - b).max() / np.abs(b).max()) for a, b in zip(Tm, T64))
     for _ in range(args.warmup):
         sv.spectrum_rerun()
@@ -280,51 +298,52 @@ def run_gpu(args):
     clk = ClockSampler()
     clk.start()
     barrier_sync()
-    ev0 = torch.cuda.Event(enable_timing=True)
-    ev1 = torch.cuda.Event(enable_timing=True)
     infos = []
-    t_wall = time.perf_counter()
     for _ in range(args.steps):
         infos.append(sv.spectrum_rerun())
     barrier_sync()
-    wall = time.perf_counter() - t_wall
     # device time of the spectrum: sum of the phases timed by CUDA events on the solver's stream
     dev_ms = [i["ms_assemble"] + i["ms_factor"] + i["ms_solve"] + i["ms_refine"] for i in infos]
     ms_step = max_over_ranks(statistics.mean(dev_ms))
     value = n_all / (ms_step / 1000.0)
 
-    # end to end through the C-ABI from host buffers
-    h2d = d2h = 0
-    e2e_times = []
-    for s in range(args.steps):
-        barrier_sync()
-        t0 = time.perf_counter()
-        sv.spectrum_begin("mixed", n_e)
-        for ei, ri in items:
-            sv.spectrum_add(ei, ri)
-        sv.spectrum_run()
-        out = sv.taull_all()
-        barrier_sync()
-        e2e_times.append(time.perf_counter() - t0)
-        if s == 0:
-            h2d = sum(ei.phiato.nbytes + ei.besselr.nbytes + ei.neumanr.nbytes + st.Vr[:, 0].nbytes +
-                      4 * (st.grid.npoint + 1 + 2 * st.natome) for ei, _ in items)
-            d2h = sum(t.nbytes for t in out)
+    def e2e_run(its, gen: bool):
+        """Per step through the C-ABI from host buffers: pack and copy every
+        energy's inputs host -> device, run, copy every Taull back."""
+        times = []
+        h2d = d2h = 0
+        for s_ in range(args.steps):
+            barrier_sync()
+            t0 = time.perf_counter()
+            sv.spectrum_begin("mixed", n_e)
+            for ei, ri in its:
+                sv.spectrum_add(ei, ri)
+            sv.spectrum_run()
+            out = sv.taull_all()
+            barrier_sync()
+            times.append(time.perf_counter() - t0)
+            if s_ == 0:
+                ints = sum(4 * (st.grid.npoint + 1 + 2 * st.natome) for _ in its)
+                vr = sum(st.Vr[:, 0].nbytes for _ in its)
+                fun = 0 if gen else sum(ei.phiato.nbytes + ei.besselr.nbytes + ei.neumanr.nbytes for ei, _ in its)
+                h2d = ints + vr + fun
+                d2h = sum(t.nbytes for t in out)
+        return max_over_ranks(statistics.mean(times)), h2d, d2h
+
+    e2e_s, h2d, d2h = e2e_run(items_gen, True)
+    e2e_host_s, h2d_host, _ = e2e_run(items, False)
     clocks = clk.stop()
-    e2e_s = max_over_ranks(statistics.mean(e2e_times))
 
     peaks, peak_kind = _peaks()
     last = infos[-1]
-    # FP32 / FP64 FMA pipe rates of this GPU, measured here (fdmgpu_measure_pipe_peaks)
-    from fdmnes_gb300.solver import measure_pipe_peaks
-    pipes = measure_pipe_peaks()
+    pipes = measure_pipe_peaks()  # FP32 / FP64 FMA rates of this GPU, measured here
     FP32_PIPE_TFLOPS = pipes["fp32_tflops"]
 
-    def roof(flops, ms, kernel, note):
+    def roof(flops, ms, kernel, note, traffic_key=None):
         ach = flops / (ms / 1000.0) / 1e12 if ms > 0 else 0.0
         return {"bound": "tensor", "achieved": ach, "peak": peaks["bf16_tflops"], "unit": "TFLOP/s",
-                "frac": ach / peaks["bf16_tflops"], "traffic": None, "kernel": kernel,
-                "peak_note": f"bf16 dense tensor peak ({peak_kind}); {note}",
+                "frac": ach / peaks["bf16_tflops"], "traffic": _traffic(traffic_key) if traffic_key else None,
+                "kernel": kernel, "peak_note": f"bf16 dense tensor peak ({peak_kind}); {note}",
                 "frac_of_fp32_pipe": ach / FP32_PIPE_TFLOPS}
 
     # dominant phase of the step (launch list in profiles/): the double-float
@@ -332,12 +351,16 @@ def run_gpu(args):
     roof_main = roof(last["flops_escalate_factor"], last["ms_escalate_factor"],
                      "double-float escalation factor (k_diag/k_panel/k_trailing<dfl>), one launch sequence per step",
                      "runs on the FP32 pipes, ~12 FP32 instructions per double-float multiply-add; flops counted "
-                     "as 2 per multiply-add of the profile")
+                     "as 2 per multiply-add of the profile", "k_trailing<dfl, 128>")
     roof_res = roof(last["flops_residual"], last["ms_residual_first"],
                     "k_residual_df, first refinement step (all energies active)",
-                    "double-float residual on the FP32 pipes; 2 flops per CSR nonzero per right-hand side")
-    roof_fac = roof(last["flops_factor"], last["ms_factor"], "FP32 profile LU (k_diag + k_panel + k_trailing<float>)",
-                    "FP32 SIMT pipes")
+                    "double-float residual on the FP32 pipes; 2 flops per CSR nonzero per right-hand side",
+                    "k_residual_df")
+    fac_kernel = ("k_tc_update<0> (tcgen05 split-TF32)" if args.tile_engine != "simt" else "k_trailing<float, 128>")
+    roof_fac = roof(last["flops_factor"], last["ms_factor"],
+                    f"FP32 profile LU (k_diag + k_panel + {fac_kernel})",
+                    "tensor cores, three TF32 products per FP32 product" if args.tile_engine != "simt"
+                    else "FP32 SIMT pipes", fac_kernel.split(" ")[0])
     if rank != 0:
         return
     cb = cpu_baseline(min(os.cpu_count() or 1, 16)) if not args.no_cpu else None
@@ -346,26 +369,36 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": "energies/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32 factor + f64 refinement (df64 residual)", "data": "synthetic",
-        "config": {"workload": "Cu fcc a=3.61 A, 13-atom cluster, FDM radius 3.0 A, step 0.25 A, C1, "
-                               f"{n_all} energies -5..35 eV step {step / world:.2g} eV, batched mixed precision",
-                   "energies": n_all, "energies_per_gpu": n_e, "e_step_ev": step / world, "nligne": [min(r.nligne for _, r in items), max(r.nligne for _, r in items)],
+        "config": {"workload": WORKLOAD_CU401 if world == 1 and args.energies == 401 else
+                   "Cu fcc a=3.61 A, 13-atom cluster, FDM radius 3.0 A, step 0.25 A, C1, "
+                   f"{n_all} energies -5..35 eV step {step / world:.2g} eV, batched mixed precision",
+                   "energies": n_all, "energies_per_gpu": n_e, "e_step_ev": step / world,
+                   "nligne": [min(r.nligne for _, r in items), max(r.nligne for _, r in items)],
                    "nrhs": [min(e.nlmso for e, _ in items), max(e.nlmso for e, _ in items)],
+                   "inputs": "phiato, Bessel and Neumann generated on the device (fdmgpu_set_radial)",
                    "l2": "working set ~100 GB per step, far above the 126 MB L2 (no flush needed)",
                    "refine_tol": TOL, "refine_tol_accept": TOL_ACCEPT, "factor_mode": args.factor_mode,
+                   "tile_engine": args.tile_engine,
                    "autotune": {"mixed": sv.tuning("mixed"), "fp64": sv.tuning("fp64")}},
         "roofline": roof_main,
         "roofline_other": [roof_res, roof_fac],
-        "cpu_baseline": cb and {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "pipes_measured": pipes,
+        "cpu_baseline": cb and {k: cb[k] for k in ("value", "unit", "cores", "kind", "build", "sample")},
         "cpu_superlu_standin": slu,
         "e2e": {"value": n_all / e2e_s, "unit": "energies/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h),
+                "inputs": "energies with NULL phiato/Bessel/Neumann: generated on the device"},
+        "e2e_host_inputs": {"value": n_all / e2e_host_s, "unit": "energies/s", "h2d_bytes_per_step": int(h2d_host),
+                            "d2h_bytes_per_step": int(d2h), "inputs": "phiato/Bessel/Neumann built on the host"},
         "gpu_launches": int(last["n_kernels"]),
         "clocks": clocks,
         "plain_fp64": {"value": n_e / (fp64_ms / 1000.0), "unit": "energies/s", "ms_per_step": fp64_ms,
                        "first_call_wall_s": fp64_wall, "gpu_launches": int(info64["n_kernels"])},
-        "accuracy": {"convolved_rel_err_vs_fp64": err_conv, "taull_max_rel_err_vs_fp64": err_taull,
-                     "refine_iters_max": last["refine_iters"], "fp64_escalations": last["n_fallback"]},
-        "phases_ms": {k: last[k] for k in ("ms_assemble", "ms_factor", "ms_solve", "ms_refine")},
+        "accuracy": {"convolved_rel_err_vs_fp64": err_conv, "convolved_rel_err_vs_fp64_host": err_conv_host,
+                     "taull_max_rel_err_vs_fp64": err_taull, "refine_iters_max": last["refine_iters"],
+                     "fp64_escalations": last["n_fallback"]},
+        "phases_ms": {k: last[k] for k in ("ms_assemble", "ms_factor", "ms_solve", "ms_refine",
+                                           "ms_escalate_factor")},
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -381,8 +414,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--energies", type=int, default=401,
                     help="energies of the spectrum over -5..35 eV (401: step 0.1 eV; 41: step 1 eV)")
-    ap.add_argument("--factor-mode", default="fp32", choices=["fp32", "wide_atom"],
+    ap.add_argument("--factor-mode", default="fp32", choices=["fp32", "wide_atom", "wide_all"],
                     help="accumulation of the FP32 factor (wide_atom: double-float sums at the atom-harmonic steps)")
+    ap.add_argument("--tile-engine", default="simt", choices=["simt", "tcgen05", "tcgen05_factor"],
+                    help="FP32 tile updates on the FP32 pipes or on the tensor cores (split TF32)")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

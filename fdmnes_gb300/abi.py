@@ -47,7 +47,9 @@ class FdmInfo(C.Structure):
                 ("ms_assemble", C.c_double), ("ms_factor", C.c_double), ("ms_solve", C.c_double),
                 ("ms_refine", C.c_double), ("n_fallback", C.c_int32), ("n_kernels", C.c_int64),
                 ("ms_residual_first", C.c_double), ("flops_residual", C.c_double),
-                ("ms_escalate_factor", C.c_double), ("flops_escalate_factor", C.c_double)]
+                ("ms_escalate_factor", C.c_double), ("flops_escalate_factor", C.c_double),
+                ("n_wide_refactor", C.c_int32), ("ms_wide_refactor", C.c_double),
+                ("flops_wide_refactor", C.c_double)]
 
 
 def _pi(a: np.ndarray, keep: List):

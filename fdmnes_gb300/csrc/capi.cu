@@ -86,11 +86,18 @@ struct Batch {
   // results
   std::vector<int> iters;
   std::vector<int> fallback;   // solved again in FP64 after the mixed path missed its tolerance
+  std::vector<int> wide;       // factorised again with double-float sums in every trailing update
   std::vector<int> inner;      // GMRES steps summed over the refinement
   std::vector<double> resid;
   std::vector<int> err;
   bool ran = false;
   bool lam_valid = false;  // the adjoint Lambda of the last vjp matches the batch's factors
+  // a batch larger than the memory budget runs in consecutive chunks; its
+  // Taull then lives on the host (concatenated in add order)
+  bool chunked = false;
+  int nchunks = 0;
+  std::vector<double> taull_host;
+  std::vector<int64_t> taull_off;   // per problem, in doubles
   std::vector<fdmgpu_handle*> sites;  // grids of the batch's problems; sites[0] is the batch's own handle
 };
 
@@ -142,6 +149,9 @@ struct fdmgpu_handle {
   int refine_gmres = 0;   // GMRES-IR (1) or classical refinement (0)
   int refine_recur = 0;   // classical refinement with the residual updated by recurrence (1)
   int escalate_dfl = 1;   // escalation by a double-float (1) or an FP64 (0) factorisation
+  int escalate_wide = 0;  // first a wide-accumulation FP32 re-factorisation of the stalled energies
+  double mem_budget = 0;  // device bytes a batch's pools may take before it runs in chunks (0: 85% of the device)
+  DevBuf<unsigned char> d_wide_all;  // every step wide (the re-factorisation's table)
   int gmres_m = 12;       // Krylov dimension of one GMRES cycle
   int autotune = 1;         // time the trailing-update layouts on each new plan
   int factor_mode = 0;      // FDMGPU_FACTOR_*: wide accumulation at the atom-harmonic steps of the FP32 factor
@@ -620,6 +630,7 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   CK(upload(h->d_Imin, Imin, s));
   CK(upload(h->d_strip, strip, s));
   CK(upload(h->d_wide, L.wide, s));
+  CK(upload(h->d_wide_all, std::vector<unsigned char>(L.wide.size(), 1), s));
   if (h->d_env64.reserve((size_t)env * TS2) != cudaSuccess || h->d_B64.reserve(rhs) != cudaSuccess ||
       h->d_X64.reserve(rhs) != cudaSuccess || h->d_err.reserve(np) != cudaSuccess ||
       h->d_active.reserve(np) != cudaSuccess || h->d_red.reserve(3 * (size_t)np) != cudaSuccess ||
@@ -1063,10 +1074,14 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   int64_t nkern = h->nk_asm + h->nk_fac + h->nk_sol;
   b.iters.assign(np, 0);
   b.fallback.assign(np, 0);
+  b.wide.assign(np, 0);
   b.inner.assign(np, 0);
   b.resid.assign(np, 0.0);
   b.err.assign(np, 0);
   float ms_refine = 0;
+  float wide_ms = 0;
+  double wide_flops = 0.0;
+  std::vector<int> wide_esc(np, 0);
   bool esc_timed = false;
   double esc_ms_overlap = -1.0, esc_flops_overlap = 0.0;
   if (b.precision == FDMGPU_PREC_MIXED) {
@@ -1271,6 +1286,62 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
         CK(cudaStreamSynchronize(h->stream));
       }
     }
+    // First escalation stage (FDMGPU_ESCALATE_WIDE_DF64): the stalled
+    // problems are factorised again in FP32 with double-float sums in every
+    // trailing update (the FP32 band converted again from the FP64 one), and
+    // the device refinement loop continues from their current solution.
+    int n_wide = 0;
+    if (dev_loop && h->escalate_wide) {
+      std::vector<RefineState> rs(np);
+      for (int k = 0; k < np; ++k) {
+        const bool w = !(b.resid[k] <= tol_accept);
+        n_wide += w;
+        rs[k].active = w ? 1 : 0;
+        rs[k].slow = 0;
+        rs[k].iters = 0;
+        rs[k].pad = 0;
+        rs[k].prev = 1e300;
+        rs[k].resid = b.resid[k];
+        active[k] = w ? 1 : 0;
+      }
+      if (n_wide > 0) {
+        CK(cudaEventRecord(h->ev[8], h->stream));
+        CK(cudaMemcpyAsync(h->d_active.p, active.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+        CK(cudaMemcpyAsync(h->d_rstate.p, rs.data(), np * sizeof(RefineState), cudaMemcpyHostToDevice, h->stream));
+        const RefineCtl c0{0, max_iter, tol, n_wide, 0};
+        CK(cudaMemcpyAsync(h->d_rctl.p, &c0, sizeof c0, cudaMemcpyHostToDevice, h->stream));
+        launch_convert_masked(h->d_probs.p, h->pl, h->tb, h->dims, h->stream);
+        Tables tw = h->tb;
+        tw.wide = h->d_wide_all.p;
+        StepPlan sw = h->sp;
+        sw.wide_any.assign(sw.ntmax, 1);
+        nkern += 1 + launch_factor<float>(sw, h->pl.env32, h->pl.Y32, h->d_probs.p, tw, np, 0, h->d_active.p,
+                                          h->pl.err, 1e-30, h->pl.piv, h->stream,
+                                          h->trail_threads[1]);
+        CK(cudaEventRecord(h->ev[9], h->stream));
+        CK(cudaGraphLaunch(h->g_res, h->stream));
+        CK(cudaGraphLaunch(h->g_iter, h->stream));
+        CK(cudaGraphLaunch(h->g_loop, h->stream));
+        std::vector<RefineState> rs2(np);
+        RefineCtl c1;
+        CK(cudaMemcpyAsync(rs2.data(), h->d_rstate.p, np * sizeof(RefineState), cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaMemcpyAsync(&c1, h->d_rctl.p, sizeof c1, cudaMemcpyDeviceToHost, h->stream));
+        CK(cudaStreamSynchronize(h->stream));
+        CK(cudaGetLastError());
+        nkern += h->nk_res + h->nk_iter + 1 + (int64_t)std::max(c1.it - 1, 0) * h->nk_loop_body;
+        for (int k = 0; k < np; ++k)
+          if (rs[k].active) {
+            b.iters[k] += rs2[k].iters;
+            b.resid[k] = rs2[k].resid;
+            wide_esc[k] = 1;
+          }
+        float t = 0;
+        CK(cudaEventElapsedTime(&t, h->ev[8], h->ev[9]));
+        wide_ms = t;
+        for (int k = 0; k < np; ++k)
+          if (rs[k].active) wide_flops += b.probs[k].flops_factor;
+      }
+    }
     // Precision escalation: problems whose refinement missed tol_accept are
     // factorised again in double-float (or FP64) arithmetic and solved.
     int nfail = 0;
@@ -1392,6 +1463,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
     CK(cudaEventRecord(h->ev[5], h->stream));
     for (int k = 0; k < np; ++k)
       if (!(b.resid[k] <= tol_accept)) b.err[k] = FDMGPU_ERR_NOT_CONVERGED;
+    for (int k = 0; k < np; ++k) b.wide[k] = wide_esc[k];
   }
   if (b.probs[0].P.nlm_abs > 0) {
     if (b.cplx == 1) {
@@ -1457,6 +1529,9 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
       info->refine_iters = mi;
       info->residual = mr;
       for (int k = 0; k < np; ++k) info->n_fallback += b.fallback[k];
+      for (int k = 0; k < np; ++k) info->n_wide_refactor += b.wide[k];
+      info->ms_wide_refactor = wide_ms;
+      info->flops_wide_refactor = wide_flops;
     }
   }
   // hard errors first; a refinement that did not reach its tolerance still
@@ -1711,6 +1786,7 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   h->d_act_rec.release();
   h->d_strip.release();
   h->d_wide.release();
+  h->d_wide_all.release();
   h->d_probs.release();
   h->d_red.release();
   if (h->h_pinned_i) cudaFreeHost(h->h_pinned_i);
@@ -1898,10 +1974,13 @@ fdmgpu_status fdmgpu_get_tuning(fdmgpu_handle* h, int32_t precision, int32_t* tr
 }
 
 fdmgpu_status fdmgpu_set_escalation(fdmgpu_handle* h, int32_t mode) {
-  if (!h || (mode != FDMGPU_ESCALATE_FP64 && mode != FDMGPU_ESCALATE_DF64 && mode != FDMGPU_ESCALATE_DF64_OVERLAP))
+  if (!h || (mode != FDMGPU_ESCALATE_FP64 && mode != FDMGPU_ESCALATE_DF64 && mode != FDMGPU_ESCALATE_DF64_OVERLAP &&
+             mode != FDMGPU_ESCALATE_WIDE_DF64))
     return fail(FDMGPU_ERR_ARG, "unknown escalation mode");
   h->escalate_dfl = mode != FDMGPU_ESCALATE_FP64;
   h->overlap_escalation = mode == FDMGPU_ESCALATE_DF64_OVERLAP;
+  h->escalate_wide = mode == FDMGPU_ESCALATE_WIDE_DF64;
+  h->plan_sig = 0;
   return FDMGPU_OK;
 }
 
@@ -1979,14 +2058,126 @@ fdmgpu_status fdmgpu_batch_add(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t
   return fdmgpu_batch_add_site(h, h, e, iaabs);
 }
 
+// Device bytes of one problem's pools (band FP64 + FP32, right-hand-side
+// tiles, CSR copy, per-row vectors), the quantities allocate_and_upload_plan
+// reserves per problem.
+static double problem_bytes(const HostProb& hp, bool mixed) {
+  const double tiles = (double)hp.ntiles * TS2, rhs = (double)hp.P.nt * hp.P.nrt * TS2;
+  const double rowv = (double)hp.P.nt * TS + 1;
+  if (!mixed) return tiles * 8 + rhs * 16 + rowv * 4;
+  return tiles * 12 + rhs * 44 + (double)hp.nnz_cap * 24 + rowv * 28;
+}
+
+// A batch whose pools exceed the budget runs in consecutive chunks of
+// problems (add order), each planned, captured and run like a batch of its
+// own; Taull, refinement statistics and statuses are gathered per problem.
+static fdmgpu_status run_chunked(fdmgpu_handle* h, fdmgpu_info* info, double budget) {
+  Batch& b = h->batch;
+  std::vector<HostProb> all = std::move(b.probs);
+  const int np = (int)all.size();
+  const bool mixed = b.precision == FDMGPU_PREC_MIXED;
+  std::vector<int> iters(np), fallback(np), wide(np), inner(np), err(np);
+  std::vector<double> resid(np);
+  b.taull_off.assign(np + 1, 0);
+  for (int k = 0; k < np; ++k) b.taull_off[k + 1] = b.taull_off[k] + 2 * (int64_t)all[k].P.nlm_abs * all[k].P.nlm_abs;
+  b.taull_host.assign(b.taull_off[np], 0.0);
+  fdmgpu_info acc;
+  memset(&acc, 0, sizeof(acc));
+  fdmgpu_status worst = FDMGPU_OK;
+  int k0 = 0, nchunks = 0;
+  while (k0 < np) {
+    int k1 = k0;
+    double bytes = 0;
+    while (k1 < np && (k1 == k0 || bytes + problem_bytes(all[k1], mixed) <= budget)) bytes += problem_bytes(all[k1++], mixed);
+    b.probs.clear();
+    for (int k = k0; k < k1; ++k) b.probs.push_back(all[k]);
+    fdmgpu_info ci;
+    fdmgpu_status st = run_batch(h, &ci, false);
+    if (st && st != FDMGPU_ERR_NOT_CONVERGED) {
+      b.probs = std::move(all);
+      b.ran = false;
+      return st;
+    }
+    if (st) worst = st;
+    // Taull of the chunk (contiguous in its pool)
+    if (b.taull_off[k1] > b.taull_off[k0])
+      CK(cudaMemcpy(b.taull_host.data() + b.taull_off[k0], h->d_taull.p + 2 * b.probs[0].P.taull,
+                    sizeof(double) * (b.taull_off[k1] - b.taull_off[k0]), cudaMemcpyDeviceToHost));
+    for (int k = k0; k < k1; ++k) {
+      const int j = k - k0;
+      iters[k] = b.iters.empty() ? 0 : b.iters[j];
+      resid[k] = b.resid.empty() ? 0.0 : b.resid[j];
+      fallback[k] = b.fallback.empty() ? 0 : b.fallback[j];
+      wide[k] = b.wide.empty() ? 0 : b.wide[j];
+      inner[k] = b.inner.empty() ? 0 : b.inner[j];
+      err[k] = b.err.empty() ? 0 : b.err[j];
+    }
+    acc.nnz_profile += ci.nnz_profile;
+    acc.flops_factor += ci.flops_factor;
+    acc.flops_solve += ci.flops_solve;
+    acc.refine_iters = std::max(acc.refine_iters, ci.refine_iters);
+    acc.residual = std::max(acc.residual, ci.residual);
+    acc.ms_assemble += ci.ms_assemble;
+    acc.ms_factor += ci.ms_factor;
+    acc.ms_solve += ci.ms_solve;
+    acc.ms_refine += ci.ms_refine;
+    acc.n_fallback += ci.n_fallback;
+    acc.n_kernels += ci.n_kernels;
+    acc.ms_residual_first += ci.ms_residual_first;
+    acc.flops_residual += ci.flops_residual;
+    acc.ms_escalate_factor += ci.ms_escalate_factor;
+    acc.flops_escalate_factor += ci.flops_escalate_factor;
+    acc.n_wide_refactor += ci.n_wide_refactor;
+    acc.ms_wide_refactor += ci.ms_wide_refactor;
+    acc.flops_wide_refactor += ci.flops_wide_refactor;
+    ++nchunks;
+    k0 = k1;
+  }
+  b.probs = std::move(all);
+  b.iters = iters;
+  b.resid = resid;
+  b.fallback = fallback;
+  b.wide = wide;
+  b.inner = inner;
+  b.err = err;
+  b.ran = true;
+  b.chunked = true;
+  b.nchunks = nchunks;
+  h->plan_sig = 0;  // the pools hold the last chunk only
+  if (info) *info = acc;
+  return worst;
+}
+
+static double batch_budget(fdmgpu_handle* h) {
+  if (h->mem_budget > 0) return h->mem_budget;
+  size_t fr = 0, tot = 0;
+  if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return 1e300;
+  return 0.85 * (double)tot;
+}
+
 fdmgpu_status fdmgpu_batch_run(fdmgpu_handle* h, fdmgpu_info* info) {
   if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
+  Batch& b = h->batch;
+  b.chunked = false;
+  b.taull_host.clear();
+  const bool mixed = b.precision == FDMGPU_PREC_MIXED;
+  double total = 0;
+  for (auto& hp : b.probs) total += problem_bytes(hp, mixed);
+  const double budget = batch_budget(h);
+  if (total > budget && b.probs.size() > 1) return run_chunked(h, info, budget);
   return run_batch(h, info, false);
 }
 
 fdmgpu_status fdmgpu_batch_rerun(fdmgpu_handle* h, fdmgpu_info* info) {
   if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
+  if (h->batch.chunked) return run_chunked(h, info, batch_budget(h));
   return run_batch(h, info, true);
+}
+
+fdmgpu_status fdmgpu_set_memory_budget(fdmgpu_handle* h, double bytes) {
+  if (!h || !(bytes >= 0)) return fail(FDMGPU_ERR_ARG, "bad memory budget");
+  h->mem_budget = bytes;
+  return FDMGPU_OK;
 }
 
 fdmgpu_status fdmgpu_batch_taull(fdmgpu_handle* h, int32_t k, double* taull, int32_t* nlm) {
@@ -1995,6 +2186,10 @@ fdmgpu_status fdmgpu_batch_taull(fdmgpu_handle* h, int32_t k, double* taull, int
   const Prob& P = h->batch.probs[k].P;
   if (nlm) *nlm = P.nlm_abs;
   if (!taull) return FDMGPU_OK;
+  if (h->batch.chunked) {
+    memcpy(taull, h->batch.taull_host.data() + h->batch.taull_off[k], sizeof(double) * 2 * P.nlm_abs * P.nlm_abs);
+    return FDMGPU_OK;
+  }
   CK(cudaMemcpy(taull, h->d_taull.p + 2 * P.taull, sizeof(double) * 2 * P.nlm_abs * P.nlm_abs,
                 cudaMemcpyDeviceToHost));
   return FDMGPU_OK;
@@ -2005,6 +2200,10 @@ fdmgpu_status fdmgpu_batch_taull_all(fdmgpu_handle* h, double* taull, int64_t ca
   int64_t n = 0;
   for (auto& hp : h->batch.probs) n += (int64_t)hp.P.nlm_abs * hp.P.nlm_abs;
   if (!taull || capacity < 2 * n) return fail(FDMGPU_ERR_ARG, "Taull buffer too small");
+  if (h->batch.chunked) {
+    memcpy(taull, h->batch.taull_host.data(), sizeof(double) * 2 * n);
+    return FDMGPU_OK;
+  }
   // the pool holds the energies' Taull contiguously in add order
   CK(cudaMemcpy(taull, h->d_taull.p + 2 * h->batch.probs[0].P.taull, sizeof(double) * 2 * n,
                 cudaMemcpyDeviceToHost));
@@ -2012,6 +2211,7 @@ fdmgpu_status fdmgpu_batch_taull_all(fdmgpu_handle* h, double* taull, int64_t ca
 }
 
 fdmgpu_status fdmgpu_batch_solution(fdmgpu_handle* h, int32_t k, double* smr) {
+  if (h && h->batch.chunked) return fail(FDMGPU_ERR_UNSUPPORTED, "a batch that ran in chunks keeps only its Taull (solutions of the last chunk are gone)");
   if (!h || !h->batch.ran || k < 0 || k >= (int)h->batch.probs.size())
     return fail(FDMGPU_ERR_ARG, "no such batch result");
   const Prob& P = h->batch.probs[k].P;
@@ -2152,6 +2352,7 @@ static fdmgpu_status vjp_mixed(fdmgpu_handle* h, int64_t nrhs) {
 }
 
 fdmgpu_status fdmgpu_batch_vjp(fdmgpu_handle* h, const double* gtaull, double* grad_vr, double* ms) {
+  if (h && h->batch.chunked) return fail(FDMGPU_ERR_UNSUPPORTED, "vjp of a batch that ran in chunks");
   if (!h || !gtaull || !grad_vr) return fail(FDMGPU_ERR_ARG, "null argument");
   Batch& b = h->batch;
   if (!b.ran) return fail(FDMGPU_ERR_ARG, "vjp needs a batch that has run");
@@ -2270,6 +2471,7 @@ fdmgpu_status fdmgpu_update_grid_values(fdmgpu_handle* h, const fdmgpu_grid* g) 
 }
 
 fdmgpu_status fdmgpu_batch_adjoint_dot(fdmgpu_handle* h, const fdmgpu_energy* const* e, int32_t n, double* out) {
+  if (h && h->batch.chunked) return fail(FDMGPU_ERR_UNSUPPORTED, "adjoint of a batch that ran in chunks");
   if (!h || !e || !out) return fail(FDMGPU_ERR_ARG, "null argument");
   Batch& b = h->batch;
   const int np = (int)b.probs.size();
@@ -2343,6 +2545,7 @@ fdmgpu_status fdmgpu_batch_adjoint_dot(fdmgpu_handle* h, const fdmgpu_energy* co
 }
 
 fdmgpu_status fdmgpu_batch_inputs(fdmgpu_handle* h, int32_t k, double* phiato, double* besselr, double* neumanr) {
+  if (h && h->batch.chunked) return fail(FDMGPU_ERR_UNSUPPORTED, "a batch that ran in chunks keeps only its Taull (inputs of the last chunk are gone)");
   if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
   Batch& b = h->batch;
   if (k < 0 || k >= (int)b.probs.size() || !b.ran) return fail(FDMGPU_ERR_ARG, "no such energy in the last run");
@@ -2373,6 +2576,7 @@ fdmgpu_status fdmgpu_batch_xanes(fdmgpu_handle* h, const double* energies_ev, co
                                  double* tensor) {
   if (!h || !energies_ev || !half_width || !sigma) return fail(FDMGPU_ERR_ARG, "null argument");
   Batch& b = h->batch;
+  if (b.chunked) return fail(FDMGPU_ERR_UNSUPPORTED, "cross-section of a batch that ran in chunks");
   const int n = (int)b.probs.size();
   if (!b.ran || n == 0) return fail(FDMGPU_ERR_ARG, "run a batch first");
   if (b.probs[0].P.nlm_abs < 4) return fail(FDMGPU_ERR_ARG, "the absorber needs its p harmonics (lmax >= 1)");

@@ -152,6 +152,7 @@ void launch_taull_c(const StaticDev* sites, const Prob* probs, const Pools& pl, 
                     cudaStream_t s);
 void launch_equilibrate_convert(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s);
 void launch_csr(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s);
+void launch_convert_masked(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s);
 // X64 = cs * Y32 (first solve) or X64 += cs * Y32 (refinement), with max reductions.
 void launch_update_x(const Prob* probs, const Pools& pl, const LaunchDims& d, int first, cudaStream_t s);
 // Y32 = rs * (B64 - A X64) using the CSR copy of A, in FP64 or in double-float.

@@ -83,7 +83,8 @@ __global__ void k_colscale_finish(const Prob* probs, double* cs) {
 
 // E32 = float(rs * cs * E64), tile by tile.
 __global__ void k_convert(const Prob* probs, const double* env64, float* env32, const double* rs, const double* cs,
-                          Tables tb) {
+                          Tables tb, const int* active) {
+  if (active && !active[blockIdx.y]) return;
   const Prob P = probs[blockIdx.y];
   const int64_t w = blockIdx.x;
   const int64_t ntiles = tb.strip[P.trow + P.nt];
@@ -437,8 +438,14 @@ void launch_equilibrate_convert(const Prob* probs, const Pools& pl, Tables tb, c
   k_colmax<<<dim3(d.max_tiles, np), 256, 0, s>>>(probs, pl.env64, pl.rs, reinterpret_cast<unsigned long long*>(pl.cs),
                                                  tb);
   k_colscale_finish<<<dim3((d.max_rows + 255) / 256, np), 256, 0, s>>>(probs, pl.cs);
-  k_convert<<<dim3(d.max_tiles, np), 256, 0, s>>>(probs, pl.env64, pl.env32, pl.rs, pl.cs, tb);
+  k_convert<<<dim3(d.max_tiles, np), 256, 0, s>>>(probs, pl.env64, pl.env32, pl.rs, pl.cs, tb, nullptr);
   k_rhs_scale<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, pl.B64, pl.Y32, pl.rs);
+}
+
+// FP32 band of the problems marked in pl.active converted again from the FP64
+// band with the batch's equilibration scales (before a re-factorisation).
+void launch_convert_masked(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s) {
+  k_convert<<<dim3(d.max_tiles, d.nprob), 256, 0, s>>>(probs, pl.env64, pl.env32, pl.rs, pl.cs, tb, pl.active);
 }
 
 void launch_csr(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s) {

@@ -75,6 +75,8 @@ def load_library(path: str = LIB_PATH):
     L.fdmgpu_set_radial.restype = C.c_int
     L.fdmgpu_batch_xanes.argtypes = [vp, vp, vp, C.c_int32, vp, vp, vp, vp]
     L.fdmgpu_batch_xanes.restype = C.c_int
+    L.fdmgpu_set_memory_budget.argtypes = [vp, C.c_double]
+    L.fdmgpu_set_memory_budget.restype = C.c_int
     L.fdmgpu_set_tile_engine.argtypes = [vp, C.c_int32]
     L.fdmgpu_set_tile_engine.restype = C.c_int
     L.fdmgpu_get_tuning.argtypes = [vp, C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_double), C.POINTER(C.c_double)]
@@ -143,7 +145,8 @@ class FdmSolver:
 
     def set_escalation(self, mode: str = "df64"):
         """Re-solve of energies the FP32 factors cannot refine: 'df64' (default), 'df64_overlap' or 'fp64'."""
-        _check(self.lib.fdmgpu_set_escalation(self.h, {"fp64": 0, "df64": 1, "df64_overlap": 2}[mode]))
+        _check(self.lib.fdmgpu_set_escalation(self.h, {"fp64": 0, "df64": 1, "df64_overlap": 2,
+                                                       "wide_df64": 3}[mode]))
 
     def set_tolerance(self, tol: float = 0.0, tol_accept: float = 0.0):
         """Refinement stop (max|dx|/max|x|) and the stalled-but-accepted level; 0 = default."""
@@ -170,6 +173,10 @@ class FdmSolver:
         nm = np.zeros((g.nsort, lmaxso + 1), order="F")
         _check(self.lib.fdmgpu_batch_inputs(self.h, k, phi.ctypes.data, bs.ctypes.data, nm.ctypes.data))
         return phi, bs, nm
+
+    def set_memory_budget(self, nbytes: float = 0.0):
+        """Device bytes a batch may take before it runs in chunks (0: 85% of the device)."""
+        _check(self.lib.fdmgpu_set_memory_budget(self.h, float(nbytes)))
 
     def set_tile_engine(self, engine: str = "tcgen05"):
         """FP32 tile updates of mixed batches on the FP32 pipes ("simt"), on

@@ -24,10 +24,13 @@ import numpy as np
 from . import cluster as CL
 
 
-def spectrum_inputs(st: CL.Structure, energies: Sequence[float]) -> List[Tuple[CL.EnergyInputs, CL.RowIndex]]:
+def spectrum_inputs(st: CL.Structure, energies: Sequence[float], functions: bool = True,
+                    ispin: int = 1) -> List[Tuple[CL.EnergyInputs, CL.RowIndex]]:
+    """Per-energy inputs and row numbering of a spectrum.  functions=False
+    leaves phiato / Bessel / Neumann to the device (FdmSolver.set_radial)."""
     out = []
     for E in energies:
-        ei = CL.energy_inputs(st, float(E))
+        ei = CL.energy_inputs(st, float(E), ispin=ispin, functions=functions)
         ri = CL.newind(st, ei.nlmsa, ei.nlmso)
         out.append((ei, ri))
     return out

@@ -70,8 +70,11 @@ typedef enum {
   FDMGPU_ESCALATE_DF64 = 1,    /* double-float LU of the equilibrated matrix with
                                   tile-local pivoting + refinement, after the FP32
                                   refinement of every energy has ended (default)        */
-  FDMGPU_ESCALATE_DF64_OVERLAP = 2 /* the same, started on a second stream as soon as an
+  FDMGPU_ESCALATE_DF64_OVERLAP = 2, /* the same, started on a second stream as soon as an
                                   energy stalls, while the others keep refining         */
+  FDMGPU_ESCALATE_WIDE_DF64 = 3 /* first the FP32 factor again with double-float sums in
+                                  every trailing update and FP32 refinement, then
+                                  double-float for the energies still stalled            */
 } fdmgpu_escalation;
 
 /* Energy-independent arguments of mat_solve (source/mat_solve_gaussian.f90:17-67). */
@@ -174,6 +177,11 @@ typedef struct fdmgpu_info {
    * and the escalation's factorisation, each with its algorithmic flops       */
   double ms_residual_first, flops_residual;
   double ms_escalate_factor, flops_escalate_factor;
+  /* mixed precision with FDMGPU_ESCALATE_WIDE_DF64: problems factorised again
+   * with double-float sums in every trailing update, and that factorisation's
+   * device time and algorithmic flops                                         */
+  int32_t n_wide_refactor;
+  double ms_wide_refactor, flops_wide_refactor;
 } fdmgpu_info;
 
 /* Accumulation of the FP32 factor of the mixed path. */
@@ -322,6 +330,15 @@ fdmgpu_status fdmgpu_batch_add(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t
  * single-site batch. */
 fdmgpu_status fdmgpu_batch_add_site(fdmgpu_handle* h, fdmgpu_handle* site, const fdmgpu_energy* e, int32_t iaabs);
 fdmgpu_status fdmgpu_batch_run(fdmgpu_handle* h, fdmgpu_info* info);
+/* Device memory a batch's pools may take (bytes; 0, the default, selects 85%
+ * of the device's memory).  A batch above it runs in consecutive chunks of
+ * energies, each planned and launched like a batch of its own; Taull and the
+ * statistics of every energy are kept (on the host), while solutions,
+ * cross-sections, inputs and the adjoint (which need the pools) return
+ * FDMGPU_ERR_UNSUPPORTED.  fdmgpu_batch_rerun of a chunked batch runs every
+ * chunk again.  No counterpart in the reference, whose energies each hold
+ * their own matrix. */
+fdmgpu_status fdmgpu_set_memory_budget(fdmgpu_handle* h, double bytes);
 /* Run the last batch again on the inputs already in device memory (no host
  * copies): the device-resident timing of a spectrum.  No counterpart in the
  * reference. */

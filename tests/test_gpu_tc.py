@@ -103,3 +103,26 @@ def test_tcgen05_with_wide_atom_steps(solver_mod):
     assert xanes.convolved_relative_error(energies, Tm, T64) < 1e-6
     assert max(rel(a, b) for a, b in zip(Tm, T64)) < 1e-5
     sv.close()
+
+
+def test_chunked_batch_equals_one_batch(solver_mod):
+    """A batch above the memory budget runs in consecutive chunks of energies
+    (each planned and launched on its own) and gives the same Taull, bit for
+    bit, as one batch: the kernels treat every energy independently."""
+    from fdmnes_gb300 import cluster as CL, xanes
+    st = CL.cu_structure()
+    energies = np.linspace(-5.0, 35.0, 7)
+    items = xanes.spectrum_inputs(st, energies)
+    sv = solver_mod.FdmSolver(st)
+    sv.set_tolerance(1e-8, 1e-6)
+    for prec in ("fp64", "mixed"):
+        sv.set_memory_budget(0.0)
+        T1, i1 = sv.spectrum(items, prec)
+        sv.set_memory_budget(1.5e9)   # about two Cu energies per chunk
+        T2, i2 = sv.spectrum(items, prec)
+        assert all(np.array_equal(a, b) for a, b in zip(T1, T2)), prec
+        assert [sv.stats(k)[0] for k in range(len(items))] == [sv.stats(k)[0] for k in range(len(items))]
+        with pytest.raises(solver_mod.FdmError):
+            sv.solution(0, items[0][0].nlmso, items[0][1].nligne)
+    sv.set_memory_budget(0.0)
+    sv.close()
