@@ -260,6 +260,7 @@ def run_gpu(args):
     sv.set_tolerance(TOL, TOL_ACCEPT)
     sv.set_factor_mode(args.factor_mode)
     sv.set_tile_engine(args.tile_engine)
+    sv.set_escalation(args.escalation)
 
     def barrier_sync():
         torch.cuda.synchronize()
@@ -378,7 +379,7 @@ def run_gpu(args):
                    "inputs": "phiato, Bessel and Neumann generated on the device (fdmgpu_set_radial)",
                    "l2": "working set ~100 GB per step, far above the 126 MB L2 (no flush needed)",
                    "refine_tol": TOL, "refine_tol_accept": TOL_ACCEPT, "factor_mode": args.factor_mode,
-                   "tile_engine": args.tile_engine,
+                   "tile_engine": args.tile_engine, "escalation": args.escalation,
                    "autotune": {"mixed": sv.tuning("mixed"), "fp64": sv.tuning("fp64")}},
         "roofline": roof_main,
         "roofline_other": [roof_res, roof_fac],
@@ -405,6 +406,83 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_tio2(args):
+    """Configuration 3: rutile TiO2, Ti K edge, two spin blocks, three
+    absorbing-site clusters with FDM radii 4.0 / 4.5 / 5.0 A at step 0.2 A, in
+    one batch over the sites (fdmgpu_batch_add_site) that the library splits
+    into chunks fitting the device memory.  The full configuration has 200
+    energies per site; a step here solves --tio2-energies of them (spread over
+    the 200-point grid) for every site and spin.  One energy point is one
+    energy of the spectrum over all three sites and both spins."""
+    import torch
+    from fdmnes_gb300 import build as B, cluster as CL, xanes
+    from fdmnes_gb300.solver import FdmSolver
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    B.build()
+    grid200 = np.linspace(-5.0, 35.0, 200)
+    idx = np.round(np.linspace(0, 199, args.tio2_energies)).astype(int)
+    energies = grid200[idx]
+    radii = (4.0, 4.5, 5.0)
+    sites = []
+    t0 = time.perf_counter()
+    for r in radii:
+        st = CL.build_structure(CL.rutile_cluster(r - 0.4), 0.2, r, 35.0, nspin=2, spin_split_ev=1.5)
+        sv = FdmSolver(st)
+        sv.set_radial()
+        sites.append((st, sv))
+    host_build_s = time.perf_counter() - t0
+    items = []  # (site solver, ei, ri)
+    for st, sv in sites:
+        for isp in (1, 2):
+            for ei, ri in xanes.spectrum_inputs(st, energies, functions=False, ispin=isp):
+                items.append((sv, ei, ri))
+    main_sv = sites[0][1]
+    main_sv.set_tolerance(1e-8, 1e-6)
+    main_sv.set_tile_engine(args.tile_engine)
+    main_sv.set_escalation(args.escalation)
+
+    def run():
+        main_sv.spectrum_begin("mixed", len(items))
+        for sv, ei, ri in items:
+            if sv is main_sv:
+                main_sv.spectrum_add(ei, ri)
+            else:
+                main_sv.spectrum_add_site(sv, ei, ri)
+        return main_sv.spectrum_run()
+
+    run()  # warm-up: plans and graphs of every chunk
+    times, infos = [], []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        infos.append(run())
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    last = infos[-1]
+    wall = statistics.mean(times)
+    nlig = [ri.nligne for _, _, ri in items]
+    n_e = len(energies)
+    line = {
+        "metric": METRIC, "value": n_e / wall, "unit": "energies/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": 1, "ms_per_step": 1000.0 * wall, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 factor + f64 refinement (df64 residual)", "data": "synthetic",
+        "config": {"workload": "rutile TiO2 a=4.594 c=2.959 A u=0.305, Ti K edge, 2 spin blocks, 3 absorbing-site "
+                               "clusters with FDM radii 4.0/4.5/5.0 A at step 0.2 A, batched over sites and spins",
+                   "energies_per_site": n_e, "full_configuration_energies": 200, "problems": len(items),
+                   "nligne": [min(nlig), max(nlig)], "chunks": "fdmgpu_set_memory_budget default (85% of HBM)",
+                   "host_structure_build_s": host_build_s, "tile_engine": args.tile_engine,
+                   "escalation": args.escalation},
+        "phases_ms": {k: last[k] for k in ("ms_assemble", "ms_factor", "ms_solve", "ms_refine")},
+        "flops_factor": last["flops_factor"],
+        "factor_tflops": last["flops_factor"] / (last["ms_factor"] / 1000.0) / 1e12 if last["ms_factor"] > 0 else None,
+        "fp64_escalations": last["n_fallback"], "wide_refactors": last["n_wide_refactor"],
+        "projected_full_spectrum_s": wall * 200.0 / n_e,
+    }
+    print(json.dumps(line), flush=True)
+    for _, sv in sites:
+        sv.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -418,9 +496,17 @@ def main():
                     help="accumulation of the FP32 factor (wide_atom: double-float sums at the atom-harmonic steps)")
     ap.add_argument("--tile-engine", default="simt", choices=["simt", "tcgen05", "tcgen05_factor"],
                     help="FP32 tile updates on the FP32 pipes or on the tensor cores (split TF32)")
+    ap.add_argument("--escalation", default="df64", choices=["df64", "wide_df64", "fp64"],
+                    help="re-solve of energies whose FP32 refinement stalls")
+    ap.add_argument("--config", default="cu401", choices=["cu401", "tio2"],
+                    help="cu401: the 401-energy Cu spectrum (the metric's configuration); tio2: the rutile "
+                         "three-site, two-spin batch")
+    ap.add_argument("--tio2-energies", type=int, default=4, help="energies per site of the tio2 configuration")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.config == "tio2":
+        run_tio2(args)
     else:
         run_gpu(args)
 

@@ -2495,10 +2495,18 @@ fdmgpu_status fdmgpu_batch_adjoint_dot(fdmgpu_handle* h, const fdmgpu_energy* co
     HostProb hp;
     hp.P = b.probs[k].P;
     pack_inputs(h, e[k], hp);
-    if (hp.in_i.size() != b.probs[k].in_i.size() || hp.in_d.size() != b.probs[k].in_d.size())
+    if (hp.in_i.size() != b.probs[k].in_i.size() || hp.in_d.size() != b.probs[k].in_d.size() ||
+        hp.P.gen != b.probs[k].P.gen)
       return fail(FDMGPU_ERR_ARG, "energy " + std::to_string(k) + ": input sizes differ from the batch's");
     b.probs[k].in_i.swap(hp.in_i);
     b.probs[k].in_d.swap(hp.in_d);
+    b.probs[k].P = hp.P;
+    b.probs[k].rel_grad = hp.rel_grad;
+    b.probs[k].rel_phi = hp.rel_phi;
+    b.probs[k].rel_bes = hp.rel_bes;
+    b.probs[k].rel_neu = hp.rel_neu;
+    b.probs[k].gen_phi = hp.gen_phi;
+    b.probs[k].gen_bes = hp.gen_bes;
   }
   b.ran = false;  // the factors are overwritten below; X and Lambda stay valid
   // CSR copy of the new matrices: an FP64 batch plans no CSR, so place it here
@@ -2531,6 +2539,8 @@ fdmgpu_status fdmgpu_batch_adjoint_dot(fdmgpu_handle* h, const fdmgpu_energy* co
   CK(cudaMemsetAsync(pl.env64, 0, env * sizeof(double), s));
   CK(cudaMemsetAsync(pl.B64, 0, rhs * sizeof(double), s));
   CK(cudaMemsetAsync(pl.err, 0, np * sizeof(int), s));
+  launch_generate_inputs(h->d_probs.p, h->d_rads.p, h->d_sites.p, h->d_ipool.p, h->dims, h->gdims, h->d_radU.p,
+                         h->d_dpool.p, s);
   launch_assemble(h->d_sites.p, h->d_probs.p, pl, h->tb, h->dims, s);
   launch_csr(h->d_probs.p, pl, h->tb, h->dims, s);
   launch_lambda_dot(h->d_probs.p, pl, h->dims, h->d_lam.p, h->d_gpart.p, h->d_gpart.p + rowv, s);

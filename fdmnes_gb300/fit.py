@@ -29,7 +29,8 @@ from .solver import FdmSolver
 
 def sigma_spectrum(st: CL.Structure, energies: Sequence[float]) -> np.ndarray:
     sv = FdmSolver(st)
-    T, _ = sv.spectrum(xanes.spectrum_inputs(st, energies), "fp64")
+    sv.set_radial()
+    T, _ = sv.spectrum(xanes.spectrum_inputs(st, energies, functions=False), "fp64")
     sv.close()
     return np.array([xanes.absorption(t) for t in T])
 
@@ -39,7 +40,10 @@ def loss_grad(build: Callable[[float], CL.Structure], theta: float, energies: Se
     """L(theta) and dL/dtheta through the adjoint of the batch of ``precision``."""
     st = build(theta)
     sv = FdmSolver(st)
-    items = xanes.spectrum_inputs(st, energies)
+    sv.set_radial()   # phiato / Bessel / Neumann of every energy generated on the device
+    if precision == "mixed":
+        sv.set_tolerance(1e-8, 1e-6)
+    items = xanes.spectrum_inputs(st, energies, functions=False)
     T, _ = sv.spectrum(items, precision)
     sig = np.array([xanes.absorption(t) for t in T])
     r = sig - target
@@ -48,7 +52,8 @@ def loss_grad(build: Callable[[float], CL.Structure], theta: float, energies: Se
     for sgn in (1.0, -1.0):
         st_s = build(theta + sgn * h)
         sv.update_grid_values(st_s)
-        dots.append(sv.adjoint_dot(xanes.spectrum_inputs(st_s, energies)).sum())
+        sv.set_radial()
+        dots.append(sv.adjoint_dot(xanes.spectrum_inputs(st_s, energies, functions=False)).sum())
     sv.close()
     return float((r ** 2).sum()), (dots[0] - dots[1]) / (2.0 * h)
 

@@ -40,15 +40,20 @@ def loss_and_gradients(sv, build_structure: Callable[[float], CL.Structure], the
     as theta).  Returns (L, T list, grad_vr, dL/dtheta, device ms of the vjp).
     """
     st0 = sv.st
-    items = xanes.spectrum_inputs(st0, energies)
+    gen = getattr(sv, "radial_args", None) is not None   # inputs generated on the device
+    items = xanes.spectrum_inputs(st0, energies, functions=not gen)
     L, T = spectrum_loss(sv, items, weights, precision)
     grad_vr, ms = sv.vjp([xanes.absorption_cotangent(t, w) for t, w in zip(T, weights)])
     dots = []
     for sgn in (1.0, -1.0):
         st_s = build_structure(theta + sgn * h)
         sv.update_grid_values(st_s)
-        dots.append(sv.adjoint_dot(xanes.spectrum_inputs(st_s, energies)).sum())
+        if gen:
+            sv.set_radial()
+        dots.append(sv.adjoint_dot(xanes.spectrum_inputs(st_s, energies, functions=not gen)).sum())
     sv.update_grid_values(st0)
+    if gen:
+        sv.set_radial()
     return L, T, grad_vr, (dots[0] - dots[1]) / (2.0 * h), ms
 
 

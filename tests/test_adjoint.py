@@ -139,3 +139,62 @@ def test_shell_gradient_matches_central_differences(precision):
     fd = (Ls[0] - Ls[1]) / (2 * H)
     assert np.isfinite(L)
     assert abs(dth - fd) <= TOL * abs(fd), (dth, fd)
+
+
+def _oracle_loss(st, energies, w):
+    """The loss evaluated entirely by the oracle (CPU restatement of the
+    reference's Gaussian solve and Taull)."""
+    import oracle
+    from fdmnes_gb300 import abi, cluster as CL, xanes
+    ga = abi.GridArgs(st)
+    L = 0.0
+    for E, wk in zip(energies, w):
+        ei = CL.energy_inputs(st, E)
+        ri = CL.newind(st, ei.nlmsa, ei.nlmso)
+        ea = abi.EnergyArgs(st, ei, ri)
+        X, _ = oracle.mat_solve(ga, ea)
+        L += wk * xanes.absorption(oracle.taull(ga, ea, X))
+    return L
+
+
+def test_vjp_matches_oracle_central_differences(setup, oracle_lib):
+    """The device gradient dL/dVr against central differences of the
+    oracle's loss (Vr(i) +- 1e-4 Ry, the oracle's own solves), at four grid
+    points: bar 1e-5 relative, as against the GPU's own differences."""
+    from fdmnes_gb300 import xanes
+    st, sv, items, w, loss = setup
+    energies = [ei.energy_ev for ei, _ in items]
+    _, T = loss()
+    grad, _ = sv.vjp([xanes.absorption_cotangent(t, wk) for t, wk in zip(T, w)])
+    g = st.grid
+    inter = np.nonzero(g.numia[:g.npoint] == 0)[0]
+    gmax = np.abs(grad[inter, 0]).max()
+    order = np.argsort(-np.abs(grad[inter, 0]))
+    for i in [inter[order[k]] for k in (0, 5, 20, 60)]:
+        v0 = st.Vr[i, 0]
+        st.Vr[i, 0] = v0 + H
+        Lp = _oracle_loss(st, energies, w)
+        st.Vr[i, 0] = v0 - H
+        Lm = _oracle_loss(st, energies, w)
+        st.Vr[i, 0] = v0
+        fd = (Lp - Lm) / (2 * H)
+        assert abs(grad[i, 0] - fd) <= TOL * abs(fd) + 1e-3 * TOL * gmax, (i, grad[i, 0], fd)
+
+
+def test_shell_gradient_matches_oracle_differences(oracle_lib):
+    """The adjoint shell-distance gradient (13-atom Cu cluster on a 0.35 A
+    grid, FP64 batch, inputs generated on the device) against central
+    differences of the oracle's loss (host-built inputs, the oracle's solves)
+    at theta +- 1e-4 A.  These matrices' conditioning puts ~1e-9 relative
+    noise on each oracle loss, ~1e-5 on the quotient: bar 1e-4 relative."""
+    from fdmnes_gb300 import build, gradients as G
+    from fdmnes_gb300.solver import FdmSolver
+    build.build()
+    energies, w = [3.0, 12.0, 27.0], [1.0, -0.7, 0.4]
+    mk = lambda d: G.cu_shell_structure(d, adimp_ang=0.35)
+    sv = FdmSolver(mk(0.0))
+    sv.set_radial()
+    _, _, _, dth, _ = G.loss_and_gradients(sv, mk, 0.0, energies, w, h=H, precision="fp64")
+    sv.close()
+    fd = (_oracle_loss(mk(H), energies, w) - _oracle_loss(mk(-H), energies, w)) / (2 * H)
+    assert abs(dth - fd) <= 1e-4 * abs(fd), (dth, fd)
