@@ -156,6 +156,7 @@ struct fdmgpu_handle {
   int autotune = 1;         // time the trailing-update layouts on each new plan
   int factor_mode = 0;      // FDMGPU_FACTOR_*: wide accumulation at the atom-harmonic steps of the FP32 factor
   int tile_engine = FDMGPU_ENGINE_SIMT;  // FDMGPU_ENGINE_*: FP32 tile updates on the FP32 pipes or the tensor cores
+  int solve_order = FDMGPU_SOLVE_COLUMNS;  // FDMGPU_SOLVE_*: refinement solves step by step or row by row
   DevBuf<unsigned char> d_wide;
   int trail_threads[2] = {0, 0};        // chosen layout per precision (FP64, FP32); 0: built-in default
   double trail_ms[2][2] = {{0, 0}, {0, 0}};  // trial device ms [precision][64 | 128 threads]
@@ -663,6 +664,7 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   // real mixed batches may run their FP32 tile updates on the tensor cores
   h->sp.tc = (mixed && !cplx && h->tile_engine != FDMGPU_ENGINE_SIMT) ? 1 : 0;
   h->sp.tc_solve = (mixed && !cplx && h->tile_engine == FDMGPU_ENGINE_TCGEN05) ? 1 : 0;
+  h->sp.row_solve = (mixed && h->solve_order == FDMGPU_SOLVE_ROWS) ? 1 : 0;
   h->sp.tc_err = h->d_err.p;
   Pools& pl = h->pl;
   pl = Pools();
@@ -1010,6 +1012,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   sig = mix(sig, (uint64_t)(h->refine_gmres * 1000 + h->gmres_m));
   sig = mix(sig, (uint64_t)h->factor_mode + 77u);
   sig = mix(sig, (uint64_t)h->tile_engine + 191u);
+  sig = mix(sig, (uint64_t)h->solve_order + 733u);
   for (auto& hp : b.probs) {
     sig = mix(sig, (uint64_t)hp.P.gen * 31u);
     if (hp.P.gen)
@@ -1943,6 +1946,13 @@ fdmgpu_status fdmgpu_set_radial(fdmgpu_handle* h, const fdmgpu_radial* rd) {
   h->rad_v0bd = rd->v0bd;
   h->has_radial = true;
   h->plan_sig = 0;
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_set_solve_order(fdmgpu_handle* h, int32_t order) {
+  if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
+  if (order != FDMGPU_SOLVE_COLUMNS && order != FDMGPU_SOLVE_ROWS) return fail(FDMGPU_ERR_ARG, "unknown solve order");
+  h->solve_order = order;
   return FDMGPU_OK;
 }
 

@@ -259,8 +259,100 @@ __global__ void __launch_bounds__(MMThreads<T>::value) k_tbwd_update(const T* en
                            (const int*)nullptr, As, Bs);
 }
 
+// Row-oriented (left-looking) solves: one launch per tile row, one CTA per
+// (right-hand-side tile, problem).  The CTA accumulates the products of its
+// row's strip in registers and finishes with the diagonal tile, so Y(I,R) is
+// written once per solve instead of at every step of the right-looking form,
+// and the forward step needs one launch instead of two:
+//   forward  Y(I) <- L(I,I)^-1 P_I (Y(I) - sum_{K in [J0(I), I)} L(I,K) Y(K))
+//   backward Y(I) <- U(I,I)^-1     (Y(I) - sum_{K in (I, J1(I)]} U(I,K) Y(K))
+// (the same eliminations as the reference's, source/mat_solve_gaussian.f90:
+// 231-262 and 348-358, summed per row instead of per column).
+template <typename T, bool FWD>
+__global__ void __launch_bounds__(MMThreads<T>::value) k_solve_row(const T* env, T* rhs, const Prob* probs, Tables tb,
+                                                                   int I, const int* active, const int* piv) {
+  constexpr int NT = MMThreads<T>::value;
+  constexpr int CW = NT == 128 ? 4 : 8;
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (I >= P.nt || (active && !active[e])) return;
+  const int R = blockIdx.x;
+  if (R >= P.nrt) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* As = reinterpret_cast<T*>(smem_raw);
+  T* Bs = As + TS * SPA;
+  T* D = Bs + TS * SP;
+  const int k0 = FWD ? tb.J0[P.trow + I] : I + 1;
+  const int k1 = FWD ? I : tb.J1[P.trow + I] + 1;
+  const int t = threadIdx.x;
+  const int tx = t % (NT / 8), ty = t / (NT / 8);
+  T acc[8][CW];
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+#pragma unroll
+    for (int j = 0; j < CW; ++j) acc[i][j] = T(0);
+  for (int K = k0; K < k1; ++K) {
+    const T* A = tile_ptr(const_cast<T*>(env), P, tb, I, K);
+    const T* B = rhs_ptr(rhs, P, K, R);
+    for (int idx = t; idx < TS2 / 4; idx += NT) {
+      const int r = idx / (TS / 4), c4 = (idx % (TS / 4)) * 4;
+      T a[4], b[4];
+      ld4(A + r * TS + c4, a);
+      ld4(B + r * TS + c4, b);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        As[r * SPA + c4 + q] = a[q];
+        Bs[r * SP + c4 + q] = b[q];
+      }
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int k = 0; k < TS; ++k) {
+      T a[8], b[CW];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        a[i] = As[(4 * ty + i) * SPA + k];
+        a[4 + i] = As[(32 + 4 * ty + i) * SPA + k];
+      }
+      ld4(Bs + k * SP + 4 * tx, b);
+      if (CW == 8) ld4(Bs + k * SP + 32 + 4 * tx, b + 4);
+#pragma unroll
+      for (int i = 0; i < 8; ++i)
+#pragma unroll
+        for (int j = 0; j < CW; ++j) mac(acc[i][j], a[i], b[j]);
+    }
+    // renormalise the double-float sums once per tile (no-op for float and double)
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < CW; ++j) acc[i][j] = mac_finish(acc[i][j]);
+    __syncthreads();
+  }
+  // Y(I,R) - acc, then the diagonal tile's triangular solve
+  T* y = rhs_ptr(rhs, P, I, R);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const int row = (i < 4 ? 4 * ty + i : 32 + 4 * ty + (i - 4));
+#pragma unroll
+    for (int h = 0; h < CW / 4; ++h) {
+      T* cp = y + row * TS + 32 * h + 4 * tx;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) cp[j] = acc_apply<T, T>(cp[j], acc[i][4 * h + j], true);
+    }
+  }
+  load_tile_n(D, tile_ptr(const_cast<T*>(env), P, tb, I, I), NT);
+  __syncthreads();  // the block's writes of Y(I,R) and D are visible to every thread
+  if (FWD)
+    col_solve_lower_unit(y, D, piv ? piv + P.rowv + (int64_t)I * TS : (const int*)nullptr);
+  else
+    col_solve_upper(y, D);
+}
+
 template <typename T>
 static size_t smem_bytes() { return 2 * TS * SP * sizeof(T); }
+// the row solve holds the left operand (stride SPA), the right one and the diagonal tile
+template <typename T>
+static size_t smem_bytes_row() { return (TS * SPA + 2 * TS * SP) * sizeof(T); }
 // the panel holds the diagonal tile plus two SPA-strided work tiles
 template <typename T>
 static size_t smem_bytes_panel() { return (TS * SP + 2 * TS * SPA) * sizeof(T); }
@@ -284,6 +376,8 @@ void setup_factor_kernels() {
   cudaFuncSetAttribute(k_tfwd_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_tbwd_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   cudaFuncSetAttribute(k_tbwd_update<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  cudaFuncSetAttribute(k_solve_row<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes_row<T>());
+  cudaFuncSetAttribute(k_solve_row<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes_row<T>());
 }
 
 template <typename T>
@@ -333,6 +427,14 @@ int launch_forward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, 
                    const int* active, const int* piv, cudaStream_t s) {
   const size_t sm = smem_bytes<T>();
   int nk = 0;
+  if (sp.row_solve) {
+    for (int I = 0; I < sp.ntmax; ++I) {
+      k_solve_row<T, true><<<dim3(sp.nrtmax, nprob), MMThreads<T>::value, smem_bytes_row<T>(), s>>>(
+          env, rhs, probs, tb, I, active, piv);
+      ++nk;
+    }
+    return nk;
+  }
   for (int K = 0; K < sp.ntmax; ++K) {
     k_fwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active, piv);
     ++nk;
@@ -353,6 +455,14 @@ int launch_backward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs,
                     const int* active, cudaStream_t s) {
   const size_t sm = smem_bytes<T>();
   int nk = 0;
+  if (sp.row_solve) {
+    for (int I = sp.ntmax - 1; I >= 0; --I) {
+      k_solve_row<T, false><<<dim3(sp.nrtmax, nprob), MMThreads<T>::value, smem_bytes_row<T>(), s>>>(
+          env, rhs, probs, tb, I, active, nullptr);
+      ++nk;
+    }
+    return nk;
+  }
   for (int K = sp.ntmax - 1; K >= 0; --K) {
     k_bwd_diag<T><<<dim3(sp.nrtmax, nprob), GEMM_THREADS, sm, s>>>(env, rhs, probs, tb, K, active);
     ++nk;

@@ -24,6 +24,7 @@ struct StepPlan {
   int tc_solve = 0;  // forward / backward updates of the FP32 solves on the tensor cores
   std::vector<int> trail_tc, fwd_tc, bwd_tc;
   int* tc_err = nullptr;               // per-problem status word of the solve updates (mbarrier timeout)
+  int row_solve = 0;                   // forward / backward solves row by row (one launch per tile row)
 };
 
 // Split-TF32 tcgen05 tile updates (tc_update.cu).  mode 0: factor trailing

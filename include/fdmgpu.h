@@ -207,6 +207,17 @@ typedef enum {
                                   the refinement solves on the FP32 pipes                */
 } fdmgpu_tile_engine;
 
+/* Order of the triangular solves of the mixed path's refinement (the
+ * resolution loop of source/mat_solve_gaussian.f90:348-358 and its forward
+ * counterpart, in tile form). */
+typedef enum {
+  FDMGPU_SOLVE_COLUMNS = 0,    /* step by step: the diagonal tile, then the update of every
+                                  row below (above) it, two launches per tile step       */
+  FDMGPU_SOLVE_ROWS = 1        /* row by row: each row's strip of products summed in
+                                  registers, then its diagonal tile, one launch per tile
+                                  row; every right-hand-side tile written once           */
+} fdmgpu_solve_order;
+
 /* Library version string. */
 const char* fdmgpu_version(void);
 
@@ -285,6 +296,10 @@ typedef struct fdmgpu_radial {
   double v0bd;            /* interstitial level: kinetic energy = Enervide - v0bd - dv (Ry) */
 } fdmgpu_radial;
 fdmgpu_status fdmgpu_set_radial(fdmgpu_handle* h, const fdmgpu_radial* radial);
+
+/* Solve order of the mixed batches planned after the call (fdmgpu_solve_order).
+ * No counterpart in the reference. */
+fdmgpu_status fdmgpu_set_solve_order(fdmgpu_handle* h, int32_t order);
 
 /* Tile engine of the FP32 updates (fdmgpu_tile_engine) for the real mixed
  * batches planned after the call; steps that accumulate wide

@@ -118,11 +118,42 @@ def test_chunked_batch_equals_one_batch(solver_mod):
     for prec in ("fp64", "mixed"):
         sv.set_memory_budget(0.0)
         T1, i1 = sv.spectrum(items, prec)
-        sv.set_memory_budget(1.5e9)   # about two Cu energies per chunk
+        s1 = [sv.stats(k)[:3] for k in range(len(items))]
+        sv.set_memory_budget(4e8)   # one to three Cu energies per chunk
         T2, i2 = sv.spectrum(items, prec)
         assert all(np.array_equal(a, b) for a, b in zip(T1, T2)), prec
-        assert [sv.stats(k)[0] for k in range(len(items))] == [sv.stats(k)[0] for k in range(len(items))]
+        assert [sv.stats(k)[:3] for k in range(len(items))] == s1
         with pytest.raises(solver_mod.FdmError):
             sv.solution(0, items[0][0].nlmso, items[0][1].nligne)
     sv.set_memory_budget(0.0)
+    sv.close()
+
+
+def test_row_solves_match_column_solves(solver_mod, golden):
+    """Refinement solves row by row (each row's strip summed in registers,
+    one launch per tile row) against the step-by-step solves: the refined
+    solution meets the oracle bars (1e-8 with the df64 residual), and on full
+    Cu energies the cross-section bar and about the same refinement steps."""
+    from fdmnes_gb300 import abi, cluster as CL, xanes
+    grid, energies = golden
+    sv = solver_mod.FdmSolver(grid)
+    sv.set_solve_order("rows")
+    for e in energies:
+        X, info = sv.mat_solve_args(abi.EnergyArgs(e), "mixed")
+        assert info["converged"]
+        assert rel(X, e["smr"]) < 1e-8
+    sv.close()
+    st = CL.cu_structure()
+    E = np.array([2.0, 14.0, 26.0, 34.0])
+    items = xanes.spectrum_inputs(st, E)
+    sv = solver_mod.FdmSolver(st)
+    T64, _ = sv.spectrum(items, "fp64")
+    sv.set_tolerance(1e-8, 1e-6)
+    its = {}
+    for order in ("columns", "rows"):
+        sv.set_solve_order(order)
+        Tm, _ = sv.spectrum(items, "mixed")
+        assert xanes.convolved_relative_error(E, Tm, T64) < 1e-6, order
+        its[order] = [sv.stats(k)[0] for k in range(len(items))]
+    assert sum(its["rows"]) <= sum(its["columns"]) + 8, its
     sv.close()
