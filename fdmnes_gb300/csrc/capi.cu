@@ -157,6 +157,9 @@ struct fdmgpu_handle {
   int factor_mode = 0;      // FDMGPU_FACTOR_*: wide accumulation at the atom-harmonic steps of the FP32 factor
   int tile_engine = FDMGPU_ENGINE_SIMT;  // FDMGPU_ENGINE_*: FP32 tile updates on the FP32 pipes or the tensor cores
   int solve_order = FDMGPU_SOLVE_COLUMNS;  // FDMGPU_SOLVE_*: refinement solves step by step or row by row
+  int df64_engine = FDMGPU_DF64_SIMT;      // FDMGPU_DF64_*: double-float trailing update on the FP32 pipes or the tensor cores
+  DevBuf<unsigned char> d_oz_img;          // integer-slice images of one factor step
+  DevBuf<int> d_oz_exp;
   DevBuf<unsigned char> d_wide;
   int trail_threads[2] = {0, 0};        // chosen layout per precision (FP64, FP32); 0: built-in default
   double trail_ms[2][2] = {{0, 0}, {0, 0}};  // trial device ms [precision][64 | 128 threads]
@@ -530,10 +533,19 @@ void build_step_plan(fdmgpu_handle* h) {
   sp.trail_tc.assign(N, 0);
   sp.fwd_tc.assign(N, 0);
   sp.bwd_tc.assign(N, 0);
+  sp.oz_nI.assign(N, 0);
+  sp.oz_nC.assign(N, 0);
+  sp.oz_items.assign(N, 0);
+  sp.oz_capI = sp.oz_capC = 0;
   for (auto& hp : pr) {
     for (int K = 0; K < hp.P.nt; ++K) {
       const int nI = hp.Imax[K] - K, nJ = hp.J1[K] - K, nR = hp.P.nrt;
       sp.trail_tc[K] = std::max(sp.trail_tc[K], tc_items(nI, nJ + nR));
+      sp.oz_nI[K] = std::max(sp.oz_nI[K], nI);
+      sp.oz_nC[K] = std::max(sp.oz_nC[K], nJ + nR);
+      sp.oz_items[K] = std::max(sp.oz_items[K], nI > 0 ? ((nI + 1) / 2) * (nJ + nR) : 0);
+      sp.oz_capI = std::max(sp.oz_capI, nI);
+      sp.oz_capC = std::max(sp.oz_capC, nJ + nR);
       sp.fwd_tc[K] = std::max(sp.fwd_tc[K], tc_items(nI, nR));
       sp.bwd_tc[K] = std::max(sp.bwd_tc[K], tc_items(K - hp.Imin[K], nR));
       sp.panel[K] = std::max(sp.panel[K], nI + nJ);
@@ -704,6 +716,18 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
     pl.val = h->d_val.p;
   }
   build_step_plan(h);
+  h->sp.oz = 0;
+  h->sp.oz_img = nullptr;
+  h->sp.oz_exp = nullptr;
+  if (mixed && h->df64_engine == FDMGPU_DF64_TCGEN05 && h->sp.oz_capI > 0) {
+    const size_t slot = (size_t)(h->sp.oz_capI + h->sp.oz_capC);
+    if (h->d_oz_img.reserve((size_t)np * slot * (size_t)oz_tile_bytes()) != cudaSuccess ||
+        h->d_oz_exp.reserve((size_t)np * slot * TS) != cudaSuccess)
+      return fail(FDMGPU_ERR_NOMEM, "integer-slice scratch of the double-float update");
+    h->sp.oz = 1;
+    h->sp.oz_img = h->d_oz_img.p;
+    h->sp.oz_exp = h->d_oz_exp.p;
+  }
   return FDMGPU_OK;
 }
 
@@ -1013,6 +1037,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   sig = mix(sig, (uint64_t)h->factor_mode + 77u);
   sig = mix(sig, (uint64_t)h->tile_engine + 191u);
   sig = mix(sig, (uint64_t)h->solve_order + 733u);
+  sig = mix(sig, (uint64_t)h->df64_engine + 919u);
   for (auto& hp : b.probs) {
     sig = mix(sig, (uint64_t)hp.P.gen * 31u);
     if (hp.P.gen)
@@ -1040,7 +1065,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
                         h->d_gstate.p, h->d_inner.p, h->d_jdone.p, h->d_notconv.p, h->d_active_gm.p,
                         h->d_nb_coef.p, h->d_rvol.p, h->d_poidsa.p, h->d_poidso.p, h->d_Kar.p, h->d_YsoT.p,
                         h->d_Ylmato.p, h->d_R32.p, h->d_act_df.p, h->d_act_rec.p, h->d_sites.p, h->d_wide.p,
-                        h->d_rads.p,  h->d_radU.p};
+                        h->d_rads.p,  h->d_radU.p,  h->d_oz_img.p, h->d_oz_exp.p};
   for (const void* q : ptrs) ps = mix(ps, (uint64_t)(uintptr_t)q);
   if (replan && h->autotune) {
     st = tune_trailing(h);
@@ -1739,6 +1764,7 @@ fdmgpu_status fdmgpu_create(const fdmgpu_grid* g, fdmgpu_handle** out) {
   setup_factor_kernels<double>();
   setup_factor_kernels<dfl>();
   setup_tc_kernels();
+  setup_oz_kernels();
   *out = h;
   return FDMGPU_OK;
 }
@@ -1790,6 +1816,8 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   h->d_strip.release();
   h->d_wide.release();
   h->d_wide_all.release();
+  h->d_oz_img.release();
+  h->d_oz_exp.release();
   h->d_probs.release();
   h->d_red.release();
   if (h->h_pinned_i) cudaFreeHost(h->h_pinned_i);
@@ -1953,6 +1981,13 @@ fdmgpu_status fdmgpu_set_solve_order(fdmgpu_handle* h, int32_t order) {
   if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
   if (order != FDMGPU_SOLVE_COLUMNS && order != FDMGPU_SOLVE_ROWS) return fail(FDMGPU_ERR_ARG, "unknown solve order");
   h->solve_order = order;
+  return FDMGPU_OK;
+}
+
+fdmgpu_status fdmgpu_set_df64_engine(fdmgpu_handle* h, int32_t engine) {
+  if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
+  if (engine != FDMGPU_DF64_SIMT && engine != FDMGPU_DF64_TCGEN05) return fail(FDMGPU_ERR_ARG, "unknown engine");
+  h->df64_engine = engine;
   return FDMGPU_OK;
 }
 

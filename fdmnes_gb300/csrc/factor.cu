@@ -402,6 +402,9 @@ int launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables 
       if (std::is_same<T, float>::value && sp.tc && fuse_rhs)
         launch_tc_update(0, sp.trail_tc[K], nprob, reinterpret_cast<float*>(env), reinterpret_cast<float*>(rhs),
                          probs, tb, K, active, err, s);
+      else if (std::is_same<T, dfl>::value && sp.oz && fuse_rhs && sp.oz_img)
+        nk += launch_oz_update(sp, reinterpret_cast<dfl*>(env), reinterpret_cast<dfl*>(rhs), probs, tb, nprob, K,
+                               active, err, s) - 1;
       else if (trail_threads == 128)
         k_trailing<T, 128><<<dim3(nt, nprob), 128, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
       else

@@ -25,7 +25,20 @@ struct StepPlan {
   std::vector<int> trail_tc, fwd_tc, bwd_tc;
   int* tc_err = nullptr;               // per-problem status word of the solve updates (mbarrier timeout)
   int row_solve = 0;                   // forward / backward solves row by row (one launch per tile row)
+  // double-float trailing update on the tensor cores through integer slices
+  // (oz_update.cu): per step the operand tiles (max over problems) and the
+  // CTAs; per problem a scratch slot of oz_capI + oz_capC tiles of images
+  int oz = 0;
+  std::vector<int> oz_nI, oz_nC, oz_items;
+  int oz_capI = 0, oz_capC = 0;
+  unsigned char* oz_img = nullptr;
+  int* oz_exp = nullptr;
 };
+
+void setup_oz_kernels();
+int64_t oz_tile_bytes();
+int launch_oz_update(const StepPlan& sp, dfl* env, dfl* rhs, const Prob* probs, Tables tb, int nprob, int K,
+                     const int* active, int* err, cudaStream_t s);
 
 // Split-TF32 tcgen05 tile updates (tc_update.cu).  mode 0: factor trailing
 // update C -= L U with the fused right-hand sides; 1: forward solve update

@@ -77,6 +77,8 @@ def load_library(path: str = LIB_PATH):
     L.fdmgpu_batch_xanes.restype = C.c_int
     L.fdmgpu_set_memory_budget.argtypes = [vp, C.c_double]
     L.fdmgpu_set_memory_budget.restype = C.c_int
+    L.fdmgpu_set_df64_engine.argtypes = [vp, C.c_int32]
+    L.fdmgpu_set_df64_engine.restype = C.c_int
     L.fdmgpu_set_solve_order.argtypes = [vp, C.c_int32]
     L.fdmgpu_set_solve_order.restype = C.c_int
     L.fdmgpu_set_tile_engine.argtypes = [vp, C.c_int32]
@@ -179,6 +181,11 @@ class FdmSolver:
     def set_memory_budget(self, nbytes: float = 0.0):
         """Device bytes a batch may take before it runs in chunks (0: 85% of the device)."""
         _check(self.lib.fdmgpu_set_memory_budget(self.h, float(nbytes)))
+
+    def set_df64_engine(self, engine: str = "tcgen05"):
+        """Double-float trailing update of the escalation factor on the FP32
+        pipes ("simt") or on the tensor cores through integer slices ("tcgen05")."""
+        _check(self.lib.fdmgpu_set_df64_engine(self.h, {"simt": 0, "tcgen05": 1}[engine]))
 
     def set_solve_order(self, order: str = "rows"):
         """Refinement solves of mixed batches step by step ("columns") or row by row ("rows")."""

@@ -29,10 +29,13 @@ def spectrum_inputs(st: CL.Structure, energies: Sequence[float], functions: bool
     """Per-energy inputs and row numbering of a spectrum.  functions=False
     leaves phiato / Bessel / Neumann to the device (FdmSolver.set_radial)."""
     out = []
+    rows = {}  # newind depends on the energy only through the l cut-offs: a few distinct numberings per spectrum
     for E in energies:
         ei = CL.energy_inputs(st, float(E), ispin=ispin, functions=functions)
-        ri = CL.newind(st, ei.nlmsa, ei.nlmso)
-        out.append((ei, ri))
+        key = (tuple(int(x) for x in ei.nlmsa), int(ei.nlmso))
+        if key not in rows:
+            rows[key] = CL.newind(st, ei.nlmsa, ei.nlmso)
+        out.append((ei, rows[key]))
     return out
 
 

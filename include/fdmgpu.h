@@ -218,6 +218,17 @@ typedef enum {
                                   row; every right-hand-side tile written once           */
 } fdmgpu_solve_order;
 
+/* Arithmetic units of the double-float trailing update of the escalation
+ * factor (the energies whose FP32 refinement stalls). */
+typedef enum {
+  FDMGPU_DF64_SIMT = 0,        /* FP32 pipes, about 12 instructions per multiply-add      */
+  FDMGPU_DF64_TCGEN05 = 1      /* tensor cores: rows of L and columns of U scaled by powers
+                                  of two and cut into seven 7-bit integer slices (exact
+                                  bf16), the 34 slice pairs of orders <= 9 multiplied by
+                                  tcgen05.mma kind::f16 into one FP32 accumulator per
+                                  order, exact (sums below 2^24), combined in double-float */
+} fdmgpu_df64_engine;
+
 /* Library version string. */
 const char* fdmgpu_version(void);
 
@@ -296,6 +307,10 @@ typedef struct fdmgpu_radial {
   double v0bd;            /* interstitial level: kinetic energy = Enervide - v0bd - dv (Ry) */
 } fdmgpu_radial;
 fdmgpu_status fdmgpu_set_radial(fdmgpu_handle* h, const fdmgpu_radial* radial);
+
+/* Engine of the double-float trailing update (fdmgpu_df64_engine) for the
+ * mixed batches planned after the call.  No counterpart in the reference. */
+fdmgpu_status fdmgpu_set_df64_engine(fdmgpu_handle* h, int32_t engine);
 
 /* Solve order of the mixed batches planned after the call (fdmgpu_solve_order).
  * No counterpart in the reference. */
