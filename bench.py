@@ -397,9 +397,9 @@ def run_gpu(args):
                        "first_call_wall_s": fp64_wall, "gpu_launches": int(info64["n_kernels"])},
         "accuracy": {"convolved_rel_err_vs_fp64": err_conv, "convolved_rel_err_vs_fp64_host": err_conv_host,
                      "taull_max_rel_err_vs_fp64": err_taull, "refine_iters_max": last["refine_iters"],
-                     "fp64_escalations": last["n_fallback"]},
+                     "fp64_escalations": last["n_fallback"], "refine_steps": int(last["refine_steps"])},
         "phases_ms": {k: last[k] for k in ("ms_assemble", "ms_factor", "ms_solve", "ms_refine",
-                                           "ms_escalate_factor")},
+                                           "ms_refine_loop", "ms_escalate_factor")},
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -496,7 +496,7 @@ def main():
                     help="accumulation of the FP32 factor (wide_atom: double-float sums at the atom-harmonic steps)")
     ap.add_argument("--tile-engine", default="simt", choices=["simt", "tcgen05", "tcgen05_factor"],
                     help="FP32 tile updates on the FP32 pipes or on the tensor cores (split TF32)")
-    ap.add_argument("--escalation", default="df64", choices=["df64", "wide_df64", "fp64"],
+    ap.add_argument("--escalation", default="df64", choices=["df64", "df64_f32", "wide_df64", "fp64"],
                     help="re-solve of energies whose FP32 refinement stalls")
     ap.add_argument("--config", default="cu401", choices=["cu401", "tio2"],
                     help="cu401: the 401-energy Cu spectrum (the metric's configuration); tio2: the rutile "

@@ -49,7 +49,8 @@ class FdmInfo(C.Structure):
                 ("ms_residual_first", C.c_double), ("flops_residual", C.c_double),
                 ("ms_escalate_factor", C.c_double), ("flops_escalate_factor", C.c_double),
                 ("n_wide_refactor", C.c_int32), ("ms_wide_refactor", C.c_double),
-                ("flops_wide_refactor", C.c_double)]
+                ("flops_wide_refactor", C.c_double), ("ms_refine_loop", C.c_double),
+                ("refine_steps", C.c_int64)]
 
 
 def _pi(a: np.ndarray, keep: List):

@@ -150,6 +150,7 @@ struct fdmgpu_handle {
   int refine_recur = 0;   // classical refinement with the residual updated by recurrence (1)
   int escalate_dfl = 1;   // escalation by a double-float (1) or an FP64 (0) factorisation
   int escalate_wide = 0;  // first a wide-accumulation FP32 re-factorisation of the stalled energies
+  int escalate_f32 = 0;   // double-float factors rounded to FP32, then FP32 refinement
   double mem_budget = 0;  // device bytes a batch's pools may take before it runs in chunks (0: 85% of the device)
   DevBuf<unsigned char> d_wide_all;  // every step wide (the re-factorisation's table)
   int gmres_m = 12;       // Krylov dimension of one GMRES cycle
@@ -202,7 +203,7 @@ struct fdmgpu_handle {
   LaunchDims dims;
   Tables tb{};
   Pools pl{};
-  cudaEvent_t ev[10] = {};
+  cudaEvent_t ev[11] = {};
   DevBuf<StaticDev> d_sites;  // static tables of every site of the batch, indexed by Prob::site
   DevBuf<int> d_nnz;  // CSR nonzeros per problem (algorithmic work of the residual)
 };
@@ -1314,6 +1315,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
         CK(cudaStreamSynchronize(h->stream));
       }
     }
+    CK(cudaEventRecord(h->ev[10], h->stream));  // end of the classical refinement loop
     // First escalation stage (FDMGPU_ESCALATE_WIDE_DF64): the stalled
     // problems are factorised again in FP32 with double-float sums in every
     // trailing update (the FP32 band converted again from the FP64 one), and
@@ -1450,11 +1452,55 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
         // step whose correction is within tol_accept is far more accurate than
         // that correction: stop there (one step is the rule, three at most).
         dfl* D = reinterpret_cast<dfl*>(h->pl.V);
-        nkern += launch_dfl_escalation(h->sp, h->d_probs.p, h->pl, h->tb, h->dims, D, h->stream, h->ev[8], h->ev[9]);
-        esc_timed = true;
         std::vector<int> act2 = active;
         std::vector<unsigned long long> red2(3 * np);
-        for (int step = 0; step < 3; ++step) {
+        int dfl_steps = 3;
+        if (h->escalate_f32 && dev_loop) {
+          // double-float factors rounded to FP32, then the device FP32
+          // refinement loop from the current solution; the energies it leaves
+          // above the accepted level take double-float steps below
+          nkern += launch_dfl_factor_f32(h->sp, h->d_probs.p, h->pl, h->tb, h->dims, D, h->stream, h->ev[8],
+                                         h->ev[9]);
+          esc_timed = true;
+          std::vector<RefineState> rs(np);
+          for (int k = 0; k < np; ++k) {
+            rs[k].active = active[k];
+            rs[k].slow = 0;
+            rs[k].iters = 0;
+            rs[k].pad = 0;
+            rs[k].prev = 1e300;
+            rs[k].resid = b.resid[k];
+          }
+          CK(cudaMemcpyAsync(h->d_rstate.p, rs.data(), np * sizeof(RefineState), cudaMemcpyHostToDevice, h->stream));
+          const RefineCtl c0{0, max_iter, tol, nfail, 0};
+          CK(cudaMemcpyAsync(h->d_rctl.p, &c0, sizeof c0, cudaMemcpyHostToDevice, h->stream));
+          CK(cudaGraphLaunch(h->g_res, h->stream));
+          CK(cudaGraphLaunch(h->g_iter, h->stream));
+          CK(cudaGraphLaunch(h->g_loop, h->stream));
+          std::vector<RefineState> rs2(np);
+          RefineCtl c1;
+          CK(cudaMemcpyAsync(rs2.data(), h->d_rstate.p, np * sizeof(RefineState), cudaMemcpyDeviceToHost, h->stream));
+          CK(cudaMemcpyAsync(&c1, h->d_rctl.p, sizeof c1, cudaMemcpyDeviceToHost, h->stream));
+          CK(cudaStreamSynchronize(h->stream));
+          CK(cudaGetLastError());
+          nkern += h->nk_res + h->nk_iter + (int64_t)std::max(c1.it - 1, 0) * h->nk_loop_body;
+          int more = 0;
+          for (int k = 0; k < np; ++k)
+            if (active[k]) {
+              b.iters[k] += rs2[k].iters;
+              b.resid[k] = rs2[k].resid;
+              act2[k] = !(b.resid[k] <= tol_accept);
+              more += act2[k];
+            } else {
+              act2[k] = 0;
+            }
+          if (more) CK(cudaMemcpyAsync(h->d_active.p, act2.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+          else dfl_steps = 0;
+        } else {
+          nkern += launch_dfl_escalation(h->sp, h->d_probs.p, h->pl, h->tb, h->dims, D, h->stream, h->ev[8], h->ev[9]);
+          esc_timed = true;
+        }
+        for (int step = 0; step < dfl_steps; ++step) {
           CK(cudaMemsetAsync(h->pl.dmax, 0, 3 * np * sizeof(unsigned long long), h->stream));
           nkern += launch_dfl_refine_step(h->sp, h->d_probs.p, h->pl, h->tb, h->dims, D, h->stream);
           CK(cudaMemcpyAsync(red2.data(), h->d_red.p, 3 * np * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
@@ -1560,6 +1606,9 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
       for (int k = 0; k < np; ++k) info->n_wide_refactor += b.wide[k];
       info->ms_wide_refactor = wide_ms;
       info->flops_wide_refactor = wide_flops;
+      CK(cudaEventElapsedTime(&t, h->ev[4], h->ev[10]));
+      info->ms_refine_loop = t;
+      for (int k = 0; k < np; ++k) info->refine_steps += b.iters[k];
     }
   }
   // hard errors first; a refinement that did not reach its tolerance still
@@ -2020,11 +2069,12 @@ fdmgpu_status fdmgpu_get_tuning(fdmgpu_handle* h, int32_t precision, int32_t* tr
 
 fdmgpu_status fdmgpu_set_escalation(fdmgpu_handle* h, int32_t mode) {
   if (!h || (mode != FDMGPU_ESCALATE_FP64 && mode != FDMGPU_ESCALATE_DF64 && mode != FDMGPU_ESCALATE_DF64_OVERLAP &&
-             mode != FDMGPU_ESCALATE_WIDE_DF64))
+             mode != FDMGPU_ESCALATE_WIDE_DF64 && mode != FDMGPU_ESCALATE_DF64_F32))
     return fail(FDMGPU_ERR_ARG, "unknown escalation mode");
   h->escalate_dfl = mode != FDMGPU_ESCALATE_FP64;
   h->overlap_escalation = mode == FDMGPU_ESCALATE_DF64_OVERLAP;
   h->escalate_wide = mode == FDMGPU_ESCALATE_WIDE_DF64;
+  h->escalate_f32 = mode == FDMGPU_ESCALATE_DF64_F32;
   h->plan_sig = 0;
   return FDMGPU_OK;
 }

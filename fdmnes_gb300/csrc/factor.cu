@@ -353,9 +353,12 @@ static size_t smem_bytes() { return 2 * TS * SP * sizeof(T); }
 // the row solve holds the left operand (stride SPA), the right one and the diagonal tile
 template <typename T>
 static size_t smem_bytes_row() { return (TS * SPA + 2 * TS * SP) * sizeof(T); }
-// the panel holds the diagonal tile plus two SPA-strided work tiles
+// the panel holds the diagonal tile plus one SPA-strided work tile (two for
+// FP64, whose row solve also stages the transposed diagonal tile)
 template <typename T>
-static size_t smem_bytes_panel() { return (TS * SP + 2 * TS * SPA) * sizeof(T); }
+static size_t smem_bytes_panel() {
+  return (TS * SP + (std::is_same<T, double>::value ? 2 : 1) * TS * SPA) * sizeof(T);
+}
 
 template <typename T>
 void setup_factor_kernels() {

@@ -17,6 +17,7 @@
 #pragma once
 
 #include <cstdint>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include "../../include/fdmgpu.h"
@@ -390,7 +391,7 @@ __device__ __forceinline__ void ld4<double>(const double* p, double* v) {
   v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
 }
 
-constexpr int SPA = TS + 1;  // odd stride of the A tile: conflict-free scalar column reads
+constexpr int SPA = TS + 1;  // odd stride: conflict-free reads of a row per thread
 
 // acc += a * b inside a dot product.  For double-float the accumulator is
 // kept unnormalised: the high parts are summed with Knuth's two-sum, the
@@ -459,28 +460,49 @@ template <typename T> struct MMThreads { static constexpr int value = GEMM_THREA
 template <> struct MMThreads<dfl> { static constexpr int value = 128; };
 template <> struct MMThreads<float> { static constexpr int value = 128; };
 
+template <typename T>
+__device__ __forceinline__ void st4(T* p, const T* v) {
+  p[0] = v[0]; p[1] = v[1]; p[2] = v[2]; p[3] = v[3];
+}
+template <>
+__device__ __forceinline__ void st4<float>(float* p, const float* v) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+template <>
+__device__ __forceinline__ void st4<double>(double* p, const double* v) {
+  *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+  *reinterpret_cast<double2*>(p + 2) = make_double2(v[2], v[3]);
+}
+template <>
+__device__ __forceinline__ void st4<dfl>(dfl* p, const dfl* v) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0].hi, v[0].lo, v[1].hi, v[1].lo);
+  *reinterpret_cast<float4*>(p + 2) = make_float4(v[2].hi, v[2].lo, v[3].hi, v[3].lo);
+}
+
 // TA: use the transpose of A (C (-)= A^T * P B).  Thread (tx, ty) owns rows
 // {4ty + i, 32 + 4ty + i} (i < 4) and columns {4tx + j, 32 + 4tx + j} (64
-// threads) or {4tx + j} (128 threads), j < 4.
+// threads) or {4tx + j} (128 threads), j < 4.  Both operands sit k-major in
+// shared memory (As[k][r], Bs[k][c], stride SP), so one k step reads its 8
+// rows of A and its 4 or 8 columns of B with 16-byte loads.  Staging order:
+// a warp covers 16 rows x 2 column quads, so the global reads use whole
+// 32-byte sectors and the transposing stores fall on distinct banks.
 template <typename T, bool SUB, bool TA = false, int NT = MMThreads<T>::value, typename Acc = T>
 __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const int* perm, T* As, T* Bs) {
   static_assert(NT == 64 || NT == 128, "tile_mm64 runs on 64 or 128 threads");
   constexpr int CW = NT == 128 ? 4 : 8;  // columns per thread
   const int t = threadIdx.x;
-  // stage: As[r][k] = A[r][k] (A[k][r] when TA; stride SPA), Bs[r][c] = B[perm ? perm[r] : r][c] (stride SP)
   for (int idx = t; idx < TS2 / 4; idx += NT) {
-    const int r = idx / (TS / 4), c4 = (idx % (TS / 4)) * 4;
+    const int r = idx % 16 + 16 * (idx / 256), c4 = ((idx / 16) % 16) * 4;
     T a[4], b[4];
     ld4(A + r * TS + c4, a);
     ld4(B + (perm ? perm[r] : r) * TS + c4, b);
+    if (TA) {
+      st4(As + r * SP + c4, a);
+    } else {
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      if (TA)
-        As[(c4 + q) * SPA + r] = a[q];
-      else
-        As[r * SPA + c4 + q] = a[q];
-      Bs[r * SP + c4 + q] = b[q];
+      for (int q = 0; q < 4; ++q) As[(c4 + q) * SP + r] = a[q];
     }
+    st4(Bs + r * SP + c4, b);
   }
   __syncthreads();
   const int tx = t % (NT / 8), ty = t / (NT / 8);
@@ -492,11 +514,8 @@ __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const in
 #pragma unroll 2
   for (int k = 0; k < TS; ++k) {
     T a[8], b[CW];
-#pragma unroll
-    for (int i = 0; i < 4; ++i) {
-      a[i] = As[(4 * ty + i) * SPA + k];
-      a[4 + i] = As[(32 + 4 * ty + i) * SPA + k];
-    }
+    ld4(As + k * SP + 4 * ty, a);
+    ld4(As + k * SP + 32 + 4 * ty, a + 4);
     ld4(Bs + k * SP + 4 * tx, b);
     if (CW == 8) ld4(Bs + k * SP + 32 + 4 * tx, b + 4);
 #pragma unroll
@@ -522,7 +541,10 @@ __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const in
 // The factored diagonal tile sits in shared memory with stride SP.
 // -------------------------------------------------------------------------
 
-// g <- L^-1 P g (L unit lower): thread c owns column c of the tile.
+// g <- L^-1 P g (L unit lower): thread c owns column c of the tile.  Column
+// (axpy) order: once x[k] is final it is subtracted from every later row, so
+// the 63 - k updates of step k are independent (instruction-level parallelism
+// for the dependent double-float operations) instead of one dot-product chain.
 template <typename T>
 __device__ __forceinline__ void col_solve_lower_unit(T* g, const T* Ls, const int* perm) {
   const int c = threadIdx.x;
@@ -530,18 +552,31 @@ __device__ __forceinline__ void col_solve_lower_unit(T* g, const T* Ls, const in
   T x[TS];
 #pragma unroll
   for (int r = 0; r < TS; ++r) x[r] = g[(perm ? perm[r] : r) * TS + c];
+  if constexpr (std::is_same<T, double>::value) {
+    // FP64 (the reference's arithmetic): dot-product order
 #pragma unroll
-  for (int k = 1; k < TS; ++k) {
-    T acc = x[k];
+    for (int k = 1; k < TS; ++k) {
+      T acc = x[k];
 #pragma unroll
-    for (int i = 0; i < k; ++i) acc -= Ls[k * SP + i] * x[i];
-    x[k] = acc;
+      for (int i = 0; i < k; ++i) acc -= Ls[k * SP + i] * x[i];
+      x[k] = acc;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < TS - 1; ++k) {
+      const T xk = x[k];
+#pragma unroll
+      for (int i = k + 1; i < TS; ++i) x[i] -= Ls[i * SP + k] * xk;
+    }
   }
 #pragma unroll
   for (int r = 0; r < TS; ++r) g[r * TS + c] = x[r];
 }
 
-// g <- U^-1 g (U upper with diagonal): thread c owns column c.
+// g <- U^-1 g (U upper with diagonal): thread c owns column c.  Dot-product
+// order from the last row up; for FP32 and double-float each dot product runs
+// as four interleaved partial sums (independent dependency chains), combined
+// before the division.
 template <typename T>
 __device__ __forceinline__ void col_solve_upper(T* g, const T* Us) {
   const int c = threadIdx.x;
@@ -549,12 +584,22 @@ __device__ __forceinline__ void col_solve_upper(T* g, const T* Us) {
   T x[TS];
 #pragma unroll
   for (int r = 0; r < TS; ++r) x[r] = g[r * TS + c];
+  if constexpr (std::is_same<T, double>::value) {
 #pragma unroll
-  for (int k = TS - 1; k >= 0; --k) {
-    T acc = x[k];
+    for (int k = TS - 1; k >= 0; --k) {
+      T acc = x[k];
 #pragma unroll
-    for (int i = k + 1; i < TS; ++i) acc -= Us[k * SP + i] * x[i];
-    x[k] = acc / Us[k * SP + k];
+      for (int i = k + 1; i < TS; ++i) acc -= Us[k * SP + i] * x[i];
+      x[k] = acc / Us[k * SP + k];
+    }
+  } else {
+#pragma unroll
+    for (int k = TS - 1; k >= 0; --k) {
+      T acc[4] = {x[k], T(0), T(0), T(0)};
+#pragma unroll
+      for (int i = k + 1; i < TS; ++i) acc[(i - k - 1) & 3] -= Us[k * SP + i] * x[i];
+      x[k] = ((acc[0] + acc[2]) + (acc[1] + acc[3])) / Us[k * SP + k];
+    }
   }
 #pragma unroll
   for (int r = 0; r < TS; ++r) g[r * TS + c] = x[r];
@@ -616,17 +661,21 @@ __device__ __forceinline__ void load_tile_trans_n(T* __restrict__ s, const T* __
   for (int idx = threadIdx.x; idx < TS2; idx += nthreads) s[(idx % TS) * SP + idx / TS] = g[idx];
 }
 
-// g <- g U^-1 (U upper with diagonal): thread r owns row r, i.e. solves
-// U^T x = a by forward substitution.  The rows pass through shared memory Ws
-// (stride SPA) so that the global accesses stay coalesced and the row reads
-// conflict-free; U^T is staged into Ws's tail rows-first for contiguous reads.
+// g <- g U^-1 (U upper with diagonal): thread r owns row r.  The rows pass
+// through shared memory Ws (stride SPA) so that the global accesses stay
+// coalesced and the row reads conflict-free.  FP32 and double-float eliminate
+// in column order: x[k] /= U(k,k), then x[j] -= x[k] U(k,j) for every j > k
+// (independent updates, U's row k read as a broadcast; Ws holds TS x SPA
+// elements).  FP64 solves U^T x = a by forward substitution in dot-product
+// order, with U^T staged into Ws's tail (2 TS x SPA elements in all).
 template <typename T>
 __device__ __forceinline__ void row_solve_upper(T* g, const T* Us, T* Ws) {
-  T* Ut = Ws + TS * SPA;  // Ut[k][i] = U[i][k], stride SPA
+  constexpr bool F64 = std::is_same<T, double>::value;
+  T* Ut = Ws + TS * SPA;  // FP64 only: Ut[k][i] = U[i][k], stride SPA
   for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) {
     const int a = idx / TS, b = idx % TS;
     Ws[a * SPA + b] = g[idx];
-    Ut[b * SPA + a] = Us[a * SP + b];
+    if (F64) Ut[b * SPA + a] = Us[a * SP + b];
   }
   __syncthreads();
   const int r = threadIdx.x;
@@ -634,12 +683,22 @@ __device__ __forceinline__ void row_solve_upper(T* g, const T* Us, T* Ws) {
     T x[TS];
 #pragma unroll
     for (int k = 0; k < TS; ++k) x[k] = Ws[r * SPA + k];
+    if constexpr (F64) {
 #pragma unroll
-    for (int k = 0; k < TS; ++k) {
-      T acc = x[k];
+      for (int k = 0; k < TS; ++k) {
+        T acc = x[k];
 #pragma unroll
-      for (int i = 0; i < k; ++i) acc -= Ut[k * SPA + i] * x[i];
-      x[k] = acc / Ut[k * SPA + k];
+        for (int i = 0; i < k; ++i) acc -= Ut[k * SPA + i] * x[i];
+        x[k] = acc / Ut[k * SPA + k];
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < TS; ++k) {
+        const T xk = x[k] / Us[k * SP + k];
+        x[k] = xk;
+#pragma unroll
+        for (int j = k + 1; j < TS; ++j) x[j] -= xk * Us[k * SP + j];
+      }
     }
 #pragma unroll
     for (int k = 0; k < TS; ++k) Ws[r * SPA + k] = x[k];

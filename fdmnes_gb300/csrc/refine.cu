@@ -577,6 +577,42 @@ int launch_dfl_escalation(const StepPlan& sp, const Prob* probs, const Pools& pl
   return nk + 1;
 }
 
+// The FP32 band <- the high parts of the double-float band (the high part of a
+// normalised double-float is its value rounded to FP32), active problems.
+__global__ void k_dfl_to_f32(const Prob* probs, const double* env, float* env32, Tables tb, const int* active) {
+  if (!active[blockIdx.y]) return;
+  const Prob P = probs[blockIdx.y];
+  const int64_t w = blockIdx.x;
+  if (w >= tb.strip[P.trow + P.nt]) return;
+  const float2* t = reinterpret_cast<const float2*>(env + P.env + w * TS2);
+  float* o = env32 + P.env + w * TS2;
+  for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) o[idx] = t[idx].x;
+}
+
+// Double-float factorisation of the active problems' equilibrated bands (in
+// place of their FP64 bands), its factors then rounded into the FP32 band.
+// Right-hand sides ride along only for the tensor-core update, which handles
+// them in the same launch; the double-float refinement steps that may follow
+// read the double-float factors, which stay in place.
+int launch_dfl_factor_f32(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
+                          dfl* D, cudaStream_t s, cudaEvent_t ev_f0, cudaEvent_t ev_f1) {
+  const int np = d.nprob;
+  dfl* envd = reinterpret_cast<dfl*>(pl.env64);
+  const int fuse = sp.oz ? 1 : 0;
+  int nk = 0;
+  k_env_to_dfl<<<dim3(d.max_tiles, np), 256, 0, s>>>(probs, pl.env64, pl.rs, pl.cs, tb, pl.active);
+  ++nk;
+  if (fuse) {
+    k_rhs_to_dfl<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, pl.B64, pl.Y32, pl.rs, D, 1, pl.active);
+    ++nk;
+  }
+  if (ev_f0) cudaEventRecord(ev_f0, s);
+  nk += launch_factor<dfl>(sp, envd, D, probs, tb, np, fuse, pl.active, pl.err, 1e-30, pl.piv, s);
+  if (ev_f1) cudaEventRecord(ev_f1, s);
+  k_dfl_to_f32<<<dim3(d.max_tiles, np), 256, 0, s>>>(probs, pl.env64, pl.env32, tb, pl.active);
+  return nk + 1;
+}
+
 // One refinement step with the double-float factors: residual, solve, x += d;
 // dmax / xmax receive max|d| and max|x| of each active problem.
 int launch_dfl_refine_step(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,

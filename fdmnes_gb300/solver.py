@@ -148,9 +148,10 @@ class FdmSolver:
         _check(self.lib.fdmgpu_set_refinement(self.h, {"classic": 0, "gmres": 1, "recurrence": 2}[mode], krylov_dim))
 
     def set_escalation(self, mode: str = "df64"):
-        """Re-solve of energies the FP32 factors cannot refine: 'df64' (default), 'df64_overlap' or 'fp64'."""
+        """Re-solve of energies the FP32 factors cannot refine: 'df64' (default), 'df64_overlap',
+        'wide_df64', 'df64_f32' (double-float factors rounded to FP32, FP32 refinement) or 'fp64'."""
         _check(self.lib.fdmgpu_set_escalation(self.h, {"fp64": 0, "df64": 1, "df64_overlap": 2,
-                                                       "wide_df64": 3}[mode]))
+                                                       "wide_df64": 3, "df64_f32": 4}[mode]))
 
     def set_tolerance(self, tol: float = 0.0, tol_accept: float = 0.0):
         """Refinement stop (max|dx|/max|x|) and the stalled-but-accepted level; 0 = default."""

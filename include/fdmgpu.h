@@ -72,9 +72,16 @@ typedef enum {
                                   refinement of every energy has ended (default)        */
   FDMGPU_ESCALATE_DF64_OVERLAP = 2, /* the same, started on a second stream as soon as an
                                   energy stalls, while the others keep refining         */
-  FDMGPU_ESCALATE_WIDE_DF64 = 3 /* first the FP32 factor again with double-float sums in
+  FDMGPU_ESCALATE_WIDE_DF64 = 3, /* first the FP32 factor again with double-float sums in
                                   every trailing update and FP32 refinement, then
                                   double-float for the energies still stalled            */
+  FDMGPU_ESCALATE_DF64_F32 = 4 /* double-float LU (no right-hand sides), its factors
+                                  rounded to FP32 in place of the stalled FP32 factors,
+                                  then FP32 refinement steps from the current solution:
+                                  the rounded factors of an accurate LU contract the
+                                  error by about 1e-3 per step where the FP32-computed
+                                  ones stall; double-float steps for energies still
+                                  above the accepted level                               */
 } fdmgpu_escalation;
 
 /* Energy-independent arguments of mat_solve (source/mat_solve_gaussian.f90:17-67). */
@@ -182,6 +189,11 @@ typedef struct fdmgpu_info {
    * device time and algorithmic flops                                         */
   int32_t n_wide_refactor;
   double ms_wide_refactor, flops_wide_refactor;
+  /* mixed precision: device time of the classical refinement loop alone (from
+   * the first residual until every problem has stopped; ms_refine less this
+   * is the escalation), and the refinement steps summed over the problems     */
+  double ms_refine_loop;
+  int64_t refine_steps;
 } fdmgpu_info;
 
 /* Accumulation of the FP32 factor of the mixed path. */

@@ -270,7 +270,8 @@ def test_overlapped_escalation_gives_the_same_spectrum(solver_mod):
 def test_every_refinement_and_escalation_mode(solver_mod):
     """Each documented mode of the mixed path meets the metric's bar against
     the FP64 path on full Cu energies that include escalated ones: classical,
-    GMRES-IR and recurrence refinement; double-float and FP64 escalation."""
+    GMRES-IR and recurrence refinement; double-float, double-float rounded to
+    FP32 and FP64 escalation."""
     from fdmnes_gb300 import cluster as CL, xanes
     st = CL.cu_structure()
     energies = [2.0, 14.0, 26.0, 30.0, 34.0]
@@ -278,13 +279,44 @@ def test_every_refinement_and_escalation_mode(solver_mod):
     sv = solver_mod.FdmSolver(st)
     T64, _ = sv.spectrum(items, "fp64")
     sv.set_tolerance(1e-8, 1e-6)
-    for refine, esc in (("classic", "df64"), ("gmres", "df64"), ("recurrence", "df64"), ("classic", "fp64")):
+    for refine, esc in (("classic", "df64"), ("gmres", "df64"), ("recurrence", "df64"), ("classic", "fp64"),
+                        ("classic", "df64_f32")):
         sv.set_refinement(refine, 12)
         sv.set_escalation(esc)
         T, info = sv.spectrum(items, "mixed")
         err = max(rel(a, b) for a, b in zip(T, T64))
         assert err < 1e-5, (refine, esc, err)
         assert xanes.convolved_relative_error(energies, T, T64) < 1e-6, (refine, esc)
+    sv.close()
+
+
+def test_rounded_double_float_factors_refine_in_fp32(solver_mod):
+    """Escalation by double-float factors rounded to FP32: on full Cu energies
+    whose FP32 refinement stalls, the FP32 steps with the rounded factors
+    reach the stopping tolerance in a few steps (an accurate LU rounded to
+    FP32 contracts the error by ~1e-3 per step), so no energy needs a
+    double-float step, and the spectrum meets the FP64 bars."""
+    from fdmnes_gb300 import cluster as CL, xanes
+    st = CL.cu_structure()
+    E = np.array([2.0, 22.0, 26.0, 30.0, 34.0])
+    items = xanes.spectrum_inputs(st, E)
+    sv = solver_mod.FdmSolver(st)
+    T64, _ = sv.spectrum(items, "fp64")
+    sv.set_tolerance(1e-8, 1e-6)
+    sv.set_escalation("df64")
+    _, info0 = sv.spectrum(items, "mixed")
+    it0 = [sv.stats(k)[0] for k in range(len(E))]
+    sv.set_escalation("df64_f32")
+    T, info = sv.spectrum(items, "mixed")
+    st_ = [sv.stats(k) for k in range(len(E))]
+    assert info["n_fallback"] == info0["n_fallback"] >= 1
+    assert not info["not_converged"]
+    for k, s in enumerate(st_):
+        if s[2]:   # escalated: at most eight FP32 steps after the rounded factors
+            assert s[0] - it0[k] <= 8 and s[1] <= 1e-8, (E[k], s, it0[k])
+    assert max(rel(a, b) for a, b in zip(T, T64)) < 1e-5
+    assert xanes.convolved_relative_error(E, T, T64) < 1e-6
+    sv.set_escalation("df64")
     sv.close()
 
 
