@@ -494,7 +494,7 @@ def main():
                     help="energies of the spectrum over -5..35 eV (401: step 0.1 eV; 41: step 1 eV)")
     ap.add_argument("--factor-mode", default="fp32", choices=["fp32", "wide_atom", "wide_all"],
                     help="accumulation of the FP32 factor (wide_atom: double-float sums at the atom-harmonic steps)")
-    ap.add_argument("--tile-engine", default="simt", choices=["simt", "tcgen05", "tcgen05_factor"],
+    ap.add_argument("--tile-engine", default="simt", choices=["simt", "simt_stream", "tcgen05", "tcgen05_factor"],
                     help="FP32 tile updates on the FP32 pipes or on the tensor cores (split TF32)")
     ap.add_argument("--escalation", default="df64", choices=["df64", "df64_f32", "wide_df64", "fp64"],
                     help="re-solve of energies whose FP32 refinement stalls")

@@ -16,7 +16,8 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libfdmgpu.so")
 SOURCES = ["capi.cu", "factor.cu", "assemble.cu", "complex.cu", "refine.cu", "taull.cu", "gmres.cu", "taull_noalloc.cu",
-           "adjoint.cu", "tc_update.cu", "peaks.cu", "xsection.cu", "radial.cu", "oz_update.cu"]
+           "adjoint.cu", "tc_update.cu", "peaks.cu", "xsection.cu", "radial.cu", "oz_update.cu",
+           "strip_update.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

@@ -538,6 +538,10 @@ void build_step_plan(fdmgpu_handle* h) {
   sp.oz_nC.assign(N, 0);
   sp.oz_items.assign(N, 0);
   sp.oz_capI = sp.oz_capC = 0;
+  sp.strip_trail.assign(N, 0);
+  sp.strip_trail_rhs.assign(N, 0);
+  sp.strip_fwd.assign(N, 0);
+  sp.strip_bwd.assign(N, 0);
   for (auto& hp : pr) {
     for (int K = 0; K < hp.P.nt; ++K) {
       const int nI = hp.Imax[K] - K, nJ = hp.J1[K] - K, nR = hp.P.nrt;
@@ -547,6 +551,10 @@ void build_step_plan(fdmgpu_handle* h) {
       sp.oz_items[K] = std::max(sp.oz_items[K], nI > 0 ? ((nI + 1) / 2) * (nJ + nR) : 0);
       sp.oz_capI = std::max(sp.oz_capI, nI);
       sp.oz_capC = std::max(sp.oz_capC, nJ + nR);
+      sp.strip_trail[K] = std::max(sp.strip_trail[K], strip_items(nI, nJ, strip_rows(0)));
+      sp.strip_trail_rhs[K] = std::max(sp.strip_trail_rhs[K], strip_items(nI, nJ + nR, strip_rows(0)));
+      sp.strip_fwd[K] = std::max(sp.strip_fwd[K], strip_items(nI, nR, strip_rows(1)));
+      sp.strip_bwd[K] = std::max(sp.strip_bwd[K], strip_items(K - hp.Imin[K], nR, strip_rows(2)));
       sp.fwd_tc[K] = std::max(sp.fwd_tc[K], tc_items(nI, nR));
       sp.bwd_tc[K] = std::max(sp.bwd_tc[K], tc_items(K - hp.Imin[K], nR));
       sp.panel[K] = std::max(sp.panel[K], nI + nJ);
@@ -675,9 +683,11 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
   h->tb.strip = h->d_strip.p;
   h->tb.wide = (mixed && h->factor_mode != FDMGPU_FACTOR_FP32) ? h->d_wide.p : nullptr;
   // real mixed batches may run their FP32 tile updates on the tensor cores
-  h->sp.tc = (mixed && !cplx && h->tile_engine != FDMGPU_ENGINE_SIMT) ? 1 : 0;
+  h->sp.tc = (mixed && !cplx && (h->tile_engine == FDMGPU_ENGINE_TCGEN05 ||
+                                  h->tile_engine == FDMGPU_ENGINE_TCGEN05_FACTOR)) ? 1 : 0;
   h->sp.tc_solve = (mixed && !cplx && h->tile_engine == FDMGPU_ENGINE_TCGEN05) ? 1 : 0;
   h->sp.row_solve = (mixed && h->solve_order == FDMGPU_SOLVE_ROWS) ? 1 : 0;
+  h->sp.strip = (mixed && !cplx && h->tile_engine == FDMGPU_ENGINE_SIMT_STREAM) ? 1 : 0;
   h->sp.tc_err = h->d_err.p;
   Pools& pl = h->pl;
   pl = Pools();
@@ -1814,6 +1824,7 @@ fdmgpu_status fdmgpu_create(const fdmgpu_grid* g, fdmgpu_handle** out) {
   setup_factor_kernels<dfl>();
   setup_tc_kernels();
   setup_oz_kernels();
+  setup_strip_kernels();
   *out = h;
   return FDMGPU_OK;
 }
@@ -2042,7 +2053,8 @@ fdmgpu_status fdmgpu_set_df64_engine(fdmgpu_handle* h, int32_t engine) {
 
 fdmgpu_status fdmgpu_set_tile_engine(fdmgpu_handle* h, int32_t engine) {
   if (!h) return fail(FDMGPU_ERR_ARG, "null handle");
-  if (engine != FDMGPU_ENGINE_SIMT && engine != FDMGPU_ENGINE_TCGEN05 && engine != FDMGPU_ENGINE_TCGEN05_FACTOR)
+  if (engine != FDMGPU_ENGINE_SIMT && engine != FDMGPU_ENGINE_TCGEN05 && engine != FDMGPU_ENGINE_TCGEN05_FACTOR &&
+      engine != FDMGPU_ENGINE_SIMT_STREAM)
     return fail(FDMGPU_ERR_ARG, "unknown tile engine");
   h->tile_engine = engine;
   return FDMGPU_OK;

@@ -383,6 +383,15 @@ void setup_factor_kernels() {
   cudaFuncSetAttribute(k_solve_row<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_bytes_row<T>());
 }
 
+// The solve updates as strips (FP32 and double-float only; the FP64 path keeps
+// the one-tile kernels).
+template <typename T>
+static void launch_strip_t(int mode, int items, int nprob, T* env, T* rhs, const Prob* probs, Tables tb, int K,
+                           int fuse_rhs, const int* active, int* err, cudaStream_t s, bool wide) {
+  if constexpr (!std::is_same<T, double>::value)
+    launch_strip<T>(mode, items, nprob, env, rhs, probs, tb, K, fuse_rhs, active, err, s, wide);
+}
+
 template <typename T>
 int launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables tb, int nprob, int fuse_rhs,
                   const int* active, int* err, double piv_thr, int* piv, cudaStream_t s, int trail_threads,
@@ -408,6 +417,9 @@ int launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables 
       else if (std::is_same<T, dfl>::value && sp.oz && fuse_rhs && sp.oz_img)
         nk += launch_oz_update(sp, reinterpret_cast<dfl*>(env), reinterpret_cast<dfl*>(rhs), probs, tb, nprob, K,
                                active, err, s) - 1;
+      else if (!std::is_same<T, double>::value && sp.strip)
+        launch_strip_t(0, fuse_rhs ? sp.strip_trail_rhs[K] : sp.strip_trail[K], nprob, env, rhs, probs, tb, K,
+                       fuse_rhs, active, err, s, false);
       else if (trail_threads == 128)
         k_trailing<T, 128><<<dim3(nt, nprob), 128, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
       else
@@ -416,7 +428,10 @@ int launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables 
       // the problems whose step K is marked wide run in the wide instantiation
       if constexpr (std::is_same<T, float>::value) {
         if (tb.wide && K < (int)sp.wide_any.size() && sp.wide_any[K]) {
-          if (trail_threads == 128)
+          if (sp.strip)
+            launch_strip_t(0, fuse_rhs ? sp.strip_trail_rhs[K] : sp.strip_trail[K], nprob, env, rhs, probs, tb, K,
+                           fuse_rhs, active, err, s, true);
+          else if (trail_threads == 128)
             k_trailing<T, 128, true><<<dim3(nt, nprob), 128, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
           else
             k_trailing<T, 64, true><<<dim3(nt, nprob), 64, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, active);
@@ -448,6 +463,9 @@ int launch_forward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs, 
       if (std::is_same<T, float>::value && sp.tc_solve)
         launch_tc_update(1, sp.fwd_tc[K], nprob, reinterpret_cast<float*>(const_cast<T*>(env)),
                          reinterpret_cast<float*>(rhs), probs, tb, K, active, sp.tc_err, s);
+      else if (!std::is_same<T, double>::value && sp.strip)
+        launch_strip_t(1, sp.strip_fwd[K], nprob, const_cast<T*>(env), rhs, probs, tb, K, 0, active, sp.tc_err, s,
+                       false);
       else
         k_fwd_update<T><<<dim3(sp.fwd[K], nprob), MMThreads<T>::value, sm, s>>>(env, rhs, probs, tb, K, active);
       ++nk;
@@ -476,6 +494,9 @@ int launch_backward(const StepPlan& sp, const T* env, T* rhs, const Prob* probs,
       if (std::is_same<T, float>::value && sp.tc_solve)
         launch_tc_update(2, sp.bwd_tc[K], nprob, reinterpret_cast<float*>(const_cast<T*>(env)),
                          reinterpret_cast<float*>(rhs), probs, tb, K, active, sp.tc_err, s);
+      else if (!std::is_same<T, double>::value && sp.strip)
+        launch_strip_t(2, sp.strip_bwd[K], nprob, const_cast<T*>(env), rhs, probs, tb, K, 0, active, sp.tc_err, s,
+                       false);
       else
         k_bwd_update<T><<<dim3(sp.bwd[K], nprob), MMThreads<T>::value, sm, s>>>(env, rhs, probs, tb, K, active);
       ++nk;

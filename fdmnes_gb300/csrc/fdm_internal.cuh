@@ -481,28 +481,26 @@ __device__ __forceinline__ void st4<dfl>(dfl* p, const dfl* v) {
 
 // TA: use the transpose of A (C (-)= A^T * P B).  Thread (tx, ty) owns rows
 // {4ty + i, 32 + 4ty + i} (i < 4) and columns {4tx + j, 32 + 4tx + j} (64
-// threads) or {4tx + j} (128 threads), j < 4.  Both operands sit k-major in
-// shared memory (As[k][r], Bs[k][c], stride SP), so one k step reads its 8
-// rows of A and its 4 or 8 columns of B with 16-byte loads.  Staging order:
-// a warp covers 16 rows x 2 column quads, so the global reads use whole
-// 32-byte sectors and the transposing stores fall on distinct banks.
+// threads) or {4tx + j} (128 threads), j < 4.
 template <typename T, bool SUB, bool TA = false, int NT = MMThreads<T>::value, typename Acc = T>
 __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const int* perm, T* As, T* Bs) {
   static_assert(NT == 64 || NT == 128, "tile_mm64 runs on 64 or 128 threads");
   constexpr int CW = NT == 128 ? 4 : 8;  // columns per thread
   const int t = threadIdx.x;
+  // stage: As[r][k] = A[r][k] (A[k][r] when TA; stride SPA), Bs[r][c] = B[perm ? perm[r] : r][c] (stride SP)
   for (int idx = t; idx < TS2 / 4; idx += NT) {
-    const int r = idx % 16 + 16 * (idx / 256), c4 = ((idx / 16) % 16) * 4;
+    const int r = idx / (TS / 4), c4 = (idx % (TS / 4)) * 4;
     T a[4], b[4];
     ld4(A + r * TS + c4, a);
     ld4(B + (perm ? perm[r] : r) * TS + c4, b);
-    if (TA) {
-      st4(As + r * SP + c4, a);
-    } else {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) As[(c4 + q) * SP + r] = a[q];
+    for (int q = 0; q < 4; ++q) {
+      if (TA)
+        As[(c4 + q) * SPA + r] = a[q];
+      else
+        As[r * SPA + c4 + q] = a[q];
+      Bs[r * SP + c4 + q] = b[q];
     }
-    st4(Bs + r * SP + c4, b);
   }
   __syncthreads();
   const int tx = t % (NT / 8), ty = t / (NT / 8);
@@ -514,8 +512,11 @@ __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const in
 #pragma unroll 2
   for (int k = 0; k < TS; ++k) {
     T a[8], b[CW];
-    ld4(As + k * SP + 4 * ty, a);
-    ld4(As + k * SP + 32 + 4 * ty, a + 4);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      a[i] = As[(4 * ty + i) * SPA + k];
+      a[4 + i] = As[(32 + 4 * ty + i) * SPA + k];
+    }
     ld4(Bs + k * SP + 4 * tx, b);
     if (CW == 8) ld4(Bs + k * SP + 32 + 4 * tx, b + 4);
 #pragma unroll

@@ -30,10 +30,25 @@ struct StepPlan {
   // CTAs; per problem a scratch slot of oz_capI + oz_capC tiles of images
   int oz = 0;
   std::vector<int> oz_nI, oz_nC, oz_items;
+  // FP32 / double-float tile updates as bulk-copy-staged strips
+  // (strip_update.cu): CTAs per step of the trailing update (without and with
+  // the right-hand-side columns) and of the forward / backward solve updates
+  int strip = 0;
+  std::vector<int> strip_trail, strip_trail_rhs, strip_fwd, strip_bwd;
   int oz_capI = 0, oz_capC = 0;
   unsigned char* oz_img = nullptr;
   int* oz_exp = nullptr;
 };
+
+void setup_strip_kernels();
+int strip_items(int nI, int nC, int G);
+int strip_rows(int mode);
+// mode 0: factor trailing update (fuse_rhs: with the right-hand-side columns;
+// wide: the FP32 problems whose step is marked wide, with double-float sums);
+// 1: forward solve update; 2: backward solve update
+template <typename T>
+void launch_strip(int mode, int items, int nprob, T* env, T* rhs, const Prob* probs, Tables tb, int K, int fuse_rhs,
+                  const int* active, int* err, cudaStream_t s, bool wide);
 
 void setup_oz_kernels();
 int64_t oz_tile_bytes();

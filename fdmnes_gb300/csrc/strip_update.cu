@@ -1,0 +1,303 @@
+// strip_update.cu - tile updates of the factor and of the refinement solves on
+// the FP32 pipes, with the streamed operand tiles staged by bulk copies.
+//
+// Every update of the band LU has the form  C(I) -= A(I) B  for a run of tile
+// rows I sharing one operand tile B:
+//   factor trailing update (source/mat_solve_gaussian.f90:231-262 in tile
+//   form): A(I) = L(I,K), B = U(K,J) or the right-hand-side tile Y(K,R),
+//   C(I) = A(I,J) or Y(I,R), I in (K, Imax(K)];
+//   forward solve update: A(I) = L(I,K), B = Y(K,R), C(I) = Y(I,R);
+//   backward solve update (:348-358): A(I) = U(I,K), I in [Imin(K), K).
+// One CTA takes one B tile and up to G consecutive tile rows: B is staged once
+// (plain coalesced loads), the A tiles stream through a two-stage shared ring
+// filled by cp.async.bulk row copies that complete on an mbarrier, so the
+// next A tile is in flight while the current one is multiplied; C is read,
+// updated and written with 16-byte accesses (FP32: loaded into registers
+// before the product).  The product is register-blocked like the one-tile
+// kernels (128 threads, 8 rows x 4 columns per thread) but reads A along k
+// with 16-byte loads (row-major A, padded stride), three 16-byte shared loads
+// per 32 multiply-adds for FP32.
+//
+// Waits are bounded: a stage whose copy does not land within the limit sets
+// the problem's status word and the CTA stops after waiting (bounded) for the
+// copies it issued.
+#include <cstdint>
+#include <type_traits>
+
+#include "fdm_internal.cuh"
+#include "fdm_kernels.h"
+
+namespace fdm {
+namespace strip {
+
+constexpr int NT = 128;
+constexpr int NS = 2;  // A stages
+constexpr long long WAIT_LIMIT = 1ll << 22;
+
+// padded shared stride (elements): rows stay 16-byte aligned and the two row
+// groups a warp reads in one k step fall on different bank groups
+template <typename T> struct Stride { static constexpr int value = 68; };
+template <> struct Stride<dfl> { static constexpr int value = 66; };
+
+template <typename T>
+constexpr int smem_bytes() {
+  return (1 + NS) * TS * Stride<T>::value * (int)sizeof(T) + 64;
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity) {
+  for (long long i = 0; i < WAIT_LIMIT; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+
+// 16 bytes of consecutive elements: 4 floats or 2 double-floats
+template <typename T> struct KVec { static constexpr int value = 16 / (int)sizeof(T); };
+template <typename T>
+__device__ __forceinline__ void ldv(const T* p, T* v);
+template <>
+__device__ __forceinline__ void ldv<float>(const float* p, float* v) {
+  const float4 q = *reinterpret_cast<const float4*>(p);
+  v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+}
+template <>
+__device__ __forceinline__ void ldv<dfl>(const dfl* p, dfl* v) {
+  const float4 q = *reinterpret_cast<const float4*>(p);
+  v[0] = dfl(q.x, q.y); v[1] = dfl(q.z, q.w);
+}
+
+// Copy tile A (TS x TS, row-major in global memory) into a padded stage: warp
+// 0 only; lane 0 announces the byte count, every lane copies two rows.
+template <typename T>
+__device__ __forceinline__ void issue_tile(T* stage, const T* A, uint32_t bar) {
+  constexpr int SPS = Stride<T>::value;
+  const int lane = threadIdx.x & 31;
+  if (lane == 0) {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"((uint32_t)(TS2 * sizeof(T)))
+                 : "memory");
+  }
+  __syncwarp();
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int r = lane + 32 * h;
+    bulk_g2s(smem_u32(stage + r * SPS), A + r * TS, TS * sizeof(T), bar);
+  }
+}
+
+// MODE 0: factor trailing update (with the fused right-hand-side columns when
+// fuse_rhs); 1: forward solve update; 2: backward solve update.  Acc is the
+// accumulator type (facc: double-float sums of FP32 products); WIDE selects
+// the FP32 problems whose step K is marked for wide accumulation.
+template <typename T, int MODE, typename Acc, bool WIDE>
+__global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs, Tables tb, int K, int fuse_rhs,
+                                              int G, const int* active, int* err) {
+  constexpr int SPS = Stride<T>::value;
+  constexpr int KV = KVec<T>::value;
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (K >= P.nt || (active && !active[e])) return;
+  if (MODE == 0 && std::is_same<T, float>::value) {
+    const bool w = tb.wide && tb.wide[P.trow + K];
+    if (w != WIDE) return;
+  }
+  int i0, nI, nC, nJ = 0;
+  if (MODE == 2) {
+    i0 = tb.Imin[P.trow + K];
+    nI = K - i0;
+  } else {
+    i0 = K + 1;
+    nI = tb.Imax[P.trow + K] - K;
+  }
+  if (MODE == 0) {
+    nJ = tb.J1[P.trow + K] - K;
+    nC = nJ + (fuse_rhs ? P.nrt : 0);
+  } else {
+    nC = P.nrt;
+  }
+  if (nI <= 0) return;
+  const int nch = (nI + G - 1) / G;
+  if ((int)blockIdx.x >= nC * nch) return;
+  const int c = blockIdx.x / nch, ch = blockIdx.x % nch;
+  const int ia = i0 + ch * G;
+  const int nt = min(G, i0 + nI - ia);
+  const T* B;
+  if (MODE == 0 && c < nJ)
+    B = tile_ptr(env, P, tb, K, K + 1 + c);
+  else
+    B = rhs_ptr(rhs, P, K, MODE == 0 ? c - nJ : c);
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* Bs = reinterpret_cast<T*>(smem_raw);
+  T* As = Bs + TS * SPS;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(As + NS * TS * SPS);
+  const int t = threadIdx.x;
+  if (t == 0) {
+    for (int s = 0; s < NS; ++s) mbar_init(smem_u32(&bars[s]), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  if (t < 32)
+    for (int s = 0; s < NS && s < nt; ++s) issue_tile(As + s * TS * SPS, tile_ptr(env, P, tb, ia + s, K), smem_u32(&bars[s]));
+  // B while the first A tiles are in flight
+  for (int idx = t; idx < TS2 / 4; idx += NT) {
+    const int r = idx / (TS / 4), c4 = (idx % (TS / 4)) * 4;
+    T b[4];
+    ld4(B + r * TS + c4, b);
+    st4(Bs + r * SPS + c4, b);
+  }
+  __syncthreads();
+
+  const int tx = t % 16, ty = t / 16;
+  int issued = min(NS, nt), done = 0;
+  bool ok = true;
+  for (int it = 0; it < nt; ++it) {
+    const int s = it % NS;
+    const uint32_t parity = (uint32_t)((it / NS) & 1);
+    ok = __syncthreads_and(mbar_wait(smem_u32(&bars[s]), parity)) != 0;
+    if (!ok) break;
+    done = it + 1;
+    const int I = ia + it;
+    T* C;
+    if (MODE == 0 && c < nJ)
+      C = tile_ptr(env, P, tb, I, K + 1 + c);
+    else
+      C = rhs_ptr(rhs, P, I, MODE == 0 ? c - nJ : c);
+    // FP32: this tile's C rows in registers before the product
+    constexpr bool PF = std::is_same<T, float>::value;
+    T cv[8][4];
+    if (PF) {
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int row = i < 4 ? 4 * ty + i : 32 + 4 * ty + (i - 4);
+        ld4(C + row * TS + 4 * tx, cv[i]);
+      }
+    }
+    const T* A = As + s * TS * SPS;
+    Acc acc[8][4];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = acc_zero<Acc>();
+#pragma unroll 2
+    for (int k0 = 0; k0 < TS; k0 += KV) {
+      T a[8][KV], b[KV][4];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        const int row = i < 4 ? 4 * ty + i : 32 + 4 * ty + (i - 4);
+        ldv(A + row * SPS + k0, a[i]);
+      }
+#pragma unroll
+      for (int kk = 0; kk < KV; ++kk) ld4(Bs + (k0 + kk) * SPS + 4 * tx, b[kk]);
+#pragma unroll
+      for (int kk = 0; kk < KV; ++kk)
+#pragma unroll
+        for (int i = 0; i < 8; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) mac(acc[i][j], a[i][kk], b[kk][j]);
+    }
+    __syncthreads();  // every thread is done with stage s
+    if (t < 32 && issued < nt) {
+      issue_tile(As + s * TS * SPS, tile_ptr(env, P, tb, ia + issued, K), smem_u32(&bars[s]));
+      ++issued;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const int row = i < 4 ? 4 * ty + i : 32 + 4 * ty + (i - 4);
+      T* cp = C + row * TS + 4 * tx;
+      T v[4];
+      if (PF) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) v[j] = cv[i][j];
+      } else {
+        ld4(cp, v);
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) v[j] = acc_apply<T, Acc>(v[j], acc[i][j], true);
+      st4(cp, v);
+    }
+  }
+  if (!ok) {
+    if (t == 0) atomicExch(&err[e], (int)FDMGPU_ERR_CUDA);
+    // the copies issued but not consumed must land before the CTA leaves
+    for (int it = done; it < issued; ++it) mbar_wait(smem_u32(&bars[it % NS]), (uint32_t)((it / NS) & 1));
+  }
+}
+
+template <typename T, int MODE, typename Acc, bool WIDE>
+void set_smem() {
+  cudaFuncSetAttribute(k_strip<T, MODE, Acc, WIDE>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes<T>());
+}
+
+}  // namespace strip
+
+// Tile rows per CTA: the trailing update has ~25 rows per B tile and many B
+// tiles; the solves have few B tiles (the right-hand-side columns), so they
+// take shorter runs for more CTAs.
+constexpr int STRIP_G_TRAIL = 8;
+constexpr int STRIP_G_SOLVE = 4;
+
+int strip_items(int nI, int nC, int G) { return nI > 0 ? nC * ((nI + G - 1) / G) : 0; }
+int strip_rows(int mode) { return mode == 0 ? STRIP_G_TRAIL : STRIP_G_SOLVE; }
+
+void setup_strip_kernels() {
+  using namespace strip;
+  set_smem<float, 0, float, false>();
+  set_smem<float, 0, facc, true>();
+  set_smem<float, 1, float, false>();
+  set_smem<float, 2, float, false>();
+  set_smem<dfl, 0, dfl, false>();
+  set_smem<dfl, 1, dfl, false>();
+  set_smem<dfl, 2, dfl, false>();
+}
+
+template <typename T>
+void launch_strip(int mode, int items, int nprob, T* env, T* rhs, const Prob* probs, Tables tb, int K, int fuse_rhs,
+                  const int* active, int* err, cudaStream_t s, bool wide) {
+  using namespace strip;
+  if (items <= 0) return;
+  const dim3 grid(items, nprob);
+  const int G = strip_rows(mode);
+  const size_t sm = smem_bytes<T>();
+  if constexpr (std::is_same<T, float>::value) {
+    if (mode == 0 && wide)
+      k_strip<float, 0, facc, true><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, G, active, err);
+    else if (mode == 0)
+      k_strip<float, 0, float, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, G, active, err);
+    else if (mode == 1)
+      k_strip<float, 1, float, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, 0, G, active, err);
+    else
+      k_strip<float, 2, float, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, 0, G, active, err);
+  } else {
+    if (mode == 0)
+      k_strip<dfl, 0, dfl, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, G, active, err);
+    else if (mode == 1)
+      k_strip<dfl, 1, dfl, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, 0, G, active, err);
+    else
+      k_strip<dfl, 2, dfl, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, 0, G, active, err);
+  }
+}
+
+template void launch_strip<float>(int, int, int, float*, float*, const Prob*, Tables, int, int, const int*, int*,
+                                  cudaStream_t, bool);
+template void launch_strip<dfl>(int, int, int, dfl*, dfl*, const Prob*, Tables, int, int, const int*, int*,
+                                cudaStream_t, bool);
+
+}  // namespace fdm

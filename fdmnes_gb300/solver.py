@@ -193,10 +193,13 @@ class FdmSolver:
         _check(self.lib.fdmgpu_set_solve_order(self.h, {"columns": 0, "rows": 1}[order]))
 
     def set_tile_engine(self, engine: str = "tcgen05"):
-        """FP32 tile updates of mixed batches on the FP32 pipes ("simt"), on
-        the tensor cores as split-TF32 products ("tcgen05"), or the factor's
-        trailing update only on the tensor cores ("tcgen05_factor")."""
-        _check(self.lib.fdmgpu_set_tile_engine(self.h, {"simt": 0, "tcgen05": 1, "tcgen05_factor": 2}[engine]))
+        """FP32 tile updates of mixed batches on the FP32 pipes ("simt"), the
+        same with the streamed operand tiles staged by bulk copies
+        ("simt_stream", also the double-float updates), on the tensor cores as
+        split-TF32 products ("tcgen05"), or the factor's trailing update only
+        on the tensor cores ("tcgen05_factor")."""
+        _check(self.lib.fdmgpu_set_tile_engine(self.h, {"simt": 0, "tcgen05": 1, "tcgen05_factor": 2,
+                                                        "simt_stream": 3}[engine]))
 
     def set_autotune(self, on: bool = True):
         _check(self.lib.fdmgpu_set_autotune(self.h, 1 if on else 0))

@@ -215,8 +215,13 @@ typedef enum {
   FDMGPU_ENGINE_TCGEN05 = 1,   /* tensor cores (tcgen05.mma kind::tf32), operands split
                                   hi + lo into TF32 pairs, three products per tile pair:
                                   the accuracy of FP32 products, FP32 accumulation       */
-  FDMGPU_ENGINE_TCGEN05_FACTOR = 2 /* tensor cores for the factor's trailing update only;
+  FDMGPU_ENGINE_TCGEN05_FACTOR = 2, /* tensor cores for the factor's trailing update only;
                                   the refinement solves on the FP32 pipes                */
+  FDMGPU_ENGINE_SIMT_STREAM = 3 /* FP32 pipes, one operand tile per CTA held in shared
+                                  memory while the tiles it multiplies stream through
+                                  a two-stage ring filled by bulk copies (cp.async.bulk,
+                                  mbarrier completion); also the double-float updates
+                                  of the escalation                                     */
 } fdmgpu_tile_engine;
 
 /* Order of the triangular solves of the mixed path's refinement (the

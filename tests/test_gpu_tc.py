@@ -185,3 +185,43 @@ def test_escalation_on_tensor_cores_integer_slices(solver_mod):
     assert [r[2] for r in res["simt"]] == [r[2] for r in res["tcgen05"]]
     sv.set_df64_engine("simt")
     sv.close()
+
+
+def test_streamed_strips_match_one_tile_kernels(solver_mod, golden):
+    """The bulk-copy-staged strip updates (one shared operand tile per CTA,
+    the streamed tiles in a two-stage ring) sum every product in the same k
+    order as the one-tile kernels: the refined solutions meet the oracle bars,
+    and on full Cu energies (with escalated ones, whose double-float factor
+    and solves also run as strips, and with the wide-accumulation factor
+    mode) the spectrum agrees with the one-tile engine's to 1e-9 with the
+    same escalations."""
+    from fdmnes_gb300 import abi, cluster as CL, xanes
+    grid, energies = golden
+    sv = solver_mod.FdmSolver(grid)
+    sv.set_tile_engine("simt_stream")
+    for mode, tol in (("df64", 1e-8), ("fp64", 1e-10)):
+        sv.set_residual(mode)
+        for e in energies:
+            X, info = sv.mat_solve_args(abi.EnergyArgs(e), "mixed")
+            assert info["converged"]
+            assert rel(X, e["smr"]) < tol, (mode, rel(X, e["smr"]))
+    sv.close()
+    st = CL.cu_structure()
+    E = np.array([2.0, 14.0, 26.0, 30.0, 34.0])
+    items = xanes.spectrum_inputs(st, E)
+    sv = solver_mod.FdmSolver(st)
+    T64, _ = sv.spectrum(items, "fp64")
+    sv.set_tolerance(1e-8, 1e-6)
+    for factor in ("fp32", "wide_atom"):
+        sv.set_factor_mode(factor)
+        out = {}
+        for engine in ("simt", "simt_stream"):
+            sv.set_tile_engine(engine)
+            T, info = sv.spectrum(items, "mixed")
+            out[engine] = (T, info["n_fallback"])
+            assert xanes.convolved_relative_error(E, T, T64) < 1e-6, (factor, engine)
+        assert out["simt"][1] == out["simt_stream"][1] >= 1, factor
+        assert max(rel(a, b) for a, b in zip(out["simt"][0], out["simt_stream"][0])) < 1e-9, factor
+    sv.set_factor_mode("fp32")
+    sv.set_tile_engine("simt")
+    sv.close()
