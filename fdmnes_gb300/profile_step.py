@@ -12,7 +12,10 @@ bracketed by the NVTX range "timed", so that
     ncu --nvtx --nvtx-include "timed/" -k regex:<kernel> -c <n> ... \\
         python -m fdmnes_gb300.profile_step --energies 11
 
-captures only that step's launches.  Inputs (phiato, Bessel and Neumann
+captures only that step's launches (the kernels of the refinement loop's
+graph body are not attributed to the range; for a launch list with them, skip
+the first two runs' launches, ``kernels_per_run`` in the printed line, with
+``-s`` and capture the third run's count with ``-c``).  Inputs (phiato, Bessel and Neumann
 functions) are generated on the device, as in the benchmark.  The energies
 default to an even grid over -5..35 eV; --elist picks exact ones (the energies
 above about 22 eV are those whose FP32 refinement stalls and escalates).
@@ -60,14 +63,15 @@ def main(argv=None) -> dict:
     sv.spectrum_begin("mixed", len(E))
     for ei, ri in items:
         sv.spectrum_add(ei, ri)
-    sv.spectrum_run()
-    sv.spectrum_rerun()
+    n1 = int(sv.spectrum_run()["n_kernels"])
+    n2 = int(sv.spectrum_rerun()["n_kernels"])
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_push("timed")
     info = sv.spectrum_rerun()
     torch.cuda.synchronize()
     torch.cuda.nvtx.range_pop()
-    out = {"energies": len(E), "n_kernels": int(info["n_kernels"]), "n_fallback": int(info["n_fallback"]),
+    out = {"energies": len(E), "n_kernels": int(info["n_kernels"]), "kernels_per_run": [n1, n2, int(info["n_kernels"])],
+           "n_fallback": int(info["n_fallback"]),
            "ms": info["ms_assemble"] + info["ms_factor"] + info["ms_solve"] + info["ms_refine"],
            "phases_ms": {k: info[k] for k in ("ms_assemble", "ms_factor", "ms_solve", "ms_refine",
                                               "ms_refine_loop", "ms_escalate_factor")}}

@@ -220,7 +220,9 @@ def test_streamed_strips_match_one_tile_kernels(solver_mod, golden):
             T, info = sv.spectrum(items, "mixed")
             out[engine] = (T, info["n_fallback"])
             assert xanes.convolved_relative_error(E, T, T64) < 1e-6, (factor, engine)
-        assert out["simt"][1] == out["simt_stream"][1] >= 1, factor
+        assert out["simt"][1] == out["simt_stream"][1], factor
+        if factor == "fp32":
+            assert out["simt"][1] >= 1
         assert max(rel(a, b) for a, b in zip(out["simt"][0], out["simt_stream"][0])) < 1e-9, factor
     sv.set_factor_mode("fp32")
     sv.set_tile_engine("simt")
