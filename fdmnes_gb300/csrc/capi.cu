@@ -140,6 +140,7 @@ struct fdmgpu_handle {
   DevBuf<float2> d_lams, d_cscval2;              // Lambda as double-float pairs; A^T values
   DevBuf<int> d_colptr, d_cursor, d_cscrow;      // CSR of A^T
   DevBuf<float> d_env32, d_Y32, d_R32;
+  DevBuf<float2> d_dfl_inv;  // inverted diagonal triangles of the double-float factor (strip engine)
   DevBuf<int> d_act_df, d_act_rec;
   DevBuf<float2> d_val2, d_Xs;
   DevBuf<float> d_valS, d_V, d_W;
@@ -542,6 +543,9 @@ void build_step_plan(fdmgpu_handle* h) {
   sp.strip_trail_rhs.assign(N, 0);
   sp.strip_fwd.assign(N, 0);
   sp.strip_bwd.assign(N, 0);
+  sp.strip_panel_l.assign(N, 0);
+  sp.strip_panel_u.assign(N, 0);
+  sp.strip_panel_u_rhs.assign(N, 0);
   for (auto& hp : pr) {
     for (int K = 0; K < hp.P.nt; ++K) {
       const int nI = hp.Imax[K] - K, nJ = hp.J1[K] - K, nR = hp.P.nrt;
@@ -555,6 +559,9 @@ void build_step_plan(fdmgpu_handle* h) {
       sp.strip_trail_rhs[K] = std::max(sp.strip_trail_rhs[K], strip_items(nI, nJ + nR, strip_rows(0)));
       sp.strip_fwd[K] = std::max(sp.strip_fwd[K], strip_items(nI, nR, strip_rows(1)));
       sp.strip_bwd[K] = std::max(sp.strip_bwd[K], strip_items(K - hp.Imin[K], nR, strip_rows(2)));
+      sp.strip_panel_l[K] = std::max(sp.strip_panel_l[K], strip_items(nI, 1, strip_rows(0)));
+      sp.strip_panel_u[K] = std::max(sp.strip_panel_u[K], strip_items(nJ, 1, strip_rows(0)));
+      sp.strip_panel_u_rhs[K] = std::max(sp.strip_panel_u_rhs[K], strip_items(nJ + nR, 1, strip_rows(0)));
       sp.fwd_tc[K] = std::max(sp.fwd_tc[K], tc_items(nI, nR));
       sp.bwd_tc[K] = std::max(sp.bwd_tc[K], tc_items(K - hp.Imin[K], nR));
       sp.panel[K] = std::max(sp.panel[K], nI + nJ);
@@ -727,6 +734,12 @@ fdmgpu_status allocate_and_upload_plan(fdmgpu_handle* h, const Layout& L) {
     pl.val = h->d_val.p;
   }
   build_step_plan(h);
+  h->sp.dfl_inv = nullptr;
+  if (h->sp.strip) {
+    if (h->d_dfl_inv.reserve((size_t)np * 2 * TS2) != cudaSuccess)
+      return fail(FDMGPU_ERR_NOMEM, "inverse scratch of the double-float panel");
+    h->sp.dfl_inv = reinterpret_cast<dfl*>(h->d_dfl_inv.p);
+  }
   h->sp.oz = 0;
   h->sp.oz_img = nullptr;
   h->sp.oz_exp = nullptr;
@@ -1076,7 +1089,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
                         h->d_gstate.p, h->d_inner.p, h->d_jdone.p, h->d_notconv.p, h->d_active_gm.p,
                         h->d_nb_coef.p, h->d_rvol.p, h->d_poidsa.p, h->d_poidso.p, h->d_Kar.p, h->d_YsoT.p,
                         h->d_Ylmato.p, h->d_R32.p, h->d_act_df.p, h->d_act_rec.p, h->d_sites.p, h->d_wide.p,
-                        h->d_rads.p,  h->d_radU.p,  h->d_oz_img.p, h->d_oz_exp.p};
+                        h->d_rads.p,  h->d_radU.p,  h->d_oz_img.p, h->d_oz_exp.p, h->d_dfl_inv.p};
   for (const void* q : ptrs) ps = mix(ps, (uint64_t)(uintptr_t)q);
   if (replan && h->autotune) {
     st = tune_trailing(h);
@@ -1878,6 +1891,7 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   h->d_wide_all.release();
   h->d_oz_img.release();
   h->d_oz_exp.release();
+  h->d_dfl_inv.release();
   h->d_probs.release();
   h->d_red.release();
   if (h->h_pinned_i) cudaFreeHost(h->h_pinned_i);

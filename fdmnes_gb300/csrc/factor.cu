@@ -401,10 +401,16 @@ int launch_factor(const StepPlan& sp, T* env, T* rhs, const Prob* probs, Tables 
   int nk = 0;
   if (k_end < 0 || k_end > sp.ntmax) k_end = sp.ntmax;
   for (int K = std::max(k_begin, 0); K < k_end; ++K) {
-    k_diag<T><<<dim3(1, nprob), NTHREADS, sm, s>>>(env, probs, tb, K, active, err, piv_thr, piv);
-    ++nk;
     const int np = fuse_rhs ? sp.panel_rhs[K] : sp.panel[K];
-    if (np > 0) {
+    if (std::is_same<T, dfl>::value && sp.strip && sp.dfl_inv && piv) {
+      // double-float diagonal tile with its inverted triangles, the panel as products
+      nk += launch_dfl_panel_inv(sp, reinterpret_cast<dfl*>(env), reinterpret_cast<dfl*>(rhs), probs, tb, nprob, K,
+                                 fuse_rhs, active, err, piv_thr, piv, sp.dfl_inv, s);
+    } else {
+      k_diag<T><<<dim3(1, nprob), NTHREADS, sm, s>>>(env, probs, tb, K, active, err, piv_thr, piv);
+      ++nk;
+    }
+    if (np > 0 && !(std::is_same<T, dfl>::value && sp.strip && sp.dfl_inv && piv)) {
       k_panel<T><<<dim3(np, nprob), GEMM_THREADS, smem_bytes_panel<T>(), s>>>(env, rhs, probs, tb, K, fuse_rhs,
                                                                              active, piv);
       ++nk;

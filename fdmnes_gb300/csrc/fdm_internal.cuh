@@ -542,13 +542,14 @@ __device__ __forceinline__ void tile_mm64(T* C, const T* A, const T* B, const in
 // The factored diagonal tile sits in shared memory with stride SP.
 // -------------------------------------------------------------------------
 
-// g <- L^-1 P g (L unit lower): thread c owns column c of the tile.  Column
+// g <- L^-1 P g (L unit lower): thread c (threadIdx.x unless given) owns
+// column c of the tile.  Column
 // (axpy) order: once x[k] is final it is subtracted from every later row, so
 // the 63 - k updates of step k are independent (instruction-level parallelism
 // for the dependent double-float operations) instead of one dot-product chain.
 template <typename T>
-__device__ __forceinline__ void col_solve_lower_unit(T* g, const T* Ls, const int* perm) {
-  const int c = threadIdx.x;
+__device__ __forceinline__ void col_solve_lower_unit(T* g, const T* Ls, const int* perm, int c = -1) {
+  if (c < 0) c = threadIdx.x;
   if (c >= TS) return;
   T x[TS];
 #pragma unroll
@@ -579,8 +580,8 @@ __device__ __forceinline__ void col_solve_lower_unit(T* g, const T* Ls, const in
 // as four interleaved partial sums (independent dependency chains), combined
 // before the division.
 template <typename T>
-__device__ __forceinline__ void col_solve_upper(T* g, const T* Us) {
-  const int c = threadIdx.x;
+__device__ __forceinline__ void col_solve_upper(T* g, const T* Us, int c = -1) {
+  if (c < 0) c = threadIdx.x;
   if (c >= TS) return;
   T x[TS];
 #pragma unroll

@@ -35,6 +35,11 @@ struct StepPlan {
   // the right-hand-side columns) and of the forward / backward solve updates
   int strip = 0;
   std::vector<int> strip_trail, strip_trail_rhs, strip_fwd, strip_bwd;
+  // double-float panel as products with the inverted diagonal triangles (with
+  // the strips): CTAs per step for the L tiles and the U (+ RHS) tiles, and the
+  // per-problem inverse scratch (U^-1, L^-1)
+  std::vector<int> strip_panel_l, strip_panel_u, strip_panel_u_rhs;
+  dfl* dfl_inv = nullptr;
   int oz_capI = 0, oz_capC = 0;
   unsigned char* oz_img = nullptr;
   int* oz_exp = nullptr;
@@ -49,6 +54,10 @@ int strip_rows(int mode);
 template <typename T>
 void launch_strip(int mode, int items, int nprob, T* env, T* rhs, const Prob* probs, Tables tb, int K, int fuse_rhs,
                   const int* active, int* err, cudaStream_t s, bool wide);
+
+int launch_dfl_panel_inv(const StepPlan& sp, dfl* env, dfl* rhs, const Prob* probs, Tables tb, int nprob, int K,
+                         int fuse_rhs, const int* active, int* err, double piv_thr, int* piv, dfl* inv,
+                         cudaStream_t s);
 
 void setup_oz_kernels();
 int64_t oz_tile_bytes();

@@ -18,6 +18,15 @@
 // with 16-byte loads (row-major A, padded stride), three 16-byte shared loads
 // per 32 multiply-adds for FP32.
 //
+// The double-float factor's panel uses the same kernel on the inverted
+// triangles of the factored diagonal tile (k_diag_inv below):
+//   mode 3: L(I,K) = A(I,K) U(K,K)^-1, streamed A(I,K), fixed U^-1, in place;
+//   mode 4: U(K,J) = L(K,K)^-1 P A(K,J) (and Y(K,R) alike when the right-hand
+//           sides ride along): fixed left operand L^-1, streamed right operand
+//           whose rows the copies take in the pivot order P, in place.
+// These replace the 64-step triangular substitutions (one dependent chain per
+// thread, two warps per tile) by tile products.
+//
 // Waits are bounded: a stage whose copy does not land within the limit sets
 // the problem's status word and the CTA stops after waiting (bounded) for the
 // copies it issued.
@@ -86,7 +95,7 @@ __device__ __forceinline__ void ldv<dfl>(const dfl* p, dfl* v) {
 // Copy tile A (TS x TS, row-major in global memory) into a padded stage: warp
 // 0 only; lane 0 announces the byte count, every lane copies two rows.
 template <typename T>
-__device__ __forceinline__ void issue_tile(T* stage, const T* A, uint32_t bar) {
+__device__ __forceinline__ void issue_tile(T* stage, const T* A, uint32_t bar, const int* perm = nullptr) {
   constexpr int SPS = Stride<T>::value;
   const int lane = threadIdx.x & 31;
   if (lane == 0) {
@@ -98,19 +107,23 @@ __device__ __forceinline__ void issue_tile(T* stage, const T* A, uint32_t bar) {
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const int r = lane + 32 * h;
-    bulk_g2s(smem_u32(stage + r * SPS), A + r * TS, TS * sizeof(T), bar);
+    bulk_g2s(smem_u32(stage + r * SPS), A + (perm ? perm[r] : r) * TS, TS * sizeof(T), bar);
   }
 }
 
 // MODE 0: factor trailing update (with the fused right-hand-side columns when
-// fuse_rhs); 1: forward solve update; 2: backward solve update.  Acc is the
+// fuse_rhs); 1: forward solve update; 2: backward solve update; 3 and 4: the
+// double-float panel from the inverted diagonal triangles (inv: U^-1 then
+// L^-1 of every problem, piv: the diagonal tile's row order).  Acc is the
 // accumulator type (facc: double-float sums of FP32 products); WIDE selects
 // the FP32 problems whose step K is marked for wide accumulation.
 template <typename T, int MODE, typename Acc, bool WIDE>
 __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs, Tables tb, int K, int fuse_rhs,
-                                              int G, const int* active, int* err) {
+                                              int G, const int* active, int* err, const T* inv, const int* piv) {
   constexpr int SPS = Stride<T>::value;
   constexpr int KV = KVec<T>::value;
+  constexpr bool STREAM_B = MODE == 4;  // the streamed tiles are the right operand
+  constexpr bool SUB = MODE <= 2;       // C -= A B, else C = A B
   const int e = blockIdx.y;
   const Prob P = probs[e];
   if (K >= P.nt || (active && !active[e])) return;
@@ -118,36 +131,58 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
     const bool w = tb.wide && tb.wide[P.trow + K];
     if (w != WIDE) return;
   }
-  int i0, nI, nC, nJ = 0;
+  // n: streamed tiles of the step; nC: fixed-operand tiles (B columns, or one)
+  int i0 = 0, n, nC, nJ = 0;
   if (MODE == 2) {
     i0 = tb.Imin[P.trow + K];
-    nI = K - i0;
+    n = K - i0;
+  } else if (MODE == 4) {
+    nJ = tb.J1[P.trow + K] - K;
+    n = nJ + (fuse_rhs ? P.nrt : 0);
   } else {
     i0 = K + 1;
-    nI = tb.Imax[P.trow + K] - K;
+    n = tb.Imax[P.trow + K] - K;
   }
   if (MODE == 0) {
     nJ = tb.J1[P.trow + K] - K;
     nC = nJ + (fuse_rhs ? P.nrt : 0);
+  } else if (MODE >= 3) {
+    nC = 1;
   } else {
     nC = P.nrt;
   }
-  if (nI <= 0) return;
-  const int nch = (nI + G - 1) / G;
+  if (n <= 0) return;
+  const int nch = (n + G - 1) / G;
   if ((int)blockIdx.x >= nC * nch) return;
   const int c = blockIdx.x / nch, ch = blockIdx.x % nch;
-  const int ia = i0 + ch * G;
-  const int nt = min(G, i0 + nI - ia);
-  const T* B;
-  if (MODE == 0 && c < nJ)
-    B = tile_ptr(env, P, tb, K, K + 1 + c);
+  const int ia = ch * G;  // first streamed tile (index into the step's run)
+  const int nt = min(G, n - ia);
+  const int* prow = (MODE == 4 && piv) ? piv + P.rowv + (int64_t)K * TS : nullptr;
+  // fixed operand, streamed tile q, output tile q
+  const T* F;
+  if (MODE == 3)
+    F = inv + (int64_t)e * 2 * TS2;
+  else if (MODE == 4)
+    F = inv + (int64_t)e * 2 * TS2 + TS2;
+  else if (MODE == 0 && c < nJ)
+    F = tile_ptr(env, P, tb, K, K + 1 + c);
   else
-    B = rhs_ptr(rhs, P, K, MODE == 0 ? c - nJ : c);
+    F = rhs_ptr(rhs, P, K, MODE == 0 ? c - nJ : c);
+  auto streamed = [&](int q) -> T* {
+    if (MODE == 4) return q < nJ ? tile_ptr(env, P, tb, K, K + 1 + q) : rhs_ptr(rhs, P, K, q - nJ);
+    return tile_ptr(env, P, tb, i0 + q, K);
+  };
+  auto output = [&](int q) -> T* {
+    if (MODE >= 3) return streamed(q);
+    const int I = i0 + q;
+    if (MODE == 0 && c < nJ) return tile_ptr(env, P, tb, I, K + 1 + c);
+    return rhs_ptr(rhs, P, I, MODE == 0 ? c - nJ : c);
+  };
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* Bs = reinterpret_cast<T*>(smem_raw);
-  T* As = Bs + TS * SPS;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(As + NS * TS * SPS);
+  T* Fs = reinterpret_cast<T*>(smem_raw);
+  T* Ring = Fs + TS * SPS;
+  uint64_t* bars = reinterpret_cast<uint64_t*>(Ring + NS * TS * SPS);
   const int t = threadIdx.x;
   if (t == 0) {
     for (int s = 0; s < NS; ++s) mbar_init(smem_u32(&bars[s]), 1);
@@ -155,13 +190,13 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
   }
   __syncthreads();
   if (t < 32)
-    for (int s = 0; s < NS && s < nt; ++s) issue_tile(As + s * TS * SPS, tile_ptr(env, P, tb, ia + s, K), smem_u32(&bars[s]));
-  // B while the first A tiles are in flight
+    for (int s = 0; s < NS && s < nt; ++s) issue_tile(Ring + s * TS * SPS, streamed(ia + s), smem_u32(&bars[s]), prow);
+  // the fixed operand while the first streamed tiles are in flight
   for (int idx = t; idx < TS2 / 4; idx += NT) {
     const int r = idx / (TS / 4), c4 = (idx % (TS / 4)) * 4;
     T b[4];
-    ld4(B + r * TS + c4, b);
-    st4(Bs + r * SPS + c4, b);
+    ld4(F + r * TS + c4, b);
+    st4(Fs + r * SPS + c4, b);
   }
   __syncthreads();
 
@@ -174,14 +209,9 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
     ok = __syncthreads_and(mbar_wait(smem_u32(&bars[s]), parity)) != 0;
     if (!ok) break;
     done = it + 1;
-    const int I = ia + it;
-    T* C;
-    if (MODE == 0 && c < nJ)
-      C = tile_ptr(env, P, tb, I, K + 1 + c);
-    else
-      C = rhs_ptr(rhs, P, I, MODE == 0 ? c - nJ : c);
-    // FP32: this tile's C rows in registers before the product
-    constexpr bool PF = std::is_same<T, float>::value;
+    T* C = output(ia + it);
+    // FP32 updates: this tile's C rows in registers before the product
+    constexpr bool PF = std::is_same<T, float>::value && SUB;
     T cv[8][4];
     if (PF) {
 #pragma unroll
@@ -190,7 +220,8 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
         ld4(C + row * TS + 4 * tx, cv[i]);
       }
     }
-    const T* A = As + s * TS * SPS;
+    const T* As = STREAM_B ? Fs : Ring + s * TS * SPS;
+    const T* Bs = STREAM_B ? Ring + s * TS * SPS : Fs;
     Acc acc[8][4];
 #pragma unroll
     for (int i = 0; i < 8; ++i)
@@ -202,7 +233,7 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
 #pragma unroll
       for (int i = 0; i < 8; ++i) {
         const int row = i < 4 ? 4 * ty + i : 32 + 4 * ty + (i - 4);
-        ldv(A + row * SPS + k0, a[i]);
+        ldv(As + row * SPS + k0, a[i]);
       }
 #pragma unroll
       for (int kk = 0; kk < KV; ++kk) ld4(Bs + (k0 + kk) * SPS + 4 * tx, b[kk]);
@@ -215,7 +246,7 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
     }
     __syncthreads();  // every thread is done with stage s
     if (t < 32 && issued < nt) {
-      issue_tile(As + s * TS * SPS, tile_ptr(env, P, tb, ia + issued, K), smem_u32(&bars[s]));
+      issue_tile(Ring + s * TS * SPS, streamed(ia + issued), smem_u32(&bars[s]), prow);
       ++issued;
     }
 #pragma unroll
@@ -226,11 +257,11 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
       if (PF) {
 #pragma unroll
         for (int j = 0; j < 4; ++j) v[j] = cv[i][j];
-      } else {
+      } else if (SUB) {
         ld4(cp, v);
       }
 #pragma unroll
-      for (int j = 0; j < 4; ++j) v[j] = acc_apply<T, Acc>(v[j], acc[i][j], true);
+      for (int j = 0; j < 4; ++j) v[j] = acc_apply<T, Acc>(v[j], acc[i][j], SUB);
       st4(cp, v);
     }
   }
@@ -238,6 +269,45 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
     if (t == 0) atomicExch(&err[e], (int)FDMGPU_ERR_CUDA);
     // the copies issued but not consumed must land before the CTA leaves
     for (int it = done; it < issued; ++it) mbar_wait(smem_u32(&bars[it % NS]), (uint32_t)((it / NS) & 1));
+  }
+}
+
+// Factor the diagonal tile (K,K) of every active problem as k_diag does
+// (tile-local partial pivoting, smallest pivot checked) and write the inverses
+// of its triangles to inv (per problem U^-1, then L^-1 of the unit lower
+// triangle): column j of each inverse solves a triangular system with the
+// unit vector e_j (the substitutions of the solves), threads 0-63 for U,
+// 64-127 for L.
+template <typename T>
+__global__ void __launch_bounds__(NTHREADS) k_diag_inv(T* env, const Prob* probs, Tables tb, int K, const int* active,
+                                                       int* err, double piv_thr, int* piv, T* inv) {
+  const int e = blockIdx.y;
+  const Prob P = probs[e];
+  if (K >= P.nt || (active && !active[e])) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* D = reinterpret_cast<T*>(smem_raw);
+  __shared__ double mp;
+  __shared__ int perm[TS];
+  if (threadIdx.x < TS) perm[threadIdx.x] = threadIdx.x;
+  T* dtile = tile_ptr(env, P, tb, K, K);
+  load_tile(D, dtile);
+  __syncthreads();
+  tile_lu(D, &mp, perm);
+  __syncthreads();
+  store_tile(dtile, D);
+  if (threadIdx.x < TS) piv[P.rowv + (int64_t)K * TS + threadIdx.x] = perm[threadIdx.x];
+  if (threadIdx.x == 0 && !(mp >= piv_thr)) atomicExch(&err[e], (int)FDMGPU_ERR_ZERO_PIVOT);
+  T* Ui = inv + (int64_t)e * 2 * TS2;
+  T* Li = Ui + TS2;
+  // each thread starts its column of the identity and solves it in place
+  const int j = threadIdx.x % TS;
+  if (threadIdx.x < 2 * TS) {
+    T* g = threadIdx.x < TS ? Ui : Li;
+    for (int r = 0; r < TS; ++r) g[r * TS + j] = T(r == j ? 1.0f : 0.0f, 0.0f);
+    if (threadIdx.x < TS)
+      col_solve_upper(Ui, D, j);
+    else
+      col_solve_lower_unit(Li, D, (const int*)nullptr, j);
   }
 }
 
@@ -259,6 +329,9 @@ int strip_rows(int mode) { return mode == 0 ? STRIP_G_TRAIL : STRIP_G_SOLVE; }
 
 void setup_strip_kernels() {
   using namespace strip;
+  cudaFuncSetAttribute(k_diag_inv<dfl>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(TS * SP * sizeof(dfl)));
+  set_smem<dfl, 3, dfl, false>();
+  set_smem<dfl, 4, dfl, false>();
   set_smem<float, 0, float, false>();
   set_smem<float, 0, facc, true>();
   set_smem<float, 1, float, false>();
@@ -278,21 +351,48 @@ void launch_strip(int mode, int items, int nprob, T* env, T* rhs, const Prob* pr
   const size_t sm = smem_bytes<T>();
   if constexpr (std::is_same<T, float>::value) {
     if (mode == 0 && wide)
-      k_strip<float, 0, facc, true><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, G, active, err);
+      k_strip<float, 0, facc, true><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, G, active, err, nullptr,
+                                                         nullptr);
     else if (mode == 0)
-      k_strip<float, 0, float, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, G, active, err);
+      k_strip<float, 0, float, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, G, active, err, nullptr, nullptr);
     else if (mode == 1)
-      k_strip<float, 1, float, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, 0, G, active, err);
+      k_strip<float, 1, float, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, 0, G, active, err, nullptr, nullptr);
     else
-      k_strip<float, 2, float, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, 0, G, active, err);
+      k_strip<float, 2, float, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, 0, G, active, err, nullptr, nullptr);
   } else {
     if (mode == 0)
-      k_strip<dfl, 0, dfl, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, G, active, err);
+      k_strip<dfl, 0, dfl, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, G, active, err, nullptr, nullptr);
     else if (mode == 1)
-      k_strip<dfl, 1, dfl, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, 0, G, active, err);
+      k_strip<dfl, 1, dfl, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, 0, G, active, err, nullptr, nullptr);
     else
-      k_strip<dfl, 2, dfl, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, 0, G, active, err);
+      k_strip<dfl, 2, dfl, false><<<grid, NT, sm, s>>>(env, rhs, probs, tb, K, 0, G, active, err, nullptr, nullptr);
   }
+}
+
+// Step K of the double-float factor's diagonal tile and panel with the
+// inverted triangles: k_diag_inv, then the L tiles (mode 3) and the U and
+// right-hand-side tiles (mode 4) as products; returns the launches.
+int launch_dfl_panel_inv(const StepPlan& sp, dfl* env, dfl* rhs, const Prob* probs, Tables tb, int nprob, int K,
+                         int fuse_rhs, const int* active, int* err, double piv_thr, int* piv, dfl* inv,
+                         cudaStream_t s) {
+  using namespace strip;
+  k_diag_inv<dfl><<<dim3(1, nprob), NTHREADS, TS * SP * sizeof(dfl), s>>>(env, probs, tb, K, active, err, piv_thr,
+                                                                          piv, inv);
+  int nk = 1;
+  const size_t sm = smem_bytes<dfl>();
+  const int G = strip_rows(0);
+  const int nL = sp.strip_panel_l[K], nU = fuse_rhs ? sp.strip_panel_u_rhs[K] : sp.strip_panel_u[K];
+  if (nL > 0) {
+    k_strip<dfl, 3, dfl, false><<<dim3(nL, nprob), NT, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, G, active, err,
+                                                                inv, piv);
+    ++nk;
+  }
+  if (nU > 0) {
+    k_strip<dfl, 4, dfl, false><<<dim3(nU, nprob), NT, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, G, active, err,
+                                                                inv, piv);
+    ++nk;
+  }
+  return nk;
 }
 
 template void launch_strip<float>(int, int, int, float*, float*, const Prob*, Tables, int, int, const int*, int*,
