@@ -349,19 +349,27 @@ def run_gpu(args):
 
     # dominant phase of the step (launch list in profiles/): the double-float
     # re-factorisation of the energies FP32 refinement cannot converge
+    stream = args.tile_engine == "simt_stream"
+    if stream:
+        esc_kernels = ("k_diag_inv<dfl> + panel products k_strip<dfl, 3/4> + trailing strips k_strip<dfl, 0>",
+                       "k_strip<dfl, 0>")
+    else:
+        esc_kernels = ("k_diag/k_panel/k_trailing<dfl>", "k_trailing<dfl, 128>")
     roof_main = roof(last["flops_escalate_factor"], last["ms_escalate_factor"],
-                     "double-float escalation factor (k_diag/k_panel/k_trailing<dfl>), one launch sequence per step",
+                     f"double-float escalation factor ({esc_kernels[0]}), one launch sequence per step",
                      "runs on the FP32 pipes, ~12 FP32 instructions per double-float multiply-add; flops counted "
-                     "as 2 per multiply-add of the profile", "k_trailing<dfl, 128>")
+                     "as 2 per multiply-add of the profile", esc_kernels[1])
     roof_res = roof(last["flops_residual"], last["ms_residual_first"],
                     "k_residual_df, first refinement step (all energies active)",
                     "double-float residual on the FP32 pipes; 2 flops per CSR nonzero per right-hand side",
                     "k_residual_df")
-    fac_kernel = ("k_tc_update<0> (tcgen05 split-TF32)" if args.tile_engine != "simt" else "k_trailing<float, 128>")
+    tc = args.tile_engine in ("tcgen05", "tcgen05_factor")
+    fac_kernel = ("k_tc_update<0> (tcgen05 split-TF32)" if tc else
+                  "k_strip<float, 0>" if stream else "k_trailing<float, 128>")
     roof_fac = roof(last["flops_factor"], last["ms_factor"],
                     f"FP32 profile LU (k_diag + k_panel + {fac_kernel})",
-                    "tensor cores, three TF32 products per FP32 product" if args.tile_engine != "simt"
-                    else "FP32 SIMT pipes", fac_kernel.split(" ")[0])
+                    "tensor cores, three TF32 products per FP32 product" if tc else "FP32 SIMT pipes",
+                    fac_kernel.split(" (")[0])
     if rank != 0:
         return
     cb = cpu_baseline(min(os.cpu_count() or 1, 16)) if not args.no_cpu else None
@@ -494,9 +502,9 @@ def main():
                     help="energies of the spectrum over -5..35 eV (401: step 0.1 eV; 41: step 1 eV)")
     ap.add_argument("--factor-mode", default="fp32", choices=["fp32", "wide_atom", "wide_all"],
                     help="accumulation of the FP32 factor (wide_atom: double-float sums at the atom-harmonic steps)")
-    ap.add_argument("--tile-engine", default="simt", choices=["simt", "simt_stream", "tcgen05", "tcgen05_factor"],
+    ap.add_argument("--tile-engine", default="simt_stream", choices=["simt", "simt_stream", "tcgen05", "tcgen05_factor"],
                     help="FP32 tile updates on the FP32 pipes or on the tensor cores (split TF32)")
-    ap.add_argument("--escalation", default="df64", choices=["df64", "df64_f32", "wide_df64", "fp64"],
+    ap.add_argument("--escalation", default="df64_f32", choices=["df64", "df64_f32", "wide_df64", "fp64"],
                     help="re-solve of energies whose FP32 refinement stalls")
     ap.add_argument("--config", default="cu401", choices=["cu401", "tio2"],
                     help="cu401: the 401-energy Cu spectrum (the metric's configuration); tio2: the rutile "

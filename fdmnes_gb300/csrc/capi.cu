@@ -151,13 +151,13 @@ struct fdmgpu_handle {
   int refine_recur = 0;   // classical refinement with the residual updated by recurrence (1)
   int escalate_dfl = 1;   // escalation by a double-float (1) or an FP64 (0) factorisation
   int escalate_wide = 0;  // first a wide-accumulation FP32 re-factorisation of the stalled energies
-  int escalate_f32 = 0;   // double-float factors rounded to FP32, then FP32 refinement
+  int escalate_f32 = 1;   // double-float factors rounded to FP32, then FP32 refinement (default)
   double mem_budget = 0;  // device bytes a batch's pools may take before it runs in chunks (0: 85% of the device)
   DevBuf<unsigned char> d_wide_all;  // every step wide (the re-factorisation's table)
   int gmres_m = 12;       // Krylov dimension of one GMRES cycle
   int autotune = 1;         // time the trailing-update layouts on each new plan
   int factor_mode = 0;      // FDMGPU_FACTOR_*: wide accumulation at the atom-harmonic steps of the FP32 factor
-  int tile_engine = FDMGPU_ENGINE_SIMT;  // FDMGPU_ENGINE_*: FP32 tile updates on the FP32 pipes or the tensor cores
+  int tile_engine = FDMGPU_ENGINE_SIMT_STREAM;  // FDMGPU_ENGINE_*: FP32 tile updates (default: streamed strips)
   int solve_order = FDMGPU_SOLVE_COLUMNS;  // FDMGPU_SOLVE_*: refinement solves step by step or row by row
   int df64_engine = FDMGPU_DF64_SIMT;      // FDMGPU_DF64_*: double-float trailing update on the FP32 pipes or the tensor cores
   DevBuf<unsigned char> d_oz_img;          // integer-slice images of one factor step

@@ -148,8 +148,9 @@ class FdmSolver:
         _check(self.lib.fdmgpu_set_refinement(self.h, {"classic": 0, "gmres": 1, "recurrence": 2}[mode], krylov_dim))
 
     def set_escalation(self, mode: str = "df64"):
-        """Re-solve of energies the FP32 factors cannot refine: 'df64' (default), 'df64_overlap',
-        'wide_df64', 'df64_f32' (double-float factors rounded to FP32, FP32 refinement) or 'fp64'."""
+        """Re-solve of energies the FP32 factors cannot refine: 'df64_f32' (the library's
+        default: double-float factors rounded to FP32, FP32 refinement), 'df64'
+        (double-float refinement steps), 'df64_overlap', 'wide_df64' or 'fp64'."""
         _check(self.lib.fdmgpu_set_escalation(self.h, {"fp64": 0, "df64": 1, "df64_overlap": 2,
                                                        "wide_df64": 3, "df64_f32": 4}[mode]))
 
@@ -195,7 +196,8 @@ class FdmSolver:
     def set_tile_engine(self, engine: str = "tcgen05"):
         """FP32 tile updates of mixed batches on the FP32 pipes ("simt"), the
         same with the streamed operand tiles staged by bulk copies
-        ("simt_stream", also the double-float updates), on the tensor cores as
+        ("simt_stream", the library's default, also the double-float updates),
+        on the tensor cores as
         split-TF32 products ("tcgen05"), or the factor's trailing update only
         on the tensor cores ("tcgen05_factor")."""
         _check(self.lib.fdmgpu_set_tile_engine(self.h, {"simt": 0, "tcgen05": 1, "tcgen05_factor": 2,

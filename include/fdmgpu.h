@@ -68,20 +68,20 @@ typedef enum {
 typedef enum {
   FDMGPU_ESCALATE_FP64 = 0,    /* FP64 profile LU (no pivoting, as the reference)       */
   FDMGPU_ESCALATE_DF64 = 1,    /* double-float LU of the equilibrated matrix with
-                                  tile-local pivoting + refinement, after the FP32
-                                  refinement of every energy has ended (default)        */
+                                  tile-local pivoting + double-float refinement steps,
+                                  after the FP32 refinement of every energy has ended   */
   FDMGPU_ESCALATE_DF64_OVERLAP = 2, /* the same, started on a second stream as soon as an
                                   energy stalls, while the others keep refining         */
   FDMGPU_ESCALATE_WIDE_DF64 = 3, /* first the FP32 factor again with double-float sums in
                                   every trailing update and FP32 refinement, then
                                   double-float for the energies still stalled            */
-  FDMGPU_ESCALATE_DF64_F32 = 4 /* double-float LU (no right-hand sides), its factors
-                                  rounded to FP32 in place of the stalled FP32 factors,
-                                  then FP32 refinement steps from the current solution:
-                                  the rounded factors of an accurate LU contract the
-                                  error by about 1e-3 per step where the FP32-computed
-                                  ones stall; double-float steps for energies still
-                                  above the accepted level                               */
+  FDMGPU_ESCALATE_DF64_F32 = 4 /* (default) double-float LU (no right-hand sides), its
+                                  factors rounded to FP32 in place of the stalled FP32
+                                  factors, then FP32 refinement steps from the current
+                                  solution: the rounded factors of an accurate LU
+                                  contract the error by about 1e-3 per step where the
+                                  FP32-computed ones stall; double-float steps for
+                                  energies still above the accepted level               */
 } fdmgpu_escalation;
 
 /* Energy-independent arguments of mat_solve (source/mat_solve_gaussian.f90:17-67). */
@@ -211,13 +211,14 @@ typedef enum {
  * update of the factor, source/mat_solve_gaussian.f90:231-262 in tile form,
  * and the forward / backward updates of the refinement solves). */
 typedef enum {
-  FDMGPU_ENGINE_SIMT = 0,      /* FP32 FMA pipes, register-blocked 64x64x64 products     */
+  FDMGPU_ENGINE_SIMT = 0,      /* FP32 FMA pipes, one register-blocked 64x64x64 product
+                                  per CTA                                                */
   FDMGPU_ENGINE_TCGEN05 = 1,   /* tensor cores (tcgen05.mma kind::tf32), operands split
                                   hi + lo into TF32 pairs, three products per tile pair:
                                   the accuracy of FP32 products, FP32 accumulation       */
   FDMGPU_ENGINE_TCGEN05_FACTOR = 2, /* tensor cores for the factor's trailing update only;
                                   the refinement solves on the FP32 pipes                */
-  FDMGPU_ENGINE_SIMT_STREAM = 3 /* FP32 pipes, one operand tile per CTA held in shared
+  FDMGPU_ENGINE_SIMT_STREAM = 3 /* (default) FP32 pipes, one operand tile per CTA held in shared
                                   memory while the tiles it multiplies stream through
                                   a two-stage ring filled by bulk copies (cp.async.bulk,
                                   mbarrier completion); also the double-float updates
