@@ -104,6 +104,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t* r) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// 16 columns of one TMEM lane quarter; the caller waits (tcgen05.wait::ld) once
+// for a batch of such loads.
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
 // Operand tiles of step K: A tile a is L(K+1+a, K); B tile c is U(K, K+1+c)
 // for c < nJ, then the right-hand-side tiles Y(K, c - nJ).
 struct StepShape {
@@ -268,39 +278,59 @@ __global__ void __launch_bounds__(MMA_THREADS, 1) k_oz_mma(dfl* env, dfl* rhs, c
   }
   if (ok) ok = __syncthreads_and(mbar_wait(bar_mma, 0u)) != 0;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  // Epilogue.  The operand images are no longer read: their shared memory
+  // holds the 128 x 64 double-float products, written row per thread from the
+  // TMEM lanes, then C -= products with coalesced 16-byte accesses.
+  constexpr int SXS = TS + 1;  // staging stride in float2 (odd: conflict-free row writes)
+  float2* Sx = reinterpret_cast<float2*>(base);
   if (ok) {
-    // thread (warp, lane): accumulator row r = 32 warp + lane = row r % 64 of A tile a0 or a1
+    // thread (warp, lane): accumulator row r = 32 warp + lane
     const int r = 32 * warp + lane;
-    const int h = r >> 6, row = r & 63;
-    const bool live = h == 0 || has1;
-    const int I = K + 1 + (h == 0 ? a0 : a1);
-    dfl* C = !live ? nullptr
-                   : (c < sh.nJ ? tile_ptr(env, P, tb, I, K + 1 + c) : rhs_ptr(rhs, P, I, c - sh.nJ));
     const int er = EA[r];
-    for (int half = 0; half < 2; ++half) {
-      float hi[32], lo[32];
+    for (int q0 = 0; q0 < TS; q0 += 16) {
+      uint32_t v[SMAX - 1][16];
 #pragma unroll
-      for (int q = 0; q < 32; ++q) hi[q] = lo[q] = 0.f;
-      for (int s = SMAX; s >= 2; --s) {   // smallest order first
-        uint32_t v[32];
-        tmem_ld32(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)((s - 2) * TS + 32 * half), v);
+      for (int s = 2; s <= SMAX; ++s)
+        tmem_ld16_nowait(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)((s - 2) * TS + q0), v[s - 2]);
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-        for (int q = 0; q < 32; ++q) two_sum_acc(hi[q], lo[q], ldexpf(__uint_as_float(v[q]), er + EB[32 * half + q] - 7 * s));
+      for (int q = 0; q < 16; ++q) {
+        // sum of the orders in units of 2^(-7 SMAX), smallest first: each order
+        // scaled by 2^(7 (SMAX - s)) (exact), then one scaling to the row and
+        // column exponents
+        float hi = 0.f, lo = 0.f;
+#pragma unroll
+        for (int s = SMAX; s >= 2; --s)
+          two_sum_acc(hi, lo, __uint_as_float(v[s - 2][q]) * __int_as_float((127 + 7 * (SMAX - s)) << 23));
+        const int sc = er + EB[q0 + q] - 7 * SMAX;
+        Sx[r * SXS + q0 + q] = make_float2(ldexpf(hi, sc), ldexpf(lo, sc));
       }
-      if (C) {
-        float2* cp = reinterpret_cast<float2*>(C) + row * TS + 32 * half;
-#pragma unroll 8
-        for (int q = 0; q < 32; ++q) {
-          const float2 x = cp[q];
-          // (x.hi + x.lo) - (hi + lo) in double-float
-          const float s1 = x.x - hi[q];
-          const float bb = s1 - x.x;
-          const float err1 = (x.x - (s1 - bb)) + (-hi[q] - bb);
-          const float l = err1 + (x.y - lo[q]);
-          const float sh2 = s1 + l;
-          cp[q] = make_float2(sh2, l - (sh2 - s1));
-        }
+    }
+  }
+  __syncthreads();
+  if (ok) {
+    const int ntile = has1 ? 2 : 1;
+    for (int idx = threadIdx.x; idx < ntile * TS2 / 2; idx += MMA_THREADS) {
+      const int h = idx / (TS2 / 2), w2 = idx % (TS2 / 2);
+      const int row = w2 / (TS / 2), col = (w2 % (TS / 2)) * 2;
+      const int I = K + 1 + (h == 0 ? a0 : a1);
+      dfl* C = c < sh.nJ ? tile_ptr(env, P, tb, I, K + 1 + c) : rhs_ptr(rhs, P, I, c - sh.nJ);
+      float4* cp = reinterpret_cast<float4*>(C + row * TS + col);
+      const float4 x = *cp;
+      const float2 p0 = Sx[(64 * h + row) * SXS + col], p1 = Sx[(64 * h + row) * SXS + col + 1];
+      float2 o[2];
+      const float xh[2] = {x.x, x.z}, xl[2] = {x.y, x.w}, ph[2] = {p0.x, p1.x}, pl[2] = {p0.y, p1.y};
+#pragma unroll
+      for (int u = 0; u < 2; ++u) {
+        // (xh + xl) - (ph + pl) in double-float
+        const float s1 = xh[u] - ph[u];
+        const float bb = s1 - xh[u];
+        const float err1 = (xh[u] - (s1 - bb)) + (-ph[u] - bb);
+        const float l = err1 + (xl[u] - pl[u]);
+        const float sh2 = s1 + l;
+        o[u] = make_float2(sh2, l - (sh2 - s1));
       }
+      *cp = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
     }
   } else if (threadIdx.x == 0) {
     atomicExch(&err[e], (int)FDMGPU_ERR_CUDA);
