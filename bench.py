@@ -214,14 +214,16 @@ def run_reference(args):
 
 # ---------------------------------------------------------------- GPU arm
 def _traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` from the committed ncu capture summary
-    (profiles/traffic.json, written from `ncu --metrics dram__bytes_read.sum,
-    dram__bytes_write.sum`), or None."""
+    """DRAM bytes per launch of `kernel` at the benchmark's size from the
+    committed ncu capture summary (profiles/traffic.json: dram__bytes_read.sum
+    + dram__bytes_write.sum per launch of a small case, scaled by the problems
+    a launch processes), or None."""
     try:
         with open(os.path.join(HERE, "profiles", "traffic.json")) as f:
-            return json.load(f).get(kernel)
+            t = json.load(f).get(kernel)
     except (OSError, ValueError):
         return None
+    return t.get("bytes") if isinstance(t, dict) else t
 
 
 def run_gpu(args):

@@ -218,8 +218,8 @@ __global__ void __launch_bounds__(MMA_THREADS, 1) k_oz_mma(dfl* env, dfl* rhs, c
   int* EA = reinterpret_cast<int*>(SB + TILE_IMGS);
   int* EB = EA + 2 * TS;
   uint64_t* bars = reinterpret_cast<uint64_t*>(EB + TS);
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2);
-  const uint32_t bar_ld = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3);
+  const uint32_t bar_ld = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]), bar_c = smem_u32(&bars[2]);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned char* ia0 = img + ((int64_t)e * slot_tiles + a0) * TILE_IMGS;
   const unsigned char* ia1 = img + ((int64_t)e * slot_tiles + a1) * TILE_IMGS;
@@ -228,6 +228,7 @@ __global__ void __launch_bounds__(MMA_THREADS, 1) k_oz_mma(dfl* env, dfl* rhs, c
   if (threadIdx.x == 0) {
     mbar_init(bar_ld, 1);
     mbar_init(bar_mma, 1);
+    mbar_init(bar_c, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -279,10 +280,25 @@ __global__ void __launch_bounds__(MMA_THREADS, 1) k_oz_mma(dfl* env, dfl* rhs, c
   if (ok) ok = __syncthreads_and(mbar_wait(bar_mma, 0u)) != 0;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   // Epilogue.  The operand images are no longer read: their shared memory
-  // holds the 128 x 64 double-float products, written row per thread from the
-  // TMEM lanes, then C -= products with coalesced 16-byte accesses.
+  // receives the C tiles (bulk copies issued at once, in flight while the
+  // products are formed) and the 128 x 64 double-float products, written row
+  // per thread from the TMEM lanes; then C -= products with coalesced 16-byte
+  // stores.
   constexpr int SXS = TS + 1;  // staging stride in float2 (odd: conflict-free row writes)
   float2* Sx = reinterpret_cast<float2*>(base);
+  float4* Cs = reinterpret_cast<float4*>(base + 80 * 1024);  // two C tiles, 32 KB each
+  const int ntile = has1 ? 2 : 1;
+  auto c_tile = [&](int h) -> dfl* {
+    const int I = K + 1 + (h == 0 ? a0 : a1);
+    return c < sh.nJ ? tile_ptr(env, P, tb, I, K + 1 + c) : rhs_ptr(rhs, P, I, c - sh.nJ);
+  };
+  const bool c_armed = ok;
+  if (ok && threadIdx.x == 0) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_c),
+                 "r"((uint32_t)(ntile * TS2 * 8))
+                 : "memory");
+    for (int h = 0; h < ntile; ++h) bulk_g2s(smem_u32(Cs + h * (TS2 / 2)), c_tile(h), TS2 * 8, bar_c);
+  }
   if (ok) {
     // thread (warp, lane): accumulator row r = 32 warp + lane
     const int r = 32 * warp + lane;
@@ -307,16 +323,12 @@ __global__ void __launch_bounds__(MMA_THREADS, 1) k_oz_mma(dfl* env, dfl* rhs, c
       }
     }
   }
-  __syncthreads();
+  if (ok) ok = __syncthreads_and(mbar_wait(bar_c, 0u)) != 0;
   if (ok) {
-    const int ntile = has1 ? 2 : 1;
     for (int idx = threadIdx.x; idx < ntile * TS2 / 2; idx += MMA_THREADS) {
       const int h = idx / (TS2 / 2), w2 = idx % (TS2 / 2);
       const int row = w2 / (TS / 2), col = (w2 % (TS / 2)) * 2;
-      const int I = K + 1 + (h == 0 ? a0 : a1);
-      dfl* C = c < sh.nJ ? tile_ptr(env, P, tb, I, K + 1 + c) : rhs_ptr(rhs, P, I, c - sh.nJ);
-      float4* cp = reinterpret_cast<float4*>(C + row * TS + col);
-      const float4 x = *cp;
+      const float4 x = Cs[idx];
       const float2 p0 = Sx[(64 * h + row) * SXS + col], p1 = Sx[(64 * h + row) * SXS + col + 1];
       float2 o[2];
       const float xh[2] = {x.x, x.z}, xl[2] = {x.y, x.w}, ph[2] = {p0.x, p1.x}, pl[2] = {p0.y, p1.y};
@@ -330,10 +342,13 @@ __global__ void __launch_bounds__(MMA_THREADS, 1) k_oz_mma(dfl* env, dfl* rhs, c
         const float sh2 = s1 + l;
         o[u] = make_float2(sh2, l - (sh2 - s1));
       }
-      *cp = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+      reinterpret_cast<float4*>(c_tile(h))[w2] = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
     }
   } else if (threadIdx.x == 0) {
     atomicExch(&err[e], (int)FDMGPU_ERR_CUDA);
+    // the copies this CTA started must land before its shared memory is reused
+    mbar_wait(bar_ld, 0u);
+    if (c_armed) mbar_wait(bar_c, 0u);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
