@@ -262,6 +262,7 @@ def run_gpu(args):
     sv.set_tolerance(TOL, TOL_ACCEPT)
     sv.set_factor_mode(args.factor_mode)
     sv.set_tile_engine(args.tile_engine)
+    sv.set_df64_engine(args.df64_engine)
     sv.set_escalation(args.escalation)
 
     def barrier_sync():
@@ -352,15 +353,21 @@ def run_gpu(args):
     # dominant phase of the step (launch list in profiles/): the double-float
     # re-factorisation of the energies FP32 refinement cannot converge
     stream = args.tile_engine == "simt_stream"
-    if stream:
-        esc_kernels = ("k_diag_inv<dfl> + panel products k_strip<dfl, 3/4> + trailing strips k_strip<dfl, 0>",
-                       "k_strip<dfl, 0>")
+    oz = args.df64_engine == "tcgen05"
+    panel = "k_diag_inv<dfl> + panel products k_strip<dfl, 3/4>" if stream else "k_diag/k_panel<dfl>"
+    if oz:
+        esc_kernels = (f"{panel} + integer-slice trailing update k_oz_slice + k_oz_mma (tcgen05.mma kind::f16)",
+                       "k_oz_mma")
+        esc_note = ("trailing update on the tensor cores: 34 exact bf16 slice products per double-float product; "
+                    "flops counted as 2 per double-float multiply-add of the profile")
     else:
-        esc_kernels = ("k_diag/k_panel/k_trailing<dfl>", "k_trailing<dfl, 128>")
+        esc_kernels = (f"{panel} + trailing {'strips k_strip<dfl, 0>' if stream else 'k_trailing<dfl>'}",
+                       "k_strip<dfl, 0>" if stream else "k_trailing<dfl, 128>")
+        esc_note = ("runs on the FP32 pipes, ~12 FP32 instructions per double-float multiply-add; flops counted "
+                    "as 2 per multiply-add of the profile")
     roof_main = roof(last["flops_escalate_factor"], last["ms_escalate_factor"],
                      f"double-float escalation factor ({esc_kernels[0]}), one launch sequence per step",
-                     "runs on the FP32 pipes, ~12 FP32 instructions per double-float multiply-add; flops counted "
-                     "as 2 per multiply-add of the profile", esc_kernels[1])
+                     esc_note, esc_kernels[1])
     roof_res = roof(last["flops_residual"], last["ms_residual_first"],
                     "k_residual_df, first refinement step (all energies active)",
                     "double-float residual on the FP32 pipes; 2 flops per CSR nonzero per right-hand side",
@@ -389,7 +396,7 @@ def run_gpu(args):
                    "inputs": "phiato, Bessel and Neumann generated on the device (fdmgpu_set_radial)",
                    "l2": "working set ~100 GB per step, far above the 126 MB L2 (no flush needed)",
                    "refine_tol": TOL, "refine_tol_accept": TOL_ACCEPT, "factor_mode": args.factor_mode,
-                   "tile_engine": args.tile_engine, "escalation": args.escalation,
+                   "tile_engine": args.tile_engine, "df64_engine": args.df64_engine, "escalation": args.escalation,
                    "autotune": {"mixed": sv.tuning("mixed"), "fp64": sv.tuning("fp64")}},
         "roofline": roof_main,
         "roofline_other": [roof_res, roof_fac],
@@ -449,6 +456,7 @@ def run_tio2(args):
     main_sv = sites[0][1]
     main_sv.set_tolerance(1e-8, 1e-6)
     main_sv.set_tile_engine(args.tile_engine)
+    main_sv.set_df64_engine(args.df64_engine)
     main_sv.set_escalation(args.escalation)
 
     def run():
@@ -506,6 +514,8 @@ def main():
                     help="accumulation of the FP32 factor (wide_atom: double-float sums at the atom-harmonic steps)")
     ap.add_argument("--tile-engine", default="simt_stream", choices=["simt", "simt_stream", "tcgen05", "tcgen05_factor"],
                     help="FP32 tile updates on the FP32 pipes or on the tensor cores (split TF32)")
+    ap.add_argument("--df64-engine", default="tcgen05", choices=["simt", "tcgen05"],
+                    help="double-float escalation trailing update: FP32 pipes or tensor-core integer slices")
     ap.add_argument("--escalation", default="df64_f32", choices=["df64", "df64_f32", "wide_df64", "fp64"],
                     help="re-solve of energies whose FP32 refinement stalls")
     ap.add_argument("--config", default="cu401", choices=["cu401", "tio2"],

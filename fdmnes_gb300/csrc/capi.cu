@@ -159,7 +159,7 @@ struct fdmgpu_handle {
   int factor_mode = 0;      // FDMGPU_FACTOR_*: wide accumulation at the atom-harmonic steps of the FP32 factor
   int tile_engine = FDMGPU_ENGINE_SIMT_STREAM;  // FDMGPU_ENGINE_*: FP32 tile updates (default: streamed strips)
   int solve_order = FDMGPU_SOLVE_COLUMNS;  // FDMGPU_SOLVE_*: refinement solves step by step or row by row
-  int df64_engine = FDMGPU_DF64_SIMT;      // FDMGPU_DF64_*: double-float trailing update on the FP32 pipes or the tensor cores
+  int df64_engine = FDMGPU_DF64_TCGEN05;   // FDMGPU_DF64_*: double-float trailing update (default: tensor cores)
   DevBuf<unsigned char> d_oz_img;          // integer-slice images of one factor step
   DevBuf<int> d_oz_exp;
   DevBuf<unsigned char> d_wide;
@@ -2186,7 +2186,9 @@ static double problem_bytes(const HostProb& hp, bool mixed) {
   const double tiles = (double)hp.ntiles * TS2, rhs = (double)hp.P.nt * hp.P.nrt * TS2;
   const double rowv = (double)hp.P.nt * TS + 1;
   if (!mixed) return tiles * 8 + rhs * 16 + rowv * 4;
-  return tiles * 12 + rhs * 44 + (double)hp.nnz_cap * 24 + rowv * 28;
+  // + the integer-slice images of one step's L and U / RHS tiles (7 bf16 images a tile)
+  const double slices = (double)(hp.P.nt + hp.P.nrt) * 7 * TS2 * 2;
+  return tiles * 12 + rhs * 44 + (double)hp.nnz_cap * 24 + rowv * 28 + slices;
 }
 
 // A batch whose pools exceed the budget runs in consecutive chunks of

@@ -40,7 +40,7 @@ constexpr int SMAX = NSL + 2;                 // highest slice order kept (8 acc
 constexpr int IMG = TS * TS * 2;              // one bf16 image of a 64x64 tile: 8 KB
 constexpr int TILE_IMGS = NSL * IMG;          // 56 KB per tile
 constexpr int MMA_THREADS = 128;
-constexpr int SMEM_MMA = 2 * TILE_IMGS + TILE_IMGS + (2 * TS + TS) * 4 + 1024 + 8 * (NSL + 2) + 16;
+constexpr int SMEM_MMA = 2 * TILE_IMGS + TILE_IMGS + (2 * TS + TS) * 4 + 1024 + 64;
 constexpr int SMEM_SLICE = TS * TS * 8 + TILE_IMGS + TS * 4 + 64;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr long long WAIT_LIMIT = 1ll << 20;
@@ -217,31 +217,28 @@ __global__ void __launch_bounds__(MMA_THREADS, 1) k_oz_mma(dfl* env, dfl* rhs, c
   unsigned char* SB = SA + 2 * TILE_IMGS;       // slice j of the B tile at j * 8 KB
   int* EA = reinterpret_cast<int*>(SB + TILE_IMGS);
   int* EB = EA + 2 * TS;
-  uint64_t* bars = reinterpret_cast<uint64_t*>(EB + TS);  // NSL slice loads, MMA completion, C tiles
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + NSL + 2);
-  const uint32_t bar_ld = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[NSL]), bar_c = smem_u32(&bars[NSL + 1]);
+  uint64_t* bars = reinterpret_cast<uint64_t*>(EB + TS);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 3);
+  const uint32_t bar_ld = smem_u32(&bars[0]), bar_mma = smem_u32(&bars[1]), bar_c = smem_u32(&bars[2]);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const unsigned char* ia0 = img + ((int64_t)e * slot_tiles + a0) * TILE_IMGS;
   const unsigned char* ia1 = img + ((int64_t)e * slot_tiles + a1) * TILE_IMGS;
   const unsigned char* ib = img + ((int64_t)e * slot_tiles + capI + c) * TILE_IMGS;
 
   if (threadIdx.x == 0) {
-    for (int i = 0; i < NSL; ++i) mbar_init(bar_ld + 8 * i, 1);
+    mbar_init(bar_ld, 1);
     mbar_init(bar_mma, 1);
     mbar_init(bar_c, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    // slice i of both operands completes on its own barrier, so the products of
-    // the first slices run while the later ones are in flight
-    const uint32_t bytes = (uint32_t)((has1 ? 2 : 1) * IMG + IMG);
+    const uint32_t bytes = (uint32_t)((has1 ? 2 : 1) * TILE_IMGS + TILE_IMGS);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar_ld), "r"(bytes) : "memory");
     for (int i = 0; i < NSL; ++i) {
-      const uint32_t bar = bar_ld + 8 * i;
-      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-      bulk_g2s(smem_u32(SA + i * 2 * IMG), ia0 + i * IMG, IMG, bar);
-      if (has1) bulk_g2s(smem_u32(SA + i * 2 * IMG + IMG), ia1 + i * IMG, IMG, bar);
-      bulk_g2s(smem_u32(SB + i * IMG), ib + i * IMG, IMG, bar);
+      bulk_g2s(smem_u32(SA + i * 2 * IMG), ia0 + i * IMG, IMG, bar_ld);
+      if (has1) bulk_g2s(smem_u32(SA + i * 2 * IMG + IMG), ia1 + i * IMG, IMG, bar_ld);
+      bulk_g2s(smem_u32(SB + i * IMG), ib + i * IMG, IMG, bar_ld);
     }
   }
   if (threadIdx.x < TS) {
@@ -260,41 +257,27 @@ __global__ void __launch_bounds__(MMA_THREADS, 1) k_oz_mma(dfl* env, dfl* rhs, c
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  // one thread issues the products as the slices land: after slice m, every
-  // pair (i, j) with max(i, j) = m and order s = i + j <= SMAX, into the TMEM
-  // columns (s - 2) * 64 of order s (the first product of an order overwrites)
-  bool ok = true;
-  if (threadIdx.x == 0) {
-    bool first[SMAX + 1];
-    for (int s2 = 0; s2 <= SMAX; ++s2) first[s2] = true;
-    for (int m = 1; m <= NSL && ok; ++m) {
-      ok = mbar_wait(bar_ld + 8 * (m - 1), 0u);
-      if (!ok) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      for (int i = 1; i <= m; ++i) {
-        // pairs (i, m) and, for i < m, (m, i)
-        for (int pass = 0; pass < (i < m ? 2 : 1); ++pass) {
-          const int ia = pass ? m : i, jb = pass ? i : m;
-          const int s2 = ia + jb;
-          if (s2 > SMAX) continue;
-          const uint32_t a = smem_u32(SA + (ia - 1) * 2 * IMG), b = smem_u32(SB + (jb - 1) * IMG);
+  bool ok = __syncthreads_and(mbar_wait(bar_ld, 0u)) != 0;
+  if (ok && threadIdx.x == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    // order s = i + j (2..SMAX) accumulates in TMEM columns (s - 2) * 64
+    for (int s = 2; s <= SMAX; ++s) {
+      bool first = true;
+      for (int i = 1; i <= NSL; ++i) {
+        const int j = s - i;
+        if (j < 1 || j > NSL) continue;
+        const uint32_t a = smem_u32(SA + (i - 1) * 2 * IMG), b = smem_u32(SB + (j - 1) * IMG);
 #pragma unroll
-          for (int kk = 0; kk < TS / 16; ++kk) {
-            mma_bf16(tmem + (uint32_t)((s2 - 2) * TS), sdesc(a + kk * 256), sdesc(b + kk * 256),
-                     first[s2] ? 0u : 1u);
-            first[s2] = false;
-          }
+        for (int kk = 0; kk < TS / 16; ++kk) {
+          mma_bf16(tmem + (uint32_t)((s - 2) * TS), sdesc(a + kk * 256), sdesc(b + kk * 256), first ? 0u : 1u);
+          first = false;
         }
       }
     }
-    // committed in every case: the barrier completes once the products issued
-    // so far have finished (at once when none were), so TMEM and the operand
-    // memory are idle before anything else uses them
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar_mma)
                  : "memory");
   }
-  ok = __syncthreads_and(ok) != 0;
-  ok = (__syncthreads_and(mbar_wait(bar_mma, 0u)) != 0) && ok;
+  if (ok) ok = __syncthreads_and(mbar_wait(bar_mma, 0u)) != 0;
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   // Epilogue.  The operand images are no longer read: their shared memory
   // receives the C tiles (bulk copies issued at once, in flight while the
@@ -364,7 +347,7 @@ __global__ void __launch_bounds__(MMA_THREADS, 1) k_oz_mma(dfl* env, dfl* rhs, c
   } else if (threadIdx.x == 0) {
     atomicExch(&err[e], (int)FDMGPU_ERR_CUDA);
     // the copies this CTA started must land before its shared memory is reused
-    for (int i = 0; i < NSL; ++i) mbar_wait(bar_ld + 8 * i, 0u);
+    mbar_wait(bar_ld, 0u);
     if (c_armed) mbar_wait(bar_c, 0u);
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");

@@ -33,7 +33,7 @@ def main(argv=None) -> dict:
     ap.add_argument("--energies", type=int, default=401)
     ap.add_argument("--elist", default="", help="comma-separated energies in eV (overrides --energies)")
     ap.add_argument("--tile-engine", default="simt_stream", choices=["simt", "simt_stream", "tcgen05", "tcgen05_factor"])
-    ap.add_argument("--df64-engine", default="simt", choices=["simt", "tcgen05"])
+    ap.add_argument("--df64-engine", default="tcgen05", choices=["simt", "tcgen05"])
     ap.add_argument("--factor-mode", default="fp32", choices=["fp32", "wide_atom", "wide_all"])
     ap.add_argument("--escalation", default="df64_f32", choices=["df64", "df64_f32", "wide_df64", "fp64"])
     ap.add_argument("--solve-order", default="columns", choices=["columns", "rows"])

@@ -240,7 +240,7 @@ typedef enum {
  * factor (the energies whose FP32 refinement stalls). */
 typedef enum {
   FDMGPU_DF64_SIMT = 0,        /* FP32 pipes, about 12 instructions per multiply-add      */
-  FDMGPU_DF64_TCGEN05 = 1      /* tensor cores: rows of L and columns of U scaled by powers
+  FDMGPU_DF64_TCGEN05 = 1      /* (default) tensor cores: rows of L and columns of U scaled by powers
                                   of two and cut into seven 7-bit integer slices (exact
                                   bf16), the 34 slice pairs of orders <= 9 multiplied by
                                   tcgen05.mma kind::f16 into one FP32 accumulator per
