@@ -111,6 +111,8 @@ struct fdmgpu_handle {
   cudaEvent_t ev_join = nullptr;
   cudaEvent_t ev_esc[2 * 16] = {};  // factor start / end of up to 16 overlapped escalation batches
   DevBuf<int> d_esc_mask;
+  DevBuf<int> d_esc_list, d_err_esc;  // the escalated problems and their status words (compact launches)
+  DevBuf<Prob> d_probs_esc;
   int* h_esc_mask = nullptr;  // pinned, 16 slots of nprob ints
   size_t h_esc_mask_cap = 0;
   DevBuf<unsigned long long> d_red_esc, d_red_tmp;
@@ -1482,8 +1484,26 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
           // double-float factors rounded to FP32, then the device FP32
           // refinement loop from the current solution; the energies it leaves
           // above the accepted level take double-float steps below
-          nkern += launch_dfl_factor_f32(h->sp, h->d_probs.p, h->pl, h->tb, h->dims, D, h->stream, h->ev[8],
-                                         h->ev[9]);
+          // the factor runs over the escalated problems only (one grid row each)
+          std::vector<int> list;
+          for (int k = 0; k < np; ++k)
+            if (active[k]) list.push_back(k);
+          const int ne = (int)list.size();
+          if (h->d_esc_list.reserve(ne) != cudaSuccess || h->d_err_esc.reserve(ne) != cudaSuccess ||
+              h->d_probs_esc.reserve(ne) != cudaSuccess)
+            return fail(FDMGPU_ERR_NOMEM, "escalation descriptors");
+          CK(cudaMemcpyAsync(h->d_esc_list.p, list.data(), ne * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+          CK(cudaMemsetAsync(h->d_err_esc.p, 0, ne * sizeof(int), h->stream));
+          launch_gather_probs(h->d_probs.p, h->d_esc_list.p, ne, h->d_probs_esc.p, h->stream);
+          Pools pe = h->pl;
+          pe.active = nullptr;
+          pe.err = h->d_err_esc.p;
+          LaunchDims de = h->dims;
+          de.nprob = ne;
+          nkern += 2 + launch_dfl_factor_f32(h->sp, h->d_probs_esc.p, pe, h->tb, de, D, h->stream, h->ev[8],
+                                             h->ev[9]);
+          launch_scatter_err(h->d_esc_list.p, ne, h->d_err_esc.p, h->pl.err, h->stream);
+          CK(cudaStreamSynchronize(h->stream));  // the host list lives until here
           esc_timed = true;
           std::vector<RefineState> rs(np);
           for (int k = 0; k < np; ++k) {
@@ -1892,6 +1912,9 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   h->d_oz_img.release();
   h->d_oz_exp.release();
   h->d_dfl_inv.release();
+  h->d_esc_list.release();
+  h->d_err_esc.release();
+  h->d_probs_esc.release();
   h->d_probs.release();
   h->d_red.release();
   if (h->h_pinned_i) cudaFreeHost(h->h_pinned_i);

@@ -203,6 +203,8 @@ int gmres_max_dim();
 void launch_copy_rhs(const Prob* probs, const Pools& pl, const LaunchDims& d, cudaStream_t s);
 int launch_dfl_escalation(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
                            dfl* D, cudaStream_t s, cudaEvent_t ev_f0 = nullptr, cudaEvent_t ev_f1 = nullptr);
+void launch_gather_probs(const Prob* probs, const int* list, int n, Prob* out, cudaStream_t s);
+void launch_scatter_err(const int* list, int n, const int* err_c, int* err, cudaStream_t s);
 int launch_dfl_factor_f32(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
                           dfl* D, cudaStream_t s, cudaEvent_t ev_f0, cudaEvent_t ev_f1);
 int launch_dfl_refine_step(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,

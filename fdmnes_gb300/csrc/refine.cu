@@ -23,6 +23,43 @@ __device__ __forceinline__ void atomic_max_abs(unsigned long long* a, double v) 
   atomicMax(a, (unsigned long long)__double_as_longlong(fabs(v)));
 }
 
+// The equilibration and conversion passes read the whole FP64 band; GB300's
+// FP64 pipe is 1/64 of its FP32 rate, so they work on the bit patterns with
+// integer instructions where the result is exact: the bits of a non-negative
+// double order like its value, and scaling by a power of two 2^k is an add to
+// the exponent field while the input and the result are normal numbers (the
+// other cases take the FP64 expression, with the same result as before).
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+// the exponent k of a normal power of two 2^k
+__device__ __forceinline__ int pow2_exp(double s) { return (int)((__double_as_longlong(s) >> 52) & 0x7FF) - 1023; }
+// bits of |s x| for s = 2^k
+__device__ __forceinline__ unsigned long long scaled_abs_bits(double x, double s, int k) {
+  const unsigned long long b = abs_bits(x);
+  if (b == 0) return 0;
+  const int E = (int)(b >> 52);
+  if (E >= 1 && E + k >= 1 && E + k <= 2046) return b + ((unsigned long long)(long long)k << 52);
+  return abs_bits(s * x);
+}
+// float(sr sc x) rounded to nearest even, for sr sc = 2^k
+__device__ __forceinline__ float scaled_to_float(double x, double sr, double sc, int k) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long a = u & 0x7FFFFFFFFFFFFFFFull;
+  const unsigned sign = (unsigned)(u >> 63) << 31;
+  if (a == 0) return __uint_as_float(sign);
+  const int E = (int)(a >> 52);
+  const int e32 = E + k - 1023 + 127;
+  if (E >= 1 && e32 >= 1 && e32 <= 254) {
+    const unsigned long long M = a & 0xFFFFFFFFFFFFFull;
+    unsigned bits = ((unsigned)e32 << 23) | (unsigned)(M >> 29);
+    const unsigned long long rem = M & 0x1FFFFFFFull;
+    if (rem > 0x10000000ull || (rem == 0x10000000ull && (bits & 1u))) bits += 1u;  // a carry may reach inf
+    return __uint_as_float(bits | sign);
+  }
+  return (float)(sr * sc * x);
+}
+
 // Locate the row block of band tile w of a problem (strip has nt+1 entries).
 __device__ __forceinline__ int tile_row_of(const Tables& tb, const Prob& P, int64_t w) {
   int lo = 0, hi = P.nt - 1;
@@ -41,13 +78,13 @@ __global__ void k_rowscale(const Prob* probs, const double* env, double* rs, Tab
   if (p >= npad) return;
   const int I = p / TS;
   const int j0 = tb.J0[P.trow + I], j1 = tb.J1[P.trow + I];
-  double m = 0.0;
+  unsigned long long m = 0;
   for (int J = j0; J <= j1; ++J) {
     const double* t = tile_ptr(const_cast<double*>(env), P, tb, I, J) + (p % TS) * TS;
-    m = fmax(m, fmax(fabs(t[lane]), fabs(t[lane + 32])));
+    m = max(m, max(abs_bits(t[lane]), abs_bits(t[lane + 32])));
   }
-  for (int o = 16; o; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if (lane == 0) rs[P.rowv + p] = pow2_inv_scale(m);
+  for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) rs[P.rowv + p] = pow2_inv_scale(__longlong_as_double((long long)m));
 }
 
 // Column maxima of |rs(p) a(p,q)|: block per band tile, into colmax (double bits).
@@ -60,15 +97,18 @@ __global__ void k_colmax(const Prob* probs, const double* env, const double* rs,
   const int I = tile_row_of(tb, P, w);
   const int J = tb.J0[P.trow + I] + (int)(w - tb.strip[P.trow + I]);
   const double* t = env + P.env + w * TS2;
-  __shared__ double cm[4][TS];
+  __shared__ unsigned long long cm[4][TS];
   const int c = threadIdx.x % TS, r0 = threadIdx.x / TS;
-  double m = 0.0;
-  for (int r = r0; r < TS; r += 4) m = fmax(m, fabs(rs[P.rowv + I * TS + r] * t[r * TS + c]));
+  unsigned long long m = 0;
+  for (int r = r0; r < TS; r += 4) {
+    const double sr = rs[P.rowv + I * TS + r];
+    m = max(m, scaled_abs_bits(t[r * TS + c], sr, pow2_exp(sr)));
+  }
   cm[r0][c] = m;
   __syncthreads();
   if (threadIdx.x < TS) {
-    m = fmax(fmax(cm[0][c], cm[1][c]), fmax(cm[2][c], cm[3][c]));
-    atomic_max_abs(&colmax[P.rowv + J * TS + c], m);
+    m = max(max(cm[0][c], cm[1][c]), max(cm[2][c], cm[3][c]));
+    atomicMax(&colmax[P.rowv + J * TS + c], m);
   }
 }
 
@@ -95,7 +135,8 @@ __global__ void k_convert(const Prob* probs, const double* env64, float* env32, 
   float* o = env32 + P.env + w * TS2;
   for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) {
     const int r = idx / TS, c = idx % TS;
-    o[idx] = (float)(rs[P.rowv + I * TS + r] * cs[P.rowv + J * TS + c] * t[idx]);
+    const double sr = rs[P.rowv + I * TS + r], sc = cs[P.rowv + J * TS + c];
+    o[idx] = scaled_to_float(t[idx], sr, sc, pow2_exp(sr) + pow2_exp(sc));
   }
 }
 
@@ -119,7 +160,8 @@ __global__ void k_csr_count(const Prob* probs, const double* env, int* rowptr, T
   int cnt = 0;
   for (int J = tb.J0[P.trow + I]; J <= tb.J1[P.trow + I]; ++J) {
     const double* t = tile_ptr(const_cast<double*>(env), P, tb, I, J) + (p % TS) * TS;
-    cnt += __popc(__ballot_sync(0xffffffffu, t[lane] != 0.0)) + __popc(__ballot_sync(0xffffffffu, t[lane + 32] != 0.0));
+    cnt += __popc(__ballot_sync(0xffffffffu, abs_bits(t[lane]) != 0)) +
+           __popc(__ballot_sync(0xffffffffu, abs_bits(t[lane + 32]) != 0));
   }
   if (lane == 0) rowptr[P.rowv + p + 1] = cnt;
 }
@@ -158,8 +200,9 @@ __global__ void k_csr_fill(const Prob* probs, const double* env, const int* rowp
     const double* t = tile_ptr(const_cast<double*>(env), P, tb, I, J) + (p % TS) * TS;
     for (int h = 0; h < 2; ++h) {
       const double v = t[lane + 32 * h];
-      const unsigned bal = __ballot_sync(0xffffffffu, v != 0.0);
-      if (v != 0.0) {
+      const bool nz = abs_bits(v) != 0;
+      const unsigned bal = __ballot_sync(0xffffffffu, nz);
+      if (nz) {
         const int o = pos + __popc(bal & lower);
         if (o < P.csr_cap) {
           col[P.csr + o] = J * TS + lane + 32 * h;
@@ -489,7 +532,7 @@ __global__ void k_copy_rhs(const Prob* probs, const double* B, double* X, const 
 __global__ void k_env_to_dfl(const Prob* probs, double* env, const double* rs, const double* cs, Tables tb,
                              const int* active) {
   const Prob P = probs[blockIdx.y];
-  if (!active[blockIdx.y]) return;
+  if (active && !active[blockIdx.y]) return;
   const int64_t w = blockIdx.x;
   if (w >= tb.strip[P.trow + P.nt]) return;
   const int I = tile_row_of(tb, P, w);
@@ -506,7 +549,7 @@ __global__ void k_env_to_dfl(const Prob* probs, double* env, const double* rs, c
 __global__ void k_rhs_to_dfl(const Prob* probs, const double* B, const float* Y, const double* rs, dfl* D, int from_b,
                              const int* active) {
   const Prob P = probs[blockIdx.y];
-  if (!active[blockIdx.y]) return;
+  if (active && !active[blockIdx.y]) return;
   const int64_t w = blockIdx.x;
   if (w >= (int64_t)P.nt * P.nrt) return;
   const int I = (int)(w / P.nrt);
@@ -521,7 +564,7 @@ __global__ void k_dfl_to_x(const Prob* probs, const dfl* D, double* X, float2* X
                            unsigned long long* dmax, unsigned long long* xmax, const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
-  if (!active[e]) return;
+  if (active && !active[e]) return;
   const int64_t w = blockIdx.x;
   if (w >= (int64_t)P.nt * P.nrt) return;
   const int I = (int)(w / P.nrt);
@@ -580,7 +623,7 @@ int launch_dfl_escalation(const StepPlan& sp, const Prob* probs, const Pools& pl
 // The FP32 band <- the high parts of the double-float band (the high part of a
 // normalised double-float is its value rounded to FP32), active problems.
 __global__ void k_dfl_to_f32(const Prob* probs, const double* env, float* env32, Tables tb, const int* active) {
-  if (!active[blockIdx.y]) return;
+  if (active && !active[blockIdx.y]) return;
   const Prob P = probs[blockIdx.y];
   const int64_t w = blockIdx.x;
   if (w >= tb.strip[P.trow + P.nt]) return;
@@ -589,28 +632,47 @@ __global__ void k_dfl_to_f32(const Prob* probs, const double* env, float* env32,
   for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) o[idx] = t[idx].x;
 }
 
+// The descriptors of the listed problems, contiguous: launches over an
+// escalated subset then have one grid row per escalated problem instead of
+// one per problem of the batch.
+__global__ void k_gather_probs(const Prob* probs, const int* list, int n, Prob* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = probs[list[i]];
+}
+// Status words of a compact launch back to the batch's problems.
+__global__ void k_scatter_err(const int* list, int n, const int* err_c, int* err) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && err_c[i]) atomicExch(&err[list[i]], err_c[i]);
+}
+void launch_gather_probs(const Prob* probs, const int* list, int n, Prob* out, cudaStream_t s) {
+  k_gather_probs<<<(n + 127) / 128, 128, 0, s>>>(probs, list, n, out);
+}
+void launch_scatter_err(const int* list, int n, const int* err_c, int* err, cudaStream_t s) {
+  k_scatter_err<<<(n + 127) / 128, 128, 0, s>>>(list, n, err_c, err);
+}
+
 // Double-float factorisation of the active problems' equilibrated bands (in
-// place of their FP64 bands), its factors then rounded into the FP32 band.
-// Right-hand sides ride along only for the tensor-core update, which handles
-// them in the same launch; the double-float refinement steps that may follow
-// read the double-float factors, which stay in place.
+// place of their FP64 bands) with the right-hand sides riding along, the
+// double-float backward solve (X = the double-float solution, accurate to
+// about the acceptance level of the refinement), and the factors rounded into
+// the FP32 band for the FP32 refinement steps that confirm it; the
+// double-float refinement steps that may follow read the double-float
+// factors, which stay in place.
 int launch_dfl_factor_f32(const StepPlan& sp, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
                           dfl* D, cudaStream_t s, cudaEvent_t ev_f0, cudaEvent_t ev_f1) {
   const int np = d.nprob;
   dfl* envd = reinterpret_cast<dfl*>(pl.env64);
-  const int fuse = sp.oz ? 1 : 0;
   int nk = 0;
   k_env_to_dfl<<<dim3(d.max_tiles, np), 256, 0, s>>>(probs, pl.env64, pl.rs, pl.cs, tb, pl.active);
-  ++nk;
-  if (fuse) {
-    k_rhs_to_dfl<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, pl.B64, pl.Y32, pl.rs, D, 1, pl.active);
-    ++nk;
-  }
+  k_rhs_to_dfl<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, pl.B64, pl.Y32, pl.rs, D, 1, pl.active);
+  nk += 2;
   if (ev_f0) cudaEventRecord(ev_f0, s);
-  nk += launch_factor<dfl>(sp, envd, D, probs, tb, np, fuse, pl.active, pl.err, 1e-30, pl.piv, s);
+  nk += launch_factor<dfl>(sp, envd, D, probs, tb, np, 1, pl.active, pl.err, 1e-30, pl.piv, s);
   if (ev_f1) cudaEventRecord(ev_f1, s);
+  nk += launch_backward<dfl>(sp, envd, D, probs, tb, np, pl.active, s);
+  k_dfl_to_x<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, D, pl.X64, pl.Xs, pl.cs, 1, pl.dmax, pl.xmax, pl.active);
   k_dfl_to_f32<<<dim3(d.max_tiles, np), 256, 0, s>>>(probs, pl.env64, pl.env32, tb, pl.active);
-  return nk + 1;
+  return nk + 2;
 }
 
 // One refinement step with the double-float factors: residual, solve, x += d;

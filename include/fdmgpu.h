@@ -75,13 +75,14 @@ typedef enum {
   FDMGPU_ESCALATE_WIDE_DF64 = 3, /* first the FP32 factor again with double-float sums in
                                   every trailing update and FP32 refinement, then
                                   double-float for the energies still stalled            */
-  FDMGPU_ESCALATE_DF64_F32 = 4 /* (default) double-float LU (no right-hand sides), its
-                                  factors rounded to FP32 in place of the stalled FP32
-                                  factors, then FP32 refinement steps from the current
+  FDMGPU_ESCALATE_DF64_F32 = 4 /* (default) double-float LU and solve, the factors then
+                                  rounded to FP32 in place of the stalled FP32 factors
+                                  and FP32 refinement steps confirm the double-float
                                   solution: the rounded factors of an accurate LU
                                   contract the error by about 1e-3 per step where the
-                                  FP32-computed ones stall; double-float steps for
-                                  energies still above the accepted level               */
+                                  FP32-computed ones stall, so no double-float
+                                  refinement step is needed; double-float steps only
+                                  for energies still above the accepted level           */
 } fdmgpu_escalation;
 
 /* Energy-independent arguments of mat_solve (source/mat_solve_gaussian.f90:17-67). */
