@@ -11,7 +11,9 @@
 // One CTA takes one B tile and up to G consecutive tile rows: B is staged once
 // (plain coalesced loads), the A tiles stream through a two-stage shared ring
 // filled by cp.async.bulk row copies that complete on an mbarrier, so the
-// next A tile is in flight while the current one is multiplied; C is read,
+// next A tile is in flight while the current one is multiplied (a second
+// mbarrier per stage collects the threads' releases before warp 0 refills
+// it; no CTA-wide barrier inside the loop); C is read,
 // updated and written with 16-byte accesses (FP32: loaded into registers
 // before the product).  The product is register-blocked like the one-tile
 // kernels (128 threads, 8 rows x 4 columns per thread) but reads A along k
@@ -50,7 +52,7 @@ template <> struct Stride<dfl> { static constexpr int value = 66; };
 
 template <typename T>
 constexpr int smem_bytes() {
-  return (1 + NS) * TS * Stride<T>::value * (int)sizeof(T) + 64;
+  return (1 + NS) * TS * Stride<T>::value * (int)sizeof(T) + 16 * NS + 16;
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -182,10 +184,15 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* Fs = reinterpret_cast<T*>(smem_raw);
   T* Ring = Fs + TS * SPS;
+  // bars[s]: stage s filled (the copies' bytes); bars[NS + s]: stage s read
+  // by every thread (NT arrivals), after which warp 0 refills it
   uint64_t* bars = reinterpret_cast<uint64_t*>(Ring + NS * TS * SPS);
   const int t = threadIdx.x;
   if (t == 0) {
-    for (int s = 0; s < NS; ++s) mbar_init(smem_u32(&bars[s]), 1);
+    for (int s = 0; s < NS; ++s) {
+      mbar_init(smem_u32(&bars[s]), 1);
+      mbar_init(smem_u32(&bars[NS + s]), NT);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -200,13 +207,16 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
   }
   __syncthreads();
 
+  // No CTA barrier inside the loop: every thread waits on the stage it reads
+  // and releases it; warp 0 waits for the release before refilling, so the
+  // other warps run ahead into the next (already filled) stage.
   const int tx = t % 16, ty = t / 16;
   int issued = min(NS, nt), done = 0;
   bool ok = true;
   for (int it = 0; it < nt; ++it) {
     const int s = it % NS;
     const uint32_t parity = (uint32_t)((it / NS) & 1);
-    ok = __syncthreads_and(mbar_wait(smem_u32(&bars[s]), parity)) != 0;
+    ok = mbar_wait(smem_u32(&bars[s]), parity);
     if (!ok) break;
     done = it + 1;
     T* C = output(ia + it);
@@ -244,8 +254,15 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
 #pragma unroll
           for (int j = 0; j < 4; ++j) mac(acc[i][j], a[i][kk], b[kk][j]);
     }
-    __syncthreads();  // every thread is done with stage s
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&bars[NS + s])) : "memory");
     if (t < 32 && issued < nt) {
+      bool rel = true;
+      if (t == 0) rel = mbar_wait(smem_u32(&bars[NS + s]), parity);
+      rel = __shfl_sync(0xffffffffu, rel ? 1 : 0, 0) != 0;
+      if (!rel) {
+        ok = false;
+        break;
+      }
       issue_tile(Ring + s * TS * SPS, streamed(ia + issued), smem_u32(&bars[s]), prow);
       ++issued;
     }
@@ -266,9 +283,11 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
     }
   }
   if (!ok) {
-    if (t == 0) atomicExch(&err[e], (int)FDMGPU_ERR_CUDA);
-    // the copies issued but not consumed must land before the CTA leaves
-    for (int it = done; it < issued; ++it) mbar_wait(smem_u32(&bars[it % NS]), (uint32_t)((it / NS) & 1));
+    atomicExch(&err[e], (int)FDMGPU_ERR_CUDA);
+    // the copies warp 0 issued but no thread consumed must land before the
+    // CTA leaves (issued is exact in warp 0)
+    if (t == 0)
+      for (int it = done; it < issued; ++it) mbar_wait(smem_u32(&bars[it % NS]), (uint32_t)((it / NS) & 1));
   }
 }
 
