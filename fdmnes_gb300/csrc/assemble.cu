@@ -4,7 +4,7 @@
 // all rows of all problems of a batch at once, writing directly into the
 // reversed-order band tiles (see fdm_internal.cuh) and the RHS tiles:
 //   k_asm_grid   grid-point rows  (mat.f90:1142-1402), one warp per point
-//   k_asm_outer  outer-sphere rows (mat.f90:1405-1511)
+//   k_asm_outer_tiled, k_asm_outer_bnd  outer-sphere rows (mat.f90:1405-1511)
 //   k_asm_atom   atom-expansion rows (mat.f90:1515-1632)
 // Within every matrix entry the contributions are summed in the reference's
 // order (neighbours iv = 1..nvois; boundary points ib ascending).
@@ -100,37 +100,83 @@ __global__ void __launch_bounds__(256) k_asm_grid(const StaticDev* sites, const 
   }
 }
 
-// Outer-sphere rows: one thread per (row Lm, column Lmp) of the outer block and
-// of the right-hand side; then the boundary-point columns.
-__global__ void __launch_bounds__(256) k_asm_outer(const StaticDev* sites, const Prob* probs, const double* dpool, double* env,
-                                                   double* B, Tables tb, int* err) {
-  const int e = blockIdx.y;
+// Outer-sphere rows (mat.f90:1405-1511): the outer block and the right-hand
+// side are sums over the outer boundary points ib,
+//   A(Lm, Lmp) = sum_ib W(ib, Lm) N(ib, Lmp),  B(Lm, Lmp) = -sum_ib W(ib, Lm) J(ib, Lmp)
+// with W = poidso(ib) Y(ib, Lm), N = Y(ib, Lmp) neumann(ib, l(Lmp)) and
+// J = Y(ib, Lmp) bessel(ib, l(Lmp)): a product of two (nsortf x nlmso) panels,
+// run as a tiled FP64 product (32 x 32 outputs per block, 2 x 2 per thread,
+// the panels' 32-point chunks computed once per block into shared memory), two
+// FMAs per term; ib ascending as in the reference, the product grouped as
+// W (Y n) where the reference forms (W Y) n.
+__global__ void __launch_bounds__(256) k_asm_outer_tiled(const StaticDev* sites, const Prob* probs, const double* dpool,
+                                                         double* env, double* B, Tables tb, int* err) {
+  const int e = blockIdx.z;
   const Prob P = probs[e];
   const StaticDev& S = sites[P.site];
+  const int nlmso = P.nlmso;
+  const int m0 = blockIdx.y * 32, q0 = blockIdx.x * 32;
+  if (m0 >= nlmso || q0 >= nlmso) return;
   const int nl = P.lmaxso + 1;
   const double* bes = dpool + P.in_bes;
   const double* neu = dpool + P.in_neu;
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int nlmso = P.nlmso;
-  if (t >= nlmso * nlmso) return;
-  const int Lm = t / nlmso + 1, Lmp = t % nlmso + 1;
-  const int Lm0 = S.lso[Lm - 1] * S.lso[Lm - 1] + S.lso[Lm - 1] + 1 + S.mso[Lm - 1];
-  const int L = S.lso[Lmp - 1];
-  const int lmp0 = L * L + L + 1 + S.mso[Lmp - 1];
-  double charm = 0.0, sm = 0.0;
-  for (int ib = 1; ib <= S.nsortf; ++ib) {
-    const double* yrow = S.YsoT + (int64_t)(ib - 1) * S.nlmomax;
-    const double fac = S.poidso[ib - 1] * yrow[Lm0 - 1];
-    const double fac2 = fac * yrow[lmp0 - 1];
-    charm = charm + fac2 * neu[(int64_t)(ib - 1) * nl + L];
-    sm = sm - fac2 * bes[(int64_t)(ib - 1) * nl + L];
+  __shared__ double W[32][33], Nn[32][33], Jb[32][33];
+  const int t = threadIdx.x, tx = t % 16, ty = t / 16;
+  double an[2][2] = {{0.0, 0.0}, {0.0, 0.0}}, ab[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+  for (int ib0 = 0; ib0 < S.nsortf; ib0 += 32) {
+    for (int q = t; q < 32 * 32; q += 256) {
+      const int i = q / 32, c = q % 32, ib = ib0 + i;
+      double w = 0.0, vn = 0.0, vb = 0.0;
+      if (ib < S.nsortf) {
+        const double* yrow = S.YsoT + (int64_t)ib * S.nlmomax;
+        const int Lm = m0 + c;
+        if (Lm < nlmso) {
+          const int l = S.lso[Lm];
+          w = S.poidso[ib] * yrow[l * l + l + S.mso[Lm]];
+        }
+        const int Lmp = q0 + c;
+        if (Lmp < nlmso) {
+          const int l = S.lso[Lmp];
+          const double y = yrow[l * l + l + S.mso[Lmp]];
+          vn = y * neu[(int64_t)ib * nl + l];
+          vb = y * bes[(int64_t)ib * nl + l];
+        }
+      }
+      W[i][c] = w;
+      Nn[i][c] = vn;
+      Jb[i][c] = vb;
+    }
+    __syncthreads();
+    const int ni = min(32, S.nsortf - ib0);
+    for (int i = 0; i < ni; ++i) {
+      const double w0 = W[i][2 * ty], w1 = W[i][2 * ty + 1];
+      const double n0 = Nn[i][2 * tx], n1 = Nn[i][2 * tx + 1];
+      const double b0 = Jb[i][2 * tx], b1 = Jb[i][2 * tx + 1];
+      an[0][0] = fma(w0, n0, an[0][0]);
+      an[0][1] = fma(w0, n1, an[0][1]);
+      an[1][0] = fma(w1, n0, an[1][0]);
+      an[1][1] = fma(w1, n1, an[1][1]);
+      ab[0][0] = fma(-w0, b0, ab[0][0]);
+      ab[0][1] = fma(-w0, b1, ab[0][1]);
+      ab[1][0] = fma(-w1, b0, ab[1][0]);
+      ab[1][1] = fma(-w1, b1, ab[1][1]);
+    }
+    __syncthreads();
   }
-  const int p = P.n - (P.nligneso + Lm);
-  double* a = env_at(env, P, tb, p, P.n - (P.nligneso + Lmp), err, e);
-  if (a) *a = charm;
-  *rhs_at(B, P, p, Lmp - 1) = sm;
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      const int Lm = m0 + 2 * ty + a + 1, Lmp = q0 + 2 * tx + b + 1;
+      if (Lm > nlmso || Lmp > nlmso) continue;
+      const int p = P.n - (P.nligneso + Lm);
+      double* ap = env_at(env, P, tb, p, P.n - (P.nligneso + Lmp), err, e);
+      if (ap) *ap = an[a][b];
+      *rhs_at(B, P, p, Lmp - 1) = ab[a][b];
+    }
 }
 
+// The boundary-point columns of the outer-sphere rows.
 __global__ void __launch_bounds__(256) k_asm_outer_bnd(const StaticDev* sites, const Prob* probs, const int* ipool, double* env,
                                                        Tables tb, int* err) {
   const int e = blockIdx.y;
@@ -196,8 +242,9 @@ void launch_assemble(const StaticDev* sites, const Prob* probs, const Pools& pl,
   if (d.npr > 0)
     k_asm_grid<<<dim3((d.npr + 7) / 8, np), 256, 0, s>>>(sites, probs, pl.ipool, pl.dpool, pl.env64, pl.B64, tb,
                                                          pl.err);
-  const int nsq = d.max_nlmso * d.max_nlmso;
-  k_asm_outer<<<dim3((nsq + 255) / 256, np), 256, 0, s>>>(sites, probs, pl.dpool, pl.env64, pl.B64, tb, pl.err);
+  const int nb32 = (d.max_nlmso + 31) / 32;
+  if (nb32 > 0)
+    k_asm_outer_tiled<<<dim3(nb32, nb32, np), 256, 0, s>>>(sites, probs, pl.dpool, pl.env64, pl.B64, tb, pl.err);
   const int nb = d.max_nlmso * d.max_nsortf;
   if (nb > 0)
     k_asm_outer_bnd<<<dim3((nb + 255) / 256, np), 256, 0, s>>>(sites, probs, pl.ipool, pl.env64, tb, pl.err);
