@@ -59,6 +59,32 @@ __device__ __forceinline__ float scaled_to_float(double x, double sr, double sc,
   }
   return (float)(sr * sc * x);
 }
+// dfl(sr sc x) (high part rounded to nearest, low part the rounded remainder)
+// for sr sc = 2^k: the remainder is the low 29 mantissa bits less the rounding
+// step, an integer below 2^28 in units of the double's last place
+__device__ __forceinline__ dfl scaled_to_dfl(double x, double sr, double sc, int k) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(x);
+  const unsigned long long a = u & 0x7FFFFFFFFFFFFFFFull;
+  const unsigned neg = (unsigned)(u >> 63);
+  if (a == 0) return dfl(__uint_as_float(neg << 31), 0.f);
+  const int E = (int)(a >> 52);
+  const int e32 = E + k - 1023 + 127, sh = E + k - 1075;
+  if (E >= 1 && e32 >= 1 && e32 <= 253 && sh >= -126 && sh <= 127) {
+    const unsigned long long M = a & 0xFFFFFFFFFFFFFull;
+    const unsigned top = (unsigned)(M >> 29);
+    const int rem = (int)(M & 0x1FFFFFFFull);
+    const int up = (rem > 0x10000000 || (rem == 0x10000000 && (top & 1u))) ? 1 : 0;
+    const float hi = __uint_as_float((((unsigned)e32 << 23) | top) + (unsigned)up | (neg << 31));
+    const int r = rem - (up << 29);
+    float lo = 0.f;
+    if (r != 0) {
+      lo = __int2float_rn(r) * __uint_as_float((unsigned)(sh + 127) << 23);
+      if (neg) lo = -lo;
+    }
+    return dfl(hi, lo);
+  }
+  return dfl(sr * sc * x);
+}
 
 // Locate the row block of band tile w of a problem (strip has nt+1 entries).
 __device__ __forceinline__ int tile_row_of(const Tables& tb, const Prob& P, int64_t w) {
@@ -540,8 +566,8 @@ __global__ void k_env_to_dfl(const Prob* probs, double* env, const double* rs, c
   double* t = env + P.env + w * TS2;
   dfl* o = reinterpret_cast<dfl*>(t);
   for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) {
-    const double v = rs[P.rowv + I * TS + idx / TS] * cs[P.rowv + J * TS + idx % TS] * t[idx];
-    o[idx] = dfl(v);
+    const double sr = rs[P.rowv + I * TS + idx / TS], sc = cs[P.rowv + J * TS + idx % TS];
+    o[idx] = scaled_to_dfl(t[idx], sr, sc, pow2_exp(sr) + pow2_exp(sc));
   }
 }
 

@@ -24,7 +24,7 @@ import numpy as np
 
 from . import cluster as CL
 from . import xanes
-from .solver import FdmSolver
+from .solver import FdmError, FdmSolver
 
 
 def sigma_spectrum(st: CL.Structure, energies: Sequence[float]) -> np.ndarray:
@@ -48,14 +48,27 @@ def loss_grad(build: Callable[[float], CL.Structure], theta: float, energies: Se
     sig = np.array([xanes.absorption(t) for t in T])
     r = sig - target
     sv.vjp([xanes.absorption_cotangent(t, 2.0 * rk) for t, rk in zip(T, r)])
-    dots = []
+    # central difference of the adjoint dot product; where a grid point
+    # changes membership between theta and theta +- h (the integer structure
+    # differs, so the handle's values cannot be swapped), that side is theta
+    # itself and the difference one-sided
+    dots, steps = [], []
     for sgn in (1.0, -1.0):
         st_s = build(theta + sgn * h)
-        sv.update_grid_values(st_s)
+        try:
+            sv.update_grid_values(st_s)
+            dt = sgn * h
+        except FdmError:
+            st_s = st
+            sv.update_grid_values(st_s)
+            dt = 0.0
         sv.set_radial()
         dots.append(sv.adjoint_dot(xanes.spectrum_inputs(st_s, energies, functions=False)).sum())
+        steps.append(dt)
     sv.close()
-    return float((r ** 2).sum()), (dots[0] - dots[1]) / (2.0 * h)
+    if steps[0] == steps[1]:
+        raise FdmError(1, "the grid structure changes on both sides of theta within h")
+    return float((r ** 2).sum()), (dots[0] - dots[1]) / (steps[0] - steps[1])
 
 
 def fit(build: Callable[[float], CL.Structure], energies: Sequence[float], target: np.ndarray,
