@@ -87,6 +87,7 @@ struct Batch {
   std::vector<int> iters;
   std::vector<int> fallback;   // solved again in FP64 after the mixed path missed its tolerance
   std::vector<int> wide;       // factorised again with double-float sums in every trailing update
+  std::vector<int> res64;      // assembled again and solved by the FP64 elimination (last resort)
   std::vector<int> inner;      // GMRES steps summed over the refinement
   std::vector<double> resid;
   std::vector<int> err;
@@ -1045,6 +1046,42 @@ fdmgpu_status capture(fdmgpu_handle* h, void (*rec)(fdmgpu_handle*), cudaGraphEx
   return FDMGPU_OK;
 }
 
+// Last resort of the mixed path: the listed problems (whose FP64 bands the
+// double-float escalation has overwritten) are assembled again in FP64 and
+// solved by the FP64 elimination, as the FP64 path solves them; one grid row
+// per listed problem.  Returns the launches.
+int64_t solve_fp64_subset(fdmgpu_handle* h, const std::vector<int>& list) {
+  cudaStream_t s = h->stream;
+  Batch& b = h->batch;
+  const int ne = (int)list.size();
+  if (ne == 0) return 0;
+  if (h->d_esc_list.reserve(ne) != cudaSuccess || h->d_err_esc.reserve(ne) != cudaSuccess ||
+      h->d_probs_esc.reserve(ne) != cudaSuccess)
+    return -1;
+  for (int k : list) {
+    const HostProb& hp = b.probs[k];
+    cudaMemsetAsync(h->pl.env64 + hp.P.env, 0, (size_t)hp.ntiles * TS2 * sizeof(double), s);
+    cudaMemsetAsync(h->pl.B64 + hp.P.rhs, 0, (size_t)hp.P.nt * hp.P.nrt * TS2 * sizeof(double), s);
+  }
+  cudaMemcpyAsync(h->d_esc_list.p, list.data(), ne * sizeof(int), cudaMemcpyHostToDevice, s);
+  cudaMemsetAsync(h->d_err_esc.p, 0, ne * sizeof(int), s);
+  launch_gather_probs(h->d_probs.p, h->d_esc_list.p, ne, h->d_probs_esc.p, s);
+  Pools pf = h->pl;
+  pf.err = h->d_err_esc.p;
+  pf.active = nullptr;
+  LaunchDims df = h->dims;
+  df.nprob = ne;
+  launch_assemble(h->d_sites.p, h->d_probs_esc.p, pf, h->tb, df, s);
+  launch_copy_rhs(h->d_probs_esc.p, pf, df, s);
+  int64_t nk = 8;
+  nk += launch_factor<double>(h->sp, h->pl.env64, h->pl.X64, h->d_probs_esc.p, h->tb, ne, 1, nullptr,
+                              h->d_err_esc.p, 1e-10, nullptr, s);
+  nk += launch_backward<double>(h->sp, h->pl.env64, h->pl.X64, h->d_probs_esc.p, h->tb, ne, nullptr, s);
+  launch_scatter_err(h->d_esc_list.p, ne, h->d_err_esc.p, h->pl.err, s);
+  cudaStreamSynchronize(s);  // the host list lives until here
+  return nk;
+}
+
 fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   Batch& b = h->batch;
   const int np = (int)b.probs.size();
@@ -1129,6 +1166,7 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
   b.iters.assign(np, 0);
   b.fallback.assign(np, 0);
   b.wide.assign(np, 0);
+  b.res64.assign(np, 0);
   b.inner.assign(np, 0);
   b.resid.assign(np, 0.0);
   b.err.assign(np, 0);
@@ -1561,6 +1599,20 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
             }
           if (!more) break;
           CK(cudaMemcpyAsync(h->d_active.p, act2.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
+        }
+        // energies still above the accepted level: FP64 assembly and elimination
+        std::vector<int> last;
+        for (int k = 0; k < np; ++k)
+          if (act2[k]) last.push_back(k);
+        if (!last.empty() && b.cplx != 1) {
+          const int64_t nk64 = solve_fp64_subset(h, last);
+          if (nk64 < 0) return fail(FDMGPU_ERR_NOMEM, "FP64 re-solve descriptors");
+          CK(cudaGetLastError());
+          nkern += nk64;
+          for (int k : last) {
+            b.resid[k] = 0.0;  // direct FP64 solve, no correction measured
+            b.res64[k] = 1;
+          }
         }
       } else {
         launch_copy_rhs(h->d_probs.p, h->pl, h->dims, h->stream);
@@ -2511,6 +2563,8 @@ fdmgpu_status fdmgpu_batch_vjp(fdmgpu_handle* h, const double* gtaull, double* g
   for (int k = 0; k < np; ++k) {
     if (b.probs[k].P.nlm_abs <= 0) return fail(FDMGPU_ERR_ARG, "vjp needs an absorber (iaabs > 0) in every energy");
     if (b.err[k]) return fail((fdmgpu_status)b.err[k], "vjp of a batch with a failed energy");
+    if (b.precision == FDMGPU_PREC_MIXED && k < (int)b.res64.size() && b.res64[k])
+      return fail(FDMGPU_ERR_UNSUPPORTED, "vjp of a mixed batch with an energy re-solved in FP64 (run it in FP64)");
   }
   cudaStream_t s = h->stream;
   int64_t ntaull = 0, nrhs = 0;

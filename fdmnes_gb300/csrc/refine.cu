@@ -547,7 +547,7 @@ void launch_update_x(const Prob* probs, const Pools& pl, const LaunchDims& d, in
 __global__ void k_copy_rhs(const Prob* probs, const double* B, double* X, const int* active) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
-  if (!active[e]) return;
+  if (active && !active[e]) return;
   const int64_t w = blockIdx.x;
   if (w >= (int64_t)P.nt * P.nrt) return;
   for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) X[P.rhs + w * TS2 + idx] = B[P.rhs + w * TS2 + idx];

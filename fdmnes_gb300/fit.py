@@ -47,7 +47,16 @@ def loss_grad(build: Callable[[float], CL.Structure], theta: float, energies: Se
     T, _ = sv.spectrum(items, precision)
     sig = np.array([xanes.absorption(t) for t in T])
     r = sig - target
-    sv.vjp([xanes.absorption_cotangent(t, 2.0 * rk) for t, rk in zip(T, r)])
+    try:
+        sv.vjp([xanes.absorption_cotangent(t, 2.0 * rk) for t, rk in zip(T, r)])
+    except FdmError:
+        # a mixed batch with an energy the mixed path could not refine (left
+        # unconverged or re-solved in FP64) has no mixed adjoint: this step
+        # runs in FP64
+        T, _ = sv.spectrum(items, "fp64")
+        sig = np.array([xanes.absorption(t) for t in T])
+        r = sig - target
+        sv.vjp([xanes.absorption_cotangent(t, 2.0 * rk) for t, rk in zip(T, r)])
     # central difference of the adjoint dot product; where a grid point
     # changes membership between theta and theta +- h (the integer structure
     # differs, so the handle's values cannot be swapped), that side is theta

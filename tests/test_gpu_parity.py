@@ -212,16 +212,25 @@ def test_two_sites_in_one_batch(solver_mod, oracle_lib):
 
 def test_unreachable_tolerance_is_reported(solver_mod, golden):
     """A refinement tolerance below what double-float arithmetic can reach
-    (1e-17) is reported per energy as not converged, after escalation, and the
-    solution is still the escalated one (1e-8 of the oracle)."""
+    (1e-17): with the double-float escalation steps (`df64`) the energy is
+    reported as not converged and keeps the escalated solution (1e-8 of the
+    oracle); with the default escalation the energy the double-float steps
+    leave above the level is assembled again and solved by the FP64
+    elimination, the FP64 path's solution (1e-10 of the oracle)."""
     from fdmnes_gb300 import abi
     grid, energies = golden
     sv = solver_mod.FdmSolver(grid)
     sv.set_tolerance(1e-17, 1e-17)
+    sv.set_escalation("df64")
     X, info = sv.mat_solve_args(abi.EnergyArgs(energies[0]), "mixed")
     assert not info["converged"]
     assert info["n_fallback"] == 1
     assert rel(X, energies[0]["smr"]) < 1e-8
+    sv.set_escalation("df64_f32")
+    X, info = sv.mat_solve_args(abi.EnergyArgs(energies[0]), "mixed")
+    assert info["converged"]
+    assert info["n_fallback"] == 1
+    assert rel(X, energies[0]["smr"]) < 1e-10
     sv.set_tolerance(0.0, 0.0)
     X, info = sv.mat_solve_args(abi.EnergyArgs(energies[0]), "mixed")
     assert info["converged"]
