@@ -1600,11 +1600,12 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
           if (!more) break;
           CK(cudaMemcpyAsync(h->d_active.p, act2.data(), np * sizeof(int), cudaMemcpyHostToDevice, h->stream));
         }
-        // energies still above the accepted level: FP64 assembly and elimination
+        // default escalation: energies still above the accepted level get the
+        // FP64 assembly and elimination (FDMGPU_ESCALATE_DF64 reports them)
         std::vector<int> last;
         for (int k = 0; k < np; ++k)
           if (act2[k]) last.push_back(k);
-        if (!last.empty() && b.cplx != 1) {
+        if (h->escalate_f32 && !last.empty() && b.cplx != 1) {
           const int64_t nk64 = solve_fp64_subset(h, last);
           if (nk64 < 0) return fail(FDMGPU_ERR_NOMEM, "FP64 re-solve descriptors");
           CK(cudaGetLastError());
