@@ -114,6 +114,7 @@ struct fdmgpu_handle {
   DevBuf<int> d_esc_mask;
   DevBuf<int> d_esc_list, d_err_esc;  // the escalated problems and their status words (compact launches)
   DevBuf<Prob> d_probs_esc;
+  DevBuf<float2> d_uinv_keep;  // U^-1 of every step of the escalation factor (strip engine)
   int* h_esc_mask = nullptr;  // pinned, 16 slots of nprob ints
   size_t h_esc_mask_cap = 0;
   DevBuf<unsigned long long> d_red_esc, d_red_tmp;
@@ -1538,8 +1539,14 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
           pe.err = h->d_err_esc.p;
           LaunchDims de = h->dims;
           de.nprob = ne;
+          // with the strips, the factor keeps every step's U^-1 and the
+          // double-float solve multiplies by them (compact problem order)
+          if (h->sp.strip && h->sp.dfl_inv &&
+              h->d_uinv_keep.reserve((size_t)ne * h->sp.ntmax * TS2) == cudaSuccess)
+            h->sp.dfl_uinv_keep = reinterpret_cast<dfl*>(h->d_uinv_keep.p);
           nkern += 2 + launch_dfl_factor_f32(h->sp, h->d_probs_esc.p, pe, h->tb, de, D, h->stream, h->ev[8],
                                              h->ev[9]);
+          h->sp.dfl_uinv_keep = nullptr;
           launch_scatter_err(h->d_esc_list.p, ne, h->d_err_esc.p, h->pl.err, h->stream);
           CK(cudaStreamSynchronize(h->stream));  // the host list lives until here
           esc_timed = true;
@@ -1968,6 +1975,7 @@ void fdmgpu_destroy(fdmgpu_handle* h) {
   h->d_esc_list.release();
   h->d_err_esc.release();
   h->d_probs_esc.release();
+  h->d_uinv_keep.release();
   h->d_probs.release();
   h->d_red.release();
   if (h->h_pinned_i) cudaFreeHost(h->h_pinned_i);

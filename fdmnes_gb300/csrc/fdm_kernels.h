@@ -40,6 +40,9 @@ struct StepPlan {
   // per-problem inverse scratch (U^-1, L^-1)
   std::vector<int> strip_panel_l, strip_panel_u, strip_panel_u_rhs;
   dfl* dfl_inv = nullptr;
+  // U^-1 of every step of the last double-float factorisation (ntmax tiles a
+  // problem), when the caller keeps them for a backward solve
+  dfl* dfl_uinv_keep = nullptr;
   int oz_capI = 0, oz_capC = 0;
   unsigned char* oz_img = nullptr;
   int* oz_exp = nullptr;
@@ -55,6 +58,8 @@ template <typename T>
 void launch_strip(int mode, int items, int nprob, T* env, T* rhs, const Prob* probs, Tables tb, int K, int fuse_rhs,
                   const int* active, int* err, cudaStream_t s, bool wide);
 
+int launch_dfl_backward_inv(const StepPlan& sp, dfl* env, dfl* rhs, const Prob* probs, Tables tb, int nprob,
+                            const int* active, int* err, cudaStream_t s);
 int launch_dfl_panel_inv(const StepPlan& sp, dfl* env, dfl* rhs, const Prob* probs, Tables tb, int nprob, int K,
                          int fuse_rhs, const int* active, int* err, double piv_thr, int* piv, dfl* inv,
                          cudaStream_t s);

@@ -695,7 +695,10 @@ int launch_dfl_factor_f32(const StepPlan& sp, const Prob* probs, const Pools& pl
   if (ev_f0) cudaEventRecord(ev_f0, s);
   nk += launch_factor<dfl>(sp, envd, D, probs, tb, np, 1, pl.active, pl.err, 1e-30, pl.piv, s);
   if (ev_f1) cudaEventRecord(ev_f1, s);
-  nk += launch_backward<dfl>(sp, envd, D, probs, tb, np, pl.active, s);
+  if (sp.strip && sp.dfl_uinv_keep)
+    nk += launch_dfl_backward_inv(sp, envd, D, probs, tb, np, pl.active, pl.err, s);
+  else
+    nk += launch_backward<dfl>(sp, envd, D, probs, tb, np, pl.active, s);
   k_dfl_to_x<<<dim3(d.max_rhs_tiles, np), 256, 0, s>>>(probs, D, pl.X64, pl.Xs, pl.cs, 1, pl.dmax, pl.xmax, pl.active);
   k_dfl_to_f32<<<dim3(d.max_tiles, np), 256, 0, s>>>(probs, pl.env64, pl.env32, tb, pl.active);
   return nk + 2;

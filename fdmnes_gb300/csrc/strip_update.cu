@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
                                               int G, const int* active, int* err, const T* inv, const int* piv) {
   constexpr int SPS = Stride<T>::value;
   constexpr int KV = KVec<T>::value;
-  constexpr bool STREAM_B = MODE == 4;  // the streamed tiles are the right operand
+  constexpr bool STREAM_B = MODE >= 4;  // the streamed tiles are the right operand
   constexpr bool SUB = MODE <= 2;       // C -= A B, else C = A B
   const int e = blockIdx.y;
   const Prob P = probs[e];
@@ -141,6 +141,8 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
   } else if (MODE == 4) {
     nJ = tb.J1[P.trow + K] - K;
     n = nJ + (fuse_rhs ? P.nrt : 0);
+  } else if (MODE == 5) {
+    n = P.nrt;
   } else {
     i0 = K + 1;
     n = tb.Imax[P.trow + K] - K;
@@ -166,11 +168,14 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
     F = inv + (int64_t)e * 2 * TS2;
   else if (MODE == 4)
     F = inv + (int64_t)e * 2 * TS2 + TS2;
+  else if (MODE == 5)
+    F = inv + ((int64_t)e * fuse_rhs + K) * TS2;  // fuse_rhs carries the slots per problem
   else if (MODE == 0 && c < nJ)
     F = tile_ptr(env, P, tb, K, K + 1 + c);
   else
     F = rhs_ptr(rhs, P, K, MODE == 0 ? c - nJ : c);
   auto streamed = [&](int q) -> T* {
+    if (MODE == 5) return rhs_ptr(rhs, P, K, q);
     if (MODE == 4) return q < nJ ? tile_ptr(env, P, tb, K, K + 1 + q) : rhs_ptr(rhs, P, K, q - nJ);
     return tile_ptr(env, P, tb, i0 + q, K);
   };
@@ -299,7 +304,8 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
 // 64-127 for L.
 template <typename T>
 __global__ void __launch_bounds__(NTHREADS) k_diag_inv(T* env, const Prob* probs, Tables tb, int K, const int* active,
-                                                       int* err, double piv_thr, int* piv, T* inv) {
+                                                       int* err, double piv_thr, int* piv, T* inv, T* keep,
+                                                       int keep_slots) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
   if (K >= P.nt || (active && !active[e])) return;
@@ -328,6 +334,12 @@ __global__ void __launch_bounds__(NTHREADS) k_diag_inv(T* env, const Prob* probs
     else
       col_solve_lower_unit(Li, D, (const int*)nullptr, j);
   }
+  if (keep) {
+    // U^-1 of every step, for the backward solve with these factors
+    __syncthreads();
+    T* k = keep + ((int64_t)e * keep_slots + K) * TS2;
+    for (int idx = threadIdx.x; idx < TS2; idx += blockDim.x) k[idx] = Ui[idx];
+  }
 }
 
 template <typename T, int MODE, typename Acc, bool WIDE>
@@ -351,6 +363,7 @@ void setup_strip_kernels() {
   cudaFuncSetAttribute(k_diag_inv<dfl>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(TS * SP * sizeof(dfl)));
   set_smem<dfl, 3, dfl, false>();
   set_smem<dfl, 4, dfl, false>();
+  set_smem<dfl, 5, dfl, false>();
   set_smem<float, 0, float, false>();
   set_smem<float, 0, facc, true>();
   set_smem<float, 1, float, false>();
@@ -396,7 +409,7 @@ int launch_dfl_panel_inv(const StepPlan& sp, dfl* env, dfl* rhs, const Prob* pro
                          cudaStream_t s) {
   using namespace strip;
   k_diag_inv<dfl><<<dim3(1, nprob), NTHREADS, TS * SP * sizeof(dfl), s>>>(env, probs, tb, K, active, err, piv_thr,
-                                                                          piv, inv);
+                                                                          piv, inv, sp.dfl_uinv_keep, sp.ntmax);
   int nk = 1;
   const size_t sm = smem_bytes<dfl>();
   const int G = strip_rows(0);
@@ -410,6 +423,27 @@ int launch_dfl_panel_inv(const StepPlan& sp, dfl* env, dfl* rhs, const Prob* pro
     k_strip<dfl, 4, dfl, false><<<dim3(nU, nprob), NT, sm, s>>>(env, rhs, probs, tb, K, fuse_rhs, G, active, err,
                                                                 inv, piv);
     ++nk;
+  }
+  return nk;
+}
+
+// Backward solve with the double-float factors of the last factorisation,
+// whose U^-1 tiles were kept (sp.dfl_uinv_keep, the same problem order):
+// per step K from the last, Y(K,R) = U(K,K)^-1 Y(K,R) as products (mode 5),
+// then the update strips Y(I,R) -= U(I,K) Y(K,R).
+int launch_dfl_backward_inv(const StepPlan& sp, dfl* env, dfl* rhs, const Prob* probs, Tables tb, int nprob,
+                            const int* active, int* err, cudaStream_t s) {
+  using namespace strip;
+  const size_t sm = smem_bytes<dfl>();
+  int nk = 0;
+  for (int K = sp.ntmax - 1; K >= 0; --K) {
+    k_strip<dfl, 5, dfl, false><<<dim3(strip_items(sp.nrtmax, 1, strip_rows(1)), nprob), NT, sm, s>>>(
+        env, rhs, probs, tb, K, sp.ntmax, strip_rows(1), active, err, sp.dfl_uinv_keep, nullptr);
+    ++nk;
+    if (sp.strip_bwd[K] > 0) {
+      launch_strip<dfl>(2, sp.strip_bwd[K], nprob, env, rhs, probs, tb, K, 0, active, err, s, false);
+      ++nk;
+    }
   }
   return nk;
 }
