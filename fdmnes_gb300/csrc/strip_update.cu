@@ -114,13 +114,15 @@ __device__ __forceinline__ void issue_tile(T* stage, const T* A, uint32_t bar, c
 }
 
 // MODE 0: factor trailing update (with the fused right-hand-side columns when
-// fuse_rhs); 1: forward solve update; 2: backward solve update; 3 and 4: the
+// aux != 0); 1: forward solve update; 2: backward solve update; 3 and 4: the
 // double-float panel from the inverted diagonal triangles (inv: U^-1 then
-// L^-1 of every problem, piv: the diagonal tile's row order).  Acc is the
+// L^-1 of every problem, piv: the diagonal tile's row order; MODE 4 with the
+// right-hand sides when aux != 0); 5: Y(K,R) = U(K,K)^-1 Y(K,R) with the kept
+// inverses (inv: aux tiles a problem, one per step).  Acc is the
 // accumulator type (facc: double-float sums of FP32 products); WIDE selects
 // the FP32 problems whose step K is marked for wide accumulation.
 template <typename T, int MODE, typename Acc, bool WIDE>
-__global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs, Tables tb, int K, int fuse_rhs,
+__global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs, Tables tb, int K, int aux,
                                               int G, const int* active, int* err, const T* inv, const int* piv) {
   constexpr int SPS = Stride<T>::value;
   constexpr int KV = KVec<T>::value;
@@ -140,7 +142,7 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
     n = K - i0;
   } else if (MODE == 4) {
     nJ = tb.J1[P.trow + K] - K;
-    n = nJ + (fuse_rhs ? P.nrt : 0);
+    n = nJ + (aux ? P.nrt : 0);
   } else if (MODE == 5) {
     n = P.nrt;
   } else {
@@ -149,7 +151,7 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
   }
   if (MODE == 0) {
     nJ = tb.J1[P.trow + K] - K;
-    nC = nJ + (fuse_rhs ? P.nrt : 0);
+    nC = nJ + (aux ? P.nrt : 0);
   } else if (MODE >= 3) {
     nC = 1;
   } else {
@@ -169,7 +171,7 @@ __global__ void __launch_bounds__(NT) k_strip(T* env, T* rhs, const Prob* probs,
   else if (MODE == 4)
     F = inv + (int64_t)e * 2 * TS2 + TS2;
   else if (MODE == 5)
-    F = inv + ((int64_t)e * fuse_rhs + K) * TS2;  // fuse_rhs carries the slots per problem
+    F = inv + ((int64_t)e * aux + K) * TS2;
   else if (MODE == 0 && c < nJ)
     F = tile_ptr(env, P, tb, K, K + 1 + c);
   else
