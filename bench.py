@@ -423,6 +423,70 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def run_pt(args):
+    """Configuration 4: fcc Pt, spin-orbit, FDM radius 4.0 A at step 0.2 A
+    (19 atoms, about 51.6k complex rows), complex energies with a 0.5 eV
+    broadening (E_comp, the regular solution), complex harmonics.  A step
+    solves --pt-energies of the 300 energies -10..50 eV (spread over the grid)
+    in one mixed-precision batch; the FP64 batch of the same energies is timed
+    once for the comparison and the agreement."""
+    import torch
+    from fdmnes_gb300 import build as B, abi, cluster as CL, complex_path as CP
+    from fdmnes_gb300.solver import FdmSolver
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    B.build()
+    grid300 = np.linspace(-10.0, 50.0, 300)
+    energies = grid300[np.round(np.linspace(0, 299, args.pt_energies)).astype(int)]
+    t0 = time.perf_counter()
+    st = CL.build_structure(CL.pt_cluster(4.4), 0.2, 4.0, 50.0, nspin=2)
+    ga = abi.GridArgs(CP.grid_dict(st, True))
+    eimag_ry = 0.5 / 13.605693122994
+    eas = [abi.EnergyArgs(CP.energy_dict(st, float(E), spinorbit=True, eimag_ry=eimag_ry)) for E in energies]
+    host_s = time.perf_counter() - t0
+    sv = FdmSolver(ga.d)
+    sv.set_tolerance(1e-8, 1e-6)
+
+    def run(prec):
+        sv.spectrum_begin(prec, len(eas))
+        for ea in eas:
+            sv.spectrum_add_args(ea)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        info = sv.spectrum_run()
+        torch.cuda.synchronize()
+        return time.perf_counter() - t, info, [sv.taull_c(k, 2) for k in range(len(eas))]
+
+    run("mixed")  # warm-up: plan and graphs
+    times, infos = [], []
+    for _ in range(args.steps):
+        dt, info, Tm = run("mixed")
+        times.append(dt)
+        infos.append(info)
+    t64, info64, T64 = run("fp64")
+    err = max(float(np.abs(a - b).max() / np.abs(b).max()) for a, b in zip(Tm, T64))
+    wall = statistics.mean(times)
+    last = infos[-1]
+    nlig = [int(ea.d["nligne"]) for ea in eas]
+    line = {
+        "metric": METRIC, "value": len(eas) / wall, "unit": "energies/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": 1, "ms_per_step": 1000.0 * wall, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 factor + f64 refinement (df64 residual), real-equivalent complex",
+        "data": "synthetic",
+        "config": {"workload": "fcc Pt a=3.92 A, spin-orbit, 19 atoms within the FDM radius 4.0 A, step 0.2 A, "
+                               "complex harmonics, complex energies (Eimag 0.5 eV), batched",
+                   "energies": len(eas), "full_configuration_energies": 300, "nligne_complex": nlig,
+                   "host_inputs_s": host_s},
+        "phases_ms": {k: last[k] for k in ("ms_assemble", "ms_factor", "ms_solve", "ms_refine")},
+        "factor_tflops": last["flops_factor"] / (last["ms_factor"] / 1000.0) / 1e12 if last["ms_factor"] > 0 else None,
+        "fp64_escalations": last["n_fallback"],
+        "plain_fp64": {"value": len(eas) / t64, "unit": "energies/s",
+                       "phases_ms": {k: info64[k] for k in ("ms_assemble", "ms_factor", "ms_solve")}},
+        "taull_max_rel_err_vs_fp64": err,
+    }
+    print(json.dumps(line), flush=True)
+    sv.close()
+
+
 def run_tio2(args):
     """Configuration 3: rutile TiO2, Ti K edge, two spin blocks, three
     absorbing-site clusters with FDM radii 4.0 / 4.5 / 5.0 A at step 0.2 A, in
@@ -518,15 +582,18 @@ def main():
                     help="double-float escalation trailing update: FP32 pipes or tensor-core integer slices")
     ap.add_argument("--escalation", default="df64_f32", choices=["df64", "df64_f32", "wide_df64", "fp64"],
                     help="re-solve of energies whose FP32 refinement stalls")
-    ap.add_argument("--config", default="cu401", choices=["cu401", "tio2"],
+    ap.add_argument("--config", default="cu401", choices=["cu401", "tio2", "pt"],
                     help="cu401: the 401-energy Cu spectrum (the metric's configuration); tio2: the rutile "
-                         "three-site, two-spin batch")
+                         "three-site, two-spin batch; pt: the Pt spin-orbit complex-energy batch")
     ap.add_argument("--tio2-energies", type=int, default=4, help="energies per site of the tio2 configuration")
+    ap.add_argument("--pt-energies", type=int, default=2, help="energies of the pt configuration")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.config == "tio2":
         run_tio2(args)
+    elif args.config == "pt":
+        run_pt(args)
     else:
         run_gpu(args)
 
