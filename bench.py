@@ -427,21 +427,27 @@ def run_pt(args):
     """Configuration 4: fcc Pt, spin-orbit, FDM radius 4.0 A at step 0.2 A
     (19 atoms, about 51.6k complex rows), complex energies with a 0.5 eV
     broadening (E_comp, the regular solution), complex harmonics.  A step
-    solves --pt-energies of the 300 energies -10..50 eV (spread over the grid)
-    in one mixed-precision batch; the FP64 batch of the same energies is timed
+    solves --pt-energies of the 300 energies -10..50 eV (spread over the grid
+    points whose outer kinetic energy is positive) in one mixed-precision batch; the FP64 batch of the same energies is timed
     once for the comparison and the agreement."""
     import torch
     from fdmnes_gb300 import build as B, abi, cluster as CL, complex_path as CP
     from fdmnes_gb300.solver import FdmSolver
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     B.build()
-    grid300 = np.linspace(-10.0, 50.0, 300)
-    energies = grid300[np.round(np.linspace(0, 299, args.pt_energies)).astype(int)]
     t0 = time.perf_counter()
     st = CL.build_structure(CL.pt_cluster(4.4), 0.2, 4.0, 50.0, nspin=2)
+    # the outer-sphere solutions are those of a real kinetic energy: keep the
+    # grid points above the outer potential of spin block 1 (0.5 eV margin)
+    e_fermi = -5.0
+    e_floor = (st.V0bd + st.spin_shift(1)) * CL.RYDB - e_fermi + 0.5
+    grid300 = np.linspace(-10.0, 50.0, 300)
+    grid_ok = grid300[grid300 > e_floor]
+    energies = grid_ok[np.round(np.linspace(0, len(grid_ok) - 1, args.pt_energies)).astype(int)]
     ga = abi.GridArgs(CP.grid_dict(st, True))
     eimag_ry = 0.5 / 13.605693122994
-    eas = [abi.EnergyArgs(CP.energy_dict(st, float(E), spinorbit=True, eimag_ry=eimag_ry)) for E in energies]
+    eas = [abi.EnergyArgs(CP.energy_dict(st, float(E), spinorbit=True, eimag_ry=eimag_ry,
+                                                e_fermi_ev=e_fermi)) for E in energies]
     host_s = time.perf_counter() - t0
     sv = FdmSolver(ga.d)
     sv.set_tolerance(1e-8, 1e-6)
@@ -474,7 +480,8 @@ def run_pt(args):
         "data": "synthetic",
         "config": {"workload": "fcc Pt a=3.92 A, spin-orbit, 19 atoms within the FDM radius 4.0 A, step 0.2 A, "
                                "complex harmonics, complex energies (Eimag 0.5 eV), batched",
-                   "energies": len(eas), "full_configuration_energies": 300, "nligne_complex": nlig,
+                   "energies": len(eas), "energies_ev": [float(e) for e in energies],
+                   "full_configuration_energies": 300, "grid_points_above_outer_potential": int(len(grid_ok)), "nligne_complex": nlig,
                    "host_inputs_s": host_s},
         "phases_ms": {k: last[k] for k in ("ms_assemble", "ms_factor", "ms_solve", "ms_refine")},
         "factor_tflops": last["flops_factor"] / (last["ms_factor"] / 1000.0) / 1e12 if last["ms_factor"] > 0 else None,
