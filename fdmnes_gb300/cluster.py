@@ -882,12 +882,19 @@ class RowIndex:
     lb2: np.ndarray
 
 
-def newind(st: Structure, nlmsa: np.ndarray, nlmso: int, nspino: int = 1) -> RowIndex:
+def newind(st: Structure, nlmsa: np.ndarray, nlmso: int, nspino: int = 1, irregular: bool = False) -> RowIndex:
+    """Row numbering and profile of the FDM matrix (source/mat.f90:1761-1921).
+    irregular: the irregular cluster solution of FDM_comp with both atomic
+    solutions (Test_reg = 0, source/mat.f90:140-147): 2 nlmsa amplitude rows per
+    atom and no outer-sphere rows; nligneso = nligne."""
     g = st.grid
     natome = st.natome
     npoint = g.npoint
-    n_ato_ri = 1
-    nligne = nspino * g.npr + nlmso + int(nlmsa.sum())
+    n_ato_ri = 2 if irregular else 1
+    if irregular:
+        nligne = nspino * g.npr + n_ato_ri * int(nlmsa.sum())
+    else:
+        nligne = nspino * g.npr + nlmso + int(nlmsa.sum())
     numia = g.numia
     new = np.zeros(npoint + 1, dtype=np.int64)   # new[0] = new(0)
     inter = numia[:npoint] == 0
@@ -943,11 +950,12 @@ def newind(st: Structure, nlmsa: np.ndarray, nlmso: int, nspino: int = 1) -> Row
         for L in range(1, n_ato_ri * nlmsa[ia] + 1):
             lb1[ianew[ia] + L - 1] = lb11
             lb2[ianew[ia] + L - 1] = lb22
-    lb11 = nligne - nlmso + 1
-    for ib in range(g.nsortf):
-        lb11 = min(lb11, new[g.isrt[ib]] - n)
-    lb1[nligne - nlmso:] = lb11
-    lb2[nligne - nlmso:] = nligne
+    if not irregular:   # there is no scattered amplitude for the irregular solution
+        lb11 = nligne - nlmso + 1
+        for ib in range(g.nsortf):
+            lb11 = min(lb11, new[g.isrt[ib]] - n)
+        lb1[nligne - nlmso:] = lb11
+        lb2[nligne - nlmso:] = nligne
     lb1 = np.minimum.accumulate(lb1[::-1])[::-1].copy()
     newinv = np.zeros(nligne, dtype=np.int64)
     for i in range(1, npoint + 1):
@@ -958,7 +966,7 @@ def newind(st: Structure, nlmsa: np.ndarray, nlmso: int, nspino: int = 1) -> Row
                 newinv[ii - 2] = i
     for ia in range(natome):
         newinv[ianew[ia]:ianew[ia] + n_ato_ri * nlmsa[ia]] = -(ia + 1)
-    return RowIndex(nligne=nligne, nligneso=nligne - nlmso, new=new.astype(np.int32),
+    return RowIndex(nligne=nligne, nligneso=nligne if irregular else nligne - nlmso, new=new.astype(np.int32),
                     newinv=newinv.astype(np.int32), ianew=ianew.astype(np.int32),
                     lb1=lb1.astype(np.int32), lb2=lb2.astype(np.int32))
 

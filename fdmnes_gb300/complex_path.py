@@ -29,8 +29,10 @@ given: the reference's default FDM path zeroes the broadening before the solve
 the complex-argument j_l, n_l of ``cbessneu`` at k = sqrt(Ecinetic + i Eimag)
 (``phiso``, ``source/mat.f90:778-785,978-990``) and the grid diagonal carries
 -i Eimag (``E_comp``); ``phiato`` stays the real-energy model.  This is the
-regular solution of the reference's complex-energy mode only: its irregular
-solution and Tau_RI (``FDM_comp``) are not generated.
+regular solution; with ``fdm_comp`` phiato also carries a model irregular
+atomic solution, and ``irregular`` builds the arguments of the irregular
+cluster solution of the reference's ``FDM_comp`` mode, whose amplitudes and the
+regular ones form Tau_RI (``source/mat.f90:219-292``).
 """
 from __future__ import annotations
 
@@ -148,28 +150,61 @@ def _so_weight(L: int, m: int, isol: int, ispo: int, so_coupling: float) -> floa
     return so_coupling * np.sqrt(max((L + m) * (L - m + 1), 0)) / (L + 1)
 
 
+def irregular_boundary_radial(st: CL.Structure, enervide: float, lmaxa: np.ndarray) -> dict:
+    """Model irregular atomic solutions at every atom's boundary points, keyed
+    like :func:`cluster.boundary_radial`: the free-space singular solution
+    -sqrt(k / pi) n_l(k r) at the kinetic energy of the spin block, r the
+    distance of the boundary point to its atom.  The reference's singular
+    radial solver (``Sch_radial_solsing``, ``source/sphere.f90:2591``) is
+    upstream of the solve; this is a model input with its structure."""
+    g = st.grid
+    out = {}
+    for isp in range(1, st.nspin + 1):
+        k = np.sqrt(enervide - (st.V0bd + st.spin_shift(isp)))
+        fn = np.sqrt(k / np.pi)
+        for ia in range(st.natome):
+            nb = int(g.nbord[ia])
+            _, nm = cbessneu(fn, k * st.rrel[:nb, ia], int(lmaxa[ia]))
+            for L in range(int(lmaxa[ia]) + 1):
+                out[(isp, ia, L)] = -nm[:, L].real
+    return out
+
+
 def energy_dict(st: CL.Structure, energy_ev: float, spinorbit: bool, ylm_comp: bool = True,
                 relativistic: Optional[bool] = None, so_coupling: float = 0.1, basereel: bool = False,
-                gradvr: Optional[np.ndarray] = None, e_fermi_ev: float = -5.0, eimag_ry: float = 0.0) -> dict:
+                gradvr: Optional[np.ndarray] = None, e_fermi_ev: float = -5.0, eimag_ry: float = 0.0,
+                fdm_comp: bool = False, irregular: bool = False) -> dict:
     """Per-energy arguments of one complex mat_solve call.
 
     spinorbit: nspino = 2 (needs nspin = 2), with the relativistic terms unless
     ``relativistic`` says otherwise.  ylm_comp: complex harmonics (forced with
     spin-orbit in the reference).  basereel: real outer basis (the reference
     never combines it with complex harmonics; kept for the reduction tests).
+    fdm_comp: the reference's FDM_comp mode (``source/fdm.f90:1734-1738``):
+    phiato carries the regular and the irregular atomic solutions (n_RI = 2);
+    irregular (implies fdm_comp, needs eimag_ry > 0): the irregular cluster
+    solution with both atomic solutions (Test_reg = 0, n_ato_RI = 2,
+    ``source/mat.f90:138-147``) instead of the regular one.
     """
     from . import abi
     g = st.grid
+    if irregular:
+        fdm_comp = True
+        if eimag_ry <= 0.0:
+            raise ValueError("the irregular solution is the complex-energy (FDM_comp) one: eimag_ry > 0")
     ei = CL.energy_inputs(st, energy_ev, e_fermi_ev)
     if relativistic is None:
         relativistic = spinorbit
     nspino = 2 if spinorbit else 1
     nlmsa = (nspino * (ei.lmaxa + 1) ** 2).astype(np.int32)
     nlmso = nspino * (ei.lmaxso + 1) ** 2
-    ri = CL.newind(st, nlmsa, nlmso, nspino)
+    ri = CL.newind(st, nlmsa, nlmso, nspino, irregular=irregular)
     nspinp = st.nspin
-    rad = CL.boundary_radial(st, ei.enervide, ei.lmaxa)
-    phi = np.zeros((g.nbtm, ei.nlmagm, nspinp, nspino, 1, st.natome, 2), order="F")
+    n_ri = 2 if fdm_comp else 1
+    rads = [CL.boundary_radial(st, ei.enervide, ei.lmaxa)]
+    if fdm_comp:
+        rads.append(irregular_boundary_radial(st, ei.enervide, ei.lmaxa))
+    phi = np.zeros((g.nbtm, ei.nlmagm, nspinp, nspino, n_ri, st.natome, 2), order="F")
 
     def harmonic(ia, nb, L, m):
         lm = L * L + L + m
@@ -191,11 +226,12 @@ def energy_dict(st: CL.Structure, energy_ev: float, spinorbit: bool, ylm_comp: b
                             # spin-orbit: the spin index of phiato is the component ispo
                             if spinorbit and isp != ispo:
                                 continue
-                            u = rad[(isp, ia, L)]
-                            v = w * u * harmonic(ia, nb, L, mr)
-                            lm0 = L * L + L + mr
-                            phi[:nb, lm0, isp - 1, isol - 1, 0, ia, 0] = v.real
-                            phi[:nb, lm0, isp - 1, isol - 1, 0, ia, 1] = v.imag
+                            for iri, rad in enumerate(rads):
+                                u = rad[(isp, ia, L)]
+                                v = w * u * harmonic(ia, nb, L, mr)
+                                lm0 = L * L + L + mr
+                                phi[:nb, lm0, isp - 1, isol - 1, iri, ia, 0] = v.real
+                                phi[:nb, lm0, isp - 1, isol - 1, iri, ia, 1] = v.imag
     nspinr = st.nspin if spinorbit else 1
     bes = np.asfortranarray(np.repeat(ei.besselr, nspinr, axis=2))
     neu = np.asfortranarray(np.repeat(ei.neumanr, nspinr, axis=2))
@@ -223,6 +259,7 @@ def energy_dict(st: CL.Structure, energy_ev: float, spinorbit: bool, ylm_comp: b
              Spinorbite=int(spinorbit), Ylm_comp=int(ylm_comp), ispin=1, phiato=phi, Besselr=bes, Neumanr=neu,
              gradvr=np.asfortranarray(gradvr), new_=ri.new, newinv=ri.newinv, lb1=ri.lb1, lb2=ri.lb2, ianew=ri.ianew)
     d.update(ecomp)
+    d.update(n_RI=n_ri, n_ato_RI=2 if irregular else 1, irregular=int(irregular), Test_reg=0)
     return d
 
 

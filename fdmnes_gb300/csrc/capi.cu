@@ -224,20 +224,23 @@ uint64_t mix(uint64_t h, uint64_t v) {
 
 // Complex problems (Cal_comp): the complex outgoing basis with real energies,
 // complex or real harmonics, optionally spin-orbit (nspino = 2, two spin
-// blocks) and the relativistic terms; C1 characters; regular solution.
+// blocks) and the relativistic terms; C1 characters; the regular solution,
+// or FDM_comp's irregular one with both atomic solutions (Test_reg = 0).
 fdmgpu_status check_energy_c(const fdmgpu_handle* h, const fdmgpu_energy* e) {
   const fdmgpu_grid& g = h->g;
-  if (e->irregular || e->Repres_comp || e->Base_hexa || e->Basereel || e->n_RI != 1 || e->n_ato_RI != 1 ||
-      e->nphiato7 != 2)
+  if (e->Repres_comp || e->Base_hexa || e->Basereel || e->nphiato7 != 2 ||
+      (e->irregular ? (e->n_RI != 2 || e->n_ato_RI != 2 || e->Test_reg != 0 || !e->E_comp)
+                    : (e->n_ato_RI != 1 || e->n_RI < 1 || e->n_RI > 2)))
     return fail(FDMGPU_ERR_UNSUPPORTED,
                 "the library's complex path: Cal_comp, real or complex energies (E_comp), the complex basis "
-                "(Basereel false), regular solution (n_RI = 1), complex phiato (nphiato7 = 2)");
+                "(Basereel false), complex phiato (nphiato7 = 2); the regular solution (n_ato_RI = 1) or, with "
+                "E_comp, the irregular one with both atomic solutions (n_RI = n_ato_RI = 2, Test_reg = 0)");
   if (!h->chars_c1) return fail(FDMGPU_ERR_UNSUPPORTED, "the complex path needs the C1 characters (Kar = 1, Kari = 0)");
   if (e->Spinorbite != (g.nspino == 2)) return fail(FDMGPU_ERR_ARG, "Spinorbite must match the grid's nspino");
   if (e->Spinorbite && (g.nspin != 2 || e->nspinp != 2 || e->nspinr != 2))
     return fail(FDMGPU_ERR_UNSUPPORTED, "spin-orbit needs two spin blocks (nspin = nspinp = nspinr = 2)");
   if (!e->Spinorbite && e->nspinr != 1) return fail(FDMGPU_ERR_ARG, "nspinr must be 1 without spin-orbit");
-  if (e->nligne <= 0 || e->nlmso <= 0 || e->nligneso != e->nligne - e->nlmso)
+  if (e->nligne <= 0 || e->nlmso <= 0 || e->nligneso != (e->irregular ? e->nligne : e->nligne - e->nlmso))
     return fail(FDMGPU_ERR_ARG, "inconsistent nligne / nlmso / nligneso");
   if ((int64_t)2 * e->nligne > (int64_t)1 << 30) return fail(FDMGPU_ERR_ARG, "nligne too large");
   if (e->lmaxso < 0 || g.nspino * (e->lmaxso + 1) * (e->lmaxso + 1) < e->nlmso ||
@@ -373,14 +376,17 @@ fdmgpu_status plan_problem(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& h
   // real-equivalent form every complex entry is a 2x2 block
   const fdmgpu_grid& g = h->g;
   const int nso = g.nspino;
+  // (the irregular solution: two amplitude columns and rows per atom harmonic)
+  const int nato = (cplx && e->irregular) ? 2 : 1;
   int64_t cap = 0;
   for (size_t k = 0; k < h->inter_pt_h.size(); ++k) {
     int64_t row = 1 + (int64_t)nso * h->n_inter_h[k] + (h->has_outer_h[k] ? e->nlmso : 0);
-    for (int ia : h->nb_atoms_h[k]) row += e->nlmsa[ia - 1];
+    for (int ia : h->nb_atoms_h[k]) row += (int64_t)nato * e->nlmsa[ia - 1];
     cap += nso * row;
   }
   cap += (int64_t)e->nlmso * (e->nlmso + g.nsortf);
-  for (int ia = 1; ia <= g.natome; ++ia) cap += (int64_t)e->nlmsa[ia - 1] * (h->nbordf_h[ia - 1] + e->nlmsa[ia - 1]);
+  for (int ia = 1; ia <= g.natome; ++ia)
+    cap += (int64_t)nato * e->nlmsa[ia - 1] * (h->nbordf_h[ia - 1] + (int64_t)nato * e->nlmsa[ia - 1]);
   if (cplx) cap *= 4;
   hp.nnz_cap = cap + (npad - n);
   // descriptor (offsets filled later)
@@ -405,10 +411,12 @@ fdmgpu_status plan_problem(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& h
   P.nspinp = e->nspinp;
   P.nspinr = std::max(1, e->nspinr);
   P.nspin = g.nspin;
+  P.irr = (cplx && e->irregular) ? 1 : 0;
+  P.nri = P.irr ? 2 : 1;
   // signature of the plan
   uint64_t s = mix(0, (uint64_t)n);
   s = mix(s, (uint64_t)e->nlmso);
-  s = mix(s, (uint64_t)(P.cplx * 8 + P.so * 4 + P.rel * 2 + P.ylmc));
+  s = mix(s, (uint64_t)(P.irr * 16 + P.cplx * 8 + P.so * 4 + P.rel * 2 + P.ylmc));
   for (int i = 0; i < e->nligne; i += 7) s = mix(s, (uint64_t)e->lb1[i] * 131 + (uint64_t)e->lb2[i]);
   for (int ia = 0; ia < g.natome; ++ia) s = mix(s, (uint64_t)e->nlmsa[ia] * 1000003u + (uint64_t)e->ianew[ia]);
   hp.sig = s;
@@ -424,11 +432,15 @@ void pack_inputs(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& hp) {
   hp.in_i.insert(hp.in_i.end(), e->new_, e->new_ + g.npoint + 1);
   hp.in_i.insert(hp.in_i.end(), e->ianew, e->ianew + g.natome);
   hp.in_i.insert(hp.in_i.end(), e->nlmsa, e->nlmsa + g.natome);
+  // atom rows per atom: nlmsa, 2 nlmsa for the irregular solution
   hp.nlmsa_max = 0;
   for (int ia = 0; ia < g.natome; ++ia) hp.nlmsa_max = std::max(hp.nlmsa_max, e->nlmsa[ia]);
+  if (e->Cal_comp && e->irregular) hp.nlmsa_max *= 2;
   if (e->Cal_comp) {
     // Vr (npoint, nspin) | gradvr (npoint, 3, nspin) | phiato real part, imaginary part
-    // (nbtm, nlmagm, nspinp, nspino, natome) | Bessel, Neumann [nspinr][nsort][lmaxso+1]
+    // (nbtm, nlmagm, nspinp, nspino, nri, natome), nri = 2 (regular, irregular
+    // atomic solution) for the irregular solution, else the regular one alone |
+    // Bessel, Neumann [nspinr][nsort][lmaxso+1]
     hp.in_d.insert(hp.in_d.end(), e->Vr, e->Vr + (int64_t)g.npoint * g.nspin);
     hp.rel_grad = (int64_t)hp.in_d.size();
     for (int isp = 1; isp <= g.nspin; ++isp)
@@ -438,15 +450,17 @@ void pack_inputs(fdmgpu_handle* h, const fdmgpu_energy* e, HostProb& hp) {
                                       : 0.0);
     hp.rel_phi = (int64_t)hp.in_d.size();
     const int64_t d1 = e->nphiato1, d2 = e->nlmagm, d3 = e->nspinp, d4 = g.nspino, d5 = e->n_RI, d6 = g.natome;
+    const int nri = e->irregular ? 2 : 1;
     for (int part = 0; part < 2; ++part)
       for (int ia = 1; ia <= g.natome; ++ia)
-        for (int isol = 1; isol <= g.nspino; ++isol)
-          for (int isp = 1; isp <= e->nspinp; ++isp)
-            for (int lm = 1; lm <= e->nlmagm; ++lm) {
-              const double* src =
-                  e->phiato + d1 * ((lm - 1) + d2 * ((isp - 1) + d3 * ((isol - 1) + d4 * (0 + d5 * ((ia - 1) + d6 * part)))));
-              hp.in_d.insert(hp.in_d.end(), src, src + g.nbtm);
-            }
+        for (int iri = 1; iri <= nri; ++iri)
+          for (int isol = 1; isol <= g.nspino; ++isol)
+            for (int isp = 1; isp <= e->nspinp; ++isp)
+              for (int lm = 1; lm <= e->nlmagm; ++lm) {
+                const double* src = e->phiato + d1 * ((lm - 1) + d2 * ((isp - 1) + d3 * ((isol - 1) + d4 * ((iri - 1) +
+                                                  d5 * ((ia - 1) + d6 * part)))));
+                hp.in_d.insert(hp.in_d.end(), src, src + g.nbtm);
+              }
     const int nl = e->lmaxso + 1;
     for (int which = 0; which < 2; ++which) {
       (which == 0 ? hp.rel_bes : hp.rel_neu) = (int64_t)hp.in_d.size();
@@ -1048,9 +1062,10 @@ fdmgpu_status capture(fdmgpu_handle* h, void (*rec)(fdmgpu_handle*), cudaGraphEx
 }
 
 // Last resort of the mixed path: the listed problems (whose FP64 bands the
-// double-float escalation has overwritten) are assembled again in FP64 and
-// solved by the FP64 elimination, as the FP64 path solves them; one grid row
-// per listed problem.  Returns the launches.
+// double-float escalation has overwritten) are assembled again in FP64 (the
+// complex assembly for a complex batch) and solved by the FP64 elimination, as
+// the FP64 path solves them; one grid row per listed problem.  Returns the
+// launches.
 int64_t solve_fp64_subset(fdmgpu_handle* h, const std::vector<int>& list) {
   cudaStream_t s = h->stream;
   Batch& b = h->batch;
@@ -1072,11 +1087,15 @@ int64_t solve_fp64_subset(fdmgpu_handle* h, const std::vector<int>& list) {
   pf.active = nullptr;
   LaunchDims df = h->dims;
   df.nprob = ne;
-  launch_assemble(h->d_sites.p, h->d_probs_esc.p, pf, h->tb, df, s);
+  if (b.cplx == 1)
+    launch_assemble_c(h->d_sites.p, h->d_probs_esc.p, pf, h->tb, df, 0, s);
+  else
+    launch_assemble(h->d_sites.p, h->d_probs_esc.p, pf, h->tb, df, s);
   launch_copy_rhs(h->d_probs_esc.p, pf, df, s);
   int64_t nk = 8;
+  // the real-equivalent form of a complex problem pivots inside the diagonal tiles, as the FP64 path does
   nk += launch_factor<double>(h->sp, h->pl.env64, h->pl.X64, h->d_probs_esc.p, h->tb, ne, 1, nullptr,
-                              h->d_err_esc.p, 1e-10, nullptr, s);
+                              h->d_err_esc.p, 1e-10, b.cplx == 1 ? h->pl.piv : nullptr, s);
   nk += launch_backward<double>(h->sp, h->pl.env64, h->pl.X64, h->d_probs_esc.p, h->tb, ne, nullptr, s);
   launch_scatter_err(h->d_esc_list.p, ne, h->d_err_esc.p, h->pl.err, s);
   cudaStreamSynchronize(s);  // the host list lives until here
@@ -2402,6 +2421,30 @@ fdmgpu_status fdmgpu_batch_taull(fdmgpu_handle* h, int32_t k, double* taull, int
   return FDMGPU_OK;
 }
 
+fdmgpu_status fdmgpu_batch_tau_ri(fdmgpu_handle* h, int32_t k_reg, int32_t k_irr, double* tau_ri, int32_t* nlm) {
+  if (!h || !h->batch.ran) return fail(FDMGPU_ERR_ARG, "run a batch first");
+  Batch& b = h->batch;
+  const int np = (int)b.probs.size();
+  if (k_reg < 0 || k_reg >= np || k_irr < 0 || k_irr >= np) return fail(FDMGPU_ERR_ARG, "no such batch result");
+  if (b.chunked) return fail(FDMGPU_ERR_UNSUPPORTED, "Tau_RI of a batch that ran in chunks (its solutions are gone)");
+  const Prob& P = b.probs[k_reg].P;
+  const Prob& Q = b.probs[k_irr].P;
+  if (!P.cplx || P.irr || !Q.irr)
+    return fail(FDMGPU_ERR_ARG, "k_reg must be a regular and k_irr an irregular complex solution");
+  if (P.site != Q.site || P.iaabs < 1 || P.iaabs != Q.iaabs || P.nlm_abs != Q.nlm_abs || P.nlmso != Q.nlmso)
+    return fail(FDMGPU_ERR_ARG, "the pair must share the site, the absorber and the outer harmonics");
+  if (nlm) *nlm = P.nlm_abs;
+  if (!tau_ri) return FDMGPU_OK;
+  const size_t n = 2 * (size_t)P.nlm_abs * P.nlm_abs;   // complex values
+  if (h->d_smr.reserve(2 * n) != cudaSuccess) return fail(FDMGPU_ERR_NOMEM, "Tau_RI buffer");
+  launch_tau_ri(h->d_sites.p, h->d_probs.p + k_reg, h->d_probs.p + k_irr, h->d_X64.p, P.nlm_abs,
+                reinterpret_cast<double2*>(h->d_smr.p), h->stream);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(tau_ri, h->d_smr.p, 2 * n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  CK(cudaStreamSynchronize(h->stream));
+  return (fdmgpu_status)(b.err[k_reg] ? b.err[k_reg] : b.err[k_irr]);
+}
+
 fdmgpu_status fdmgpu_batch_taull_all(fdmgpu_handle* h, double* taull, int64_t capacity) {
   if (!h || !h->batch.ran || h->batch.probs.empty()) return fail(FDMGPU_ERR_ARG, "no batch result");
   int64_t n = 0;
@@ -2800,6 +2843,8 @@ fdmgpu_status fdmgpu_batch_xanes(fdmgpu_handle* h, const double* energies_ev, co
   if (!b.ran || n == 0) return fail(FDMGPU_ERR_ARG, "run a batch first");
   if (b.probs[0].P.nlm_abs < 4) return fail(FDMGPU_ERR_ARG, "the absorber needs its p harmonics (lmax >= 1)");
   if (b.cplx == 1 && tensor) return fail(FDMGPU_ERR_UNSUPPORTED, "the Cartesian tensor is formed for real batches only");
+  for (auto& hp : b.probs)
+    if (hp.P.irr) return fail(FDMGPU_ERR_UNSUPPORTED, "an irregular solution has no Taull (its pair forms Tau_RI)");
   for (int k = 1; k < n; ++k)
     if (!(energies_ev[k] > energies_ev[k - 1])) return fail(FDMGPU_ERR_ARG, "energies must increase, one problem each");
   if (sigma_conv && n < 2) return fail(FDMGPU_ERR_ARG, "the convolution needs two energies");

@@ -11,19 +11,26 @@
 // two rows of a block always share a tile).
 //
 // Restates the complex branch of calcMatRow (source/mat.f90:1034-1632) for
-// Cal_comp = true, irregular = Repres_comp = false, C1 characters (Kar = 1,
-// Kari = 0), real energies or complex ones (E_comp: -i Eimag on the grid
-// diagonal, mat.f90:1151-1152, and the complex Bessel / Neumann of phiso):
+// Cal_comp = true, Repres_comp = false, C1 characters (Kar = 1, Kari = 0), real
+// energies or complex ones (E_comp: -i Eimag on the grid diagonal,
+// mat.f90:1151-1152, and the complex Bessel / Neumann of phiso), the regular
+// solution and FDM_comp's irregular one with both atomic solutions (Test_reg
+// = 0: amplitude columns of the regular then the irregular atomic solution,
+// no outer-sphere rows or columns, right-hand side from -i j_l + n_l):
 //   k_asmc_grid       grid rows with the relativistic and spin-orbit gradient
 //                     terms (mat.f90:1142-1402), one warp per point, both spin
 //                     rows of a point in turn
 //   k_asmc_outer      outer-sphere rows, outer columns and right-hand sides
-//                     (mat.f90:1405-1469, 1486-1510)
+//                     (mat.f90:1405-1469, 1486-1510; regular solution only)
 //   k_asmc_outer_bnd  outer rows, boundary-point columns (mat.f90:1471-1484)
-//   k_asmc_atom       atom rows (mat.f90:1515-1632)
-// and the Taull of the complex basis (Basereel false, mat.f90:354-405) with its
-// symmetrisation (mat.f90:594-644).  Within an entry, contributions are summed
-// in the reference's order (neighbours iv ascending, boundary points ascending).
+//   k_asmc_atom       atom rows (mat.f90:1515-1632; irregular solution: the
+//                     first half of the boundary points matches the regular,
+//                     the second half the irregular atomic solution)
+// the Taull of the complex basis (Basereel false, mat.f90:354-405) with its
+// symmetrisation (mat.f90:594-644), and FDM_comp's Tau_RI from a regular and
+// an irregular solution (mat.f90:219-292).  Within an entry, contributions are
+// summed in the reference's order (neighbours iv ascending, boundary points
+// ascending).
 #include "fdm_internal.cuh"
 #include "fdm_kernels.h"
 
@@ -81,7 +88,7 @@ __device__ __forceinline__ void add_rhs_c(double* B, const Prob& P, int ii, int 
 
 // Per-problem packed inputs of a complex problem (see pack_inputs):
 //   Vr (npoint, nspin) | gradvr (npoint, 3, nspin) | phiato re, im
-//   (nbtm, nlmagm, nspinp, nspino, natome) | Bessel [nspinr][nsort][lmaxso+1] | Neumann (same)
+//   (nbtm, nlmagm, nspinp, nspino, nri, natome) | Bessel [nspinr][nsort][lmaxso+1] | Neumann (same)
 struct CIn {
   const double* vr;
   const double* grad;
@@ -98,15 +105,16 @@ __device__ __forceinline__ CIn cin(const Prob& P, const StaticDev& S, const doub
   c.phi = dpool + P.in_phi;
   c.bes = dpool + P.in_bes;
   c.neu = dpool + P.in_neu;
-  c.phi_im = (int64_t)S.nbtm * P.nlmagm * P.nspinp * S.nspino * S.natome;
+  c.phi_im = (int64_t)S.nbtm * P.nlmagm * P.nspinp * S.nspino * P.nri * S.natome;
   c.nl = P.lmaxso + 1;
   return c;
 }
+// phiato of atomic solution iri (1 regular, 2 irregular)
 __device__ __forceinline__ double2 phic(const CIn& c, const Prob& P, const StaticDev& S, int ib, int lm0, int isp,
-                                        int isol, int ia) {
+                                        int isol, int ia, int iri = 1) {
   const int64_t off =
       (ib - 1) + (int64_t)S.nbtm * ((lm0 - 1) + (int64_t)P.nlmagm * ((isp - 1) + (int64_t)P.nspinp *
-                                    ((isol - 1) + (int64_t)S.nspino * (ia - 1))));
+                                    ((isol - 1) + (int64_t)S.nspino * ((iri - 1) + (int64_t)P.nri * (ia - 1)))));
   return make_double2(c.phi[off], c.phi[off + c.phi_im]);
 }
 __device__ __forceinline__ double besr(const CIn& c, const double* a, const StaticDev& S, int ib, int L, int isp) {
@@ -220,16 +228,20 @@ __global__ void __launch_bounds__(256) k_asmc_grid(const StaticDev* sites, const
         }
       } else if (kind > 0) {
         const int ia = kind, ib = idx;
-        for (int Lm = lane + 1; Lm <= nlmsa[ia - 1]; Lm += 32) {
+        const int nl = nlmsa[ia - 1];
+        // the irregular solution's second column block: the irregular atomic solution
+        for (int q = lane; q < P.nri * nl; q += 32) {
+          const int iri = q / nl + 1, Lm = q % nl + 1;
           const int64_t t = (Lm - 1) + (int64_t)S.nlmsam * (ia - 1);
           const int L = S.lato[t], isol = S.iato[t], mb = S.mato[t];
-          const int jjj = ianew[ia - 1] + Lm;
+          const int jjj = ianew[ia - 1] + Lm + (iri - 1) * nl;
           for (int ispo = 1; ispo <= nspino; ++ispo) {
             const int m = mb + ispo - isol;
             if (m > L || m < -L) continue;
             const int lm0 = L * L + L + 1 + m;
-            const double2 v = P.so ? c_mul(make_double2(cr[ispo - 1], ci[ispo - 1]), phic(c, P, S, ib, lm0, ispo, isol, ia))
-                                   : c_mul(make_double2(cr[isp - 1], ci[isp - 1]), phic(c, P, S, ib, lm0, ispp, isol, ia));
+            const double2 v =
+                P.so ? c_mul(make_double2(cr[ispo - 1], ci[ispo - 1]), phic(c, P, S, ib, lm0, ispo, isol, ia, iri))
+                     : c_mul(make_double2(cr[isp - 1], ci[isp - 1]), phic(c, P, S, ib, lm0, ispp, isol, ia, iri));
             add_c(env, P, tb, ii, jjj, v, err, e);
           }
         }
@@ -242,8 +254,18 @@ __global__ void __launch_bounds__(256) k_asmc_grid(const StaticDev* sites, const
           const int s = (isp == so_) ? isp : indg;
           const double2 cf = make_double2(cr[s - 1], ci[s - 1]);
           const double2 y = yso(P, S, ib, m, lm0);
-          add_c(env, P, tb, ii, P.nligneso + Lm, c_mul(c_mul(colfac(c, P, S, basereel, ib, L, iq), y), cf), err, e);
-          const double2 g = c_mul(c_mul(y, besc(c, P, c.bes, S, ib, L, iq)), cf);
+          const double2 jv = besc(c, P, c.bes, S, ib, L, iq);
+          if (!P.irr) {
+            add_c(env, P, tb, ii, P.nligneso + Lm, c_mul(c_mul(colfac(c, P, S, basereel, ib, L, iq), y), cf), err, e);
+          }
+          // regular solution: the incoming j_l; irregular: -i j_l + n_l (no
+          // scattered wave in the outer sphere)
+          double2 rf = jv;
+          if (P.irr) {
+            const double2 nv = besc(c, P, c.neu, S, ib, L, iq);
+            rf = make_double2(jv.y + nv.x, -jv.x + nv.y);
+          }
+          const double2 g = c_mul(c_mul(y, rf), cf);
           add_rhs_c(B, P, ii, Lm, make_double2(-g.x, -g.y));
         }
         ispq = min(S.iso[P.nlmso - 1], P.nspinr);
@@ -257,6 +279,7 @@ __global__ void __launch_bounds__(256) k_asmc_outer(const StaticDev* sites, cons
                                                     double* env, double* B, Tables tb, int basereel, int* err) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
+  if (P.irr) return;   // the irregular solution has no outer-sphere rows
   const StaticDev& S = sites[P.site];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int nlmso = P.nlmso;
@@ -317,6 +340,7 @@ __global__ void __launch_bounds__(256) k_asmc_outer_bnd(const StaticDev* sites, 
                                                         double* env, Tables tb, int* err) {
   const int e = blockIdx.y;
   const Prob P = probs[e];
+  if (P.irr) return;   // the irregular solution has no outer-sphere rows
   const StaticDev& S = sites[P.site];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= P.nlmso * S.nsortf) return;
@@ -338,7 +362,11 @@ __global__ void __launch_bounds__(256) k_asmc_outer_bnd(const StaticDev* sites, 
   add_c(env, P, tb, P.nligneso + Lm, new_[j] - S.nspino + isp, v, err, e);
 }
 
-// Atom rows: block per (atom, harmonic row).
+// Atom rows: block per (atom, amplitude row).  The irregular solution has
+// 2 nlmsa rows per atom (regular, then irregular amplitudes); its boundary
+// points split in halves: a row's grid columns come from the half of its own
+// atomic solution, each amplitude column block sums over the half of its
+// atomic solution (mat.f90:1528-1627 with Test_reg = 0).
 __global__ void __launch_bounds__(128) k_asmc_atom(const StaticDev* sites, const Prob* probs, const int* ipool,
                                                    const double* dpool, double* env, Tables tb, int max_nlm,
                                                    int* err) {
@@ -346,22 +374,30 @@ __global__ void __launch_bounds__(128) k_asmc_atom(const StaticDev* sites, const
   const Prob P = probs[e];
   const StaticDev& S = sites[P.site];
   const int ia = blockIdx.x / max_nlm + 1;
-  const int Lm = blockIdx.x % max_nlm + 1;
+  const int Ln = blockIdx.x % max_nlm + 1;
   const int* new_ = ipool + P.in_new;
   const int* ianew = ipool + P.in_ianew;
   const int* nlmsa = ipool + P.in_nlmsa;
-  if (ia > S.natome || Lm > nlmsa[ia - 1]) return;
+  if (ia > S.natome) return;
+  const int nl = nlmsa[ia - 1];
+  if (Ln > P.nri * nl) return;
+  const int iri = Ln > nl ? 2 : 1;
+  const int Lm = Ln - (iri - 1) * nl;
   const CIn c = cin(P, S, dpool);
   const int64_t t0 = (Lm - 1) + (int64_t)S.nlmsam * (ia - 1);
   const int L = S.lato[t0], ispt = S.iato[t0], m = S.mato[t0];
   const int lm0 = L * L + L + 1 + m;
-  const int ii = ianew[ia - 1] + Lm;
+  const int ii = ianew[ia - 1] + Ln;
   const int nbf = S.nbordf[ia - 1];
+  const int nhalf = nbf / 2;
+  // boundary points of atomic solution r: all of them, or its half
+  auto ib_lo = [&](int r) { return P.irr ? (r == 1 ? 1 : nhalf + 1) : 1; };
+  auto ib_hi = [&](int r) { return P.irr ? (r == 1 ? nhalf : nbf) : nbf; };
   auto ycon = [&](int ib) -> double2 {   // conj of the row's harmonic at boundary point ib
     if (P.ylmc && m != 0) return c_conj(yc(m, ylmato(S, ib, lm0, ia), ylmato(S, ib, lm0 - 2 * m, ia)));
     return make_double2(ylmato(S, ib, lm0, ia), 0.0);
   };
-  for (int ib = 1 + threadIdx.x; ib <= nbf; ib += blockDim.x) {
+  for (int ib = ib_lo(iri) + threadIdx.x; ib <= ib_hi(iri); ib += blockDim.x) {
     const int j = S.ibord[(ib - 1) + (int64_t)S.nbtm * (ia - 1)];
     const double po = S.poidsa[(ib - 1) + (int64_t)S.nbm * (ia - 1)];
     const double2 y = ycon(ib);
@@ -369,20 +405,21 @@ __global__ void __launch_bounds__(128) k_asmc_atom(const StaticDev* sites, const
     add_c(env, P, tb, ii, new_[j] - S.nspino + ispt, make_double2(-((po * y.x) / rvj), -((po * y.y) / rvj)), err, e);
   }
   const int ispint = P.so ? min(ispt, P.nspinp) : min(P.ispin, P.nspinp);
-  for (int Lmp = 1 + threadIdx.x; Lmp <= nlmsa[ia - 1]; Lmp += blockDim.x) {
+  for (int q = threadIdx.x; q < P.nri * nl; q += blockDim.x) {
+    const int jri = q / nl + 1, Lmp = q % nl + 1;
     const int64_t t = (Lmp - 1) + (int64_t)S.nlmsam * (ia - 1);
     const int Lp = S.lato[t], isol = S.iato[t];
     const int mp = S.mato[t] + ispt - isol;
     if (mp > Lp || mp < -Lp) continue;
     const int lmp0 = Lp * Lp + Lp + 1 + mp;
     double sr = 0.0, si = 0.0;
-    for (int ib = 1; ib <= nbf; ++ib) {
+    for (int ib = ib_lo(jri); ib <= ib_hi(jri); ++ib) {
       const double po = S.poidsa[(ib - 1) + (int64_t)S.nbm * (ia - 1)];
-      const double2 f = c_mul(phic(c, P, S, ib, lmp0, ispint, isol, ia), ycon(ib));
+      const double2 f = c_mul(phic(c, P, S, ib, lmp0, ispint, isol, ia, jri), ycon(ib));
       sr = sr + po * f.x;
       si = si + po * f.y;
     }
-    add_c(env, P, tb, ii, ianew[ia - 1] + Lmp, make_double2(sr, si), err, e);
+    add_c(env, P, tb, ii, ianew[ia - 1] + Lmp + (jri - 1) * nl, make_double2(sr, si), err, e);
   }
 }
 
@@ -449,7 +486,46 @@ __global__ void k_taullc_sym(const StaticDev* sites, const Prob* probs, const do
   taull[P.taull + t] = out;
 }
 
+// Tau_RI of FDM_comp (mat.f90:219-292): one thread per (Lm1, Lm2, i_RI) of
+// the absorber, Tau_RI(Lm1 s1, Lm2 s2, i_RI) = sum_f Ampl(f, Lm1)
+// Ampl_I(f, (i_RI - 1) nlmsa + Lm2): the regular problem's amplitudes times
+// the irregular problem's (regular atomic solution, then irregular); no
+// conjugate and no symmetrisation.  Indexed like Taull, i_RI outermost.
+__global__ void k_tau_ri(const StaticDev* sites, const Prob* preg, const Prob* pirr, const double* X,
+                         double2* out) {
+  const Prob P = *preg, Q = *pirr;
+  const StaticDev& S = sites[P.site];
+  const int nlm = P.nlm_abs;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * nlm * nlm) return;
+  const int iri = t / (nlm * nlm) + 1, r = t % (nlm * nlm);
+  const int a = r / nlm + 1, b = r % nlm + 1;
+  const int nsp = S.nspino, nlmq = nlm / nsp;
+  const int64_t ta = (a - 1) + (int64_t)S.nlmsam * (P.iaabs - 1), tbi = (b - 1) + (int64_t)S.nlmsam * (P.iaabs - 1);
+  const int L1 = S.lato[ta], m1 = S.mato[ta], is1 = P.so ? S.iato[ta] : 1;
+  const int L2 = S.lato[tbi], m2 = S.mato[tbi], is2 = P.so ? S.iato[tbi] : 1;
+  const int row = (L1 * L1 + L1 + m1) + nlmq * (is1 - 1), col = (L2 * L2 + L2 + m2) + nlmq * (is2 - 1);
+  const int ii = P.ianew_abs + a, jj = Q.ianew_abs + (iri - 1) * nlm + b;
+  const int pr = P.n - (2 * ii - 1), pi = P.n - 2 * ii, qr = Q.n - (2 * jj - 1), qi = Q.n - 2 * jj;
+  auto xv = [&](const Prob& R, int p, int f) {
+    return X[R.rhs + ((int64_t)(p / TS) * R.nrt + f / TS) * TS2 + (p % TS) * TS + (f % TS)];
+  };
+  double2 cf = make_double2(0.0, 0.0);
+  for (int f = 0; f < P.nlmso; ++f) {
+    const double2 z = c_mul(make_double2(xv(P, pr, f), xv(P, pi, f)), make_double2(xv(Q, qr, f), xv(Q, qi, f)));
+    cf = make_double2(cf.x + z.x, cf.y + z.y);
+  }
+  out[row + (int64_t)nlm * col + (int64_t)nlm * nlm * (iri - 1)] = cf;
+}
+
 }  // namespace
+
+void launch_tau_ri(const StaticDev* sites, const Prob* preg, const Prob* pirr, const double* X, int nlm, double2* out,
+                   cudaStream_t s) {
+  const int n = 2 * nlm * nlm;
+  if (n <= 0) return;
+  k_tau_ri<<<(n + 127) / 128, 128, 0, s>>>(sites, preg, pirr, X, out);
+}
 
 void launch_assemble_c(const StaticDev* sites, const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d,
                        int basereel, cudaStream_t s) {

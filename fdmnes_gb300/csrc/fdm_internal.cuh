@@ -78,6 +78,10 @@ struct Prob {
   // blocks, each [nspinr][nsort][lmaxso+1]
   int ecomp;
   double eimag;
+  // FDM_comp: irr = 1 for the irregular cluster solution (2 nlmsa amplitude
+  // rows per atom, no outer-sphere rows); nri = atomic solutions packed per
+  // harmonic in the phiato block (1, or 2 with irr)
+  int irr, nri;
 };
 constexpr int MAX_GEN_TYPES = 8;
 

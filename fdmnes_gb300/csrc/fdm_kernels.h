@@ -193,6 +193,10 @@ void launch_assemble_c(const StaticDev* sites, const Prob* probs, const Pools& p
                        int basereel, cudaStream_t s);
 void launch_taull_c(const StaticDev* sites, const Prob* probs, const Pools& pl, const LaunchDims& d, int max_nlm,
                     cudaStream_t s);
+// Tau_RI of FDM_comp from a regular problem (*preg) and an irregular one
+// (*pirr) of the same site and absorber: (nlm, nlm, 2) complex into out.
+void launch_tau_ri(const StaticDev* sites, const Prob* preg, const Prob* pirr, const double* X, int nlm, double2* out,
+                   cudaStream_t s);
 void launch_equilibrate_convert(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s);
 void launch_csr(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s);
 void launch_convert_masked(const Prob* probs, const Pools& pl, Tables tb, const LaunchDims& d, cudaStream_t s);

@@ -97,6 +97,8 @@ def load_library(path: str = LIB_PATH):
     L.fdmgpu_batch_vjp.argtypes = [vp, vp, vp, C.POINTER(C.c_double)]
     L.fdmgpu_batch_taull_all.argtypes = [vp, vp, C.c_int64]
     L.fdmgpu_batch_taull_all.restype = C.c_int
+    L.fdmgpu_batch_tau_ri.argtypes = [vp, C.c_int32, C.c_int32, vp, C.POINTER(C.c_int32)]
+    L.fdmgpu_batch_tau_ri.restype = C.c_int
     L.fdmgpu_batch_add_site.argtypes = [vp, vp, vp, C.c_int32]
     L.fdmgpu_batch_add_site.restype = C.c_int
     L.fdmgpu_update_grid_values.argtypes = [vp, vp]
@@ -302,6 +304,17 @@ class FdmSolver:
         out = np.zeros(2 * nl.value * nl.value)
         _check(self.lib.fdmgpu_batch_taull(self.h, k, out.ctypes.data, C.byref(nl)))
         return out.view(np.complex128).reshape((nl.value, nl.value), order="F").copy()
+
+    def tau_ri(self, k_reg: int, k_irr: int, nspino: int) -> np.ndarray:
+        """Tau_RI of FDM_comp from the batch's regular solution k_reg and
+        irregular solution k_irr: (nlm, nspino, nlm, nspino, 2), indexed like
+        taull_c, the last index i_RI (regular, irregular atomic solution)."""
+        nl = C.c_int32(0)
+        _check(self.lib.fdmgpu_batch_tau_ri(self.h, k_reg, k_irr, None, C.byref(nl)))
+        out = np.zeros(4 * nl.value * nl.value)
+        _check(self.lib.fdmgpu_batch_tau_ri(self.h, k_reg, k_irr, out.ctypes.data, C.byref(nl)))
+        n = nl.value // nspino
+        return out.view(np.complex128).reshape((n, nspino, n, nspino, 2), order="F").copy()
 
     def taull_all(self) -> List[np.ndarray]:
         """Taull of every energy of the last batch, in one device-to-host copy."""

@@ -397,6 +397,16 @@ fdmgpu_status fdmgpu_batch_rerun(fdmgpu_handle* h, fdmgpu_info* info);
  * batch nlm = nspino * (lmax + 1)^2 and the index is (Lm0 - 1) + (lmax + 1)^2
  * (spin - 1), the reference's Taull(Lm0, spin, Lm0', spin'). */
 fdmgpu_status fdmgpu_batch_taull(fdmgpu_handle* h, int32_t k, double* taull, int32_t* nlm);
+/* Tau_RI of FDM_comp (source/mat.f90:219-292, the complex-energy mode with
+ * the irregular solution, source/fdm.f90:1734-1738) from the batch's regular
+ * solution k_reg and irregular solution k_irr (irregular = 1, n_ato_RI = 2) of
+ * the same energy, site and absorber: writes 2*nlm*nlm complex values, the
+ * Taull layout of fdmgpu_batch_taull for i_RI = 1 (amplitudes of the
+ * irregular problem's regular atomic solution) then i_RI = 2 (irregular
+ * atomic solution).  Computed on the device from the two solutions.  Returns
+ * the pair's solve status (FDMGPU_ERR_NOT_CONVERGED if either did not
+ * converge); refuses a batch that ran in chunks. */
+fdmgpu_status fdmgpu_batch_tau_ri(fdmgpu_handle* h, int32_t k_reg, int32_t k_irr, double* tau_ri, int32_t* nlm);
 /* Taull of every energy in one copy: nlm_k*nlm_k complex values per energy,
  * concatenated in add order (capacity counts doubles). */
 fdmgpu_status fdmgpu_batch_taull_all(fdmgpu_handle* h, double* taull, int64_t capacity);

@@ -55,6 +55,7 @@ def lib():
         L.oracle_assemble_dense_c.argtypes = [vp, vp, vp, vp]
         L.oracle_taull_c.argtypes = [vp, vp, C.c_int, vp, vp, C.c_int, vp, C.POINTER(C.c_int32)]
         L.oracle_cbessneu.argtypes = [C.c_double, C.c_double, C.c_double, C.c_double, C.c_int, vp, vp]
+        L.oracle_tau_ri.argtypes = [vp, vp, vp, vp, vp, vp, vp, C.c_int, vp, C.POINTER(C.c_int32)]
         _lib = L
     return _lib
 
@@ -168,6 +169,23 @@ def taull_c(grid_args, energy_args, x, iaabs=1, symmetrise=True):
         raise RuntimeError(f"oracle_taull_c failed with status {st}")
     k = nl.value
     t = out[:2 * (k * nsp) ** 2].view(np.complex128).reshape((k, nsp, k, nsp), order="F")
+    return t.copy()
+
+
+def tau_ri(grid_args, reg_args, x_reg, irr_args, x_irr, iaabs=1):
+    """Tau_RI (nlm, nsp, nlm, nsp, 2) of FDM_comp from the regular solution
+    x_reg and the irregular one x_irr (each (nlmso, nligne) complex)."""
+    nsp = int(grid_args.d["nspino"])
+    nl = C.c_int32(0)
+    out = np.zeros(4 * (64 * nsp) ** 2)
+    a = [np.asfortranarray(v) for v in (x_reg.real, x_reg.imag, x_irr.real, x_irr.imag)]
+    st = lib().oracle_tau_ri(C.addressof(grid_args.s), C.addressof(reg_args.s), a[0].ctypes.data, a[1].ctypes.data,
+                             C.addressof(irr_args.s), a[2].ctypes.data, a[3].ctypes.data, iaabs, out.ctypes.data,
+                             C.byref(nl))
+    if st != 0:
+        raise RuntimeError(f"oracle_tau_ri failed with status {st}")
+    k = nl.value
+    t = out[:4 * (k * nsp) ** 2].view(np.complex128).reshape((k, nsp, k, nsp, 2), order="F")
     return t.copy()
 
 

@@ -11,12 +11,16 @@
 // into two spin copies when the coupling vanishes, and the unitary relation
 // between the complex- and real-harmonic Taull.
 //
-// Restated (Cal_comp = true; irregular = Repres_comp = Base_hexa = false,
-// n_ato_RI = 1, so the FDM_comp regular+irregular pair is not covered):
+// Restated (Cal_comp = true; Repres_comp = Base_hexa = false; the regular
+// solution, and the irregular solution of FDM_comp with Test_reg = 0, i.e.
+// n_RI = n_ato_RI = 2):
 //   calcMatRow, complex branch        source/mat.f90:1034-1632
 //     grid rows with the relativistic and spin-orbit gradient terms :1142-1402
-//     outer-sphere rows                                             :1405-1511
-//     atom rows                                                     :1515-1632
+//       (irregular: both atom-solution columns, no outer-sphere columns,
+//       right-hand side from -i j_l + n_l, :1266-1369)
+//     outer-sphere rows (regular solution only)                     :1405-1511
+//     atom rows (irregular: the boundary points split in halves)    :1515-1632
+//   Tau_RI, the regular x irregular amplitude products   source/mat.f90:219-292
 //   Yc (complex harmonic from two real ones)  source/mat.f90:1733-1754
 //   cbessneu (complex-argument j_l, n_l)       source/sphere.f90:7226-7254
 //   mat_solve (Gaussian), complex branch       source/mat_solve_gaussian.f90:196-358
@@ -48,18 +52,20 @@ cdouble Yc(int m, double y1, double y2) {
   return cdouble(y1, y2) * sgn * sqrt_1o2;
 }
 
-// phiato(ib, Lm, isp, isol, 1, ia, 1 + part): part 0 real, 1 imaginary.
-double PhiatoPart(const Ctx& c, int ib, int lm, int isp, int isol, int ia, int part) {
+// phiato(ib, Lm, isp, isol, i_RI, ia, 1 + part): part 0 real, 1 imaginary;
+// i_RI 1 the regular, 2 the irregular atomic solution.
+double PhiatoPart(const Ctx& c, int ib, int lm, int isp, int isol, int ia, int part, int iri = 1) {
   const fdmgpu_energy* e = c.e;
   const int64_t d1 = e->nphiato1, d2 = e->nlmagm, d3 = e->nspinp, d4 = c.nspino, d5 = e->n_RI;
   const int64_t d6 = c.g->natome;
-  const int64_t off = (ib - 1) + d1 * ((lm - 1) + d2 * ((isp - 1) + d3 * ((isol - 1) + d4 * ((0) + d5 * ((ia - 1) +
+  const int64_t off = (ib - 1) + d1 * ((lm - 1) + d2 * ((isp - 1) + d3 * ((isol - 1) + d4 * ((iri - 1) + d5 * ((ia - 1) +
                       d6 * part)))));
   return e->phiato[off];
 }
-cdouble PhiatoC(const Ctx& c, int ib, int lm, int isp, int isol, int ia) {
-  if (c.e->nphiato7 == 2) return cdouble(PhiatoPart(c, ib, lm, isp, isol, ia, 0), PhiatoPart(c, ib, lm, isp, isol, ia, 1));
-  return cdouble(PhiatoPart(c, ib, lm, isp, isol, ia, 0), 0.0);
+cdouble PhiatoC(const Ctx& c, int ib, int lm, int isp, int isol, int ia, int iri = 1) {
+  if (c.e->nphiato7 == 2)
+    return cdouble(PhiatoPart(c, ib, lm, isp, isol, ia, 0, iri), PhiatoPart(c, ib, lm, isp, isol, ia, 1, iri));
+  return cdouble(PhiatoPart(c, ib, lm, isp, isol, ia, 0, iri), 0.0);
 }
 // Complex Bessel / Neuman (2, nsort_c, 0:lmaxso, nspinr), interleaved.
 cdouble BesC(const Ctx& c, const double* a, int ib, int L, int isp) {
@@ -94,9 +100,11 @@ cdouble outer_column_factor(const Ctx& c, int ib, int L, int ispq) {
   if (e->E_comp) return BesC(c, e->Bessel, ib, L, ispq) + img * BesC(c, e->Neuman, ib, L, ispq);
   return cdouble(Bes(c, e->Besselr, ib, L, ispq), Bes(c, e->Neumanr, ib, L, ispq));
 }
-// Incoming (regular) factor of the right-hand side.
+// Radial factor of the right-hand side: the incoming j_l of the regular
+// solution, -i j_l + n_l of the irregular one (complex energies only).
 cdouble outer_rhs_factor(const Ctx& c, int ib, int L, int ispq) {
   const fdmgpu_energy* e = c.e;
+  if (e->irregular) return -img * BesC(c, e->Bessel, ib, L, ispq) + BesC(c, e->Neuman, ib, L, ispq);
   if (e->E_comp) return BesC(c, e->Bessel, ib, L, ispq);
   return cdouble(Bes(c, e->Besselr, ib, L, ispq), 0.0);
 }
@@ -202,21 +210,27 @@ void calc_mat_row_c(const Ctx& c, int ii, cdouble* row, int lb1, cdouble* rhs) {
             cfvs_r[s - 1] = c.Kar(isym, s) * cfvs_r[s - 1];
             cfvs_i[s - 1] = c.Kar(isym, s) * cfvs_i[s - 1];
           }
-        for (int Lm = 1; Lm <= e->nlmsa[ia - 1]; ++Lm) {
-          const int jjj = e->ianew[ia - 1] + Lm;
-          const int L = Lato(c, Lm, ia);
-          const int isol = Iato(c, Lm, ia);
-          for (int ispo = 1; ispo <= nspino; ++ispo) {
-            const int m = Mato(c, Lm, ia) + ispo - isol;
-            if (m > L || m < -L) continue;
-            const int Lm0 = L * L + L + 1 + m;
-            if (e->Spinorbite) {
-              A(jjj) += cdouble(cfvs_r[ispo - 1], cfvs_i[ispo - 1]) * PhiatoC(c, ib, Lm0, ispo, isol, ia);
-            } else if (e->nphiato7 == 2) {
-              A(jjj) += cdouble(cfvs_r[isp - 1], cfvs_i[isp - 1]) * PhiatoC(c, ib, Lm0, ispp, isol, ia);
-            } else {
-              const double ph = PhiatoPart(c, ib, Lm0, ispp, isol, ia, 0);
-              A(jjj) += cdouble(cfvs_r[isp - 1] * ph, cfvs_i[isp - 1] * ph);
+        // one column block per atomic solution: the regular amplitudes, and
+        // with the irregular solution the irregular ones after them
+        for (int jri = 1; jri <= e->n_ato_RI; ++jri) {
+          const int iri = e->irregular ? jri : 1;
+          for (int Lm = 1; Lm <= e->nlmsa[ia - 1]; ++Lm) {
+            int jjj = e->ianew[ia - 1] + Lm;
+            if (iri == 2 && e->n_ato_RI == 2) jjj += e->nlmsa[ia - 1];
+            const int L = Lato(c, Lm, ia);
+            const int isol = Iato(c, Lm, ia);
+            for (int ispo = 1; ispo <= nspino; ++ispo) {
+              const int m = Mato(c, Lm, ia) + ispo - isol;
+              if (m > L || m < -L) continue;
+              const int Lm0 = L * L + L + 1 + m;
+              if (e->Spinorbite) {
+                A(jjj) += cdouble(cfvs_r[ispo - 1], cfvs_i[ispo - 1]) * PhiatoC(c, ib, Lm0, ispo, isol, ia, iri);
+              } else if (e->nphiato7 == 2) {
+                A(jjj) += cdouble(cfvs_r[isp - 1], cfvs_i[isp - 1]) * PhiatoC(c, ib, Lm0, ispp, isol, ia, iri);
+              } else {
+                const double ph = PhiatoPart(c, ib, Lm0, ispp, isol, ia, 0, iri);
+                A(jjj) += cdouble(cfvs_r[isp - 1] * ph, cfvs_i[isp - 1] * ph);
+              }
             }
           }
         }
@@ -224,7 +238,8 @@ void calc_mat_row_c(const Ctx& c, int ii, cdouble* row, int lb1, cdouble* rhs) {
         int ib;
         for (ib = g->nsortf + 1; ib <= g->nsort; ++ib)
           if (j == g->isrt[ib - 1]) break;
-        for (int Lm = 1; Lm <= e->nlmso; ++Lm) {
+        // the irregular solution has no scattered wave in the outer sphere
+        for (int Lm = 1; Lm <= (e->irregular ? 0 : e->nlmso); ++Lm) {
           const int L = Lso(c, Lm), m = Mso(c, Lm);
           const int Lm0 = L * L + L + 1 + m;
           ispq = std::min(Iso(c, Lm), e->nspinr);
@@ -296,12 +311,23 @@ void calc_mat_row_c(const Ctx& c, int ii, cdouble* row, int lb1, cdouble* rhs) {
     }
   } else {
     const int ia = -i;
-    const int Lm = ii - e->ianew[ia - 1];
+    const int nl = e->nlmsa[ia - 1];
+    const int Ln = ii - e->ianew[ia - 1];
+    // with both atomic solutions the rows of the irregular amplitudes follow
+    // those of the regular ones
+    const int iri = (e->n_ato_RI == 2 && Ln > nl) ? 2 : 1;
+    const int Lm = iri == 2 ? Ln - nl : Ln;
     const int L = Lato(c, Lm, ia);
     const int ispt = Iato(c, Lm, ia);
     const int m = Mato(c, Lm, ia);
     const int Lm0 = L * L + L + 1 + m;
+    // irregular solution: the first half of the boundary points carries the
+    // regular, the second half the irregular matching
+    const int nhalf = g->nbordf[ia - 1] / 2;
+    const bool split = e->irregular && e->n_ato_RI == 2;
     for (int ib = 1; ib <= g->nbordf[ia - 1]; ++ib) {
+      if (split && iri == 1 && ib > nhalf) break;
+      if (split && iri == 2 && ib <= nhalf) continue;
       const int j = c.ibord(ib, ia);
       const int isym = std::abs(c.isbord(ib, ia));
       const int jj = e->new_[j] - nspino + ispt;
@@ -313,31 +339,44 @@ void calc_mat_row_c(const Ctx& c, int ii, cdouble* row, int lb1, cdouble* rhs) {
         cfac = c.poidsa(ib, ia) * std::conj(yc) * cdouble(c.Kar(isym, ispt), -Kari(c, isym, ispt)) / g->rvol[j - 1];
       A(jj) -= cfac;
     }
-    for (int Lmp = 1; Lmp <= e->nlmsa[ia - 1]; ++Lmp) {
-      const int Lp = Lato(c, Lmp, ia);
-      const int isol = Iato(c, Lmp, ia);
-      const int mp = Mato(c, Lmp, ia) + ispt - isol;
-      if (mp > Lp || mp < -Lp) continue;
-      const int Lmp0 = Lp * Lp + Lp + 1 + mp;
-      const int ispint = e->Spinorbite ? std::min(ispt, e->nspinp) : std::min(ispin, e->nspinp);
-      double charmr = 0.0, charmi = 0.0;
-      for (int ib = 1; ib <= g->nbordf[ia - 1]; ++ib) {
-        cdouble cfac = PhiatoC(c, ib, Lmp0, ispint, isol, ia);
-        if (e->Ylm_comp && m != 0)
-          cfac = cfac * std::conj(Yc(m, Ylmato(c, ib, Lm0, ia), Ylmato(c, ib, Lm0 - 2 * m, ia)));
-        else
-          cfac = cfac * Ylmato(c, ib, Lm0, ia);
-        charmr = charmr + c.poidsa(ib, ia) * cfac.real();
-        charmi = charmi + c.poidsa(ib, ia) * cfac.imag();
+    for (int jri = 1; jri <= (e->irregular ? 2 : 1); ++jri) {
+      for (int Lmp = 1; Lmp <= nl; ++Lmp) {
+        const int Lp = Lato(c, Lmp, ia);
+        const int isol = Iato(c, Lmp, ia);
+        const int mp = Mato(c, Lmp, ia) + ispt - isol;
+        if (mp > Lp || mp < -Lp) continue;
+        const int Lmp0 = Lp * Lp + Lp + 1 + mp;
+        const int ispint = e->Spinorbite ? std::min(ispt, e->nspinp) : std::min(ispin, e->nspinp);
+        double charmr = 0.0, charmi = 0.0;
+        for (int ib = 1; ib <= g->nbordf[ia - 1]; ++ib) {
+          if (e->irregular && jri == 1 && ib > nhalf) break;
+          if (e->irregular && jri == 2 && ib <= nhalf) continue;
+          cdouble cfac = PhiatoC(c, ib, Lmp0, ispint, isol, ia, jri);
+          if (e->Ylm_comp && m != 0)
+            cfac = cfac * std::conj(Yc(m, Ylmato(c, ib, Lm0, ia), Ylmato(c, ib, Lm0 - 2 * m, ia)));
+          else
+            cfac = cfac * Ylmato(c, ib, Lm0, ia);
+          charmr = charmr + c.poidsa(ib, ia) * cfac.real();
+          charmi = charmi + c.poidsa(ib, ia) * cfac.imag();
+        }
+        int ljj = e->ianew[ia - 1] + Lmp;
+        if (jri == 2 && e->n_ato_RI == 2) ljj += nl;
+        A(ljj) += cdouble(charmr, charmi);
       }
-      A(e->ianew[ia - 1] + Lmp) += cdouble(charmr, charmi);
     }
   }
 }
 
 int check_supported_c(const fdmgpu_grid* g, const fdmgpu_energy* e) {
-  if (!e->Cal_comp || e->irregular || e->Repres_comp || e->Base_hexa || e->n_ato_RI != 1 || e->n_RI != 1)
+  if (!e->Cal_comp || e->Repres_comp || e->Base_hexa) return FDMGPU_ERR_UNSUPPORTED;
+  if (e->irregular) {
+    // FDM_comp's irregular solution with both atomic solutions (Test_reg = 0)
+    if (e->n_RI != 2 || e->n_ato_RI != 2 || e->Test_reg != 0 || !e->E_comp || e->Basereel)
+      return FDMGPU_ERR_UNSUPPORTED;
+    if (e->nligneso != e->nligne) return FDMGPU_ERR_ARG;
+  } else if (e->n_ato_RI != 1 || e->n_RI < 1 || e->n_RI > 2) {
     return FDMGPU_ERR_UNSUPPORTED;
+  }
   if (e->Spinorbite != (g->nspino == 2)) return FDMGPU_ERR_ARG;
   if (e->Spinorbite && g->nspin != 2) return FDMGPU_ERR_UNSUPPORTED;
   if ((e->Relativiste || e->Spinorbite) && !e->gradvr) return FDMGPU_ERR_ARG;
@@ -594,6 +633,54 @@ int oracle_taull_c(const fdmgpu_grid* g, const fdmgpu_energy* e, int iaabs, cons
     }
   }
   std::memcpy(taull, T.data(), sizeof(cdouble) * T.size());
+  if (nlm_out) *nlm_out = nlmq;
+  return 0;
+}
+
+// Tau_RI of atom iaabs (FDM_comp, source/mat.f90:219-292): from the regular
+// solution (problem e_reg, smr_reg + i smi_reg) and the irregular one (e_irr),
+// Tau_RI(Lm1 s1, Lm2 s2, i_RI) = sum_f Ampl(f, Lm1) Ampl_I(f, (i_RI - 1) nlmsa + Lm2)
+// with Ampl the regular amplitudes of the atom's rows and Ampl_I the
+// irregular problem's amplitudes (regular atomic solution, then irregular);
+// no conjugate, no symmetrisation (the reference skips it with FDM_comp).
+// s = iato with spin-orbit, else 1.  tau_ri: (nlmq, nsp, nlmq, nsp, 2) complex
+// interleaved; *nlm_out = nlmq.
+int oracle_tau_ri(const fdmgpu_grid* g, const fdmgpu_energy* e_reg, const double* smr_reg, const double* smi_reg,
+                  const fdmgpu_energy* e_irr, const double* smr_irr, const double* smi_irr, int iaabs, double* tau_ri,
+                  int32_t* nlm_out) {
+  if (e_reg->irregular || !e_irr->irregular || e_irr->n_ato_RI != 2 || e_reg->nlmso != e_irr->nlmso ||
+      e_reg->nlmsa[iaabs - 1] != e_irr->nlmsa[iaabs - 1])
+    return FDMGPU_ERR_ARG;
+  Ctx c = make_ctx(g, e_reg);
+  const int nlmso = e_reg->nlmso;
+  const int ia = iaabs;
+  const int nlm = e_reg->nlmsa[ia - 1];
+  const int nsp = c.nspino;
+  int lmax = 0;
+  for (int Lm = 1; Lm <= nlm; ++Lm) lmax = std::max(lmax, Lato(c, Lm, ia));
+  const int nlmq = (lmax + 1) * (lmax + 1);
+  const int64_t dim = (int64_t)nlmq * nsp;
+  std::vector<cdouble> T((size_t)(2 * dim * dim), 0.0);
+  for (int Lm1 = 1; Lm1 <= nlm; ++Lm1) {
+    const int L1 = Lato(c, Lm1, ia), m1 = Mato(c, Lm1, ia);
+    const int is1 = e_reg->Spinorbite ? Iato(c, Lm1, ia) : 1;
+    const int64_t row = (L1 * L1 + L1 + m1) + (int64_t)nlmq * (is1 - 1);
+    const int64_t ii = e_reg->ianew[ia - 1] + Lm1;
+    for (int iri = 1; iri <= 2; ++iri)
+      for (int Lm2 = 1; Lm2 <= nlm; ++Lm2) {
+        const int L2 = Lato(c, Lm2, ia), m2 = Mato(c, Lm2, ia);
+        const int is2 = e_reg->Spinorbite ? Iato(c, Lm2, ia) : 1;
+        const int64_t col = (L2 * L2 + L2 + m2) + (int64_t)nlmq * (is2 - 1);
+        const int64_t jj = e_irr->ianew[ia - 1] + (iri - 1) * nlm + Lm2;
+        cdouble& t = T[(size_t)(row + dim * col + dim * dim * (iri - 1))];
+        for (int f = 0; f < nlmso; ++f) {
+          const cdouble a(smr_reg[f + (ii - 1) * nlmso], smi_reg[f + (ii - 1) * nlmso]);
+          const cdouble b(smr_irr[f + (jj - 1) * nlmso], smi_irr[f + (jj - 1) * nlmso]);
+          t = t + a * b;
+        }
+      }
+  }
+  std::memcpy(tau_ri, T.data(), sizeof(cdouble) * T.size());
   if (nlm_out) *nlm_out = nlmq;
   return 0;
 }

@@ -520,3 +520,38 @@ def test_complex_energy_matches_oracle(solver_mod, spinorbit):
     for k, (_, T0) in enumerate(refs):
         assert np.abs(sv.taull_c(k, nsp) - T0).max() <= 1e-9 * np.abs(T0).max()
     sv.close()
+
+
+@pytest.mark.parametrize("spinorbit", [False, True])
+def test_fdm_comp_irregular_solution_and_tau_ri(solver_mod, spinorbit):
+    """FDM_comp at 12 eV + 0.5 eV i: the irregular cluster solution (both
+    atomic solutions, boundary points split in halves, no outer-sphere rows)
+    against the oracle's complex solve (FP64 1e-9, mixed 1e-8), and Tau_RI
+    formed on the device from a batch holding the regular and the irregular
+    solution against the oracle's Tau_RI (FP64 1e-9, mixed 1e-7, per i_RI
+    block)."""
+    import oracle
+    from fdmnes_gb300 import abi, complex_path as CP
+    st = CP.pt_so_structure()
+    ga = abi.GridArgs(CP.grid_dict(st, spinorbit))
+    eim = 0.5 / 13.605693122994
+    er = abi.EnergyArgs(CP.energy_dict(st, 12.0, spinorbit=spinorbit, eimag_ry=eim, fdm_comp=True))
+    ei = abi.EnergyArgs(CP.energy_dict(st, 12.0, spinorbit=spinorbit, eimag_ry=eim, irregular=True))
+    Xr0, _ = oracle.mat_solve_c(ga, er)
+    Xi0, _ = oracle.mat_solve_c(ga, ei)
+    T0 = oracle.tau_ri(ga, er, Xr0, ei, Xi0)
+    nsp = 2 if spinorbit else 1
+    sv = solver_mod.FdmSolver(ga.d)
+    X, _ = sv.mat_solve_complex(ei, "fp64")
+    assert rel(X, Xi0) < 1e-9
+    Xm, _ = sv.mat_solve_complex(ei, "mixed")
+    assert rel(Xm, Xi0) < 1e-8
+    for prec, tol in (("fp64", 1e-9), ("mixed", 1e-7)):
+        sv.spectrum_begin(prec, 2)
+        sv.spectrum_add_args(er)
+        sv.spectrum_add_args(ei)
+        sv.spectrum_run()
+        T = sv.tau_ri(0, 1, nsp)
+        for iri in range(2):
+            assert np.abs(T[..., iri] - T0[..., iri]).max() <= tol * np.abs(T0[..., iri]).max(), (prec, iri)
+    sv.close()

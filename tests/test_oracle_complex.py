@@ -15,7 +15,11 @@ K4  spin-orbit with the coupling switched off (gradvr = 0, no relativistic
     terms, spin-diagonal atomic solutions) decouples into two copies of the
     complex-harmonic problem, bit for bit;
 K5  complex harmonics give Taull_c = U Taull_r U^H, U the unitary map of Yc
-    (source/mat.f90:1733-1754) from the real harmonics.
+    (source/mat.f90:1733-1754) from the real harmonics;
+K7  FDM_comp's irregular cluster solution (both atomic solutions, the
+    boundary points split in halves, no outer-sphere rows): the Gaussian
+    profile solve equals a dense LU solve of the same assembled matrix, and
+    Tau_RI is the product of the two solutions' amplitudes.
 """
 import numpy as np
 import pytest
@@ -229,3 +233,70 @@ def test_k6_complex_energy_is_continuous_at_real_energies(pt, spinorbit):
     assert abs(diff[1e-8] / 1e-8 - diff[1e-6] / 1e-6) <= 0.05 * diff[1e-6] / 1e-6
     ea = abi.EnergyArgs(CP.energy_dict(pt, E, spinorbit=spinorbit, eimag_ry=0.037))
     assert _dense_rel(ga, ea) < (1e-9 if spinorbit else 1e-12)
+
+
+EIMAG_RY = 0.5 / 13.605693122994
+
+
+@pytest.mark.parametrize("spinorbit", [False, True])
+def test_k7_dense_lu_irregular_solution(pt, spinorbit):
+    """Irregular solution at 12 eV + 0.5 eV i (nligne 838 / 1676); measured
+    1.8e-12 and 2.9e-12."""
+    ga = abi.GridArgs(CP.grid_dict(pt, spinorbit))
+    ea = abi.EnergyArgs(CP.energy_dict(pt, E, spinorbit=spinorbit, eimag_ry=EIMAG_RY, irregular=True))
+    assert ea.d["nligneso"] == ea.nligne
+    assert _dense_rel(ga, ea) < 1e-9
+
+
+def test_newind_irregular_numbering(pt):
+    """newind with the irregular solution (source/mat.f90:1761-1921): no
+    outer-sphere rows, 2 nlmsa amplitude rows per atom, the grid rows in the
+    regular numbering's order, a profile that brackets the diagonal."""
+    from fdmnes_gb300 import cluster as CL
+    for nspino in (1, 2):
+        ei = CL.energy_inputs(pt, E)
+        nlmsa = (nspino * (ei.lmaxa + 1) ** 2).astype(np.int32)
+        nlmso = nspino * (ei.lmaxso + 1) ** 2
+        reg = CL.newind(pt, nlmsa, nlmso, nspino)
+        irr = CL.newind(pt, nlmsa, nlmso, nspino, irregular=True)
+        assert irr.nligne == reg.nligne - nlmso + int(nlmsa.sum())
+        assert irr.nligneso == irr.nligne
+        assert not np.any(irr.newinv == 0)
+        for ia in range(pt.natome):
+            assert np.count_nonzero(irr.newinv == -(ia + 1)) == 2 * nlmsa[ia]
+        assert np.array_equal(reg.newinv[reg.newinv > 0], irr.newinv[irr.newinv > 0])
+        rows = np.arange(1, irr.nligne + 1)
+        assert np.all(irr.lb1 <= rows) and np.all(rows <= irr.lb2) and np.all(irr.lb2 <= irr.nligne)
+        assert np.all(np.diff(irr.lb1) >= 0)
+
+
+def test_k7_tau_ri_is_the_amplitude_product(pt):
+    """Tau_RI(Lm1, Lm2, i_RI) = sum_f Ampl(f, Lm1) Ampl_I(f, (i_RI - 1) nlmsa + Lm2)
+    (source/mat.f90:219-292), restated here with numpy on the oracle's solutions."""
+    from fdmnes_gb300 import cluster as CL
+    ga = abi.GridArgs(CP.grid_dict(pt, False))
+    er = abi.EnergyArgs(CP.energy_dict(pt, E, spinorbit=False, eimag_ry=EIMAG_RY, fdm_comp=True))
+    ei = abi.EnergyArgs(CP.energy_dict(pt, E, spinorbit=False, eimag_ry=EIMAG_RY, irregular=True))
+    Xr, _ = oracle.mat_solve_c(ga, er)
+    Xi, _ = oracle.mat_solve_c(ga, ei)
+    T = oracle.tau_ri(ga, er, Xr, ei, Xi)
+    nl = int(er.d["nlmsa"][0])
+    a0, b0 = int(er.d["ianew"][0]), int(ei.d["ianew"][0])
+    lato, mato = ga.d["lato"][:nl, 0], ga.d["mato"][:nl, 0]
+    idx = lato * lato + lato + mato
+    ref = np.zeros_like(T)
+    for iri in range(2):
+        P = Xr[:, a0:a0 + nl].T @ Xi[:, b0 + iri * nl:b0 + (iri + 1) * nl]
+        ref[np.ix_(idx, [0], idx, [0], [iri])] = P[:, None, :, None, None]
+    assert np.abs(T - ref).max() <= 1e-12 * np.abs(ref).max()
+    assert np.abs(T[..., 1]).max() > 0
+
+
+def test_irregular_solution_needs_complex_energies(pt):
+    with pytest.raises(ValueError):
+        CP.energy_dict(pt, E, spinorbit=False, irregular=True)
+    ga = abi.GridArgs(CP.grid_dict(pt, False))
+    d = CP.energy_dict(pt, E, spinorbit=False, eimag_ry=EIMAG_RY, irregular=True)
+    d.update(Test_reg=1)     # the reference's test keyword: not restated
+    with pytest.raises(RuntimeError):
+        oracle.mat_solve_c(ga, abi.EnergyArgs(d))
