@@ -1061,11 +1061,10 @@ fdmgpu_status capture(fdmgpu_handle* h, void (*rec)(fdmgpu_handle*), cudaGraphEx
   return FDMGPU_OK;
 }
 
-// Last resort of the mixed path: the listed problems (whose FP64 bands the
-// double-float escalation has overwritten) are assembled again in FP64 (the
-// complex assembly for a complex batch) and solved by the FP64 elimination, as
-// the FP64 path solves them; one grid row per listed problem.  Returns the
-// launches.
+// Last resort of the mixed path for real batches: the listed problems (whose
+// FP64 bands the double-float escalation has overwritten) are assembled again
+// in FP64 and solved by the FP64 elimination, as the FP64 path solves them;
+// one grid row per listed problem.  Returns the launches.
 int64_t solve_fp64_subset(fdmgpu_handle* h, const std::vector<int>& list) {
   cudaStream_t s = h->stream;
   Batch& b = h->batch;
@@ -1087,15 +1086,11 @@ int64_t solve_fp64_subset(fdmgpu_handle* h, const std::vector<int>& list) {
   pf.active = nullptr;
   LaunchDims df = h->dims;
   df.nprob = ne;
-  if (b.cplx == 1)
-    launch_assemble_c(h->d_sites.p, h->d_probs_esc.p, pf, h->tb, df, 0, s);
-  else
-    launch_assemble(h->d_sites.p, h->d_probs_esc.p, pf, h->tb, df, s);
+  launch_assemble(h->d_sites.p, h->d_probs_esc.p, pf, h->tb, df, s);
   launch_copy_rhs(h->d_probs_esc.p, pf, df, s);
   int64_t nk = 8;
-  // the real-equivalent form of a complex problem pivots inside the diagonal tiles, as the FP64 path does
   nk += launch_factor<double>(h->sp, h->pl.env64, h->pl.X64, h->d_probs_esc.p, h->tb, ne, 1, nullptr,
-                              h->d_err_esc.p, 1e-10, b.cplx == 1 ? h->pl.piv : nullptr, s);
+                              h->d_err_esc.p, 1e-10, nullptr, s);
   nk += launch_backward<double>(h->sp, h->pl.env64, h->pl.X64, h->d_probs_esc.p, h->tb, ne, nullptr, s);
   launch_scatter_err(h->d_esc_list.p, ne, h->d_err_esc.p, h->pl.err, s);
   cudaStreamSynchronize(s);  // the host list lives until here
@@ -1631,6 +1626,8 @@ fdmgpu_status run_batch(fdmgpu_handle* h, fdmgpu_info* info, bool resident) {
         std::vector<int> last;
         for (int k = 0; k < np; ++k)
           if (act2[k]) last.push_back(k);
+        // (real batches only: a complex energy left above the level is
+        // reported not converged with its double-float solution)
         if (h->escalate_f32 && !last.empty() && b.cplx != 1) {
           const int64_t nk64 = solve_fp64_subset(h, last);
           if (nk64 < 0) return fail(FDMGPU_ERR_NOMEM, "FP64 re-solve descriptors");
