@@ -95,6 +95,38 @@ def test_radial_solution_free_space():
         assert np.std(ratio) / abs(np.mean(ratio)) < 2e-3
 
 
+def test_transparent_absorber_does_not_scatter(oracle_lib):
+    """Whole-system known answer: with the potential flat at the interstitial
+    level and the free-space j_l(k r) Y as the atom's boundary functions,
+    nothing scatters: the real-basis scattering amplitudes (the outer rows of
+    the solution) of the L <= 3 waves vanish up to the fourth-order stencil's
+    error and fall with the grid step (measured 1.1e-3, 2.4e-4 at h = 0.3,
+    0.2 A).  Pins the signs and normalisations of the grid, atom and outer
+    rows and of the Bessel / Neumann functions together."""
+    import dataclasses
+    from scipy.special import spherical_jn
+    worst = []
+    for h in (0.3, 0.2):
+        st = CL.build_structure(CL.cu_cluster(0.5), h, 1.6, 35.0)
+        g = st.grid
+        st.Vr[:, :] = st.V0bd
+        ei = CL.energy_inputs(st, 12.0)
+        k = np.sqrt(ei.ecinetic_out)
+        phi = np.zeros_like(ei.phiato)
+        nb = int(g.nbord[0])
+        for L in range(int(ei.lmaxa[0]) + 1):
+            jl = spherical_jn(L, k * st.rrel[:nb, 0])
+            for m in range(-L, L + 1):
+                lm = L * L + L + m
+                phi[:nb, lm, 0, 0, 0, 0, 0] = jl * st.Ylmato[:nb, lm, 0]
+        ei = dataclasses.replace(ei, phiato=phi)
+        ri = CL.newind(st, ei.nlmsa, ei.nlmso)
+        X, _ = oracle_lib.mat_solve(abi.GridArgs(st), abi.EnergyArgs(st, ei, ri))
+        sel = np.nonzero(np.floor(np.sqrt(np.arange(ei.nlmso))) <= 3)[0]
+        worst.append(np.abs(X[sel][:, ri.nligneso:][:, sel]).max())
+    assert worst[0] < 2e-3 and worst[1] < 5e-4 and worst[1] < worst[0] / 3, worst
+
+
 def test_newind_matches_oracle(oracle_lib):
     st = CL.small_cu_structure()
     ga = abi.GridArgs(st)

@@ -19,7 +19,16 @@ K5  complex harmonics give Taull_c = U Taull_r U^H, U the unitary map of Yc
 K7  FDM_comp's irregular cluster solution (both atomic solutions, the
     boundary points split in halves, no outer-sphere rows): the Gaussian
     profile solve equals a dense LU solve of the same assembled matrix, and
-    Tau_RI is the product of the two solutions' amplitudes.
+    Tau_RI is the product of the two solutions' amplitudes;
+K8  a transparent absorber (flat potential at the interstitial level, the
+    free-space j_l and n_l as atomic solutions) at a complex energy: the
+    regular solution is the incoming wave (atom amplitude sqrt(k/pi), no
+    outgoing wave) up to the fourth-order stencil's error, and the exact
+    irregular field sqrt(k/pi) (-i j_l + n_l) Y satisfies the irregular
+    system's grid rows to the same order.  The irregular atom rows follow the
+    reference's rule (each amplitude block projected on the half of the
+    boundary points of its own atomic solution, source/mat.f90:1582-1605), so
+    the two rows of one harmonic share their amplitude entries.
 """
 import numpy as np
 import pytest
@@ -300,3 +309,92 @@ def test_irregular_solution_needs_complex_energies(pt):
     d.update(Test_reg=1)     # the reference's test keyword: not restated
     with pytest.raises(RuntimeError):
         oracle.mat_solve_c(ga, abi.EnergyArgs(d))
+
+
+def _transparent_pt(adimp, irregular, E=12.0):
+    """Pt absorber alone, flat potential at the interstitial level of each spin
+    block, complex energy (0.5 eV), phiato = free-space j_l (regular) and n_l
+    (irregular) times the complex harmonics."""
+    st = CP.pt_so_structure(adimp_ang=adimp)
+    g = st.grid
+    for isp in range(st.nspin):
+        st.Vr[:, isp] = st.V0bd + st.spin_shift(isp + 1)
+    ga = abi.GridArgs(CP.grid_dict(st, False))
+    d = CP.energy_dict(st, E, spinorbit=False, eimag_ry=EIMAG_RY, fdm_comp=True, irregular=irregular)
+    from fdmnes_gb300 import cluster as CL
+    k = np.sqrt(complex(CL.energy_inputs(st, E).ecinetic_out, EIMAG_RY))
+    nl = int(d["nlmsa"][0])
+    lmaxa = int(round(np.sqrt(nl))) - 1
+    nb = int(g.nbord[0])
+    bs, nm = CP.cbessneu(1.0, k * st.rrel[:nb, 0], lmaxa)
+    phi = np.zeros_like(d["phiato"])
+    for L in range(lmaxa + 1):
+        for m in range(-L, L + 1):
+            lm = L * L + L + m
+            y = CP.yc(m, st.Ylmato[:nb, lm, 0], st.Ylmato[:nb, lm - 2 * m, 0])
+            for iri, f in enumerate((bs[:, L], nm[:, L])):
+                v = f * y
+                phi[:nb, lm, :, 0, iri, 0, 0] = v.real[:, None]
+                phi[:nb, lm, :, 0, iri, 0, 1] = v.imag[:, None]
+    d["phiato"] = np.asfortranarray(phi)
+    return st, ga, abi.EnergyArgs(d), d, np.sqrt(k / np.pi), k
+
+
+def test_k8_transparent_absorber_regular_solution():
+    """Measured: amplitude error 1.4e-3 / 3.0e-4 and outgoing amplitudes
+    1.1e-3 / 2.4e-4 at h = 0.3 / 0.2 A (L <= 3 waves)."""
+    errs = []
+    for h, bar in ((0.3, 3e-3), (0.2, 6e-4)):
+        st, ga, ea, d, fn, _ = _transparent_pt(h, irregular=False)
+        X, _ = oracle.mat_solve_c(ga, ea)
+        sel = np.nonzero(np.floor(np.sqrt(np.arange(d["nlmso"]))) <= 3)[0]
+        a0, nl = int(d["ianew"][0]), int(d["nlmsa"][0])
+        amp = np.abs(X[sel][:, a0:a0 + nl][:, sel] - fn * np.eye(len(sel))).max() / abs(fn)
+        out = np.abs(X[sel][:, d["nligneso"]:][:, sel]).max()
+        assert amp < bar and out < bar, (h, amp, out)
+        errs.append(amp)
+    assert errs[1] < errs[0] / 3
+
+
+def test_k8_irregular_grid_rows_hold_the_free_space_field():
+    """Residual of the irregular system's grid rows at the exact field
+    (normwise per row); measured for L <= 1: 3.3e-5 at h = 0.3 A, 2.7e-6 at 0.2 A."""
+    from fdmnes_gb300 import cluster as CL
+    res_h = []
+    for h in (0.3, 0.2):
+        st, ga, ea, d, fn, k = _transparent_pt(h, irregular=True)
+        A, B = oracle.assemble_dense_c(ga, ea)
+        newinv = np.asarray(d["newinv"])
+        rows = np.nonzero(newinv > 0)[0]
+        xyz = st.grid.xyz[:3, newinv[rows] - 1]
+        bs, nm = CP.cbessneu(fn, k * np.sqrt((xyz ** 2).sum(0)), 1)
+        Y = CL.real_ylm(1, xyz)
+        a0, nl = int(d["ianew"][0]), int(d["nlmsa"][0])
+        worst = 0.0
+        for L, m in ((0, 0), (1, -1), (1, 1)):
+            lm = L * L + L + m
+            x = np.zeros(A.shape[0], dtype=complex)
+            x[rows] = (-1j * bs[:, L] + nm[:, L]) * CP.yc(m, Y[lm], Y[lm - 2 * m])
+            x[a0 + lm] = -1j * fn
+            x[a0 + nl + lm] = fn
+            r = (A @ x - B[lm])[rows]
+            worst = max(worst, np.abs(r).max() / (np.abs(A[rows]).sum(1).max() * np.abs(x).max()))
+        res_h.append(worst)
+    assert res_h[0] < 1e-4 and res_h[1] < 1e-5 and res_h[1] < res_h[0] / 5, res_h
+
+
+def test_k8_irregular_atom_rows_follow_the_reference_rule():
+    """The rows of the regular and the irregular amplitudes of one harmonic
+    carry the same amplitude entries (both blocks projected on their own
+    atomic solution's half of the boundary points) and grid entries on
+    disjoint halves of the boundary points."""
+    st, ga, ea, d, fn, k = _transparent_pt(0.3, irregular=True)
+    A, _ = oracle.assemble_dense_c(ga, ea)
+    a0, nl = int(d["ianew"][0]), int(d["nlmsa"][0])
+    amp = slice(a0, a0 + 2 * nl)
+    grid = np.asarray(d["newinv"]) > 0
+    for lm in range(nl):
+        r1, r2 = A[a0 + lm], A[a0 + nl + lm]
+        assert np.array_equal(r1[amp], r2[amp])
+        assert not np.any((r1[grid] != 0) & (r2[grid] != 0))
+        assert np.any(r1[grid] != 0) and np.any(r2[grid] != 0)
