@@ -9,7 +9,10 @@
 // restatement could not be compared with reference-produced numbers ("parity
 // unpinned" against the reference binary).  It is pinned instead by
 // known-answer tests: closed-form Bessel functions and harmonics, the exact
-// stencil coefficients, and a dense LU solve of the same assembled matrix.
+// stencil coefficients, a dense LU solve of the same assembled matrix, and
+// the free-space answer of the whole system (a transparent absorber - flat
+// potential, free-space j_l as its boundary functions - scatters nothing, up
+// to the fourth-order stencil's error).
 //
 // Restated routines (real-arithmetic path: Cal_comp = E_comp = Spinorbite =
 // Relativiste = Repres_comp = Ylm_comp = irregular = false, nspino = 1):

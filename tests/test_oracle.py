@@ -3,7 +3,9 @@
 The reference ships no tests or golden outputs and cannot be compiled here
 (Fortran), so the oracle is pinned by known-answer tests: exact stencil
 coefficients, closed-form/scipy special functions, a dense LU solve of the
-same assembled matrix, and committed golden outputs (tests/golden).
+same assembled matrix, the free-space answer of the whole system (a
+transparent absorber scatters nothing), and committed golden outputs
+(tests/golden).
 """
 import numpy as np
 import pytest
