@@ -398,3 +398,53 @@ def test_k8_irregular_atom_rows_follow_the_reference_rule():
         assert np.array_equal(r1[amp], r2[amp])
         assert not np.any((r1[grid] != 0) & (r2[grid] != 0))
         assert np.any(r1[grid] != 0) and np.any(r2[grid] != 0)
+
+
+def test_k8_transparent_absorber_spin_orbit():
+    """Spin-orbit assembly (interleaved spin rows, lmrep tables, relativistic
+    diagonal) on a flat potential, where gradvr and with it every spin-orbit
+    coupling term vanishes, with spin-diagonal free-space j_l boundary
+    functions: the atom amplitude of harmonic (L, m, s) is sqrt(k/pi) for the
+    outer wave (L, m, s) and nothing scatters, in both spin channels.
+    Measured 1.5e-3 / 7.7e-4 (amplitudes), 1.1e-3 / 5.9e-4 (outgoing) at
+    h = 0.3 / 0.25 A."""
+    from fdmnes_gb300 import cluster as CL
+    errs = []
+    for h, bar in ((0.3, 3e-3), (0.25, 1.5e-3)):
+        st = CP.pt_so_structure(adimp_ang=h)
+        g = st.grid
+        st.Vr[:, :] = st.V0bd
+        st.spin_split = 0.0
+        ga = abi.GridArgs(CP.grid_dict(st, True))
+        d = CP.energy_dict(st, E, spinorbit=True)
+        assert np.abs(d["gradvr"]).max() < 1e-12
+        k = np.sqrt(CL.energy_inputs(st, E).ecinetic_out)
+        fn = np.sqrt(k / np.pi)
+        nl = int(d["nlmsa"][0])
+        lmaxa = int(round(np.sqrt(nl // 2))) - 1
+        nb = int(g.nbord[0])
+        bs, _ = CP.cbessneu(1.0, k * st.rrel[:nb, 0], lmaxa)
+        phi = np.zeros_like(d["phiato"])
+        for L in range(lmaxa + 1):
+            for m in range(-L, L + 1):
+                lm = L * L + L + m
+                v = bs[:, L].real * CP.yc(m, st.Ylmato[:nb, lm, 0], st.Ylmato[:nb, lm - 2 * m, 0])
+                for sp in range(2):
+                    phi[:nb, lm, sp, sp, 0, 0, 0] = v.real
+                    phi[:nb, lm, sp, sp, 0, 0, 1] = v.imag
+        d["phiato"] = np.asfortranarray(phi)
+        X, _ = oracle.mat_solve_c(ga, abi.EnergyArgs(d))
+        nlmso = int(d["nlmso"])
+        lso, mso, iso = (ga.d[k_][:nlmso] for k_ in ("lso", "mso", "iso"))
+        lato, mato, iato = (ga.d[k_][:nl, 0] for k_ in ("lato", "mato", "iato"))
+        sel = np.nonzero(lso <= 3)[0]
+        expect = np.zeros((nlmso, nl), dtype=complex)
+        for f in sel:
+            q = np.nonzero((lato == lso[f]) & (mato == mso[f]) & (iato == iso[f]))[0]
+            expect[f, q] = fn
+        a0 = int(d["ianew"][0])
+        amp = np.abs(X[sel][:, a0:a0 + nl] - expect[sel]).max() / abs(fn)
+        out = np.abs(X[sel][:, d["nligneso"]:][:, sel]).max()
+        assert amp < bar and out < bar, (h, amp, out)
+        errs.append(amp)
+    assert errs[1] < errs[0] / 1.6
