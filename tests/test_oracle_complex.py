@@ -23,7 +23,8 @@ K7  FDM_comp's irregular cluster solution (both atomic solutions, the
 K8  a transparent absorber (flat potential at the interstitial level, the
     free-space j_l and n_l as atomic solutions) at a complex energy: the
     regular solution is the incoming wave (atom amplitude sqrt(k/pi), no
-    outgoing wave) up to the fourth-order stencil's error, and the exact
+    outgoing wave; with the spin-orbit assembly in each spin channel) up to
+    the fourth-order stencil's error, and the exact
     irregular field sqrt(k/pi) (-i j_l + n_l) Y satisfies the irregular
     system's grid rows to the same order.  The irregular atom rows follow the
     reference's rule (each amplitude block projected on the half of the
