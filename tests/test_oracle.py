@@ -129,6 +129,42 @@ def test_transparent_absorber_does_not_scatter(oracle_lib):
     assert worst[0] < 2e-3 and worst[1] < 5e-4 and worst[1] < worst[0] / 3, worst
 
 
+def test_transparent_cluster_scattering_falls_with_the_atoms_l_cutoff(oracle_lib):
+    """The 13-atom Cu cluster made transparent (flat potential, free-space j_l
+    about each atom as its boundary functions): the incoming wave about the
+    absorber, seen from a neighbour 2.55 A away, needs many harmonics, so the
+    residual scattering is that of the atoms' l cut-off and falls fast as the
+    cut-off grows (measured max |S| of the L <= 3 waves 0.127 at lmax 4,
+    0.037 at lmax 5, h = 0.3 A).  Pins the multi-atom couplings (amplitude
+    blocks, boundary points of every atom) physically."""
+    import dataclasses
+    from scipy.special import spherical_jn
+    st = CL.build_structure(CL.cu_cluster(2.6), 0.3, 3.0, 300.0)
+    g = st.grid
+    st.Vr[:, :] = st.V0bd
+    ei0 = CL.energy_inputs(st, 12.0)
+    k = np.sqrt(ei0.ecinetic_out)
+    smax = []
+    for lmx in (4, 5):
+        lmaxa = np.minimum(st.lmaxat_max[st.cluster.itype], lmx).astype(np.int32)
+        assert lmaxa.min() == lmx
+        nlmsa = ((lmaxa + 1) ** 2).astype(np.int32)
+        phi = np.zeros((g.nbtm, int(nlmsa.max()), 1, 1, 1, st.natome, 1), order="F")
+        for ia in range(st.natome):
+            nb = int(g.nbord[ia])
+            for L in range(lmx + 1):
+                jl = spherical_jn(L, k * st.rrel[:nb, ia])
+                for m in range(-L, L + 1):
+                    lm = L * L + L + m
+                    phi[:nb, lm, 0, 0, 0, ia, 0] = jl * st.Ylmato[:nb, lm, ia]
+        ei = dataclasses.replace(ei0, phiato=phi, lmaxa=lmaxa, nlmsa=nlmsa, nlmagm=int(nlmsa.max()))
+        ri = CL.newind(st, ei.nlmsa, ei.nlmso)
+        X, _ = oracle_lib.mat_solve(abi.GridArgs(st), abi.EnergyArgs(st, ei, ri))
+        sel = np.nonzero(np.floor(np.sqrt(np.arange(ei.nlmso))) <= 3)[0]
+        smax.append(np.abs(X[sel][:, ri.nligneso:][:, sel]).max())
+    assert smax[0] < 0.2 and smax[1] < smax[0] / 2.5, smax
+
+
 def test_newind_matches_oracle(oracle_lib):
     st = CL.small_cu_structure()
     ga = abi.GridArgs(st)
