@@ -165,6 +165,25 @@ def test_transparent_cluster_scattering_falls_with_the_atoms_l_cutoff(oracle_lib
     assert smax[0] < 0.2 and smax[1] < smax[0] / 2.5, smax
 
 
+def test_single_atom_scattering_is_reciprocal_and_unitary(oracle_lib):
+    """A real potential at real energies: the T-matrix T = K (I + iK)^-1 built
+    from the real-basis scattering amplitudes K of the absorber alone (the
+    Taull renormalisation of source/mat.f90:312-343) is symmetric
+    (reciprocity) and bounded by 1 (unitarity), up to the discretisation
+    (measured asymmetry 8e-5..1.6e-3, |T| 0.91..1.00 at h = 0.25 A)."""
+    st = CL.build_structure(CL.cu_cluster(0.5), 0.25, 1.6, 35.0)
+    for E in (6.0, 12.0, 25.0):
+        ei = CL.energy_inputs(st, E)
+        ri = CL.newind(st, ei.nlmsa, ei.nlmso)
+        X, _ = oracle_lib.mat_solve(abi.GridArgs(st), abi.EnergyArgs(st, ei, ri))
+        K = X[:, ri.nligneso:].T
+        T = K @ np.linalg.inv(np.eye(K.shape[0]) + 1j * K)
+        sel = np.nonzero(np.floor(np.sqrt(np.arange(K.shape[0]))) <= 3)[0]
+        Ts = T[np.ix_(sel, sel)]
+        assert np.abs(Ts - Ts.T).max() < 3e-3 * np.abs(Ts).max(), E
+        assert np.abs(Ts).max() < 1.001, E
+
+
 def test_newind_matches_oracle(oracle_lib):
     st = CL.small_cu_structure()
     ga = abi.GridArgs(st)
