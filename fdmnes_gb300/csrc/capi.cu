@@ -2430,6 +2430,8 @@ fdmgpu_status fdmgpu_batch_tau_ri(fdmgpu_handle* h, int32_t k_reg, int32_t k_irr
     return fail(FDMGPU_ERR_ARG, "k_reg must be a regular and k_irr an irregular complex solution");
   if (P.site != Q.site || P.iaabs < 1 || P.iaabs != Q.iaabs || P.nlm_abs != Q.nlm_abs || P.nlmso != Q.nlmso)
     return fail(FDMGPU_ERR_ARG, "the pair must share the site, the absorber and the outer harmonics");
+  if (P.enervide != Q.enervide || P.eimag != Q.eimag || P.ispin != Q.ispin)
+    return fail(FDMGPU_ERR_ARG, "the pair must be one energy and spin block");
   if (nlm) *nlm = P.nlm_abs;
   if (!tau_ri) return FDMGPU_OK;
   const size_t n = 2 * (size_t)P.nlm_abs * P.nlm_abs;   // complex values
