@@ -170,10 +170,73 @@ def irregular_boundary_radial(st: CL.Structure, enervide: float, lmaxa: np.ndarr
     return out
 
 
+def sch_radial_singular(r: np.ndarray, V: np.ndarray, enervide: float, eimag: float, k: complex, L: int,
+                        i0: int) -> np.ndarray:
+    """Singular radial solution R_L(r) = us_L(r) / r on mesh r, complex
+    (source/sphere.f90:2591-2812 with Classic_irreg, scalar potential, no
+    spin-orbit, no Hubbard term): us = -i r h_L(k r), h_L = sqrt(k/pi)
+    (j_L + i n_L), from mesh index i0 outward, then the three-point recursion
+    of the regular solver (:324-396) run inward, with -i Eimag on the diagonal
+    for complex energies (:2752)."""
+    nr = len(r)
+    rp = np.empty(nr)
+    rm = np.empty(nr)
+    rp[:-1] = r[1:]
+    rp[-1] = r[-1] ** 2 / r[-2]
+    rm[1:] = r[:-1]
+    rm[0] = r[0] ** 2 / r[1]
+    dr = 0.5 * (rp - rm)
+    claplm = 1.0 / ((r - rm) * dr)
+    claplp = 1.0 / ((rp - r) * dr)
+    g0 = (claplm + claplp) + (V - enervide)
+    gm = -claplm
+    gp = -claplp
+    f2 = 1.0 / r ** 2
+    us = np.zeros(nr, dtype=np.complex128)
+    bs, nm = cbessneu(np.sqrt(k / np.pi), k * r[i0:], L)
+    us[i0:] = -1j * r[i0:] * (bs[:, L] + 1j * nm[:, L])
+    L2 = L * (L + 1)
+    for ir in range(i0, 0, -1):
+        td = g0[ir] + L2 * f2[ir]
+        v = td * us[ir] + gp[ir] * us[ir + 1]
+        if eimag != 0.0:
+            v = v - 1j * eimag * us[ir]
+        us[ir - 1] = -v / gm[ir]
+    return us / r
+
+
+def singular_boundary_radial(st: CL.Structure, enervide: float, lmaxa: np.ndarray, eimag: float = 0.0) -> dict:
+    """Irregular atomic solutions at every atom's boundary points from the
+    singular radial solver (:func:`sch_radial_singular`, started at the atom
+    type's radius rmtg, or at the end of its radial mesh if that is shorter)
+    and the quadratic interpolation of cal_phiato (source/sphere.f90:3186-3370),
+    keyed like :func:`cluster.boundary_radial`."""
+    cl, g = st.cluster, st.grid
+    out = {}
+    cache = {}
+    for isp in range(1, st.nspin + 1):
+        dvs = st.spin_shift(isp)
+        k = np.sqrt(complex(enervide - (st.V0bd + dvs), eimag))
+        for ia in range(cl.natome):
+            ipr = int(cl.itype[ia])
+            r = st.radial_r[ipr]
+            i0 = min(int(np.searchsorted(r, cl.rmtg[ipr])), len(r) - 2)
+            nb = int(g.nbord[ia])
+            rr = st.rrel[:nb, ia]
+            idx = np.clip(np.searchsorted(r, rr, side="right"), 2, len(r) - 1)
+            for L in range(int(lmaxa[ia]) + 1):
+                key = (isp, ipr, L)
+                if key not in cache:
+                    cache[key] = sch_radial_singular(r, st.radial_V[ipr] + dvs, enervide, eimag, k, L, i0)
+                u = cache[key]
+                out[(isp, ia, L)] = CL.f_interp2(rr, r[idx - 2], r[idx - 1], r[idx], u[idx - 2], u[idx - 1], u[idx])
+    return out
+
+
 def energy_dict(st: CL.Structure, energy_ev: float, spinorbit: bool, ylm_comp: bool = True,
                 relativistic: Optional[bool] = None, so_coupling: float = 0.1, basereel: bool = False,
                 gradvr: Optional[np.ndarray] = None, e_fermi_ev: float = -5.0, eimag_ry: float = 0.0,
-                fdm_comp: bool = False, irregular: bool = False) -> dict:
+                fdm_comp: bool = False, irregular: bool = False, irregular_radial: str = "free") -> dict:
     """Per-energy arguments of one complex mat_solve call.
 
     spinorbit: nspino = 2 (needs nspin = 2), with the relativistic terms unless
@@ -185,6 +248,9 @@ def energy_dict(st: CL.Structure, energy_ev: float, spinorbit: bool, ylm_comp: b
     irregular (implies fdm_comp, needs eimag_ry > 0): the irregular cluster
     solution with both atomic solutions (Test_reg = 0, n_ato_RI = 2,
     ``source/mat.f90:138-147``) instead of the regular one.
+    irregular_radial: the irregular atomic solution, "free" (the free-space
+    model of :func:`irregular_boundary_radial`) or "singular" (the singular
+    radial solver through the atom's potential, :func:`singular_boundary_radial`).
     """
     from . import abi
     g = st.grid
@@ -203,7 +269,12 @@ def energy_dict(st: CL.Structure, energy_ev: float, spinorbit: bool, ylm_comp: b
     n_ri = 2 if fdm_comp else 1
     rads = [CL.boundary_radial(st, ei.enervide, ei.lmaxa)]
     if fdm_comp:
-        rads.append(irregular_boundary_radial(st, ei.enervide, ei.lmaxa))
+        if irregular_radial == "singular":
+            rads.append(singular_boundary_radial(st, ei.enervide, ei.lmaxa, eimag_ry))
+        elif irregular_radial == "free":
+            rads.append(irregular_boundary_radial(st, ei.enervide, ei.lmaxa))
+        else:
+            raise ValueError("irregular_radial is 'free' or 'singular'")
     phi = np.zeros((g.nbtm, ei.nlmagm, nspinp, nspino, n_ri, st.natome, 2), order="F")
 
     def harmonic(ia, nb, L, m):

@@ -449,3 +449,31 @@ def test_k8_transparent_absorber_spin_orbit():
         assert amp < bar and out < bar, (h, amp, out)
         errs.append(amp)
     assert errs[1] < errs[0] / 1.6
+
+
+@pytest.mark.parametrize("eimag", [0.0, 0.04])
+def test_singular_radial_solution_free_space(eimag):
+    """The singular radial solver (source/sphere.f90:2591-2812) on a flat
+    potential is sqrt(k/pi) (n_l - i j_l) everywhere inside its starting
+    radius, at real and complex energies (measured 3e-4..8e-4, the radial
+    mesh's error)."""
+    from fdmnes_gb300 import cluster as CL
+    r = CL.radial_mesh(78, 3.0)
+    i0 = int(np.searchsorted(r, 2.6))
+    k = np.sqrt(complex(1.3, eimag))
+    sel = (r > 0.4) & (r < 2.5)
+    for L in range(4):
+        R = CP.sch_radial_singular(r, np.zeros_like(r), 1.3, eimag, k, L, i0)
+        bs, nm = CP.cbessneu(np.sqrt(k / np.pi), k * r[sel], L)
+        exact = nm[:, L] - 1j * bs[:, L]
+        assert np.abs(R[sel] - exact).max() < 2e-3 * np.abs(exact).max(), L
+
+
+@pytest.mark.parametrize("spinorbit", [False, True])
+def test_k7_dense_lu_irregular_solution_singular_inputs(pt, spinorbit):
+    """The irregular system with the singular radial solver's atomic
+    solutions: Gaussian profile solve vs dense LU (measured 7.4e-12 / 2.2e-11)."""
+    ga = abi.GridArgs(CP.grid_dict(pt, spinorbit))
+    ea = abi.EnergyArgs(CP.energy_dict(pt, E, spinorbit=spinorbit, eimag_ry=EIMAG_RY, irregular=True,
+                                       irregular_radial="singular"))
+    assert _dense_rel(ga, ea) < 1e-9
