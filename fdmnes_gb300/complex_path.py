@@ -29,8 +29,9 @@ given: the reference's default FDM path zeroes the broadening before the solve
 the complex-argument j_l, n_l of ``cbessneu`` at k = sqrt(Ecinetic + i Eimag)
 (``phiso``, ``source/mat.f90:778-785,978-990``) and the grid diagonal carries
 -i Eimag (``E_comp``); ``phiato`` stays the real-energy model.  This is the
-regular solution; with ``fdm_comp`` phiato also carries a model irregular
-atomic solution, and ``irregular`` builds the arguments of the irregular
+regular solution; with ``fdm_comp`` phiato also carries an irregular atomic
+solution (a free-space model, or the singular radial solver's restatement),
+and ``irregular`` builds the arguments of the irregular
 cluster solution of the reference's ``FDM_comp`` mode, whose amplitudes and the
 regular ones form Tau_RI (``source/mat.f90:219-292``).
 """
