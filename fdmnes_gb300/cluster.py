@@ -551,14 +551,20 @@ def radial_mesh(Z: int, rmax: float, n_per_decade: int = 120) -> np.ndarray:
     return r0 * 10.0 ** (np.arange(nr) / n_per_decade)
 
 
-def sch_radial(r: np.ndarray, V: np.ndarray, enervide: float, ecinetic: float, L: int, Z: float) -> np.ndarray:
+def sch_radial(r: np.ndarray, V: np.ndarray, enervide: float, ecinetic: float, L: int, Z: float,
+               eimag: float = 0.0) -> np.ndarray:
     """Regular radial solution R_L(r) = u_L(r)/r on mesh r.
 
     Three-point finite-difference recursion of source/sphere.f90:324-396
     (coefficients) and :583-695 (outward integration), started from the
     expansion at the origin of :519-523 with p = L+1.  Renormalisation is
-    off (the reference default, source/lecture.f90:2156).
+    off (the reference default, source/lecture.f90:2156).  With eimag > 0
+    (a complex energy) the solution is complex: the expansion gains the
+    imaginary term ci r^(p+2), ci = -Eimag / (4L + 6) (:471, :548), and the
+    recursion -i Eimag on its diagonal (:631-633).
     """
+    if eimag != 0.0:
+        return _sch_radial_complex(r, V, enervide, ecinetic, L, Z, eimag)
     nr = len(r)
     rp = np.empty(nr)
     rm = np.empty(nr)
@@ -584,6 +590,34 @@ def sch_radial(r: np.ndarray, V: np.ndarray, enervide: float, ecinetic: float, L
     for ir in range(1, nr - 1):
         td = g0[ir] + L2 * f2[ir]
         u[ir + 1] = -(td * u[ir] + gm[ir] * u[ir - 1]) / gp[ir]
+    return u / r
+
+
+def _sch_radial_complex(r, V, enervide, ecinetic, L, Z, eimag):
+    nr = len(r)
+    rp = np.empty(nr)
+    rm = np.empty(nr)
+    rp[:-1] = r[1:]
+    rp[-1] = r[-1] ** 2 / r[-2]
+    rm[1:] = r[:-1]
+    rm[0] = r[0] ** 2 / r[1]
+    dr = 0.5 * (rp - rm)
+    claplm = 1.0 / ((r - rm) * dr)
+    claplp = 1.0 / ((rp - r) * dr)
+    g0 = (claplm + claplp) + (V - enervide)
+    gm = -claplm
+    gp = -claplp
+    f2 = 1.0 / r ** 2
+    br = -Z / (L + 1.0)
+    cr = -(2 * Z * br + ecinetic) / (4 * L + 6)
+    ci = -eimag / (4 * L + 6)
+    p = L + 1.0
+    u = np.zeros(nr, dtype=np.complex128)
+    u[0:2] = (1 + br * r[0:2] + cr * r[0:2] ** 2) * r[0:2] ** p + 1j * ci * r[0:2] ** (p + 2)
+    L2 = L * (L + 1)
+    for ir in range(1, nr - 1):
+        td = g0[ir] + L2 * f2[ir]
+        u[ir + 1] = -(td * u[ir] + gm[ir] * u[ir - 1] - 1j * eimag * u[ir]) / gp[ir]
     return u / r
 
 
@@ -766,10 +800,11 @@ class EnergyInputs:
     ispin: int = 1
 
 
-def boundary_radial(st: Structure, enervide: float, lmaxa: np.ndarray) -> Dict[tuple, np.ndarray]:
+def boundary_radial(st: Structure, enervide: float, lmaxa: np.ndarray, eimag: float = 0.0) -> Dict[tuple, np.ndarray]:
     """Radial solutions u_L(r) of every atom at its boundary points (Sch_radial,
     then f_interp2 as in cal_phiato), keyed by (spin block, atom index 0-based,
-    L) for every spin block of the structure and L <= lmaxa[ia]."""
+    L) for every spin block of the structure and L <= lmaxa[ia]; complex at a
+    complex energy (eimag > 0)."""
     cl, g = st.cluster, st.grid
     out: Dict[tuple, np.ndarray] = {}
     ur_cache: Dict[tuple, np.ndarray] = {}
@@ -788,7 +823,7 @@ def boundary_radial(st: Structure, enervide: float, lmaxa: np.ndarray) -> Dict[t
                 key = (isp, ipr, L)
                 if key not in ur_cache:
                     ur_cache[key] = sch_radial(r, Vrad, enervide, ecs, L, float(cl.zproto[ipr]) +
-                                               (1.0 if ipr == 0 else 0.0))
+                                               (1.0 if ipr == 0 else 0.0), eimag)
                 u = ur_cache[key]
                 out[(isp, ia, L)] = f_interp2(rr, r[idx - 2], r[idx - 1], r[idx], u[idx - 2], u[idx - 1], u[idx])
     return out

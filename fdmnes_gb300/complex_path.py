@@ -28,7 +28,8 @@ given: the reference's default FDM path zeroes the broadening before the solve
 (``source/lecture.f90:5410``).  With ``eimag_ry`` > 0 the outer functions are
 the complex-argument j_l, n_l of ``cbessneu`` at k = sqrt(Ecinetic + i Eimag)
 (``phiso``, ``source/mat.f90:778-785,978-990``) and the grid diagonal carries
--i Eimag (``E_comp``); ``phiato`` stays the real-energy model.  This is the
+-i Eimag (``E_comp``); ``phiato`` stays the real-energy model unless
+``complex_radial`` asks for the radial solutions at the complex energy.  This is the
 regular solution; with ``fdm_comp`` phiato also carries an irregular atomic
 solution (a free-space model, or the singular radial solver's restatement),
 and ``irregular`` builds the arguments of the irregular
@@ -237,7 +238,8 @@ def singular_boundary_radial(st: CL.Structure, enervide: float, lmaxa: np.ndarra
 def energy_dict(st: CL.Structure, energy_ev: float, spinorbit: bool, ylm_comp: bool = True,
                 relativistic: Optional[bool] = None, so_coupling: float = 0.1, basereel: bool = False,
                 gradvr: Optional[np.ndarray] = None, e_fermi_ev: float = -5.0, eimag_ry: float = 0.0,
-                fdm_comp: bool = False, irregular: bool = False, irregular_radial: str = "free") -> dict:
+                fdm_comp: bool = False, irregular: bool = False, irregular_radial: str = "free",
+                complex_radial: bool = False) -> dict:
     """Per-energy arguments of one complex mat_solve call.
 
     spinorbit: nspino = 2 (needs nspin = 2), with the relativistic terms unless
@@ -252,6 +254,9 @@ def energy_dict(st: CL.Structure, energy_ev: float, spinorbit: bool, ylm_comp: b
     irregular_radial: the irregular atomic solution, "free" (the free-space
     model of :func:`irregular_boundary_radial`) or "singular" (the singular
     radial solver through the atom's potential, :func:`singular_boundary_radial`).
+    complex_radial: at a complex energy, the regular atomic solution of the
+    radial equation at that energy (complex, as the reference's Sphere with
+    Ecomp computes it) instead of the real-energy one.
     """
     from . import abi
     g = st.grid
@@ -268,7 +273,7 @@ def energy_dict(st: CL.Structure, energy_ev: float, spinorbit: bool, ylm_comp: b
     ri = CL.newind(st, nlmsa, nlmso, nspino, irregular=irregular)
     nspinp = st.nspin
     n_ri = 2 if fdm_comp else 1
-    rads = [CL.boundary_radial(st, ei.enervide, ei.lmaxa)]
+    rads = [CL.boundary_radial(st, ei.enervide, ei.lmaxa, eimag_ry if complex_radial else 0.0)]
     if fdm_comp:
         if irregular_radial == "singular":
             rads.append(singular_boundary_radial(st, ei.enervide, ei.lmaxa, eimag_ry))

@@ -184,6 +184,20 @@ def test_single_atom_scattering_is_reciprocal_and_unitary(oracle_lib):
         assert np.abs(Ts).max() < 1.001, E
 
 
+def test_radial_solution_free_space_complex_energy():
+    # V = 0 at E + i Eimag: the regular solution is proportional to r j_l(k r),
+    # k = sqrt(E + i Eimag) complex (source/sphere.f90:471,548,631-633)
+    from fdmnes_gb300 import complex_path as CP
+    r = CL.radial_mesh(29, 4.0)
+    k = np.sqrt(complex(1.3, 0.04))
+    sel = (r > 0.5) & (r < 2.0)
+    for L in range(4):
+        R = CL.sch_radial(r, np.zeros_like(r), 1.3, 1.3, L, 0.0, 0.04)
+        bs, _ = CP.cbessneu(1.0, k * r[sel], L)
+        ratio = R[sel] / bs[:, L]
+        assert np.std(ratio) / abs(np.mean(ratio)) < 1e-3
+
+
 def test_newind_matches_oracle(oracle_lib):
     st = CL.small_cu_structure()
     ga = abi.GridArgs(st)
