@@ -47,6 +47,7 @@ def lib():
         L.oracle_assemble_csr.argtypes = [vp, vp, vp, vp, vp, vp]
         L.oracle_assemble_csr_c.argtypes = [vp, vp, vp, vp, vp, vp]
         L.oracle_newind.argtypes = [vp, vp, vp, vp, C.c_int, C.c_int32, vp, vp, vp, vp, vp]
+        L.oracle_newind_irregular.argtypes = [vp, vp, vp, vp, C.c_int32, vp, vp, vp, vp, vp]
         L.oracle_cbessneur.argtypes = [C.c_double, C.c_double, C.c_int, vp, vp]
         L.oracle_invcomp.argtypes = [C.c_int, vp]
         L.oracle_taull.argtypes = [vp, vp, C.c_int, vp, vp, C.POINTER(C.c_int32)]
@@ -98,7 +99,9 @@ def taull(grid_args, energy_args, smr, iaabs=1):
     return t.copy()
 
 
-def newind(grid_args, xyz4, distai, nlmsa, nlmso, nligne, npoint, natome):
+def newind(grid_args, xyz4, distai, nlmsa, nlmso, nligne, npoint, natome, irregular=False):
+    """Row numbering and profile; irregular: FDM_comp's irregular solution
+    (both atomic solutions, no outer-sphere rows; nlmso is then unused)."""
     new = np.zeros(npoint + 1, dtype=np.int32)
     newinv = np.zeros(nligne, dtype=np.int32)
     ianew = np.zeros(natome, dtype=np.int32)
@@ -107,9 +110,14 @@ def newind(grid_args, xyz4, distai, nlmsa, nlmso, nligne, npoint, natome):
     xyz4 = np.ascontiguousarray(xyz4, dtype=np.float64)
     distai = np.ascontiguousarray(distai, dtype=np.float64)
     nlmsa = np.ascontiguousarray(nlmsa, dtype=np.int32)
-    st = lib().oracle_newind(C.addressof(grid_args.s), xyz4.ctypes.data, distai.ctypes.data, nlmsa.ctypes.data,
-                             nlmso, nligne, new.ctypes.data, newinv.ctypes.data, ianew.ctypes.data,
-                             lb1.ctypes.data, lb2.ctypes.data)
+    if irregular:
+        st = lib().oracle_newind_irregular(C.addressof(grid_args.s), xyz4.ctypes.data, distai.ctypes.data,
+                                           nlmsa.ctypes.data, nligne, new.ctypes.data, newinv.ctypes.data,
+                                           ianew.ctypes.data, lb1.ctypes.data, lb2.ctypes.data)
+    else:
+        st = lib().oracle_newind(C.addressof(grid_args.s), xyz4.ctypes.data, distai.ctypes.data, nlmsa.ctypes.data,
+                                 nlmso, nligne, new.ctypes.data, newinv.ctypes.data, ianew.ctypes.data,
+                                 lb1.ctypes.data, lb2.ctypes.data)
     if st != 0:
         raise RuntimeError("oracle_newind failed")
     return new, newinv, ianew, lb1, lb2

@@ -375,11 +375,14 @@ int oracle_mat_solve(const fdmgpu_grid* g, const fdmgpu_energy* e, double* smr, 
   return 0;
 }
 
-// newind, source/mat.f90:1761-1921, regular solution (n_ato_RI = 1), nspino 1 or 2.
+// newind, source/mat.f90:1761-1921, nspino 1 or 2: the regular solution
+// (n_ato_RI = 1), or with irregular != 0 FDM_comp's irregular one with both
+// atomic solutions (n_ato_RI = 2, no outer-sphere rows, :1862).
 // xyz4: (npsom) distance of each point; new_ has npoint+1 entries (index 0..npoint).
-int oracle_newind(const fdmgpu_grid* g, const double* xyz4, const double* distai, const int32_t* nlmsa, int nlmso,
-                  int32_t nligne, int32_t* new_, int32_t* newinv, int32_t* ianew, int32_t* lb1, int32_t* lb2) {
-  const int npoint = g->npoint, natome = g->natome, nspino = g->nspino, n_ato_RI = 1;
+static int newind_rows(const fdmgpu_grid* g, const double* xyz4, const double* distai, const int32_t* nlmsa,
+                       int nlmso, int32_t nligne, int irregular, int32_t* new_, int32_t* newinv, int32_t* ianew,
+                       int32_t* lb1, int32_t* lb2) {
+  const int npoint = g->npoint, natome = g->natome, nspino = g->nspino, n_ato_RI = irregular ? 2 : 1;
   int ii = 0;
   new_[0] = 0;
   for (int i = 1; i <= npoint; ++i) {
@@ -434,9 +437,11 @@ int oracle_newind(const fdmgpu_grid* g, const double* xyz4, const double* distai
       lb2[ianew[ia - 1] + L - 1] = lb22;
     }
   }
-  int lb11 = nligne - nlmso + 1;
-  for (int ib = 1; ib <= g->nsortf; ++ib) lb11 = std::min(lb11, new_[g->isrt[ib - 1]] - n);
-  for (int r = nligne - nlmso + 1; r <= nligne; ++r) { lb1[r - 1] = lb11; lb2[r - 1] = nligne; }
+  if (!irregular) {
+    int lb11 = nligne - nlmso + 1;
+    for (int ib = 1; ib <= g->nsortf; ++ib) lb11 = std::min(lb11, new_[g->isrt[ib - 1]] - n);
+    for (int r = nligne - nlmso + 1; r <= nligne; ++r) { lb1[r - 1] = lb11; lb2[r - 1] = nligne; }
+  }
   for (int r = nligne - 1; r >= 1; --r) lb1[r - 1] = std::min(lb1[r - 1], lb1[r]);
   for (int r = 0; r < nligne; ++r) newinv[r] = 0;
   for (int i = 1; i <= npoint; ++i) {
@@ -449,6 +454,17 @@ int oracle_newind(const fdmgpu_grid* g, const double* xyz4, const double* distai
   for (int ia = 1; ia <= natome; ++ia)
     for (int Lm = 1; Lm <= n_ato_RI * nlmsa[ia - 1]; ++Lm) newinv[ianew[ia - 1] + Lm - 1] = -ia;
   return 0;
+}
+
+int oracle_newind(const fdmgpu_grid* g, const double* xyz4, const double* distai, const int32_t* nlmsa, int nlmso,
+                  int32_t nligne, int32_t* new_, int32_t* newinv, int32_t* ianew, int32_t* lb1, int32_t* lb2) {
+  return newind_rows(g, xyz4, distai, nlmsa, nlmso, nligne, 0, new_, newinv, ianew, lb1, lb2);
+}
+
+int oracle_newind_irregular(const fdmgpu_grid* g, const double* xyz4, const double* distai, const int32_t* nlmsa,
+                            int32_t nligne, int32_t* new_, int32_t* newinv, int32_t* ianew, int32_t* lb1,
+                            int32_t* lb2) {
+  return newind_rows(g, xyz4, distai, nlmsa, 0, nligne, 1, new_, newinv, ianew, lb1, lb2);
 }
 
 // cbessneur, source/sphere.f90:7356-7384: fnorm*j_l(z), fnorm*n_l(z), l = 0..lmax.

@@ -157,6 +157,31 @@ def test_newind_spin_orbit_matches_oracle(pt):
     assert np.array_equal(ri.lb2[rows - 2], ri.lb2[rows - 1])
 
 
+def test_newind_irregular_matches_oracle():
+    """The irregular numbering (both atomic solutions, no outer-sphere rows):
+    the host's newind and the oracle's independent restatement agree, on the
+    13-atom Cu cluster (nspino = 1) and on a two-spin-block Pt cluster with
+    spin-orbit tables (nspino = 2)."""
+    from fdmnes_gb300 import cluster as CL
+    cases = []
+    cu = CL.build_structure(CL.cu_cluster(2.6), 0.3, 3.0, 35.0)
+    cases.append((cu, abi.GridArgs(cu), 1))
+    ptc = CL.build_structure(CL.pt_cluster(2.8), 0.3, 3.0, 35.0, nspin=2)
+    cases.append((ptc, abi.GridArgs(CP.grid_dict(ptc, True)), 2))
+    for st, ga, nspino in cases:
+        ei = CL.energy_inputs(st, E)
+        nlmsa = (nspino * (ei.lmaxa + 1) ** 2).astype(np.int32)
+        nlmso = nspino * (ei.lmaxso + 1) ** 2
+        ri = CL.newind(st, nlmsa, nlmso, nspino, irregular=True)
+        g = st.grid
+        new, newinv, ianew, lb1, lb2 = oracle.newind(ga, g.xyz[3], st.distai, nlmsa, nlmso, ri.nligne, g.npoint,
+                                                     st.natome, irregular=True)
+        assert st.natome > 1
+        assert np.array_equal(new, ri.new) and np.array_equal(newinv, ri.newinv)
+        assert np.array_equal(ianew, ri.ianew)
+        assert np.array_equal(lb1, ri.lb1) and np.array_equal(lb2, ri.lb2)
+
+
 def test_gradpot_is_exact_on_linear_potentials(pt):
     """gradvr (source/potential.f90:5436-5477) on V = a.r + b returns a at every
     point whose 12 neighbours lie inside the grid, axis k of neighbour pair iv
