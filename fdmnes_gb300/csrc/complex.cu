@@ -117,9 +117,6 @@ __device__ __forceinline__ double2 phic(const CIn& c, const Prob& P, const Stati
                                     ((isol - 1) + (int64_t)S.nspino * ((iri - 1) + (int64_t)P.nri * (ia - 1)))));
   return make_double2(c.phi[off], c.phi[off + c.phi_im]);
 }
-__device__ __forceinline__ double besr(const CIn& c, const double* a, const StaticDev& S, int ib, int L, int isp) {
-  return a[((int64_t)(isp - 1) * S.nsort + (ib - 1)) * c.nl + L];
-}
 // Complex Bessel / Neumann value: the imaginary block follows the real one
 // (complex energies); zero imaginary part for real energies.
 __device__ __forceinline__ double2 besc(const CIn& c, const Prob& P, const double* a, const StaticDev& S, int ib, int L,
