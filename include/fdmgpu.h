@@ -82,7 +82,10 @@ typedef enum {
                                   contract the error by about 1e-3 per step where the
                                   FP32-computed ones stall, so no double-float
                                   refinement step is needed; double-float steps only
-                                  for energies still above the accepted level           */
+                                  for energies still above the accepted level, and
+                                  in a real batch the FP64 assembly and elimination
+                                  for those the double-float steps leave above it
+                                  (a complex batch reports them not converged)          */
 } fdmgpu_escalation;
 
 /* Energy-independent arguments of mat_solve (source/mat_solve_gaussian.f90:17-67). */
