@@ -271,10 +271,12 @@ void fdmgpu_destroy(fdmgpu_handle* h);
  * smr (nlmso, nligne) column-major (and smi when Cal_comp).  Synchronous.
  * smr/smi are host pointers.  info may be NULL.
  * Complex problems (Cal_comp: complex harmonics, spin-orbit with nspino = 2,
- * relativistic terms; real energies, complex basis, C1 characters) are
- * solved as their real-equivalent system with tile-local pivoting, in FP64
- * or in mixed precision (FP32 factor, double-float residual refinement);
- * smi must be given. */
+ * relativistic terms; real or complex energies (E_comp), complex basis, C1
+ * characters; the regular solution, or FDM_comp's irregular one with both
+ * atomic solutions: irregular = 1, n_RI = n_ato_RI = 2, Test_reg = 0,
+ * nligneso = nligne) are solved as their real-equivalent system with
+ * tile-local pivoting, in FP64 or in mixed precision (FP32 factor,
+ * double-float residual refinement); smi must be given. */
 fdmgpu_status fdmgpu_mat_solve(fdmgpu_handle* h, const fdmgpu_energy* e, int32_t precision,
                                double* smr, double* smi, fdmgpu_info* info);
 
